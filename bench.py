@@ -1,0 +1,275 @@
+"""Benchmark: particle-steps/s of the DEM step on one GB300.
+
+Workload (default): the granular column collapse -- 50,000 convex hull grains
+(Avalanche law, linked-cell neighbour list) falling onto a rigid floor --
+generated with a fixed seed by rockable_gb300.scenes.  One "step" is one pass
+of the velocity-Verlet step loop (drift, narrow phase + force law, ordered
+resultants, accelerations, half-kick, plus the NL rebuild every interVerlet).
+
+Legs of one run:
+  value      : device-timed throughput of K steps, state resident in HBM
+               (CUDA events on the engine's stream);
+  e2e        : the same metric through the C ABI with host-owned state: every
+               step uploads the bodies' kinematics from pinned host memory and
+               downloads the stepped state;
+  roofline   : the narrow-phase kernel's algorithmic bytes (140 B per
+               neighbour-list entry) over its event-timed duration, against
+               the measured HBM copy bandwidth;
+  cpu_baseline: the oracle (CPU restatement of the reference path, OpenMP) on
+               a bounded sample of the same scene, on this host's cores.
+`--impl reference` times the CPU path alone, on this workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scene", default="column", choices=["column", "cubes"])
+    ap.add_argument("--n", type=int, default=50000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def make_scene(a):
+    from rockable_gb300 import scenes
+    if a.scene == "cubes":
+        return scenes.sphero_cube_box()
+    return scenes.column_collapse(n=a.n)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.out = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.flush()
+        rows = [l.split(",") for l in open(self.out.name).read().strip().split("\n") if l.strip()]
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, dist
+
+
+def pinned(shape):
+    """Pinned host buffer (page-locked through torch when available)."""
+    try:
+        import torch
+        return torch.empty(int(np.prod(shape)), dtype=torch.float64, pin_memory=True).numpy().reshape(shape)
+    except Exception:
+        return np.zeros(shape)
+
+
+def cpu_baseline(scene, budget_s):
+    """Oracle (CPU restatement, OpenMP) on a bounded sample of the workload."""
+    from oracle import oracle
+    from rockable_gb300 import scenes
+    oracle.build()
+    d = tempfile.mkdtemp(prefix="rk_cpu_")
+    conf = scenes.write_conf(scene, d)
+    o = oracle.Oracle(conf)
+    o.update_nl()
+    nfree = o.n - o.n_driven
+    t0 = time.perf_counter()
+    o.run(1)
+    t1 = time.perf_counter() - t0
+    steps = max(2, min(2000, int(budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.run(steps)
+    el = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": nfree * steps / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d steps of the %d-body scene (after load and the initial NL update), %.1f s" % (
+                steps, o.n, el)}
+
+
+def run_reference(a, rank):
+    if rank != 0:
+        return
+    scene = make_scene(a)
+    reps = []
+    for _ in range(max(1, a.warmup and 1)):
+        pass
+    r = cpu_baseline(scene, a.cpu_seconds)
+    value = r["value"]
+    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": a.gpus, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "impl": "reference",
+           "config": {"workload": scene["name"], "law": scene["law"], "bodies": int(len(scene["bodies"]["mass"]))},
+           "cpu_baseline": r, "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0}}
+    out["ms_per_step"] = 1000.0 * (len(scene["bodies"]["mass"]) - scene["n_driven"]) / value
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse()
+    rank, ws, dist = dist_setup()
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+    from rockable_gb300 import build_ext
+    if rank == 0:
+        build_ext.build()
+    if dist:
+        dist.barrier()
+    from rockable_gb300.abi import GpuScene, RK_LAW
+    scene = make_scene(a)
+    b = scene["bodies"]
+    N = len(b["mass"])
+    nfree = N - scene["n_driven"]
+    dev = int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0
+    g = GpuScene(device=dev)
+    g.upload_shapes(scene["shape_tables"])
+    g.upload_bodies(b, scene["n_driven"])
+    g.set_params(t=0.0, dt=scene["dt"], gravity=scene["gravity"], DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
+                 interVerlet=scene["interVerlet"], interVerletC=0.0, law=RK_LAW[scene["law"]], ngroup=scene["ngroup"],
+                 table=scene["table"])
+    g.update_nl()
+    g.step(a.warmup)
+    # ---- timed region (device-resident state)
+    clocks = Clocks()
+    if dist:
+        dist.barrier()
+    g.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    rep = g.step(a.steps)
+    wall = time.perf_counter() - t0
+    ms, launches = g.last_step_timing()
+    ck = clocks.stop()
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * nfree * a.steps / (ms / 1000.0)
+    st = g.stats()
+    # ---- per-phase profile (outside the timed region)
+    g.set_profiling(True)
+    g.step(min(50, a.steps))
+    prof = g.profile()
+    g.set_profiling(False)
+    nphase = prof["narrow_force"]
+    t_narrow = nphase[0] / max(nphase[1], 1)  # ms per launch
+    C = st["n_entries"]
+    hbm, src = peaks()
+    achieved = 140.0 * C / (t_narrow / 1000.0) / 1e9 if t_narrow > 0 else None
+    # ---- e2e through the C ABI with host-owned state
+    e2e = None
+    if not a.no_e2e:
+        hb = {k: pinned((N, 4 if k == "Q" else 3)) for k in ["pos", "vel", "acc", "Q", "vrot", "arot"]}
+        cur = g.bodies()
+        for k in hb:
+            hb[k][...] = cur[k]
+        k_e2e = max(5, min(a.steps, 50))
+        g.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            g.upload_kinematics(hb["pos"], hb["vel"], hb["acc"], hb["Q"], hb["vrot"], hb["arot"])
+            g.step(1)
+            out = g.bodies()
+            for k in hb:
+                hb[k][...] = out[k]
+        el = time.perf_counter() - t0
+        e2e = {"value": ws * nfree * k_e2e / el, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 25 * 8),
+               "steps": k_e2e, "note": "every step: kinematics H2D from pinned host, rk_step, full body state D2H"}
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        cpu = cpu_baseline(scene, a.cpu_seconds)
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": a.steps,
+               "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, rockable_gb300.scenes)",
+               "form": "plain FP64 (bit-identical to the reference CPU arithmetic)",
+               "config": {"workload": scene["name"], "law": scene["law"], "bodies": N, "free_bodies": nfree,
+                          "entries": int(C), "active": int(st["n_active"]),
+                          "nl_rebuilds_in_timed": int(rep["nl_updates"]), "dt": scene["dt"],
+                          "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
+                          "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if C * 240 > 129e6 else
+                          "working set below L2 size", "parallelism": "replicas" if ws > 1 else "single GPU"},
+               "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
+               "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
+                            "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                            "peak_source": src, "bytes_per_entry": 140, "entries": int(C),
+                            "ms_per_launch": t_narrow},
+               "phases_ms_per_step": {k: v[0] / max(1, min(50, a.steps)) for k, v in prof.items()},
+               "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    g.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,238 @@
+/*
+ * rk_gpu.h -- C ABI of the GB300 DEM step engine (librk_gpu.so).
+ *
+ * One context owns all device memory of one scene on one GPU.  The entry
+ * points replace the seams through which Rockable's step loop drives its
+ * hot path (paths relative to the Rockable source tree):
+ *
+ *   rk_step          <- Rockable::integrationStep, the velocity-Verlet step
+ *                       (src/Core/Rockable.hpp:231, Rockable.cpp:1979-2158)
+ *                       plus the loop bookkeeping of Rockable::integrate that
+ *                       schedules NL updates (Rockable.cpp:2584-2736)
+ *   rk_update_nl     <- Rockable::UpdateNL (Rockable.hpp:274; bruteForce
+ *                       Rockable.cpp:1614-1662, linkCells 1667-1809) with the
+ *                       AddOrRemoveInteractions seam (Rockable.hpp:318,
+ *                       Rockable.cpp:1309-1432)
+ *   rk_accelerations <- Rockable::accelerations (Rockable.cpp:3562-3719), the
+ *                       load-time "fake step" of Rockable::loadConf (1137)
+ *   rk_upload_* / rk_download_*
+ *                    <- the state Rockable::loadConf / saveConf read and
+ *                       write (Rockable.cpp:440-610, 886-1002)
+ *   rk_set_params    <- the force-law selection and DataTable parameters
+ *                       (Rockable.cpp:763-781, ForceLaw.hpp:44-55)
+ *   rk_set_controls  <- DrivingSystem controls and the tritri servo
+ *                       (DrivingSystem.hpp:70-75, DrivingSystem.cpp:186-268)
+ *   rk_get_stats     <- Rockable::getKineticEnergy (Rockable.cpp:3958-3970)
+ *
+ * Conventions: every call returns RK_OK (0) or a negative RK_ERR_* code and
+ * never throws; rk_last_error() describes the last failure of the context.
+ * Host buffers passed in are copied before the call returns.  One host thread
+ * per context.  No call falls back to the CPU: without a usable CUDA device,
+ * rk_create fails.
+ */
+#ifndef RK_GPU_H
+#define RK_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RK_ABI_VERSION 1
+
+enum {
+  RK_OK = 0,
+  RK_ERR_ARG = -1,         /* invalid argument (sizes, ordering, indices)      */
+  RK_ERR_CUDA = -2,        /* CUDA runtime error                               */
+  RK_ERR_CAPACITY = -3,    /* a fixed limit was exceeded (see rk_last_error)   */
+  RK_ERR_UNSUPPORTED = -4, /* feature outside this engine (periodic, BCM, ...) */
+  RK_ERR_TIMEOUT = -5,     /* a bounded device wait gave up                    */
+  RK_ERR_STATE = -6,       /* call out of order (e.g. step before upload)      */
+  RK_ERR_NUMERIC = -7      /* non-finite state detected                        */
+};
+
+enum { RK_LAW_DEFAULT = 0, RK_LAW_AVALANCHE = 1, RK_LAW_STICKEDLINKS = 2 };
+enum { RK_FORM_FP64 = 0, RK_FORM_MIXED = 1 };
+
+/* Parameter slots of the per-group-pair table (DataTable ids of
+ * Rockable.cpp:96-123).  table[(p * ngroup + g1) * ngroup + g2]. */
+enum {
+  RK_P_KN = 0, RK_P_EN2, RK_P_KT, RK_P_MU, RK_P_KR, RK_P_MUR,
+  RK_P_KN_IN, RK_P_KT_IN, RK_P_KR_IN, RK_P_EN2_IN, RK_P_FN0_IN, RK_P_FT0_IN, RK_P_MOM0_IN, RK_P_POW_IN,
+  RK_P_KN_OUT, RK_P_KT_OUT, RK_P_KR_OUT, RK_P_EN2_OUT, RK_P_FN0_OUT, RK_P_FT0_OUT, RK_P_MOM0_OUT, RK_P_POW_OUT,
+  RK_NPARAM
+};
+
+/* Control types (DrivingSystem.hpp:52-67). */
+enum {
+  RK_X_VEL = 0, RK_Y_VEL = 1, RK_Z_VEL = 2, RK_XROT_VEL = 3, RK_YROT_VEL = 4, RK_ZROT_VEL = 5,
+  RK_X_FOR = 6, RK_Y_FOR = 7, RK_Z_FOR = 8, RK_XROT_MOM = 9, RK_YROT_MOM = 10, RK_ZROT_MOM = 11,
+  RK_XYZROT_VEL = 100, RK_XYZROT_MOM = 101
+};
+
+typedef struct rk_ctx rk_ctx;
+
+typedef struct rk_config {
+  int device;              /* CUDA device ordinal                              */
+  int form;                /* RK_FORM_FP64 (bit-parity form) or RK_FORM_MIXED   */
+  int64_t entry_capacity;  /* initial neighbour-list capacity; 0 = automatic   */
+} rk_config;
+
+/* Shape library, flattened (Shape.hpp:58-111). */
+typedef struct rk_shapes {
+  int32_t nshapes;
+  const int32_t* vert_ofs;   /* nshapes+1                                      */
+  const double* vertices;    /* 3*vert_ofs[nshapes], shape frame               */
+  const int32_t* edge_ofs;   /* nshapes+1                                      */
+  const int32_t* edges;      /* 2*edge_ofs[nshapes], shape-local vertex ids    */
+  const int32_t* face_ofs;   /* nshapes+1 (faces per shape)                    */
+  const int32_t* face_vofs;  /* face_ofs[nshapes]+1, offsets into face_verts   */
+  const int32_t* face_verts; /* shape-local vertex ids                         */
+  const double* radius;      /* nshapes, Minkowski radius                      */
+  const double* obb;         /* 15*nshapes: center, e1, e2, e3, extent         */
+} rk_shapes;
+
+/* Bodies (Particle.hpp:77-127); the first n_driven are driven walls. */
+typedef struct rk_bodies {
+  int64_t n;
+  int64_t n_driven;
+  const double* pos;       /* 3n */
+  const double* vel;       /* 3n */
+  const double* acc;       /* 3n */
+  const double* Q;         /* 4n, (w, x, y, z) */
+  const double* vrot;      /* 3n */
+  const double* arot;      /* 3n */
+  const double* homothety; /* n  */
+  const double* mass;      /* n  */
+  const double* inertia;   /* 3n */
+  const int32_t* shape;    /* n  */
+  const int32_t* group;    /* n  */
+  const int32_t* cluster;  /* n  */
+} rk_bodies;
+
+typedef struct rk_params {
+  double t;                /* current time                                    */
+  double dt;
+  double gravity[3];
+  double DVerlet;          /* OBB enlargement for the body broad phase         */
+  double dVerlet;          /* sub-element proximity distance                   */
+  double interVerlet;      /* time between periodic NL updates                 */
+  double interVerletC;     /* time elapsed since the last periodic NL update   */
+  double numerical_damping;
+  int32_t law;             /* RK_LAW_*                                         */
+  int32_t params_in_interfaces;
+  int32_t dynamic_update_nl;
+  double disp_update_nl;   /* guard: max displacement                          */
+  double angle_update_nl;  /* guard: max rotation angle (radians)              */
+  int32_t ngroup;
+  const double* table;     /* RK_NPARAM * ngroup * ngroup                      */
+} rk_params;
+
+/* Neighbour-list entries (Interaction.hpp:57-100), sorted by the key
+ * (i, j, type, isub, jsub) and unique. */
+typedef struct rk_entries {
+  int64_t n;
+  const int32_t* i;
+  const int32_t* j;
+  const int32_t* type;
+  const int32_t* isub;
+  const int32_t* jsub;
+  const double* dn;     /* n  */
+  const double* fn;     /* n  */
+  const double* ft;     /* 3n */
+  const double* mom;    /* 3n */
+  const double* damp;   /* n  */
+  const int32_t* bond;  /* n, interface index or -1 */
+} rk_entries;
+
+/* Breakable interfaces (BreakableInterface.hpp:48-77), sorted by (i, j). */
+typedef struct rk_interfaces {
+  int64_t n;
+  const int32_t* i;
+  const int32_t* j;
+  const double* dn0;     /* n  */
+  const double* params;  /* 8n: kn kt kr fn0 ft0 mom0 power Gc */
+  const int32_t* is_inner;
+} rk_interfaces;
+
+typedef struct rk_control {
+  int32_t type;   /* RK_X_VEL ... */
+  int32_t body;
+  double value;
+  double vec[3];
+} rk_control;
+
+typedef struct rk_servo {
+  int32_t kind;      /* 0 none, 1 tritriIsostaticCompression */
+  int32_t icontr;    /* index of the servo's first control   */
+  int32_t walls[6];  /* Xmin Xmax Ymin Ymax Zmin Zmax         */
+  double pressure;
+} rk_servo;
+
+typedef struct rk_step_report {
+  int64_t steps_done;
+  int64_t nl_updates;
+  int64_t n_entries;
+  int64_t n_active;
+  int64_t n_broken;
+  double t;
+} rk_step_report;
+
+typedef struct rk_stats {
+  double e_trans, e_rot;  /* kinetic energies of all bodies */
+  int64_t n_entries, n_active, n_broken, nl_updates;
+  double coordination;    /* 2 * active / free bodies       */
+} rk_stats;
+
+int rk_abi_version(void);
+int rk_create(rk_ctx** out, const rk_config* cfg);
+void rk_destroy(rk_ctx* ctx);
+const char* rk_last_error(const rk_ctx* ctx);
+
+int rk_upload_shapes(rk_ctx* ctx, const rk_shapes* s);
+int rk_upload_bodies(rk_ctx* ctx, const rk_bodies* b);
+int rk_set_params(rk_ctx* ctx, const rk_params* p);
+int rk_upload_entries(rk_ctx* ctx, const rk_entries* e);
+int rk_upload_interfaces(rk_ctx* ctx, const rk_interfaces* f);
+int rk_set_controls(rk_ctx* ctx, const rk_control* c, int32_t n, const rk_servo* servo);
+/* When on, every step also stores each entry's contact normal, point and
+ * relative velocity (needed to write a conf file); off by default. */
+int rk_set_record_geometry(rk_ctx* ctx, int on);
+
+int rk_accelerations(rk_ctx* ctx);
+int rk_update_nl(rk_ctx* ctx);
+int rk_step(rk_ctx* ctx, int64_t nsteps, rk_step_report* report);
+int rk_synchronize(rk_ctx* ctx);
+
+int64_t rk_num_bodies(const rk_ctx* ctx);
+int64_t rk_num_entries(const rk_ctx* ctx);
+int64_t rk_num_interfaces(const rk_ctx* ctx);
+/* Any output pointer may be NULL. */
+int rk_download_bodies(rk_ctx* ctx, double* pos, double* vel, double* acc, double* Q, double* vrot, double* arot,
+                       double* force, double* moment);
+int rk_download_entries(rk_ctx* ctx, int32_t* i, int32_t* j, int32_t* type, int32_t* isub, int32_t* jsub, double* dn,
+                        double* fn, double* ft, double* mom, double* damp, int32_t* bond, uint8_t* active, double* n,
+                        double* pos, double* vel);
+int rk_download_interfaces(rk_ctx* ctx, int32_t* i, int32_t* j, uint8_t* broken);
+/* Overwrite the kinematic state of all bodies from host buffers (any pointer
+ * may be NULL); the host-owned Particles of Rockable are pushed back this way
+ * after a host-side plugin modified them. */
+int rk_upload_kinematics(rk_ctx* ctx, const double* pos, const double* vel, const double* acc, const double* Q,
+                         const double* vrot, const double* arot);
+int rk_get_stats(rk_ctx* ctx, rk_stats* out);
+/* Device time (ms) of the last rk_step call, measured with CUDA events on the
+ * context's stream, and the number of kernels it launched. */
+int rk_last_step_timing(const rk_ctx* ctx, double* ms, int64_t* kernels);
+/* Per-phase device time: when on, rk_step brackets each phase with CUDA
+ * events on the context stream (adds one event pair per phase and step).
+ * Phases: 0 controls, 1 drift, 2 global vertices, 3 narrow phase + law,
+ * 4 resultants + accelerations, 5 breakage, 6 NL rebuild, 7 guard. */
+#define RK_NPHASE 8
+int rk_set_profiling(rk_ctx* ctx, int on);
+int rk_get_profile(const rk_ctx* ctx, double* ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

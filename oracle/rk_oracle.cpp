@@ -426,6 +426,8 @@ struct Sim {
   std::vector<std::map<Key, Contact>> inter;   // Rockable.hpp:107
   std::vector<std::map<size_t, Iface>> ifaces;  // Rockable.hpp:108 (keyed by j)
   std::vector<Contact*> active;
+  std::vector<Contact*> flat;  // every entry in key order (Rockable.cpp:1598-1608)
+  bool flat_dirty{true};
   std::vector<Iface*> to_break;
   std::map<std::string, std::string> options;
   DataTable table;
@@ -863,6 +865,7 @@ static void update_nl_linkcells(Sim& S) {
 static void update_nl(Sim& S) {
   if (S.nl_linkcells) update_nl_linkcells(S);
   else update_nl_bruteforce(S);
+  S.flat_dirty = true;
 }
 
 // ----------------------------------------------------------- force laws ----
@@ -928,7 +931,7 @@ static void law_avalanche(Sim& S, Contact& I) {
   if (mom_square > 0.0 && mom_square > threshold_mom * threshold_mom) I.mom *= threshold_mom / sqrt(mom_square);
 }
 // ForceLaw_StickedLinks.cpp:75-215
-static void law_sticked(Sim& S, Contact& I) {
+static void law_sticked(Sim& S, Contact& I, std::vector<Iface*>& to_break) {
   const Body& Pi = S.bodies[I.k.i];
   const Body& Pj = S.bodies[I.k.j];
   if (I.stick != nullptr) {
@@ -961,7 +964,7 @@ static void law_sticked(Sim& S, Contact& I) {
     I.ft += ftv;
     I.mom += kr * (Pj.vrot - Pi.vrot) * S.dt;
     double yield = pow(norm(I.ft) / ft0, power) + pow(norm(I.mom) / mom0, power) - I.fn / fn0 - 1.0;
-    if (yield > 0.0) S.to_break.push_back(I.stick);
+    if (yield > 0.0) to_break.push_back(I.stick);
   } else {
     if (I.dn > 0.0) { I.fn = 0.0; I.ft.reset(); I.mom.reset(); return; }
     int g1 = Pi.group, g2 = Pj.group;
@@ -1057,7 +1060,9 @@ static void accelerations_from_resultants(Sim& S) {
       default: break;
     }
   }
-  for (size_t i = S.nDriven; i < S.bodies.size(); ++i) {
+  const long nb = (long)S.bodies.size();
+#pragma omp parallel for schedule(static)
+  for (long i = (long)S.nDriven; i < nb; ++i) {
     Body& P = S.bodies[i];
     P.acc = vdiv(P.force, P.mass) + S.gravity;
     Quat Qinv = qconj(P.Q);
@@ -1125,20 +1130,39 @@ static void accelerations(Sim& S) {
   init_forces(S);
   S.active.clear();
   S.to_break.clear();
-  // update_interactions (2934-2977): every NL entry, in body-row order
-  for (size_t k = 0; k < S.inter.size(); ++k)
-    for (auto& kv : S.inter[k]) update_contact(kv.second, S.bodies[kv.first.i], S.bodies[kv.first.j]);
-  // build_activeInteractions (3005-3029)
-  for (size_t k = 0; k < S.inter.size(); ++k)
-    for (auto& kv : S.inter[k])
-      if (kv.second.dn < 0.0 || kv.second.stick != nullptr) S.active.push_back(&kv.second);
-  // compute_forces_and_moments (3035-3046)
-  for (Contact* I : S.active) {
-    if (I->dn < 0.0 || I->stick != nullptr) {
-      if (S.law == 1) law_avalanche(S, *I);
-      else if (S.law == 2) law_sticked(S, *I);
-      else law_default(S, *I);
+  if (S.flat_dirty) {
+    S.flat.clear();
+    for (size_t k = 0; k < S.inter.size(); ++k)
+      for (auto& kv : S.inter[k]) S.flat.push_back(&kv.second);
+    S.flat_dirty = false;
+  }
+  // update_interactions (2934-2977): every NL entry (independent per entry)
+  const long nflat = (long)S.flat.size();
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < nflat; ++k) {
+    Contact& c = *S.flat[k];
+    update_contact(c, S.bodies[c.k.i], S.bodies[c.k.j]);
+  }
+  // build_activeInteractions (3005-3029), in key order
+  for (Contact* c : S.flat)
+    if (c->dn < 0.0 || c->stick != nullptr) S.active.push_back(c);
+  // compute_forces_and_moments (3035-3046): independent per entry; the
+  // rupture requests are collected per thread and merged (sorted later)
+  const long nact = (long)S.active.size();
+#pragma omp parallel
+  {
+    std::vector<Iface*> mine;
+#pragma omp for schedule(static)
+    for (long k = 0; k < nact; ++k) {
+      Contact* I = S.active[k];
+      if (I->dn < 0.0 || I->stick != nullptr) {
+        if (S.law == 1) law_avalanche(S, *I);
+        else if (S.law == 2) law_sticked(S, *I, mine);
+        else law_default(S, *I);
+      }
     }
+#pragma omp critical
+    S.to_break.insert(S.to_break.end(), mine.begin(), mine.end());
   }
   // compute_resultants (3220-3275)
   for (Contact* I : S.active)
@@ -1233,7 +1257,9 @@ static void verlet_step(Sim& S) {
       default: break;
     }
   }
-  for (size_t i = S.nDriven; i < S.bodies.size(); ++i) {
+  const long nb = (long)S.bodies.size();
+#pragma omp parallel for schedule(static)
+  for (long i = (long)S.nDriven; i < nb; ++i) {
     Body& P = S.bodies[i];
     P.pos += S.dt * P.vel + S.dt2_2 * P.acc;
     P.vel += S.dt_2 * P.acc;
@@ -1256,7 +1282,8 @@ static void verlet_step(Sim& S) {
       default: break;
     }
   }
-  for (size_t i = S.nDriven; i < S.bodies.size(); ++i) {
+#pragma omp parallel for schedule(static)
+  for (long i = (long)S.nDriven; i < nb; ++i) {
     Body& P = S.bodies[i];
     P.vel += S.dt_2 * P.acc;
     P.vrot += S.dt_2 * P.arot;
@@ -1529,6 +1556,7 @@ static bool parse_conf(Sim& S, std::istream& conf) {
         if (I.k.i >= S.inter.size()) { g_err = "interaction body index out of range"; return false; }
         S.inter[I.k.i].emplace(I.k, I);  // std::set::insert keeps the first
       }
+      S.flat_dirty = true;
     } else if (tok == "Interfaces") {  // Rockable.cpp:956-1002
       size_t nbi; conf >> nbi;
       for (auto& m : S.ifaces) m.clear();
@@ -1613,6 +1641,7 @@ static void prepro_stick_vertices(Sim& S, double eps) {
             update_vv(I, Pi, Pj);
             auto ins = S.inter[i].emplace(I.k, I);
             p->bonds.push_back(&ins.first->second);
+            S.flat_dirty = true;
           }
         }
       }
@@ -1944,5 +1973,85 @@ const char* orc_option(const orc_sim* s, const char* key) {
   return it == s->S.options.end() ? "" : it->second.c_str();
 }
 int orc_nshapes(const orc_sim* s) { return (int)s->S.shapes.size(); }
+
+void orc_get_shape_sizes(const orc_sim* s, int64_t* z) {
+  z[0] = (int64_t)s->S.shapes.size();
+  z[1] = z[2] = z[3] = z[4] = 0;
+  for (const Shape& sh : s->S.shapes) {
+    z[1] += (int64_t)sh.vertex.size();
+    z[2] += (int64_t)sh.edge.size();
+    z[3] += (int64_t)sh.face.size();
+    for (auto& f : sh.face) z[4] += (int64_t)f.size();
+  }
+}
+void orc_get_shapes(const orc_sim* s, int32_t* vo, double* vx, int32_t* eo, int32_t* ed, int32_t* fo, int32_t* fvo,
+                    int32_t* fv, double* rad, double* obb) {
+  int32_t nv = 0, ne = 0, nf = 0, nfv = 0;
+  size_t k = 0;
+  for (const Shape& sh : s->S.shapes) {
+    vo[k] = nv; eo[k] = ne; fo[k] = nf;
+    for (auto& v : sh.vertex) { vx[3 * nv] = v.x; vx[3 * nv + 1] = v.y; vx[3 * nv + 2] = v.z; nv++; }
+    for (auto& e : sh.edge) { ed[2 * ne] = (int32_t)e.first; ed[2 * ne + 1] = (int32_t)e.second; ne++; }
+    for (auto& f : sh.face) {
+      fvo[nf++] = nfv;
+      for (size_t id : f) fv[nfv++] = (int32_t)id;
+    }
+    rad[k] = sh.radius;
+    const Obb& o = sh.obb;
+    const V3* parts[5] = {&o.center, &o.e[0], &o.e[1], &o.e[2], &o.extent};
+    for (int q = 0; q < 5; q++) { obb[15 * k + 3 * q] = parts[q]->x; obb[15 * k + 3 * q + 1] = parts[q]->y; obb[15 * k + 3 * q + 2] = parts[q]->z; }
+    k++;
+  }
+  vo[k] = nv; eo[k] = ne; fo[k] = nf; fvo[nf] = nfv;
+}
+void orc_get_body_static(const orc_sim* s, int32_t* shape, int32_t* group, int32_t* cluster, double* hom, double* mass,
+                         double* inertia) {
+  size_t i = 0;
+  for (const Body& P : s->S.bodies) {
+    shape[i] = (int32_t)P.shape_id; group[i] = P.group; cluster[i] = P.cluster; hom[i] = P.homothety;
+    mass[i] = P.mass; inertia[3 * i] = P.inertia.x; inertia[3 * i + 1] = P.inertia.y; inertia[3 * i + 2] = P.inertia.z;
+    i++;
+  }
+}
+int orc_ngroup(const orc_sim* s) {
+  int g = (int)s->S.table.ngroup;
+  for (auto& B : s->S.bodies) g = std::max(g, B.group + 1);
+  return g < 1 ? 1 : g;
+}
+void orc_get_table(const orc_sim* s, double* t) {
+  const Sim& S = s->S;
+  const size_t ids[22] = {S.idKn, S.idEn2, S.idKt, S.idMu, S.idKr, S.idMur,
+                          S.idKnI, S.idKtI, S.idKrI, S.idEn2I, S.idFn0I, S.idFt0I, S.idMom0I, S.idPowI,
+                          S.idKnO, S.idKtO, S.idKrO, S.idEn2O, S.idFn0O, S.idFt0O, S.idMom0O, S.idPowO};
+  int G = orc_ngroup(s);
+  for (int p = 0; p < 22; p++)
+    for (int a = 0; a < G; a++)
+      for (int b = 0; b < G; b++) t[((size_t)p * G + a) * G + b] = S.table.get(ids[p], a, b);
+}
+int orc_ncontrols(const orc_sim* s) { return (int)s->S.controls.size(); }
+void orc_get_controls(const orc_sim* s, int32_t* type, int32_t* body, double* value, double* vec, int32_t* servo,
+                      double* pressure) {
+  const Sim& S = s->S;
+  for (size_t k = 0; k < S.controls.size(); k++) {
+    type[k] = S.controls[k].type; body[k] = (int32_t)S.controls[k].i; value[k] = S.controls[k].value;
+    vec[3 * k] = S.controls[k].vec.x; vec[3 * k + 1] = S.controls[k].vec.y; vec[3 * k + 2] = S.controls[k].vec.z;
+  }
+  servo[0] = S.servo ? 1 : 0;
+  servo[1] = (int32_t)S.servo_icontr;
+  servo[2] = (int32_t)S.sXmin; servo[3] = (int32_t)S.sXmax; servo[4] = (int32_t)S.sYmin;
+  servo[5] = (int32_t)S.sYmax; servo[6] = (int32_t)S.sZmin; servo[7] = (int32_t)S.sZmax;
+  *pressure = S.servo_p;
+}
+int orc_set_param(orc_sim* s, const char* name, int g1, int g2, double value) {
+  auto it = s->S.table.id.find(name);
+  if (it == s->S.table.id.end()) return -1;
+  s->S.table.set(it->second, g1, g2, value);
+  return 0;
+}
+void orc_get_flow(const orc_sim* s, double* o) {
+  const Sim& S = s->S;
+  o[0] = S.interVerletC; o[1] = S.dynamicUpdateNL; o[2] = S.dispUpdateNL; o[3] = S.angleUpdateNL;
+  o[4] = S.paramsInInterfaces; o[5] = S.needUpdate ? 1.0 : 0.0;
+}
 
 }  // extern "C"

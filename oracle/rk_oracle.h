@@ -19,9 +19,10 @@ extern "C" {
 typedef struct orc_sim orc_sim;
 
 /* Arithmetic variants for the parts of the reference that live in the
- * unvendored toofus library (quaternion / vector kernels).  Index 0 of every
- * field is the pinned choice (the one that reproduces the reference goldens);
- * the others exist only for the pinning experiment. */
+ * unvendored toofus library (quaternion / vector kernels).  The default,
+ * {qrot 1, qdot 0, qddot 0, qnorm 3, vnorm 1, vdiv 1}, is the pinned choice:
+ * it reproduces the reference's 512_particles and 518_poly regression goldens
+ * bit for bit.  The other values exist only for the pinning experiment. */
 typedef struct {
   int qrot;   /* quaternion-vector rotation form              */
   int qdot;   /* first time-derivative of a quaternion        */
@@ -61,8 +62,8 @@ int orc_save_conf(orc_sim* s, const char* path);
 /* State access ------------------------------------------------------------ */
 int orc_nbodies(const orc_sim* s);
 int orc_ndriven(const orc_sim* s);
-/* 28 doubles per body: pos3 vel3 acc3 Q(w,x,y,z) vrot3 arot3 force3 moment3
- * + homothety, mass, group(as double), cluster(as double) -> 3*8+4 = 28 */
+/* 29 doubles per body: pos3 vel3 acc3 Q(w,x,y,z) vrot3 arot3 force3 moment3
+ * + homothety, mass, group(as double), cluster(as double) */
 void orc_get_bodies(const orc_sim* s, double* out);
 /* Overwrite the kinematic state of all bodies (pos vel acc Q vrot arot:
  * 19 doubles per body). */
@@ -87,8 +88,28 @@ void orc_get_stats(const orc_sim* s, double* out); /* Etrans Erot nactive coordi
 int orc_law_id(const orc_sim* s); /* 0 Default, 1 Avalanche, 2 StickedLinks */
 const char* orc_option(const orc_sim* s, const char* key);
 
-/* Shapes (for the tests that build device shape tables independently). */
+/* Shapes, flattened like rk_shapes of include/rk_gpu.h.
+ * sizes: nshapes, total vertices, total edges, total faces, total face vertices */
 int orc_nshapes(const orc_sim* s);
+void orc_get_shape_sizes(const orc_sim* s, int64_t* sizes);
+void orc_get_shapes(const orc_sim* s, int32_t* vert_ofs, double* vertices, int32_t* edge_ofs, int32_t* edges,
+                    int32_t* face_ofs, int32_t* face_vofs, int32_t* face_verts, double* radius, double* obb);
+/* Per-body constants: shape, group, cluster, homothety, mass, inertia(3). */
+void orc_get_body_static(const orc_sim* s, int32_t* shape, int32_t* group, int32_t* cluster, double* homothety,
+                         double* mass, double* inertia);
+/* Law parameter table in the slot order of include/rk_gpu.h (RK_P_*):
+ * table[(p * ngroup + g1) * ngroup + g2].  Returns ngroup. */
+int orc_ngroup(const orc_sim* s);
+void orc_get_table(const orc_sim* s, double* table);
+/* Controls: type, body, value, vec(3); servo: kind icontr w0..w5, pressure. */
+int orc_ncontrols(const orc_sim* s);
+void orc_get_controls(const orc_sim* s, int32_t* type, int32_t* body, double* value, double* vec, int32_t* servo,
+                      double* pressure);
+/* Flow scalars: interVerletC, dynamicUpdateNL, dispUpdateNL, angleUpdateNL,
+ * paramsInInterfaces, needUpdate */
+void orc_get_flow(const orc_sim* s, double* out);
+/* Set one DataTable entry (both (g1,g2) and (g2,g1)), e.g. "fn0InnerBond". */
+int orc_set_param(orc_sim* s, const char* name, int g1, int g2, double value);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,310 @@
+"""ctypes binding of the C ABI declared in include/rk_gpu.h (librk_gpu.so).
+
+`GpuScene` owns one rk_ctx (one scene on one GPU) and converts numpy arrays to
+the ABI's structs.  The library is the in-tree build under rockable_gb300/_lib;
+there is no CPU fallback: if the library or a CUDA device is missing, the
+calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "_lib", "librk_gpu.so")
+
+RK_OK = 0
+RK_LAW = {"Default": 0, "Avalanche": 1, "StickedLinks": 2}
+RK_FORM_FP64, RK_FORM_MIXED = 0, 1
+RK_NPARAM = 22
+ERRORS = {-1: "RK_ERR_ARG", -2: "RK_ERR_CUDA", -3: "RK_ERR_CAPACITY", -4: "RK_ERR_UNSUPPORTED",
+          -5: "RK_ERR_TIMEOUT", -6: "RK_ERR_STATE", -7: "RK_ERR_NUMERIC"}
+
+P = C.c_void_p
+I32P = C.POINTER(C.c_int32)
+DP = C.POINTER(C.c_double)
+I64 = C.c_int64
+
+
+class RkConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("form", C.c_int), ("entry_capacity", I64)]
+
+
+class RkShapes(C.Structure):
+    _fields_ = [("nshapes", C.c_int32), ("vert_ofs", P), ("vertices", P), ("edge_ofs", P), ("edges", P),
+                ("face_ofs", P), ("face_vofs", P), ("face_verts", P), ("radius", P), ("obb", P)]
+
+
+class RkBodies(C.Structure):
+    _fields_ = [("n", I64), ("n_driven", I64), ("pos", P), ("vel", P), ("acc", P), ("Q", P), ("vrot", P),
+                ("arot", P), ("homothety", P), ("mass", P), ("inertia", P), ("shape", P), ("group", P),
+                ("cluster", P)]
+
+
+class RkParams(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("gravity", C.c_double * 3), ("DVerlet", C.c_double),
+                ("dVerlet", C.c_double), ("interVerlet", C.c_double), ("interVerletC", C.c_double),
+                ("numerical_damping", C.c_double), ("law", C.c_int32), ("params_in_interfaces", C.c_int32),
+                ("dynamic_update_nl", C.c_int32), ("disp_update_nl", C.c_double),
+                ("angle_update_nl", C.c_double), ("ngroup", C.c_int32), ("table", P)]
+
+
+class RkEntries(C.Structure):
+    _fields_ = [("n", I64), ("i", P), ("j", P), ("type", P), ("isub", P), ("jsub", P), ("dn", P), ("fn", P),
+                ("ft", P), ("mom", P), ("damp", P), ("bond", P)]
+
+
+class RkInterfaces(C.Structure):
+    _fields_ = [("n", I64), ("i", P), ("j", P), ("dn0", P), ("params", P), ("is_inner", P)]
+
+
+class RkControl(C.Structure):
+    _fields_ = [("type", C.c_int32), ("body", C.c_int32), ("value", C.c_double), ("vec", C.c_double * 3)]
+
+
+class RkServo(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("icontr", C.c_int32), ("walls", C.c_int32 * 6), ("pressure", C.c_double)]
+
+
+class RkStepReport(C.Structure):
+    _fields_ = [("steps_done", I64), ("nl_updates", I64), ("n_entries", I64), ("n_active", I64),
+                ("n_broken", I64), ("t", C.c_double)]
+
+
+class RkStats(C.Structure):
+    _fields_ = [("e_trans", C.c_double), ("e_rot", C.c_double), ("n_entries", I64), ("n_active", I64),
+                ("n_broken", I64), ("nl_updates", I64), ("coordination", C.c_double)]
+
+
+# every symbol the header declares, with its ctypes signature
+SIGNATURES = {
+    "rk_abi_version": (C.c_int, []),
+    "rk_create": (C.c_int, [C.POINTER(P), C.POINTER(RkConfig)]),
+    "rk_destroy": (None, [P]),
+    "rk_last_error": (C.c_char_p, [P]),
+    "rk_upload_shapes": (C.c_int, [P, C.POINTER(RkShapes)]),
+    "rk_upload_bodies": (C.c_int, [P, C.POINTER(RkBodies)]),
+    "rk_set_params": (C.c_int, [P, C.POINTER(RkParams)]),
+    "rk_upload_entries": (C.c_int, [P, C.POINTER(RkEntries)]),
+    "rk_upload_interfaces": (C.c_int, [P, C.POINTER(RkInterfaces)]),
+    "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
+    "rk_set_record_geometry": (C.c_int, [P, C.c_int]),
+    "rk_accelerations": (C.c_int, [P]),
+    "rk_update_nl": (C.c_int, [P]),
+    "rk_step": (C.c_int, [P, I64, C.POINTER(RkStepReport)]),
+    "rk_synchronize": (C.c_int, [P]),
+    "rk_num_bodies": (I64, [P]),
+    "rk_num_entries": (I64, [P]),
+    "rk_num_interfaces": (I64, [P]),
+    "rk_download_bodies": (C.c_int, [P] * 9),
+    "rk_download_entries": (C.c_int, [P] * 16),
+    "rk_download_interfaces": (C.c_int, [P] * 4),
+    "rk_get_stats": (C.c_int, [P, C.POINTER(RkStats)]),
+    "rk_last_step_timing": (C.c_int, [P, DP, C.POINTER(I64)]),
+    "rk_upload_kinematics": (C.c_int, [P] * 7),
+    "rk_set_profiling": (C.c_int, [P, C.c_int]),
+    "rk_get_profile": (C.c_int, [P, P, P]),
+}
+
+_lib = None
+
+
+def load(path=LIBPATH):
+    """Load librk_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("librk_gpu.so is not built (run __graft_entry__.build()): " + path)
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class RkError(RuntimeError):
+    pass
+
+
+class GpuScene:
+    """One rk_ctx; arrays passed in are numpy, outputs are numpy."""
+
+    def __init__(self, device=0, form=RK_FORM_FP64, entry_capacity=0):
+        self.L = load()
+        self.h = P()
+        cfg = RkConfig(device, form, entry_capacity)
+        rc = self.L.rk_create(C.byref(self.h), C.byref(cfg))
+        if rc != RK_OK:
+            raise RkError("rk_create failed: %s" % ERRORS.get(rc, rc))
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self.L.rk_destroy(self.h)
+            self.h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc != RK_OK:
+            raise RkError("%s: %s: %s" % (what, ERRORS.get(rc, rc), self.L.rk_last_error(self.h).decode()))
+
+    # ---- uploads
+    def upload_shapes(self, sh):
+        a = {k: _c(sh[k], np.int32) for k in ["vert_ofs", "edge_ofs", "edges", "face_ofs", "face_vofs", "face_verts"]}
+        a.update({k: _c(sh[k], np.float64) for k in ["vertices", "radius", "obb"]})
+        s = RkShapes(len(a["radius"]), *[_p(a[k]) for k in ["vert_ofs", "vertices", "edge_ofs", "edges", "face_ofs",
+                                                            "face_vofs", "face_verts", "radius", "obb"]])
+        self._chk(self.L.rk_upload_shapes(self.h, C.byref(s)), "rk_upload_shapes")
+
+    def upload_bodies(self, b, n_driven):
+        f = {k: _c(b[k], np.float64) for k in ["pos", "vel", "acc", "Q", "vrot", "arot", "homothety", "mass",
+                                                "inertia"]}
+        i = {k: _c(b[k], np.int32) for k in ["shape", "group", "cluster"]}
+        n = len(f["mass"])
+        s = RkBodies(n, n_driven, *[_p(f[k]) for k in ["pos", "vel", "acc", "Q", "vrot", "arot", "homothety",
+                                                       "mass", "inertia"]], *[_p(i[k]) for k in ["shape", "group",
+                                                                                                  "cluster"]])
+        self._chk(self.L.rk_upload_bodies(self.h, C.byref(s)), "rk_upload_bodies")
+
+    def set_params(self, t, dt, gravity, DVerlet, dVerlet, interVerlet, interVerletC, law, ngroup, table,
+                   numerical_damping=0.0, params_in_interfaces=0, dynamic_update_nl=0, disp_update_nl=1.0,
+                   angle_update_nl=1.0):
+        tab = _c(table, np.float64)
+        self._keep = [tab]
+        p = RkParams(t, dt, (C.c_double * 3)(*gravity), DVerlet, dVerlet, interVerlet, interVerletC,
+                     numerical_damping, law, params_in_interfaces, dynamic_update_nl, disp_update_nl,
+                     angle_update_nl, ngroup, _p(tab))
+        self._chk(self.L.rk_set_params(self.h, C.byref(p)), "rk_set_params")
+
+    def upload_entries(self, e):
+        ii = {k: _c(e[k], np.int32) for k in ["i", "j", "type", "isub", "jsub", "bond"]}
+        ff = {k: _c(e[k], np.float64) for k in ["dn", "fn", "ft", "mom", "damp"]}
+        s = RkEntries(len(ii["i"]), *[_p(ii[k]) for k in ["i", "j", "type", "isub", "jsub"]],
+                      *[_p(ff[k]) for k in ["dn", "fn", "ft", "mom", "damp"]], _p(ii["bond"]))
+        self._chk(self.L.rk_upload_entries(self.h, C.byref(s)), "rk_upload_entries")
+
+    def upload_interfaces(self, i, j, dn0, params, is_inner):
+        a = [_c(i, np.int32), _c(j, np.int32), _c(dn0, np.float64), _c(params, np.float64), _c(is_inner, np.int32)]
+        s = RkInterfaces(len(a[0]), *[_p(x) for x in a])
+        self._chk(self.L.rk_upload_interfaces(self.h, C.byref(s)), "rk_upload_interfaces")
+
+    def set_controls(self, types, bodies, values, vecs, servo=None):
+        n = len(types)
+        arr = (RkControl * max(n, 1))()
+        for k in range(n):
+            arr[k].type = int(types[k])
+            arr[k].body = int(bodies[k])
+            arr[k].value = float(values[k])
+            for d in range(3):
+                arr[k].vec[d] = float(vecs[k][d])
+        sv = RkServo()
+        if servo is not None:
+            sv.kind = int(servo["kind"])
+            sv.icontr = int(servo["icontr"])
+            for d in range(6):
+                sv.walls[d] = int(servo["walls"][d])
+            sv.pressure = float(servo["pressure"])
+        self._chk(self.L.rk_set_controls(self.h, arr, n, C.byref(sv)), "rk_set_controls")
+
+    def set_record_geometry(self, on=True):
+        self._chk(self.L.rk_set_record_geometry(self.h, 1 if on else 0), "rk_set_record_geometry")
+
+    # ---- running
+    def accelerations(self):
+        self._chk(self.L.rk_accelerations(self.h), "rk_accelerations")
+
+    def update_nl(self):
+        self._chk(self.L.rk_update_nl(self.h), "rk_update_nl")
+
+    def step(self, n=1):
+        r = RkStepReport()
+        self._chk(self.L.rk_step(self.h, int(n), C.byref(r)), "rk_step")
+        return {k: getattr(r, k) for k, _ in RkStepReport._fields_}
+
+    def synchronize(self):
+        self._chk(self.L.rk_synchronize(self.h), "rk_synchronize")
+
+    def last_step_timing(self):
+        ms = C.c_double()
+        k = I64()
+        self._chk(self.L.rk_last_step_timing(self.h, C.byref(ms), C.byref(k)), "rk_last_step_timing")
+        return ms.value, k.value
+
+    def upload_kinematics(self, pos=None, vel=None, acc=None, Q=None, vrot=None, arot=None):
+        """Host arrays must stay alive until the next synchronising call."""
+        self._chk(self.L.rk_upload_kinematics(self.h, _p(pos), _p(vel), _p(acc), _p(Q), _p(vrot), _p(arot)),
+                  "rk_upload_kinematics")
+
+    def set_profiling(self, on=True):
+        self._chk(self.L.rk_set_profiling(self.h, 1 if on else 0), "rk_set_profiling")
+
+    PHASES = ["controls", "drift", "glob_vertices", "narrow_force", "gather_accel", "breakage", "nl_rebuild", "guard"]
+
+    def profile(self):
+        ms = np.zeros(8)
+        n = np.zeros(8, np.int64)
+        self._chk(self.L.rk_get_profile(self.h, _p(ms), _p(n)), "rk_get_profile")
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PHASES)}
+
+    # ---- downloads
+    @property
+    def n(self):
+        return self.L.rk_num_bodies(self.h)
+
+    @property
+    def n_entries(self):
+        return self.L.rk_num_entries(self.h)
+
+    def bodies(self):
+        n = self.n
+        out = {k: np.zeros((n, 3)) for k in ["pos", "vel", "acc", "vrot", "arot", "force", "moment"]}
+        out["Q"] = np.zeros((n, 4))
+        self._chk(self.L.rk_download_bodies(self.h, *[_p(out[k]) for k in ["pos", "vel", "acc", "Q", "vrot", "arot",
+                                                                           "force", "moment"]]),
+                  "rk_download_bodies")
+        return out
+
+    def entries(self, geometry=False):
+        n = self.n_entries
+        o = {k: np.zeros(n, np.int32) for k in ["i", "j", "type", "isub", "jsub", "bond"]}
+        o.update({"dn": np.zeros(n), "fn": np.zeros(n), "damp": np.zeros(n), "ft": np.zeros((n, 3)),
+                  "mom": np.zeros((n, 3)), "active": np.zeros(n, np.uint8)})
+        g = {k: (np.zeros((n, 3)) if geometry else None) for k in ["n", "pos", "vel"]}
+        if n:
+            self._chk(self.L.rk_download_entries(
+                self.h, _p(o["i"]), _p(o["j"]), _p(o["type"]), _p(o["isub"]), _p(o["jsub"]), _p(o["dn"]),
+                _p(o["fn"]), _p(o["ft"]), _p(o["mom"]), _p(o["damp"]), _p(o["bond"]), _p(o["active"]),
+                _p(g["n"]), _p(g["pos"]), _p(g["vel"])), "rk_download_entries")
+        if geometry:
+            o.update(g)
+        o["active"] = o["active"].astype(bool)
+        return o
+
+    def interfaces(self):
+        n = self.L.rk_num_interfaces(self.h)
+        i = np.zeros(n, np.int32)
+        j = np.zeros(n, np.int32)
+        b = np.zeros(n, np.uint8)
+        if n:
+            self._chk(self.L.rk_download_interfaces(self.h, _p(i), _p(j), _p(b)), "rk_download_interfaces")
+        return i, j, b.astype(bool)
+
+    def stats(self):
+        s = RkStats()
+        self._chk(self.L.rk_get_stats(self.h, C.byref(s)), "rk_get_stats")
+        return {k: getattr(s, k) for k, _ in RkStats._fields_}

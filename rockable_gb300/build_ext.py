@@ -1,0 +1,73 @@
+"""Build of the in-tree native libraries (librk_gpu.so).
+
+The CUDA sources are compiled for sm_103a only.  The FP64 form is compiled
+with --fmad=false: its results must be bit-identical to the reference CPU
+arithmetic.  Objects are compiled in parallel; the shared library lands in
+rockable_gb300/_lib/.
+"""
+import os
+import platform
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "_lib")
+BUILD = os.path.join(HERE, "_build", platform.machine())
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+# translation unit -> extra flags
+UNITS = {
+    "rk_prims.cu": [],
+    "rk_step.cu": ["--fmad=false"],
+    "rk_nl.cu": ["--fmad=false"],
+    "rk_api.cu": ["--fmad=false"],
+}
+
+
+def nvcc():
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found")
+    return cand
+
+
+def _compile(src, flags):
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    srcp = os.path.join(CSRC, src)
+    deps = [srcp] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    deps.append(os.path.join(HERE, "..", "include", "rk_gpu.h"))
+    if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps if os.path.exists(d)):
+        return obj
+    cmd = [nvcc(), GENCODE, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-c", srcp, "-o", obj] + flags
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+    return obj
+
+
+def build(verbose=False):
+    """Compile every CUDA translation unit and link librk_gpu.so; returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(lambda kv: _compile(*kv), UNITS.items()))
+    out = os.path.join(LIBDIR, "librk_gpu.so")
+    stamp = os.path.join(BUILD, "librk_gpu.so.stamp")
+    if (not os.path.exists(out) or not os.path.exists(stamp)
+            or any(os.path.getmtime(o) > os.path.getmtime(stamp) for o in objs)):
+        cmd = [nvcc(), GENCODE, "-shared", "-o", out] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+        open(stamp, "w").write(out + "\n")
+    if verbose:
+        print("built", out)
+    return out
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    sys.exit(0)

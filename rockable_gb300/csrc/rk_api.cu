@@ -1,0 +1,807 @@
+// rk_api.cu -- the C ABI of librk_gpu.so: context, uploads, the step loop
+// (Rockable::integrate bookkeeping around rk::velocity-Verlet kernels) and
+// downloads.  See include/rk_gpu.h for the reference seams each call replaces.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "rk_ctx.cuh"
+
+using namespace rk;
+
+struct rk_ctx {
+  Ctx c;
+};
+
+namespace {
+
+#define CK(x)                                                            \
+  do {                                                                   \
+    cudaError_t e_ = (x);                                                \
+    if (e_ != cudaSuccess) {                                             \
+      c.err = std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #x; \
+      return RK_ERR_CUDA;                                                \
+    }                                                                    \
+  } while (0)
+
+template <typename T>
+int dalloc(Ctx& c, T*& p, int64_t n) {
+  if (p) cudaFree(p);
+  p = nullptr;
+  CK(cudaMalloc(&p, (size_t)std::max<int64_t>(n, 1) * sizeof(T)));
+  return 0;
+}
+template <typename T>
+int dupload(Ctx& c, T*& p, const T* h, int64_t n) {
+  int rc = dalloc(c, p, n);
+  if (rc) return rc;
+  if (n > 0 && h) CK(cudaMemcpyAsync(p, h, (size_t)n * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+  else if (n > 0) CK(cudaMemsetAsync(p, 0, (size_t)n * sizeof(T), c.stream));
+  return 0;
+}
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+int fail(Ctx& c, int code, const std::string& msg) {
+  c.err = msg;
+  return code;
+}
+
+static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+namespace rk {
+
+void bind_entries(Ctx& c) {
+  EntryBuf& b = c.eb[c.cur];
+  Scene& s = c.s;
+  s.ei = b.ei; s.ej = b.ej; s.etsub = b.etsub; s.ekey = b.ekey;
+  s.dn = b.dn; s.fn = b.fn; s.ft = b.ft; s.mom = b.mom; s.damp = b.damp; s.bond = b.bond;
+  s.gn = b.gn; s.gpos = b.gpos; s.gvel = b.gvel;
+}
+
+static void free_entrybuf(EntryBuf& b) {
+  dfree(b.ei); dfree(b.ej); dfree(b.etsub); dfree(b.ekey); dfree(b.dn); dfree(b.fn); dfree(b.ft); dfree(b.mom);
+  dfree(b.damp); dfree(b.bond); dfree(b.gn); dfree(b.gpos); dfree(b.gvel);
+  b.cap = 0;
+}
+
+// Grow entry buffer `which` (and the single-buffered per-step arrays) to
+// hold n entries; contents of a grown buffer are not preserved.
+int ensure_entry_capacity(Ctx& c, int which, int64_t n) {
+  EntryBuf& b = c.eb[which];
+  int rc;
+  if (b.cap < n || b.cap == 0) {
+    int64_t cap = std::max<int64_t>(n + n / 2, 1024);
+    free_entrybuf(b);
+    if ((rc = dalloc(c, b.ei, cap)) || (rc = dalloc(c, b.ej, cap)) || (rc = dalloc(c, b.etsub, cap)) ||
+        (rc = dalloc(c, b.ekey, cap)) || (rc = dalloc(c, b.dn, cap)) || (rc = dalloc(c, b.fn, cap)) ||
+        (rc = dalloc(c, b.ft, 3 * cap)) || (rc = dalloc(c, b.mom, 3 * cap)) || (rc = dalloc(c, b.damp, cap)) ||
+        (rc = dalloc(c, b.bond, cap)) || (rc = dalloc(c, b.gn, 3 * cap)) || (rc = dalloc(c, b.gpos, 3 * cap)) ||
+        (rc = dalloc(c, b.gvel, 3 * cap)))
+      return rc;
+    b.cap = cap;
+  }
+  if (c.contrib_cap < n || c.contrib_cap == 0) {
+    int64_t cap = std::max<int64_t>(n + n / 2, 1024);
+    Scene& s = c.s;
+    if ((rc = dalloc(c, s.act, cap)) || (rc = dalloc(c, s.cf, 3 * cap)) || (rc = dalloc(c, s.cmi, 3 * cap)) ||
+        (rc = dalloc(c, s.cmj, 3 * cap)) || (rc = dalloc(c, s.jlist, cap)))
+      return rc;
+    c.contrib_cap = cap;
+  }
+  return 0;
+}
+
+}  // namespace rk
+
+namespace {
+
+__global__ void k_upload_keys(Scene s, int64_t ne, const int* t, const int* isub, const int* jsub, int* bad) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  int i = s.ei[e], j = s.ej[e];
+  if (i < 0 || j < 0 || i >= s.n || j >= s.n || t[e] < 0 || t[e] > 3 || isub[e] < 0 || jsub[e] < 0 ||
+      isub[e] >= kMaxSub || jsub[e] >= kMaxSub) {
+    atomicExch(bad, 1);
+    return;
+  }
+  s.etsub[e] = pack_tsub(t[e], isub[e], jsub[e]);
+  s.ekey[e] = entry_key(i, j, t[e], isub[e], jsub[e]);
+}
+
+__global__ void k_check_sorted(const uint64_t* k, int64_t n, int* bad) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e + 1 >= n) return;
+  if (!(k[e] < k[e + 1])) atomicExch(bad, 2);
+}
+
+__global__ void k_iofs2(const uint64_t* key, int64_t ne, int64_t nb, int64_t* iofs) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b > nb) return;
+  int64_t lo = 0, hi = ne;
+  uint64_t x = (uint64_t)b << 43;
+  while (lo < hi) {
+    int64_t m = (lo + hi) >> 1;
+    if (key[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  iofs[b] = lo;
+}
+__global__ void k_jkeys2(const int* ej, int64_t ne, uint64_t* jk) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  jk[e] = ((uint64_t)ej[e] << 27) | (uint64_t)e;
+}
+__global__ void k_jlist2(const uint64_t* jk, int64_t ne, int* jlist) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  jlist[e] = (int)(jk[e] & ((1ull << 27) - 1));
+}
+__global__ void k_jofs2(const uint64_t* jk, int64_t ne, int64_t nb, int64_t* jofs) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b > nb) return;
+  int64_t lo = 0, hi = ne;
+  uint64_t x = (uint64_t)b << 27;
+  while (lo < hi) {
+    int64_t m = (lo + hi) >> 1;
+    if (jk[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  jofs[b] = lo;
+}
+
+// i-side offsets and j-side list of the current entries (after an upload).
+int build_index(Ctx& c) {
+  Scene& s = c.s;
+  NLWork& w = c.w;
+  const int64_t ne = s.ne, N = s.n;
+  if (w.fin_cap < ne + 1) {
+    int64_t cap = ne + ne / 2 + 1024;
+    dfree(w.jkeys);
+    dfree(w.jtmp);
+    dfree(w.fkey);
+    dfree(w.fsrc);
+    int rc;
+    if ((rc = dalloc(c, w.jkeys, cap)) || (rc = dalloc(c, w.jtmp, cap)) || (rc = dalloc(c, w.fkey, cap)) ||
+        (rc = dalloc(c, w.fsrc, cap)))
+      return rc;
+    w.fin_cap = cap;
+  }
+  int64_t need = (int64_t)sort_temp_bytes(ne);
+  if (need > w.tmp_bytes) {
+    dfree(w.tmp);
+    int64_t nb = need + need / 2;
+    CK(cudaMalloc(&w.tmp, (size_t)nb));
+    w.tmp_bytes = nb;
+  }
+  k_iofs2<<<nblk(N + 1, 256), 256, 0, c.stream>>>(s.ekey, ne, N, s.iofs);
+  if (ne > 0) {
+    k_jkeys2<<<nblk(ne, 256), 256, 0, c.stream>>>(s.ej, ne, w.jkeys);
+    radix_sort_u64(w.jkeys, w.jtmp, ne, 27, 51, w.tmp, c.stream);
+    k_jlist2<<<nblk(ne, 256), 256, 0, c.stream>>>(w.jkeys, ne, s.jlist);
+  }
+  k_jofs2<<<nblk(N + 1, 256), 256, 0, c.stream>>>(w.jkeys, ne, N, s.jofs);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int read_flags(Ctx& c) {
+  CK(cudaMemcpyAsync(c.h_flags, c.s.flags, FLAG_COUNT * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rk_abi_version(void) { return RK_ABI_VERSION; }
+
+int rk_create(rk_ctx** out, const rk_config* cfg) {
+  if (!out) return RK_ERR_ARG;
+  *out = nullptr;
+  rk_ctx* x = new (std::nothrow) rk_ctx();
+  if (!x) return RK_ERR_CAPACITY;
+  Ctx& c = x->c;
+  c.device = cfg ? cfg->device : 0;
+  c.form = cfg ? cfg->form : RK_FORM_FP64;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || c.device < 0 || c.device >= ndev) {
+    delete x;
+    return RK_ERR_CUDA;
+  }
+  if (c.form != RK_FORM_FP64) {
+    delete x;
+    return RK_ERR_UNSUPPORTED;
+  }
+  if (cudaSetDevice(c.device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c.ev0) != cudaSuccess || cudaEventCreate(&c.ev1) != cudaSuccess ||
+      cudaMallocHost(&c.h_flags, FLAG_COUNT * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&c.s.flags, FLAG_COUNT * sizeof(unsigned long long)) != cudaSuccess) {
+    delete x;
+    return RK_ERR_CUDA;
+  }
+  cudaMemsetAsync(c.s.flags, 0, FLAG_COUNT * sizeof(unsigned long long), c.stream);
+  c.s.n = 0;
+  c.s.ne = 0;
+  c.s.nif = 0;
+  int64_t cap0 = cfg && cfg->entry_capacity > 0 ? cfg->entry_capacity : 1024;
+  if (ensure_entry_capacity(c, 0, cap0) || ensure_entry_capacity(c, 1, cap0)) {
+    rk_destroy(x);
+    return RK_ERR_CUDA;
+  }
+  bind_entries(c);
+  // empty interface table
+  dupload(c, c.s.if_i, (const int*)nullptr, 0);
+  *out = x;
+  return RK_OK;
+}
+
+void rk_destroy(rk_ctx* x) {
+  if (!x) return;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  Scene& s = c.s;
+  dfree(s.vert_ofs); dfree(s.edge_ofs); dfree(s.edges); dfree(s.face_ofs); dfree(s.face_vofs); dfree(s.face_verts);
+  dfree(s.svert); dfree(s.sradius); dfree(s.sobb);
+  dfree(s.pos); dfree(s.vel); dfree(s.acc); dfree(s.Q); dfree(s.vrot); dfree(s.arot); dfree(s.force); dfree(s.moment);
+  dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.shape); dfree(s.group); dfree(s.cluster);
+  dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.gv); dfree(s.bobb); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
+  dfree(s.table); dfree(s.controls);
+  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jlist);
+  dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
+  dfree(s.if_break); dfree(s.if_ofs); dfree(s.flags);
+  free_entrybuf(c.eb[0]);
+  free_entrybuf(c.eb[1]);
+  NLWork& w = c.w;
+  dfree(w.pairs); dfree(w.hp); dfree(w.hp_tmp); dfree(w.hp_cnt); dfree(w.hp_mask); dfree(w.cand); dfree(w.cand_src);
+  dfree(w.flag); dfree(w.stale); dfree(w.stale_src); dfree(w.fkey); dfree(w.fsrc); dfree(w.jkeys); dfree(w.jtmp);
+  dfree(w.tmp); dfree(w.counter);
+  dfree(c.d_ke);
+  for (int k = 0; k < 2 * RK_NPHASE; k++)
+    if (c.pev[k]) cudaEventDestroy(c.pev[k]);
+  if (c.h_flags) cudaFreeHost(c.h_flags);
+  if (c.ev0) cudaEventDestroy(c.ev0);
+  if (c.ev1) cudaEventDestroy(c.ev1);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  delete x;
+}
+
+const char* rk_last_error(const rk_ctx* x) { return x ? x->c.err.c_str() : "null context"; }
+
+int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
+  if (!x || !sh || sh->nshapes <= 0) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  const int ns = sh->nshapes;
+  const int nv = sh->vert_ofs[ns], ne = sh->edge_ofs[ns], nf = sh->face_ofs[ns], nfv = sh->face_vofs[nf];
+  c.shape_nv.assign(ns, 0);
+  for (int k = 0; k < ns; k++) {
+    int v = sh->vert_ofs[k + 1] - sh->vert_ofs[k];
+    int e = sh->edge_ofs[k + 1] - sh->edge_ofs[k];
+    int f = sh->face_ofs[k + 1] - sh->face_ofs[k];
+    if (v <= 0 || v > 64) return fail(c, RK_ERR_CAPACITY, "a shape has no vertex or more than 64 vertices");
+    if (e >= kMaxSub || f >= kMaxSub) return fail(c, RK_ERR_CAPACITY, "a shape has more than 1023 edges or faces");
+    c.shape_nv[k] = v;
+  }
+  for (int f = 0; f < nf; f++)
+    if (sh->face_vofs[f + 1] - sh->face_vofs[f] < 3) return fail(c, RK_ERR_ARG, "a face has fewer than 3 vertices");
+  Scene& s = c.s;
+  int rc;
+  if ((rc = dupload(c, s.vert_ofs, sh->vert_ofs, ns + 1)) || (rc = dupload(c, s.edge_ofs, sh->edge_ofs, ns + 1)) ||
+      (rc = dupload(c, s.edges, sh->edges, 2 * (int64_t)ne)) || (rc = dupload(c, s.face_ofs, sh->face_ofs, ns + 1)) ||
+      (rc = dupload(c, s.face_vofs, sh->face_vofs, nf + 1)) ||
+      (rc = dupload(c, s.face_verts, sh->face_verts, nfv)) || (rc = dupload(c, s.svert, sh->vertices, 3 * (int64_t)nv)) ||
+      (rc = dupload(c, s.sradius, sh->radius, ns)) || (rc = dupload(c, s.sobb, sh->obb, 15 * (int64_t)ns)))
+    return rc;
+  s.nshapes = ns;
+  c.shape_radius.assign(sh->radius, sh->radius + ns);
+  c.have_shapes = true;
+  return RK_OK;
+}
+
+int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
+  if (!x || !b || b->n <= 0 || b->n_driven < 0 || b->n_driven > b->n) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_shapes) return fail(c, RK_ERR_STATE, "upload the shapes before the bodies");
+  if (b->n >= kMaxBody) return fail(c, RK_ERR_CAPACITY, "more than 2^21 - 1 bodies");
+  const int64_t n = b->n;
+  std::vector<int64_t> gv_ofs(n + 1, 0);
+  std::vector<double> rad(n);
+  for (int64_t i = 0; i < n; i++) {
+    int sh = b->shape[i];
+    if (sh < 0 || sh >= c.s.nshapes) return fail(c, RK_ERR_ARG, "body shape index out of range");
+    gv_ofs[i + 1] = gv_ofs[i] + c.shape_nv[sh];
+    rad[i] = b->homothety[i] * c.shape_radius[sh];  // Particle::MinkowskiRadius (Particle.cpp:71)
+  }
+  const int64_t nv = gv_ofs[n];
+  std::vector<int> gv_body(nv);
+  for (int64_t i = 0; i < n; i++)
+    for (int64_t k = gv_ofs[i]; k < gv_ofs[i + 1]; k++) gv_body[k] = (int)i;
+  Scene& s = c.s;
+  int rc;
+  if ((rc = dupload(c, s.pos, b->pos, 3 * n)) || (rc = dupload(c, s.vel, b->vel, 3 * n)) ||
+      (rc = dupload(c, s.acc, b->acc, 3 * n)) || (rc = dupload(c, s.Q, b->Q, 4 * n)) ||
+      (rc = dupload(c, s.vrot, b->vrot, 3 * n)) || (rc = dupload(c, s.arot, b->arot, 3 * n)) ||
+      (rc = dupload(c, s.force, (const double*)nullptr, 3 * n)) ||
+      (rc = dupload(c, s.moment, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.hom, b->homothety, n)) ||
+      (rc = dupload(c, s.mass, b->mass, n)) || (rc = dupload(c, s.inertia, b->inertia, 3 * n)) ||
+      (rc = dupload(c, s.rad, rad.data(), n)) || (rc = dupload(c, s.shape, b->shape, n)) ||
+      (rc = dupload(c, s.group, b->group, n)) || (rc = dupload(c, s.cluster, b->cluster, n)) ||
+      (rc = dupload(c, s.gv_ofs, gv_ofs.data(), n + 1)) || (rc = dupload(c, s.gv_body, gv_body.data(), nv)) ||
+      (rc = dupload(c, s.gv, (const double*)nullptr, 3 * nv)) ||
+      (rc = dupload(c, s.bobb, (const double*)nullptr, 15 * n)) ||
+      (rc = dupload(c, s.baabb, (const float*)nullptr, 6 * n)) ||
+      (rc = dupload(c, s.dpos, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.dq, (const double*)nullptr, 4 * n)) ||
+      (rc = dupload(c, s.iofs, (const int64_t*)nullptr, n + 1)) ||
+      (rc = dupload(c, s.jofs, (const int64_t*)nullptr, n + 1)) ||
+      (rc = dupload(c, s.if_ofs, (const int64_t*)nullptr, n + 1)))
+    return rc;
+  // deltaQ starts as the identity quaternion
+  std::vector<double> dq(4 * n, 0.0);
+  for (int64_t i = 0; i < n; i++) dq[4 * i] = 1.0;
+  CK(cudaMemcpyAsync(s.dq, dq.data(), dq.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  s.n = n;
+  s.n_driven = b->n_driven;
+  s.nvert = nv;
+  s.ne = 0;
+  s.nif = 0;
+  c.have_bodies = true;
+  return RK_OK;
+}
+
+int rk_set_params(rk_ctx* x, const rk_params* p) {
+  if (!x || !p || p->ngroup <= 0 || !p->table || !(p->dt > 0.0)) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (p->law < 0 || p->law > 2) return fail(c, RK_ERR_UNSUPPORTED, "unknown force law");
+  const int G = p->ngroup;
+  std::vector<LawParams> tab((size_t)G * G);
+  const double kPi = 3.14159265358979323846;
+  for (int g1 = 0; g1 < G; g1++)
+    for (int g2 = 0; g2 < G; g2++) {
+      LawParams& L = tab[(size_t)g1 * G + g2];
+      for (int k = 0; k < 24; k++) L.p[k] = 0.0;
+      for (int k = 0; k < RK_NPARAM; k++) L.p[k] = p->table[((size_t)k * G + g1) * G + g2];
+      // damping rate of Rockable.cpp:1368-1376, evaluated with the host libm
+      double en2 = L.p[RK_P_EN2];
+      if (en2 > 0.0 && en2 < 1.0) {
+        double logen = 0.5 * log(en2);
+        L.p[22] = -logen / sqrt(logen * logen + kPi * kPi);
+      } else if (en2 <= 0.0) {
+        L.p[22] = 1.0;
+      } else {
+        L.p[22] = 0.0;
+      }
+    }
+  Scene& s = c.s;
+  int rc;
+  if ((rc = dupload(c, s.table, tab.data(), (int64_t)tab.size()))) return rc;
+  s.ngroup = G;
+  s.law = p->law;
+  s.params_in_interfaces = p->params_in_interfaces;
+  s.dt = p->dt;
+  s.dt_2 = 0.5 * p->dt;
+  s.dt2_2 = s.dt_2 * p->dt;  // Rockable.cpp:2559-2560
+  for (int k = 0; k < 3; k++) s.gravity[k] = p->gravity[k];
+  s.DVerlet = p->DVerlet;
+  s.dVerlet = p->dVerlet;
+  s.num_damp = p->numerical_damping;
+  s.dynamic_nl = p->dynamic_update_nl;
+  s.disp_update = p->disp_update_nl;
+  s.angle_update = p->angle_update_nl;
+  c.t = p->t;
+  c.interVerlet = p->interVerlet;
+  c.interVerletC = p->interVerletC;
+  c.have_params = true;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_upload_entries(rk_ctx* x, const rk_entries* e) {
+  if (!x || !e || e->n < 0) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies before the entries");
+  const int64_t n = e->n;
+  int rc;
+  if ((rc = ensure_entry_capacity(c, c.cur, n))) return rc;
+  bind_entries(c);
+  Scene& s = c.s;
+  s.ne = n;
+  if (n > 0) {
+    int* d_t = nullptr;
+    int* d_is = nullptr;
+    int* d_js = nullptr;
+    int* d_bad = nullptr;
+    if ((rc = dupload(c, d_t, e->type, n)) || (rc = dupload(c, d_is, e->isub, n)) ||
+        (rc = dupload(c, d_js, e->jsub, n)) || (rc = dupload(c, d_bad, (const int*)nullptr, 1)))
+      return rc;
+    CK(cudaMemcpyAsync(s.ei, e->i, n * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.ej, e->j, n * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.dn, e->dn, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.fn, e->fn, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.ft, e->ft, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.mom, e->mom, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.damp, e->damp, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    if (e->bond) CK(cudaMemcpyAsync(s.bond, e->bond, n * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    else CK(cudaMemsetAsync(s.bond, 0xff, n * sizeof(int), c.stream));
+    CK(cudaMemsetAsync(s.gn, 0, 3 * n * sizeof(double), c.stream));
+    CK(cudaMemsetAsync(s.gpos, 0, 3 * n * sizeof(double), c.stream));
+    CK(cudaMemsetAsync(s.gvel, 0, 3 * n * sizeof(double), c.stream));
+    k_upload_keys<<<nblk(n, 256), 256, 0, c.stream>>>(s, n, d_t, d_is, d_js, d_bad);
+    k_check_sorted<<<nblk(n, 256), 256, 0, c.stream>>>(s.ekey, n, d_bad);
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    dfree(d_t); dfree(d_is); dfree(d_js); dfree(d_bad);
+    if (bad == 1) { s.ne = 0; return fail(c, RK_ERR_ARG, "entry index out of range"); }
+    if (bad == 2) { s.ne = 0; return fail(c, RK_ERR_ARG, "entries must be sorted by key and unique"); }
+  }
+  return build_index(c);
+}
+
+int rk_upload_interfaces(rk_ctx* x, const rk_interfaces* f) {
+  if (!x || !f || f->n < 0) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies before the interfaces");
+  const int64_t n = f->n, N = c.s.n;
+  std::vector<int64_t> ofs(N + 1, 0);
+  for (int64_t k = 0; k < n; k++) {
+    if (f->i[k] < 0 || f->i[k] >= N || f->j[k] < 0 || f->j[k] >= N) return fail(c, RK_ERR_ARG, "interface body out of range");
+    if (k > 0 && (f->i[k] < f->i[k - 1] || (f->i[k] == f->i[k - 1] && f->j[k] <= f->j[k - 1])))
+      return fail(c, RK_ERR_ARG, "interfaces must be sorted by (i, j) and unique");
+    ofs[f->i[k] + 1]++;
+  }
+  for (int64_t b = 0; b < N; b++) ofs[b + 1] += ofs[b];
+  Scene& s = c.s;
+  int rc;
+  if ((rc = dupload(c, s.if_i, f->i, n)) || (rc = dupload(c, s.if_j, f->j, n)) ||
+      (rc = dupload(c, s.if_dn0, f->dn0, n)) || (rc = dupload(c, s.if_par, f->params, 8 * n)) ||
+      (rc = dupload(c, s.if_inner, f->is_inner, n)) || (rc = dupload(c, s.if_broken, (const uint8_t*)nullptr, n)) ||
+      (rc = dupload(c, s.if_break, (const uint8_t*)nullptr, n)) || (rc = dupload(c, s.if_ofs, ofs.data(), N + 1)))
+    return rc;
+  s.nif = n;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_set_controls(rk_ctx* x, const rk_control* cs, int32_t n, const rk_servo* servo) {
+  if (!x || n < 0 || (n > 0 && !cs)) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies before the controls");
+  std::vector<Control> v(n);
+  for (int k = 0; k < n; k++) {
+    if (cs[k].body < 0 || cs[k].body >= c.s.n) return fail(c, RK_ERR_ARG, "control body out of range");
+    v[k].type = cs[k].type;
+    v[k].body = cs[k].body;
+    v[k].value = cs[k].value;
+    for (int d = 0; d < 3; d++) v[k].vec[d] = cs[k].vec[d];
+  }
+  Scene& s = c.s;
+  int rc;
+  if ((rc = dupload(c, s.controls, v.data(), n))) return rc;
+  s.ncontrols = n;
+  s.servo_kind = 0;
+  if (servo && servo->kind == 1) {
+    if (servo->icontr < 0 || servo->icontr + 5 >= n) return fail(c, RK_ERR_ARG, "servo control index out of range");
+    for (int k = 0; k < 6; k++) {
+      if (servo->walls[k] < 0 || servo->walls[k] >= c.s.n) return fail(c, RK_ERR_ARG, "servo wall out of range");
+      s.servo_walls[k] = servo->walls[k];
+    }
+    s.servo_kind = 1;
+    s.servo_icontr = servo->icontr;
+    s.servo_p = servo->pressure;
+  } else if (servo && servo->kind != 0) {
+    return fail(c, RK_ERR_UNSUPPORTED, "only the tritriIsostaticCompression servo is supported");
+  }
+  c.controls = v;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_set_record_geometry(rk_ctx* x, int on) {
+  if (!x) return RK_ERR_ARG;
+  x->c.s.record_geom = on ? 1 : 0;
+  return RK_OK;
+}
+
+static int ready(Ctx& c) {
+  if (!c.have_shapes || !c.have_bodies || !c.have_params)
+    return fail(c, RK_ERR_STATE, "shapes, bodies and parameters must be uploaded first");
+  return 0;
+}
+
+// Rockable::accelerations without a time increment (the load-time step).
+int rk_accelerations(rk_ctx* x) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  int rc;
+  if ((rc = ready(c))) return rc;
+  Scene& s = c.s;
+  CK(cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream));
+  launch_glob_vertices(s, c.stream);
+  launch_narrow_force(s, c.stream);
+  launch_gather_accel(s, 0, c.stream);
+  launch_breakage(s, c.stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_update_nl(rk_ctx* x) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  int rc;
+  if ((rc = ready(c))) return rc;
+  launch_glob_vertices(c.s, c.stream);
+  if ((rc = rebuild_nl(c))) return rc;
+  c.nl_updates++;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+// nsteps passes of the loop body of Rockable::integrate (Rockable.cpp:2584-2736)
+// without conf output: t += dt, velocity-Verlet step, NL update when the
+// interVerlet counter elapsed or an update was requested, dynamic guard.
+int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
+  if (!x || nsteps < 0) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  int rc;
+  if ((rc = ready(c))) return rc;
+  Scene& s = c.s;
+  const bool need_flags = s.dynamic_nl != 0 || s.nif > 0;
+  int64_t k0 = c.kernels, nl0 = c.nl_updates;
+  CK(cudaEventRecord(c.ev0, c.stream));
+  for (int64_t it = 0; it < nsteps; it++) {
+    c.t += s.dt;
+    c.interVerletC += s.dt;
+    CK(cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream));
+    int ph = 0;
+    auto mark = [&](int phase, bool end) {
+      if (c.profiling) cudaEventRecord(c.pev[2 * phase + (end ? 1 : 0)], c.stream);
+    };
+    auto phase = [&](int p, int launched) {
+      (void)ph;
+      c.kernels += launched;
+      if (c.profiling && launched) {
+        mark(p, true);
+        cudaEventSynchronize(c.pev[2 * p + 1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c.pev[2 * p], c.pev[2 * p + 1]);
+        c.prof_ms[p] += ms;
+        c.prof_n[p] += launched;
+      }
+    };
+    mark(0, false); phase(0, launch_controls_pre(s, c.stream));
+    mark(1, false); phase(1, launch_drift(s, c.stream));
+    mark(2, false); phase(2, launch_glob_vertices(s, c.stream));
+    mark(3, false); phase(3, launch_narrow_force(s, c.stream));
+    mark(4, false); phase(4, launch_gather_accel(s, 1, c.stream));
+    mark(5, false); phase(5, launch_breakage(s, c.stream));
+    bool need = false;
+    if (need_flags) {
+      if ((rc = read_flags(c))) return rc;
+      need = c.h_flags[FLAG_NEED_UPDATE] != 0ull;
+    }
+    if (need || c.interVerletC >= c.interVerlet - s.dt_2) {
+      mark(6, false);
+      int64_t k1 = c.kernels;
+      if ((rc = rebuild_nl(c))) return rc;
+      int64_t launched = c.kernels - k1;
+      c.kernels = k1;
+      phase(6, (int)launched);
+      c.nl_updates++;
+      if (!need) c.interVerletC = 0.0;
+      else CK(cudaMemsetAsync(s.flags + FLAG_NEED_UPDATE, 0, sizeof(unsigned long long), c.stream));
+    }
+    if (s.dynamic_nl) { mark(7, false); phase(7, launch_guard(s, c.stream)); }
+    c.steps++;
+  }
+  CK(cudaEventRecord(c.ev1, c.stream));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(c.ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+  c.last_ms = ms;
+  c.last_kernels = c.kernels - k0;
+  if (rep) {
+    if ((rc = read_flags(c))) return rc;
+    rep->steps_done = nsteps;
+    rep->nl_updates = c.nl_updates - nl0;
+    rep->n_entries = s.ne;
+    rep->n_active = (int64_t)c.h_flags[FLAG_NACTIVE];
+    rep->n_broken = (int64_t)c.h_flags[FLAG_NBROKEN];
+    rep->t = c.t;
+  }
+  return RK_OK;
+}
+
+int rk_synchronize(rk_ctx* x) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int64_t rk_num_bodies(const rk_ctx* x) { return x ? x->c.s.n : -1; }
+int64_t rk_num_entries(const rk_ctx* x) { return x ? x->c.s.ne : -1; }
+int64_t rk_num_interfaces(const rk_ctx* x) { return x ? x->c.s.nif : -1; }
+
+int rk_download_bodies(rk_ctx* x, double* pos, double* vel, double* acc, double* Q, double* vrot, double* arot,
+                       double* force, double* moment) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  Scene& s = c.s;
+  const size_t n3 = 3 * (size_t)s.n * sizeof(double);
+  if (pos) CK(cudaMemcpyAsync(pos, s.pos, n3, cudaMemcpyDeviceToHost, c.stream));
+  if (vel) CK(cudaMemcpyAsync(vel, s.vel, n3, cudaMemcpyDeviceToHost, c.stream));
+  if (acc) CK(cudaMemcpyAsync(acc, s.acc, n3, cudaMemcpyDeviceToHost, c.stream));
+  if (Q) CK(cudaMemcpyAsync(Q, s.Q, 4 * (size_t)s.n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  if (vrot) CK(cudaMemcpyAsync(vrot, s.vrot, n3, cudaMemcpyDeviceToHost, c.stream));
+  if (arot) CK(cudaMemcpyAsync(arot, s.arot, n3, cudaMemcpyDeviceToHost, c.stream));
+  if (force) CK(cudaMemcpyAsync(force, s.force, n3, cudaMemcpyDeviceToHost, c.stream));
+  if (moment) CK(cudaMemcpyAsync(moment, s.moment, n3, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+__global__ void k_unpack_tsub(const uint32_t* ts, int64_t n, int* t, int* isub, int* jsub) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  t[e] = tsub_type(ts[e]);
+  isub[e] = tsub_isub(ts[e]);
+  jsub[e] = tsub_jsub(ts[e]);
+}
+
+int rk_download_entries(rk_ctx* x, int32_t* i, int32_t* j, int32_t* type, int32_t* isub, int32_t* jsub, double* dn,
+                        double* fn, double* ft, double* mom, double* damp, int32_t* bond, uint8_t* active, double* n,
+                        double* pos, double* vel) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  Scene& s = c.s;
+  const int64_t ne = s.ne;
+  if (ne == 0) return RK_OK;
+  const size_t d1 = (size_t)ne * sizeof(double), d3 = 3 * d1, i1 = (size_t)ne * sizeof(int);
+  if (i) CK(cudaMemcpyAsync(i, s.ei, i1, cudaMemcpyDeviceToHost, c.stream));
+  if (j) CK(cudaMemcpyAsync(j, s.ej, i1, cudaMemcpyDeviceToHost, c.stream));
+  if (type || isub || jsub) {
+    int *dt = nullptr, *di = nullptr, *dj = nullptr;
+    int rc;
+    if ((rc = dalloc(c, dt, ne)) || (rc = dalloc(c, di, ne)) || (rc = dalloc(c, dj, ne))) return rc;
+    k_unpack_tsub<<<nblk(ne, 256), 256, 0, c.stream>>>(s.etsub, ne, dt, di, dj);
+    if (type) CK(cudaMemcpyAsync(type, dt, i1, cudaMemcpyDeviceToHost, c.stream));
+    if (isub) CK(cudaMemcpyAsync(isub, di, i1, cudaMemcpyDeviceToHost, c.stream));
+    if (jsub) CK(cudaMemcpyAsync(jsub, dj, i1, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    dfree(dt); dfree(di); dfree(dj);
+  }
+  if (dn) CK(cudaMemcpyAsync(dn, s.dn, d1, cudaMemcpyDeviceToHost, c.stream));
+  if (fn) CK(cudaMemcpyAsync(fn, s.fn, d1, cudaMemcpyDeviceToHost, c.stream));
+  if (ft) CK(cudaMemcpyAsync(ft, s.ft, d3, cudaMemcpyDeviceToHost, c.stream));
+  if (mom) CK(cudaMemcpyAsync(mom, s.mom, d3, cudaMemcpyDeviceToHost, c.stream));
+  if (damp) CK(cudaMemcpyAsync(damp, s.damp, d1, cudaMemcpyDeviceToHost, c.stream));
+  if (bond) CK(cudaMemcpyAsync(bond, s.bond, i1, cudaMemcpyDeviceToHost, c.stream));
+  if (active) CK(cudaMemcpyAsync(active, s.act, (size_t)ne, cudaMemcpyDeviceToHost, c.stream));
+  if (n) CK(cudaMemcpyAsync(n, s.gn, d3, cudaMemcpyDeviceToHost, c.stream));
+  if (pos) CK(cudaMemcpyAsync(pos, s.gpos, d3, cudaMemcpyDeviceToHost, c.stream));
+  if (vel) CK(cudaMemcpyAsync(vel, s.gvel, d3, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_download_interfaces(rk_ctx* x, int32_t* i, int32_t* j, uint8_t* broken) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  Scene& s = c.s;
+  if (s.nif == 0) return RK_OK;
+  if (i) CK(cudaMemcpyAsync(i, s.if_i, s.nif * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  if (j) CK(cudaMemcpyAsync(j, s.if_j, s.nif * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  if (broken) CK(cudaMemcpyAsync(broken, s.if_broken, s.nif, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_get_stats(rk_ctx* x, rk_stats* out) {
+  if (!x || !out) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  Scene& s = c.s;
+  std::memset(out, 0, sizeof *out);
+  if (s.n > 0) {
+    int64_t nb = (s.n + 255) / 256;
+    if (nb > c.ke_blocks) {
+      dfree(c.d_ke);
+      CK(cudaMalloc(&c.d_ke, 2 * nb * sizeof(double)));
+      c.ke_blocks = nb;
+    }
+    launch_kinetic_energy(s, c.d_ke, c.stream);
+    std::vector<double> h(2 * nb);
+    CK(cudaMemcpyAsync(h.data(), c.d_ke, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    for (int64_t k = 0; k < nb; k++) {
+      out->e_trans += h[2 * k];
+      out->e_rot += h[2 * k + 1];
+    }
+    out->e_trans *= 0.5;
+    out->e_rot *= 0.5;
+  }
+  int rc;
+  if ((rc = read_flags(c))) return rc;
+  out->n_entries = s.ne;
+  out->n_active = (int64_t)c.h_flags[FLAG_NACTIVE];
+  out->n_broken = (int64_t)c.h_flags[FLAG_NBROKEN];
+  out->nl_updates = c.nl_updates;
+  int64_t nfree = s.n - s.n_driven;
+  out->coordination = nfree > 0 ? 2.0 * (double)out->n_active / (double)nfree : 0.0;
+  return RK_OK;
+}
+
+int rk_upload_kinematics(rk_ctx* x, const double* pos, const double* vel, const double* acc, const double* Q,
+                         const double* vrot, const double* arot) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  Scene& s = c.s;
+  const size_t n3 = 3 * (size_t)s.n * sizeof(double);
+  if (pos) CK(cudaMemcpyAsync(s.pos, pos, n3, cudaMemcpyHostToDevice, c.stream));
+  if (vel) CK(cudaMemcpyAsync(s.vel, vel, n3, cudaMemcpyHostToDevice, c.stream));
+  if (acc) CK(cudaMemcpyAsync(s.acc, acc, n3, cudaMemcpyHostToDevice, c.stream));
+  if (Q) CK(cudaMemcpyAsync(s.Q, Q, 4 * (size_t)s.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  if (vrot) CK(cudaMemcpyAsync(s.vrot, vrot, n3, cudaMemcpyHostToDevice, c.stream));
+  if (arot) CK(cudaMemcpyAsync(s.arot, arot, n3, cudaMemcpyHostToDevice, c.stream));
+  return RK_OK;
+}
+
+int rk_set_profiling(rk_ctx* x, int on) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (on && !c.pev[0])
+    for (int k = 0; k < 2 * RK_NPHASE; k++) CK(cudaEventCreate(&c.pev[k]));
+  c.profiling = on ? 1 : 0;
+  for (int k = 0; k < RK_NPHASE; k++) {
+    c.prof_ms[k] = 0.0;
+    c.prof_n[k] = 0;
+  }
+  return RK_OK;
+}
+
+int rk_get_profile(const rk_ctx* x, double* ms, int64_t* launches) {
+  if (!x) return RK_ERR_ARG;
+  for (int k = 0; k < RK_NPHASE; k++) {
+    if (ms) ms[k] = x->c.prof_ms[k];
+    if (launches) launches[k] = x->c.prof_n[k];
+  }
+  return RK_OK;
+}
+
+int rk_last_step_timing(const rk_ctx* x, double* ms, int64_t* kernels) {
+  if (!x) return RK_ERR_ARG;
+  if (ms) *ms = x->c.last_ms;
+  if (kernels) *kernels = x->c.last_kernels;
+  return RK_OK;
+}
+
+}  // extern "C"

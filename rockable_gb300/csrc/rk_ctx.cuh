@@ -1,0 +1,81 @@
+// rk_ctx.cuh -- host-side context of librk_gpu.so (one scene on one GPU).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/rk_gpu.h"
+#include "rk_engine.cuh"
+
+namespace rk {
+
+// Per-entry arrays that survive a neighbour-list rebuild (double-buffered).
+struct EntryBuf {
+  int64_t cap = 0;
+  int *ei = nullptr, *ej = nullptr;
+  uint32_t* etsub = nullptr;
+  uint64_t* ekey = nullptr;
+  double *dn = nullptr, *fn = nullptr, *ft = nullptr, *mom = nullptr, *damp = nullptr;
+  int* bond = nullptr;
+  double *gn = nullptr, *gpos = nullptr, *gvel = nullptr;
+};
+
+// Scratch of the neighbour-list rebuild, grown on demand.
+struct NLWork {
+  int64_t pair_cap = 0, hp_cap = 0, cand_cap = 0, old_cap = 0, fin_cap = 0, tmp_bytes = 0;
+  uint64_t* pairs = nullptr;     // pair_cap
+  uint64_t* hp = nullptr;        // hp_cap (half-pair keys owner<<21 | partner)
+  uint64_t* hp_tmp = nullptr;    // hp_cap
+  int64_t* hp_cnt = nullptr;     // hp_cap + 1
+  uint32_t* hp_mask = nullptr;   // kMaskWords * hp_cap
+  uint64_t* cand = nullptr;      // cand_cap new entry keys
+  int64_t* cand_src = nullptr;   // cand_cap
+  int64_t* flag = nullptr;       // old_cap + 1
+  uint64_t* stale = nullptr;     // old_cap
+  int64_t* stale_src = nullptr;  // old_cap
+  uint64_t* fkey = nullptr;      // fin_cap
+  int64_t* fsrc = nullptr;       // fin_cap
+  uint64_t* jkeys = nullptr;     // fin_cap
+  uint64_t* jtmp = nullptr;      // fin_cap
+  void* tmp = nullptr;           // scan / sort temp
+  unsigned long long* counter = nullptr;
+};
+
+struct Ctx {
+  int device = 0;
+  int form = RK_FORM_FP64;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  Scene s{};
+  EntryBuf eb[2];
+  int cur = 0;
+  NLWork w;
+  // host copies of small things
+  std::vector<Control> controls;
+  std::vector<int> shape_nv;  // vertices per shape
+  std::vector<double> shape_radius;
+  bool have_shapes = false, have_bodies = false, have_params = false;
+  // loop bookkeeping (Rockable::integrate)
+  double t = 0.0, interVerlet = 0.01, interVerletC = 0.0;
+  int64_t nl_updates = 0, steps = 0;
+  double last_ms = 0.0;
+  int64_t last_kernels = 0;
+  int64_t kernels = 0;
+  unsigned long long* h_flags = nullptr;  // pinned mirror of the device flag block
+  double* d_ke = nullptr;
+  int64_t ke_blocks = 0;
+  // contributions and per-step arrays (single-buffered)
+  int64_t contrib_cap = 0;
+  // per-phase profiling
+  int profiling = 0;
+  cudaEvent_t pev[2 * RK_NPHASE] = {};
+  double prof_ms[RK_NPHASE] = {};
+  int64_t prof_n[RK_NPHASE] = {};
+};
+
+int rebuild_nl(Ctx& c);
+int ensure_entry_capacity(Ctx& c, int which, int64_t n);
+void bind_entries(Ctx& c);
+
+}  // namespace rk

@@ -1,0 +1,141 @@
+// rk_engine.cuh -- device data layout of one scene and the kernel launchers
+// shared by the translation units of librk_gpu.so.
+//
+// HBM layout (one context = one scene):
+//   bodies    : SoA, 3 doubles per vector field (pos, vel, acc, vrot, arot,
+//               force, moment), 4 per quaternion; coalesced for one thread
+//               per body.
+//   gvert     : global positions of every body's vertices, recomputed once
+//               per step (3 doubles per vertex); body b's vertices start at
+//               gv_ofs[b].  The narrow phase gathers these instead of
+//               re-rotating shape vertices per sub-contact.
+//   entries   : the neighbour list as SoA sorted by the 64-bit key
+//               (i:21 | j:21 | type:2 | isub:10 | jsub:10), with history
+//               (dn, fn, ft, mom, damp, bond) and per-step contributions
+//               (force f, moment on i, moment on j) of active entries.
+//   iofs/jofs : body -> first entry with key.i == b; body -> first slot of
+//               jlist, the entry indices with key.j == b in entry order.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rk_math.cuh"
+
+namespace rk {
+
+constexpr int kMaxSub = 1024;       // sub-element index limit of the sort key
+constexpr int kMaxBody = 1 << 21;   // body index limit of the sort key
+constexpr int kMaskWords = 2;       // vertex cull mask words per half-pair (<= 64 vertices)
+
+__host__ __device__ __forceinline__ uint64_t entry_key(uint32_t i, uint32_t j, uint32_t t, uint32_t isub,
+                                                       uint32_t jsub) {
+  return ((uint64_t)i << 43) | ((uint64_t)j << 22) | ((uint64_t)t << 20) | ((uint64_t)isub << 10) | (uint64_t)jsub;
+}
+__host__ __device__ __forceinline__ uint32_t pack_tsub(uint32_t t, uint32_t isub, uint32_t jsub) {
+  return (t << 30) | (isub << 15) | jsub;
+}
+__host__ __device__ __forceinline__ int tsub_type(uint32_t p) { return (int)(p >> 30); }
+__host__ __device__ __forceinline__ int tsub_isub(uint32_t p) { return (int)((p >> 15) & 0x7fff); }
+__host__ __device__ __forceinline__ int tsub_jsub(uint32_t p) { return (int)(p & 0x7fff); }
+
+struct LawParams {  // one group pair
+  double p[24];
+};
+
+struct Control {
+  int type;
+  int body;
+  double value;
+  double vec[3];
+};
+
+struct Scene {
+  // ---- shapes
+  int nshapes;
+  int* vert_ofs;
+  int* edge_ofs;
+  int* edges;
+  int* face_ofs;
+  int* face_vofs;
+  int* face_verts;
+  double* svert;   // 3 per shape vertex
+  double* sradius;
+  double* sobb;    // 15 per shape
+  // ---- bodies
+  int64_t n;
+  int64_t n_driven;
+  double *pos, *vel, *acc, *Q, *vrot, *arot, *force, *moment;
+  double *hom, *mass, *inertia, *rad;
+  int *shape, *group, *cluster;
+  int64_t nvert;     // total global vertices
+  int64_t* gv_ofs;   // n+1
+  int* gv_body;      // nvert
+  double* gv;        // 3*nvert
+  double* bobb;      // 15 per body (placed OBB, not enlarged)
+  float* baabb;      // 6 per body: outward-rounded AABB of the OBB enlarged by DVerlet/2
+  // dynamic guard
+  double *dpos, *dq;  // 3n, 4n
+  // ---- law
+  int law;
+  int params_in_interfaces;
+  int ngroup;
+  LawParams* table;  // ngroup*ngroup
+  double dt, dt_2, dt2_2;
+  double gravity[3];
+  double DVerlet, dVerlet;
+  double num_damp;
+  double disp_update, angle_update;
+  int dynamic_nl;
+  // ---- controls
+  int ncontrols;
+  Control* controls;
+  int servo_kind, servo_icontr, servo_walls[6];
+  double servo_p;
+  // ---- entries
+  int64_t ne, cap;
+  int *ei, *ej;
+  uint32_t* etsub;
+  uint64_t* ekey;
+  double *dn, *fn, *ft, *mom, *damp;
+  int* bond;
+  uint8_t* act;
+  double *cf, *cmi, *cmj;      // contributions (3 per entry each)
+  double *gn, *gpos, *gvel;    // stored geometry (3 per entry each)
+  int record_geom;
+  int64_t* iofs;  // n+1
+  int64_t* jofs;  // n+1
+  int* jlist;     // ne
+  // ---- interfaces
+  int64_t nif;
+  int *if_i, *if_j;
+  double* if_dn0;
+  double* if_par;   // 8 per interface
+  int* if_inner;
+  uint8_t* if_broken;
+  uint8_t* if_break;  // set by the narrow phase when the yield criterion is met
+  int64_t* if_ofs;    // n+1 (interfaces sorted by i)
+  // ---- device flags and counters (pinned-readable block)
+  unsigned long long* flags;  // [0] need_update, [1] n_active, [2] n_broken_step, [3] guard max pos2 bits,
+                              // [4] guard max rot bits, [5] guard reset pending, [6] error code
+};
+
+enum { FLAG_NEED_UPDATE = 0, FLAG_NACTIVE = 1, FLAG_NBROKEN = 2, FLAG_GPOS = 3, FLAG_GROT = 4, FLAG_GRESET = 5,
+       FLAG_ERROR = 6, FLAG_COUNT = 8 };
+
+// step kernels (rk_step.cu)
+int launch_controls_pre(const Scene& s, cudaStream_t st);
+int launch_drift(const Scene& s, cudaStream_t st);
+int launch_glob_vertices(const Scene& s, cudaStream_t st);
+int launch_narrow_force(const Scene& s, cudaStream_t st);
+int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st);
+int launch_breakage(const Scene& s, cudaStream_t st);
+int launch_guard(const Scene& s, cudaStream_t st);
+int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);
+
+// primitives (rk_prims.cu)
+size_t scan_temp_bytes(int64_t n);
+void exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* temp, cudaStream_t st);
+size_t sort_temp_bytes(int64_t n);
+void radix_sort_u64(uint64_t* keys, uint64_t* tmp, int64_t n, int lo_bit, int hi_bit, void* temp, cudaStream_t st);
+
+}  // namespace rk

@@ -1,0 +1,586 @@
+// rk_nl.cu -- neighbour-list rebuild on the GPU.
+//
+// Semantics follow Rockable's UpdateNL_bruteForce (Rockable.cpp:1614-1662)
+// with AddOrRemoveInteractions_bruteForce (Rockable.cpp:1309-1432):
+//   * a body pair (i < j, not both driven, no unbroken interface) is
+//     "visited" when their OBBs enlarged by DVerlet/2 intersect;
+//   * in a visited pair every sub-contact candidate is tested, except the
+//     vertex-owned ones whose vertex cube fails the OBB cull; a tested
+//     candidate that is NEAR is kept (history carried) or inserted (fresh
+//     history), a tested candidate that is not NEAR is removed;
+//   * entries of pairs that are not visited, and untested candidates, are
+//     kept untouched.
+// UpdateNL_linkCells visits exactly the same pairs when its cells contain the
+// enlarged boxes, so both options map onto this exact pair predicate.
+//
+// Pipeline (all on the context stream, a few host reads of counts):
+//   body_obb -> all-pairs AABB filter + FP64 SAT -> half-pairs (both
+//   directions, radix-sorted) -> per half-pair candidate count / cull mask ->
+//   scan -> candidate write (keys in sorted order per half-pair) -> old-entry
+//   classification and order-preserving compaction -> merge by key ->
+//   history carry -> i-side offsets and j-side list.
+#include <algorithm>
+#include <cstdio>
+
+#include "rk_ctx.cuh"
+
+namespace rk {
+
+__device__ __forceinline__ V3 g3(const double* a, int64_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
+
+__device__ __forceinline__ Obb load_obb(const double* o) {
+  Obb b;
+  b.c = v3(o[0], o[1], o[2]);
+  b.e0 = v3(o[3], o[4], o[5]);
+  b.e1 = v3(o[6], o[7], o[8]);
+  b.e2 = v3(o[9], o[10], o[11]);
+  b.ext = v3(o[12], o[13], o[14]);
+  return b;
+}
+__device__ __forceinline__ void enlarge(Obb& b, double d) {
+  b.ext.x += d;
+  b.ext.y += d;
+  b.ext.z += d;
+}
+
+// Particle::updateObb (Particle.cpp:78-86) and the AABB of the box enlarged
+// by DVerlet/2, rounded outward to float for the pair filter.
+__global__ void k_body_obb(Scene s) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= s.n) return;
+  const double* so = s.sobb + 15 * s.shape[b];
+  Obb o = load_obb(so);
+  Q4 q = q4(s.Q[4 * b], s.Q[4 * b + 1], s.Q[4 * b + 2], s.Q[4 * b + 3]);
+  o.e0 = qrot(q, o.e0);
+  o.e1 = qrot(q, o.e1);
+  o.e2 = qrot(q, o.e2);
+  o.c = qrot(q, o.c);
+  double h = s.hom[b];
+  o.ext = h * o.ext;
+  o.c = h * o.c;
+  o.c = o.c + v3(s.pos[3 * b], s.pos[3 * b + 1], s.pos[3 * b + 2]);
+  double* out = s.bobb + 15 * b;
+  out[0] = o.c.x; out[1] = o.c.y; out[2] = o.c.z;
+  out[3] = o.e0.x; out[4] = o.e0.y; out[5] = o.e0.z;
+  out[6] = o.e1.x; out[7] = o.e1.y; out[8] = o.e1.z;
+  out[9] = o.e2.x; out[10] = o.e2.y; out[11] = o.e2.z;
+  out[12] = o.ext.x; out[13] = o.ext.y; out[14] = o.ext.z;
+  const double d = 0.5 * s.DVerlet;
+  const double ex = o.ext.x + d, ey = o.ext.y + d, ez = o.ext.z + d;
+  const double hw[3] = {ex * fabs(o.e0.x) + ey * fabs(o.e1.x) + ez * fabs(o.e2.x),
+                        ex * fabs(o.e0.y) + ey * fabs(o.e1.y) + ez * fabs(o.e2.y),
+                        ex * fabs(o.e0.z) + ey * fabs(o.e1.z) + ez * fabs(o.e2.z)};
+  const double c[3] = {o.c.x, o.c.y, o.c.z};
+  float* bb = s.baabb + 6 * b;
+  for (int k = 0; k < 3; k++) {
+    double m = 1e-6 * (hw[k] + fabs(c[k])) + 1e-12;  // slack covering the SAT epsilon
+    bb[k] = __double2float_rd(c[k] - hw[k] - m);
+    bb[3 + k] = __double2float_ru(c[k] + hw[k] + m);
+  }
+}
+
+__device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
+  // unbroken interface (i, j) stored under its first body (Rockable.cpp:1637-1641)
+  int64_t lo = s.if_ofs[i], hi = s.if_ofs[i + 1];
+  while (lo < hi) {
+    int64_t m = (lo + hi) >> 1;
+    if (s.if_j[m] < j) lo = m + 1;
+    else hi = m;
+  }
+  return lo < s.if_ofs[i + 1] && s.if_j[lo] == j && !s.if_broken[lo];
+}
+
+// All-pairs broad phase: float AABB filter (tiled through shared memory),
+// then eligibility and the FP64 SAT of the enlarged OBBs.
+constexpr int kPairTile = 128;
+__global__ void k_pairs(Scene s, uint64_t* pairs, int64_t cap, unsigned long long* counter) {
+  __shared__ float sb[kPairTile][6];
+  const int64_t i = blockIdx.x * (int64_t)kPairTile + threadIdx.x;
+  const bool vi = i < s.n;
+  float a[6];
+  for (int k = 0; k < 6; k++) a[k] = vi ? s.baabb[6 * i + k] : 0.f;
+  const int64_t jstart = blockIdx.x * (int64_t)kPairTile;
+  for (int64_t j0 = jstart; j0 < s.n; j0 += kPairTile) {
+    __syncthreads();
+    int64_t jl = j0 + threadIdx.x;
+    if (jl < s.n)
+      for (int k = 0; k < 6; k++) sb[threadIdx.x][k] = s.baabb[6 * jl + k];
+    __syncthreads();
+    if (!vi) continue;
+    int jn = (int)min((int64_t)kPairTile, s.n - j0);
+    for (int t = 0; t < jn; t++) {
+      int64_t j = j0 + t;
+      if (j <= i) continue;
+      if (a[0] > sb[t][3] || sb[t][0] > a[3] || a[1] > sb[t][4] || sb[t][1] > a[4] || a[2] > sb[t][5] ||
+          sb[t][2] > a[5])
+        continue;
+      if (i < s.n_driven && j < s.n_driven) continue;
+      if (has_iface(s, (int)i, (int)j)) continue;
+      Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
+      enlarge(oi, 0.5 * s.DVerlet);
+      enlarge(oj, 0.5 * s.DVerlet);
+      if (!obb_intersect(oi, oj)) continue;
+      unsigned long long k = atomicAdd(counter, 1ull);
+      if ((int64_t)k < cap) pairs[k] = ((uint64_t)i << 21) | (uint64_t)j;
+    }
+  }
+}
+
+__global__ void k_half_pairs(const uint64_t* pairs, int64_t np, uint64_t* hp) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  uint64_t p = pairs[k];
+  uint64_t i = p >> 21, j = p & ((1u << 21) - 1);
+  hp[2 * k] = (i << 21) | j;
+  hp[2 * k + 1] = (j << 21) | i;
+}
+
+// ------------------------------------------------- NEAR predicates ----
+// Particle.cpp:88-209, with vertex positions from the per-step table.
+struct PairView {
+  const double* gb;  // owner global vertices
+  const double* gp;  // partner global vertices
+  int sb, sp;        // shapes
+  double Rb, Rp, dmax;
+};
+
+__device__ __forceinline__ bool near_vv(const PairView& P, int v, int w) {
+  V3 a = g3(P.gb, v), b = g3(P.gp, w);
+  double sum = P.Rb + P.Rp + P.dmax;
+  return norm2(b - a) <= sum * sum;
+}
+__device__ __forceinline__ bool near_ve(const Scene& s, const PairView& P, int v, int e) {
+  const int eo = s.edge_ofs[P.sp] + e;
+  V3 piv = g3(P.gb, v);
+  V3 p0 = g3(P.gp, s.edges[2 * eo]), p1 = g3(P.gp, s.edges[2 * eo + 1]);
+  V3 E = p1 - p0, w = piv - p0;
+  double r = dot(w, E) / dot(E, E);
+  if (r < -P.dmax) return false;
+  if (r > 1.0 + P.dmax) return false;
+  double sum = P.Rb + P.Rp + P.dmax;
+  return norm2(piv - (p0 + r * E)) <= sum * sum;
+}
+__device__ __forceinline__ bool near_vf(const Scene& s, const PairView& P, int v, int f) {
+  const int fo = s.face_ofs[P.sp] + f;
+  const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
+  const int* fv = s.face_verts + v0;
+  V3 A = g3(P.gp, fv[0]), B = g3(P.gp, fv[1]), C = g3(P.gp, fv[nbv - 1]);
+  V3 piv = g3(P.gb, v);
+  V3 w = piv - A;
+  V3 v1 = B - A;
+  normalize(v1);
+  V3 v2 = C - A;
+  V3 n = cross(v1, v2);
+  normalize(n);
+  double dist = dot(w, n);
+  if (dist < 0.0) { n = -n; dist = -dist; }
+  V3 Pp = piv - dist * n;
+  int odd = 0;
+  v2 = cross(n, v1);
+  double ori1 = dot(Pp, v1), ori2 = dot(Pp, v2);
+  for (int iva = 0; iva < nbv; ++iva) {
+    int ivb = iva + 1;
+    if (ivb == nbv) ivb = 0;
+    V3 pa = g3(P.gp, fv[iva]), pb = g3(P.gp, fv[ivb]);
+    double pa1 = dot(pa, v1), pb1 = dot(pb, v1), pa2 = dot(pa, v2), pb2 = dot(pb, v2);
+    if ((pa2 < ori2 && pb2 >= ori2) || (pb2 < ori2 && pa2 >= ori2)) {
+      if (pa1 + (ori2 - pa2) / (pb2 - pa2) * (pb1 - pa1) < ori1) odd = 1 - odd;
+    }
+  }
+  if (odd == 1) {
+    dist -= (P.Rb + P.Rp);
+    if (dist <= P.dmax) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ bool near_ee(const Scene& s, const PairView& P, int eb, int ep) {
+  const int ob = s.edge_ofs[P.sb] + eb, op = s.edge_ofs[P.sp] + ep;
+  V3 pj0 = g3(P.gp, s.edges[2 * op]), pj1 = g3(P.gp, s.edges[2 * op + 1]);
+  V3 pi0 = g3(P.gb, s.edges[2 * ob]), pi1 = g3(P.gb, s.edges[2 * ob + 1]);
+  V3 Ei = pi1 - pi0, Ej = pj1 - pj0, w = pi0 - pj0;
+  double c = dot(Ei, Ei), d = dot(Ej, Ej), e = dot(Ei, Ej);
+  double f = (c * d) - (e * e);
+  if (fabs(f) > 1.0e-12) {
+    f = 1.0 / f;
+    double a = dot(Ei, w), b = dot(Ej, w);
+    double ss = (e * b - a * d) * f;
+    double tt = (c * b - e * a) * f;
+    if (ss >= 0.0 && ss <= 1.0 && tt >= 0.0 && tt <= 1.0) {
+      V3 n = (pi0 + ss * Ei) - (pj0 + tt * Ej);
+      double sum = P.Rb + P.Rp + P.dmax;
+      return norm2(n) <= sum * sum;
+    }
+  }
+  return false;
+}
+
+// Candidates of one half-pair (owner b -> partner p), in key order.
+// MODE 0 counts (and records the vertex cull mask), MODE 1 writes keys.
+template <int MODE>
+__global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* cnt, uint32_t* mask,
+                             const int64_t* ofs, uint64_t* out) {
+  int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (h >= nhp) return;
+  const uint64_t key = hp[h];
+  const int b = (int)(key >> 21), p = (int)(key & ((1u << 21) - 1));
+  PairView P;
+  P.gb = s.gv + 3 * s.gv_ofs[b];
+  P.gp = s.gv + 3 * s.gv_ofs[p];
+  P.sb = s.shape[b];
+  P.sp = s.shape[p];
+  P.Rb = s.rad[b];
+  P.Rp = s.rad[p];
+  P.dmax = s.dVerlet;
+  const int nvb = s.vert_ofs[P.sb + 1] - s.vert_ofs[P.sb];
+  const int nvp = s.vert_ofs[P.sp + 1] - s.vert_ofs[P.sp];
+  const int neb = s.edge_ofs[P.sb + 1] - s.edge_ofs[P.sb];
+  const int nep = s.edge_ofs[P.sp + 1] - s.edge_ofs[P.sp];
+  const int nfp = s.face_ofs[P.sp + 1] - s.face_ofs[P.sp];
+  uint32_t m[kMaskWords];
+  if (MODE == 0) {
+    Obb op = load_obb(s.bobb + 15 * p);
+    enlarge(op, P.dmax);
+    for (int w = 0; w < kMaskWords; w++) m[w] = 0u;
+    for (int v = 0; v < nvb; v++) {
+      Obb sub;
+      sub.c = g3(P.gb, v);
+      sub.e0 = v3(1, 0, 0);
+      sub.e1 = v3(0, 1, 0);
+      sub.e2 = v3(0, 0, 1);
+      double r = P.Rb + P.dmax;
+      sub.ext = v3(r, r, r);
+      if (obb_intersect(op, sub)) m[v >> 5] |= 1u << (v & 31);
+    }
+    for (int w = 0; w < kMaskWords; w++) mask[kMaskWords * h + w] = m[w];
+  } else {
+    for (int w = 0; w < kMaskWords; w++) m[w] = mask[kMaskWords * h + w];
+  }
+  int64_t c = 0;
+  uint64_t* o = (MODE == 1) ? out + ofs[h] : nullptr;
+  auto emit = [&](int t, int i1, int j1) {
+    if (MODE == 1) o[c] = entry_key((uint32_t)b, (uint32_t)p, (uint32_t)t, (uint32_t)i1, (uint32_t)j1);
+    c++;
+  };
+  if (b < p) {
+    for (int v = 0; v < nvb; v++)
+      if (m[v >> 5] >> (v & 31) & 1u)
+        for (int w = 0; w < nvp; w++)
+          if (near_vv(P, v, w)) emit(0, v, w);
+  }
+  for (int v = 0; v < nvb; v++)
+    if (m[v >> 5] >> (v & 31) & 1u)
+      for (int e = 0; e < nep; e++)
+        if (near_ve(s, P, v, e)) emit(1, v, e);
+  for (int v = 0; v < nvb; v++)
+    if (m[v >> 5] >> (v & 31) & 1u)
+      for (int f = 0; f < nfp; f++)
+        if (near_vf(s, P, v, f)) emit(2, v, f);
+  if (b < p) {
+    for (int e = 0; e < neb; e++)
+      for (int e2 = 0; e2 < nep; e2++)
+        if (near_ee(s, P, e, e2)) emit(3, e, e2);
+  }
+  if (MODE == 0) cnt[h] = c;
+}
+
+__device__ __forceinline__ int64_t lower_bound_u64(const uint64_t* a, int64_t n, uint64_t x) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t m = (lo + hi) >> 1;
+    if (a[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
+}
+
+// Old entries that were not tested this time are kept as they are.
+__global__ void k_stale_flag(const uint64_t* okey, int64_t no, const uint64_t* hp, int64_t nhp, const uint32_t* mask,
+                             int64_t* flag) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= no) return;
+  const uint64_t k = okey[e];
+  const uint64_t i = k >> 43, j = (k >> 22) & ((1u << 21) - 1);
+  const int t = (int)((k >> 20) & 3u), isub = (int)((k >> 10) & 1023u);
+  const uint64_t hk = (i << 21) | j;
+  int64_t h = lower_bound_u64(hp, nhp, hk);
+  bool tested = false;
+  if (h < nhp && hp[h] == hk) {
+    // vertex-vertex and edge-edge candidates exist only in the i < j direction
+    if ((t == 0 || t == 3) && i > j) tested = false;
+    else tested = (t == 3) || ((mask[kMaskWords * h + (isub >> 5)] >> (isub & 31)) & 1u);
+  }
+  flag[e] = tested ? 0 : 1;
+}
+
+__global__ void k_stale_write(const uint64_t* okey, int64_t no, const int64_t* flag, const int64_t* pos,
+                              uint64_t* stale, int64_t* stale_src) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= no || !flag[e]) return;
+  stale[pos[e]] = okey[e];
+  stale_src[pos[e]] = e;
+}
+
+__global__ void k_merge(const uint64_t* stale, const int64_t* stale_src, int64_t ns, const uint64_t* cand, int64_t nc,
+                        const uint64_t* okey, int64_t no, uint64_t* fkey, int64_t* fsrc) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < ns) {
+    uint64_t x = stale[k];
+    int64_t p = k + lower_bound_u64(cand, nc, x);
+    fkey[p] = x;
+    fsrc[p] = stale_src[k];
+  } else if (k < ns + nc) {
+    int64_t q = k - ns;
+    uint64_t x = cand[q];
+    int64_t p = q + lower_bound_u64(stale, ns, x);
+    int64_t o = lower_bound_u64(okey, no, x);
+    fkey[p] = x;
+    fsrc[p] = (o < no && okey[o] == x) ? o : -1;
+  }
+}
+
+// Fill the next entry buffer: carried history or a fresh sub-contact with
+// the damping of Rockable.cpp:1356-1376 (rate per group pair from the host).
+__global__ void k_fill(Scene s, int64_t nf, const uint64_t* fkey, const int64_t* fsrc, EntryBuf ob, EntryBuf nb) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nf) return;
+  const uint64_t x = fkey[k];
+  const int i = (int)(x >> 43), j = (int)((x >> 22) & ((1u << 21) - 1));
+  const uint32_t t = (uint32_t)((x >> 20) & 3u), isub = (uint32_t)((x >> 10) & 1023u), jsub = (uint32_t)(x & 1023u);
+  nb.ei[k] = i;
+  nb.ej[k] = j;
+  nb.etsub[k] = pack_tsub(t, isub, jsub);
+  nb.ekey[k] = x;
+  const int64_t o = fsrc[k];
+  if (o >= 0) {
+    nb.dn[k] = ob.dn[o];
+    nb.fn[k] = ob.fn[o];
+    nb.damp[k] = ob.damp[o];
+    nb.bond[k] = ob.bond[o];
+    for (int d = 0; d < 3; d++) {
+      nb.ft[3 * k + d] = ob.ft[3 * o + d];
+      nb.mom[3 * k + d] = ob.mom[3 * o + d];
+      nb.gn[3 * k + d] = ob.gn[3 * o + d];
+      nb.gpos[3 * k + d] = ob.gpos[3 * o + d];
+      nb.gvel[3 * k + d] = ob.gvel[3 * o + d];
+    }
+  } else {
+    const double* P = s.table[s.group[i] * s.ngroup + s.group[j]].p;
+    double meff;
+    if (i < s.n_driven) meff = s.mass[j];
+    else if (j < s.n_driven) meff = s.mass[i];
+    else meff = (s.mass[i] * s.mass[j]) / (s.mass[i] + s.mass[j]);
+    nb.damp[k] = P[22] * 2.0 * sqrt(P[RK_P_KN] * meff);
+    nb.dn[k] = 0.0;
+    nb.fn[k] = 0.0;
+    nb.bond[k] = -1;
+    for (int d = 0; d < 3; d++) {
+      nb.ft[3 * k + d] = 0.0;
+      nb.mom[3 * k + d] = 0.0;
+      nb.gn[3 * k + d] = 0.0;
+      nb.gpos[3 * k + d] = 0.0;
+      nb.gvel[3 * k + d] = 0.0;
+    }
+  }
+}
+
+__global__ void k_iofs(const uint64_t* key, int64_t ne, int64_t nb, int64_t* iofs) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b > nb) return;
+  iofs[b] = lower_bound_u64(key, ne, (uint64_t)b << 43);
+}
+
+__global__ void k_jkeys(const int* ej, int64_t ne, uint64_t* jk) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  jk[e] = ((uint64_t)ej[e] << 27) | (uint64_t)e;
+}
+
+__global__ void k_jlist(const uint64_t* jk, int64_t ne, int* jlist) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  jlist[e] = (int)(jk[e] & ((1ull << 27) - 1));
+}
+
+__global__ void k_jofs(const uint64_t* jk, int64_t ne, int64_t nb, int64_t* jofs) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b > nb) return;
+  jofs[b] = lower_bound_u64(jk, ne, (uint64_t)b << 27);
+}
+
+// ----------------------------------------------------------------- host ----
+static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+#define RKCHK(x)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) {                                                  \
+      c.err = std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #x;     \
+      return RK_ERR_CUDA;                                                     \
+    }                                                                         \
+  } while (0)
+
+template <typename T>
+static int grow(Ctx& c, T*& p, int64_t n_old, int64_t n_new) {
+  (void)n_old;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cudaError_t e = cudaMalloc(&p, (size_t)std::max<int64_t>(n_new, 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    c.err = std::string("CUDA: ") + cudaGetErrorString(e) + " (neighbour-list scratch)";
+    return RK_ERR_CUDA;
+  }
+  return 0;
+}
+
+static int ensure_tmp(Ctx& c, int64_t bytes) {
+  if (bytes <= c.w.tmp_bytes) return 0;
+  int64_t nb = std::max<int64_t>(bytes, c.w.tmp_bytes * 3 / 2);
+  if (c.w.tmp) cudaFree(c.w.tmp);
+  c.w.tmp = nullptr;
+  if (cudaMalloc(&c.w.tmp, (size_t)nb) != cudaSuccess) {
+    c.err = "CUDA: cannot allocate neighbour-list temp";
+    return RK_ERR_CUDA;
+  }
+  c.w.tmp_bytes = nb;
+  return 0;
+}
+
+static int64_t read_i64(Ctx& c, const int64_t* d) {
+  int64_t v = 0;
+  cudaMemcpyAsync(&v, d, sizeof v, cudaMemcpyDeviceToHost, c.stream);
+  cudaStreamSynchronize(c.stream);
+  return v;
+}
+
+int rebuild_nl(Ctx& c) {
+  Scene& s = c.s;
+  NLWork& w = c.w;
+  cudaStream_t st = c.stream;
+  int rc;
+  const int64_t N = s.n;
+  if (N <= 0) return 0;
+  k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
+  c.kernels++;
+  // ---- pairs
+  if (w.pair_cap < 16 * N + 1024) {
+    int64_t nc = 16 * N + 1024;
+    if ((rc = grow(c, w.pairs, w.pair_cap, nc))) return rc;
+    w.pair_cap = nc;
+  }
+  if (!w.counter) RKCHK(cudaMalloc(&w.counter, 64));
+  int64_t np = 0;
+  for (int attempt = 0; attempt < 4; attempt++) {
+    RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
+    k_pairs<<<nblk(N, kPairTile), kPairTile, 0, st>>>(s, w.pairs, w.pair_cap, w.counter);
+    c.kernels++;
+    unsigned long long cnt = 0;
+    RKCHK(cudaMemcpyAsync(&cnt, w.counter, 8, cudaMemcpyDeviceToHost, st));
+    RKCHK(cudaStreamSynchronize(st));
+    np = (int64_t)cnt;
+    if (np <= w.pair_cap) break;
+    int64_t nc = np + np / 2 + 1024;
+    if ((rc = grow(c, w.pairs, w.pair_cap, nc))) return rc;
+    w.pair_cap = nc;
+    np = -1;
+  }
+  if (np < 0) { c.err = "pair buffer kept overflowing"; return RK_ERR_CAPACITY; }
+  const int64_t nhp = 2 * np;
+  if (w.hp_cap < nhp + 1) {
+    int64_t nc = nhp + nhp / 2 + 1024;
+    if ((rc = grow(c, w.hp, w.hp_cap, nc))) return rc;
+    if ((rc = grow(c, w.hp_tmp, w.hp_cap, nc))) return rc;
+    if ((rc = grow(c, w.hp_cnt, w.hp_cap, nc + 1))) return rc;
+    if ((rc = grow(c, w.hp_mask, w.hp_cap, kMaskWords * nc))) return rc;
+    w.hp_cap = nc;
+  }
+  const EntryBuf& ob = c.eb[c.cur];
+  const int64_t no = s.ne;
+  int64_t need_tmp = (int64_t)std::max(std::max(sort_temp_bytes(nhp), scan_temp_bytes(nhp + 1)),
+                                       scan_temp_bytes(no + 1));
+  if ((rc = ensure_tmp(c, need_tmp))) return rc;
+  if (np > 0) {
+    k_half_pairs<<<nblk(np, 256), 256, 0, st>>>(w.pairs, np, w.hp);
+    c.kernels++;
+    radix_sort_u64(w.hp, w.hp_tmp, nhp, 0, 48, w.tmp, st);
+    c.kernels += 13;
+  }
+  // ---- candidates: count, scan, write
+  int64_t ncand = 0;
+  if (nhp > 0) {
+    k_candidates<0><<<nblk(nhp, 64), 64, 0, st>>>(s, w.hp, nhp, w.hp_cnt, w.hp_mask, nullptr, nullptr);
+    RKCHK(cudaMemsetAsync(w.hp_cnt + nhp, 0, sizeof(int64_t), st));
+    exclusive_scan_i64(w.hp_cnt, w.hp_cnt, nhp + 1, w.tmp, st);
+    c.kernels += 3;
+    ncand = read_i64(c, w.hp_cnt + nhp);
+  }
+  if (w.cand_cap < ncand + 1) {
+    int64_t nc = ncand + ncand / 2 + 1024;
+    if ((rc = grow(c, w.cand, w.cand_cap, nc))) return rc;
+    w.cand_cap = nc;
+  }
+  if (ncand > 0) {
+    k_candidates<1><<<nblk(nhp, 64), 64, 0, st>>>(s, w.hp, nhp, nullptr, w.hp_mask, w.hp_cnt, w.cand);
+    c.kernels++;
+  }
+  // ---- old entries kept untouched
+  if (w.old_cap < no + 1) {
+    int64_t nc = no + no / 2 + 1024;
+    if ((rc = grow(c, w.flag, w.old_cap, nc + 1))) return rc;
+    if ((rc = grow(c, w.stale, w.old_cap, nc))) return rc;
+    if ((rc = grow(c, w.stale_src, w.old_cap, nc))) return rc;
+    w.old_cap = nc;
+  }
+  int64_t nstale = 0;
+  if (no > 0) {
+    k_stale_flag<<<nblk(no, 256), 256, 0, st>>>(ob.ekey, no, w.hp, nhp, w.hp_mask, w.flag);
+    RKCHK(cudaMemsetAsync(w.flag + no, 0, sizeof(int64_t), st));
+    // positions in place of the flags, keeping a copy of the flags in stale_src
+    RKCHK(cudaMemcpyAsync(w.stale_src, w.flag, (size_t)no * sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+    exclusive_scan_i64(w.flag, w.flag, no + 1, w.tmp, st);
+    c.kernels += 3;
+    nstale = read_i64(c, w.flag + no);
+  }
+  // compact (flags copied to stale_src: use a separate pass into stale / cand_src)
+  if (w.fin_cap < nstale + ncand + 1) {
+    int64_t nc = nstale + ncand + (nstale + ncand) / 2 + 1024;
+    if ((rc = grow(c, w.fkey, w.fin_cap, nc))) return rc;
+    if ((rc = grow(c, w.fsrc, w.fin_cap, nc))) return rc;
+    if ((rc = grow(c, w.jkeys, w.fin_cap, nc))) return rc;
+    if ((rc = grow(c, w.jtmp, w.fin_cap, nc))) return rc;
+    w.fin_cap = nc;
+  }
+  if (no > 0) {
+    // fsrc doubles as the compacted old-index buffer before the merge
+    k_stale_write<<<nblk(no, 256), 256, 0, st>>>(ob.ekey, no, w.stale_src, w.flag, w.stale, w.fsrc);
+    c.kernels++;
+    RKCHK(cudaMemcpyAsync(w.stale_src, w.fsrc, (size_t)std::max<int64_t>(nstale, 1) * sizeof(int64_t),
+                          cudaMemcpyDeviceToDevice, st));
+  }
+  const int64_t nf = nstale + ncand;
+  if ((rc = ensure_entry_capacity(c, 1 - c.cur, nf))) return rc;
+  if (nf > 0) {
+    k_merge<<<nblk(nf, 256), 256, 0, st>>>(w.stale, w.stale_src, nstale, w.cand, ncand, ob.ekey, no, w.fkey, w.fsrc);
+    k_fill<<<nblk(nf, 256), 256, 0, st>>>(s, nf, w.fkey, w.fsrc, c.eb[c.cur], c.eb[1 - c.cur]);
+    c.kernels += 2;
+  }
+  c.cur = 1 - c.cur;
+  s.ne = nf;
+  bind_entries(c);
+  // ---- index structures
+  need_tmp = (int64_t)sort_temp_bytes(nf);
+  if ((rc = ensure_tmp(c, need_tmp))) return rc;
+  k_iofs<<<nblk(N + 1, 256), 256, 0, st>>>(s.ekey, nf, N, s.iofs);
+  c.kernels++;
+  if (nf > 0) {
+    k_jkeys<<<nblk(nf, 256), 256, 0, st>>>(s.ej, nf, w.jkeys);
+    radix_sort_u64(w.jkeys, w.jtmp, nf, 27, 51, w.tmp, st);
+    k_jlist<<<nblk(nf, 256), 256, 0, st>>>(w.jkeys, nf, s.jlist);
+    c.kernels += 11;
+  }
+  k_jofs<<<nblk(N + 1, 256), 256, 0, st>>>(w.jkeys, nf, N, s.jofs);
+  c.kernels++;
+  RKCHK(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace rk

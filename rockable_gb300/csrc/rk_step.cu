@@ -1,0 +1,695 @@
+// rk_step.cu -- per-step kernels of the FP64 engine (velocity-Verlet step of
+// Rockable::velocityVerletStep with the accelerations() pipeline).
+//
+// Kernel sequence of one step:
+//   controls_pre  (1 thread)        servo + driven bodies        Rockable.cpp:1979-2033, DrivingSystem.cpp:251-268
+//   drift         (thread / body)   first half-kick + drift      Rockable.cpp:2036-2055
+//   glob_vertices (thread / vertex) global vertex positions      Particle.cpp:55-65
+//   narrow_force  (thread / entry)  update + force law + f, M    Interaction.cpp:143-326, ForceLaw_*.cpp,
+//                                                                Rockable.cpp:2934-3046, 2752-2789
+//   gather_accel  (thread / body)   ordered resultants, Newton-  Rockable.cpp:3220-3275, 3419-3552,
+//                                   Euler, second half-kick      3806-3868, 2131-2155
+//   bond_break / iface_break        postponed bond rupture       Rockable.cpp:3350-3413
+//
+// Bit parity: compiled with --fmad=false; the resultant of every body is
+// summed in the reference's serial order (entries in key order), so the FP64
+// form reproduces the CPU path bit for bit.
+#include <cstdio>
+
+#include "../../include/rk_gpu.h"
+#include "rk_engine.cuh"
+
+namespace rk {
+
+__device__ __forceinline__ V3 ld3(const double* a, int64_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
+__device__ __forceinline__ void st3(double* a, int64_t k, V3 v) {
+  a[3 * k] = v.x;
+  a[3 * k + 1] = v.y;
+  a[3 * k + 2] = v.z;
+}
+__device__ __forceinline__ Q4 ldq(const double* a, int64_t k) {
+  return q4(a[4 * k], a[4 * k + 1], a[4 * k + 2], a[4 * k + 3]);
+}
+__device__ __forceinline__ void stq(double* a, int64_t k, Q4 q) {
+  a[4 * k] = q.s;
+  a[4 * k + 1] = q.v.x;
+  a[4 * k + 2] = q.v.y;
+  a[4 * k + 3] = q.v.z;
+}
+
+// ----------------------------------------------------------------- K0 ----
+__global__ void k_controls_pre(Scene s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (s.servo_kind == 1) {  // tritriIsostaticCompression
+    const int* w = s.servo_walls;
+    const double Xmin = s.pos[3 * w[0] + 0] + s.rad[w[0]];
+    const double Xmax = s.pos[3 * w[1] + 0] - s.rad[w[1]];
+    const double Ymin = s.pos[3 * w[2] + 1] + s.rad[w[2]];
+    const double Ymax = s.pos[3 * w[3] + 1] - s.rad[w[3]];
+    const double Zmin = s.pos[3 * w[4] + 2] + s.rad[w[4]];
+    const double Zmax = s.pos[3 * w[5] + 2] - s.rad[w[5]];
+    const double dX = fabs(Xmax - Xmin), dY = fabs(Ymax - Ymin), dZ = fabs(Zmax - Zmin);
+    const double surfX = dY * dZ, surfY = dX * dZ, surfZ = dY * dX;
+    s.controls[s.servo_icontr + 1].value = -s.servo_p * surfX;
+    s.controls[s.servo_icontr + 3].value = -s.servo_p * surfY;
+    s.controls[s.servo_icontr + 5].value = -s.servo_p * surfZ;
+  }
+  // velocityControlledDrive (Rockable.cpp:1856-1900)
+  for (int k = 0; k < s.ncontrols; k++) {
+    const Control c = s.controls[k];
+    int b = c.body;
+    switch (c.type) {
+      case RK_X_VEL: s.vel[3 * b] = c.value; s.pos[3 * b] += s.dt * c.value; break;
+      case RK_Y_VEL: s.vel[3 * b + 1] = c.value; s.pos[3 * b + 1] += s.dt * c.value; break;
+      case RK_Z_VEL: s.vel[3 * b + 2] = c.value; s.pos[3 * b + 2] += s.dt * c.value; break;
+      case RK_XROT_VEL: case RK_YROT_VEL: case RK_ZROT_VEL: case RK_XYZROT_VEL: {
+        V3 w;
+        if (c.type == RK_XROT_VEL) w = v3(c.value, 0.0, 0.0);
+        else if (c.type == RK_YROT_VEL) w = v3(0.0, c.value, 0.0);
+        else if (c.type == RK_ZROT_VEL) w = v3(0.0, 0.0, c.value);
+        else w = v3(c.vec[0], c.vec[1], c.vec[2]);
+        Q4 q = ldq(s.Q, b);
+        qaddscaled(q, qdot(q, w), s.dt);
+        qnormalize(q);
+        stq(s.Q, b, q);
+      } break;
+      default: break;
+    }
+  }
+  // force-driven components (Rockable.cpp:1988-2033)
+  for (int k = 0; k < s.ncontrols; k++) {
+    const Control c = s.controls[k];
+    int b = c.body;
+    switch (c.type) {
+      case RK_X_FOR: case RK_Y_FOR: case RK_Z_FOR: {
+        int d = c.type - RK_X_FOR;
+        s.pos[3 * b + d] += s.dt * s.vel[3 * b + d] + s.dt2_2 * s.acc[3 * b + d];
+        s.vel[3 * b + d] += s.dt_2 * s.acc[3 * b + d];
+      } break;
+      case RK_XROT_MOM: case RK_YROT_MOM: case RK_ZROT_MOM: case RK_XYZROT_MOM: {
+        V3 wr = ld3(s.vrot, b), ar = ld3(s.arot, b);
+        V3 w;
+        if (c.type == RK_XROT_MOM) w = wr.x * v3(1.0, 0.0, 0.0);
+        else if (c.type == RK_YROT_MOM) w = wr.y * v3(0.0, 1.0, 0.0);
+        else if (c.type == RK_ZROT_MOM) w = wr.z * v3(0.0, 0.0, 1.0);
+        else w = wr;
+        Q4 q = ldq(s.Q, b);
+        qaddscaled(q, qdot(q, w), s.dt);
+        qnormalize(q);
+        stq(s.Q, b, q);
+        if (c.type == RK_XROT_MOM) wr.x += s.dt_2 * ar.x;
+        else if (c.type == RK_YROT_MOM) wr.y += s.dt_2 * ar.y;
+        else if (c.type == RK_ZROT_MOM) wr.z += s.dt_2 * ar.z;
+        else wr = wr + s.dt_2 * ar;
+        st3(s.vrot, b, wr);
+      } break;
+      default: break;
+    }
+  }
+}
+
+// ----------------------------------------------------------------- K1 ----
+__global__ void k_drift(Scene s) {
+  int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.n) return;
+  V3 p = ld3(s.pos, i), v = ld3(s.vel, i), a = ld3(s.acc, i);
+  V3 w = ld3(s.vrot, i), al = ld3(s.arot, i);
+  Q4 q = ldq(s.Q, i);
+  p = p + (s.dt * v + s.dt2_2 * a);
+  v = v + s.dt_2 * a;
+  qaddscaled(q, qdot(q, w), s.dt);
+  qaddscaled(q, qddot(q, w, al), s.dt2_2);
+  qnormalize(q);
+  w = w + s.dt_2 * al;
+  st3(s.pos, i, p);
+  st3(s.vel, i, v);
+  stq(s.Q, i, q);
+  st3(s.vrot, i, w);
+}
+
+// global vertex k of body b: pos + Q (h v)
+__global__ void k_glob_vertices(Scene s) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= s.nvert) return;
+  int b = s.gv_body[k];
+  int local = (int)(k - s.gv_ofs[b]);
+  int sh = s.shape[b];
+  double h = s.hom[b];
+  const double* sv = s.svert + 3 * (int64_t)(s.vert_ofs[sh] + local);
+  V3 u = h * v3(sv[0], sv[1], sv[2]);
+  V3 g = ld3(s.pos, b) + qrot(ldq(s.Q, b), u);
+  st3(s.gv, k, g);
+}
+
+// --------------------------------------------------------- force laws ----
+struct LawIn {
+  double dn, dn_old, damp;
+  V3 n, vel, cpos;
+  V3 wi, wj, xi, xj;
+  bool i_driven;
+  int gi, gj;     // groups
+  int ci, cj;     // clusters
+  int bond;
+};
+
+__device__ __forceinline__ void law_default(const Scene& s, const LawIn& L, double& fn, V3& ft, V3& mom) {
+  if (L.dn > 0.0) { fn = 0.0; ft = v3(0, 0, 0); mom = v3(0, 0, 0); return; }
+  const double* P = s.table[L.gi * s.ngroup + L.gj].p;
+  double kn = P[RK_P_KN], kt = P[RK_P_KT], mu = P[RK_P_MU], kr = P[RK_P_KR], mur = P[RK_P_MUR];
+  double vn = dot(L.vel, L.n);
+  double fne = -kn * L.dn;
+  double fnv = L.damp * vn;
+  fn = fne + fnv;
+  if (fn < 0.0) fn = 0.0;
+  V3 vt = L.vel - vn * L.n;
+  ft = ft + kt * (vt * s.dt);
+  double threshold = fabs(mu * fne);
+  double ft2 = dot(ft, ft);
+  if (ft2 > 0.0 && ft2 >= threshold * threshold) ft = ft * (threshold / sqrt(ft2));
+  if (kr > 0.0) {
+    mom = mom + (kr * (L.wj - L.wi)) * s.dt;
+    double thr = fabs(mur * fn);
+    double m2 = dot(mom, mom);
+    if (m2 > 0.0 && m2 >= thr * thr) mom = mom * (thr / sqrt(m2));
+  }
+}
+
+__device__ __forceinline__ void law_avalanche(const Scene& s, const LawIn& L, double& fn, V3& ft, V3& mom) {
+  if (L.dn > 0.0) { fn = 0.0; ft = v3(0, 0, 0); mom = v3(0, 0, 0); return; }
+  const double* P = s.table[L.gi * s.ngroup + L.gj].p;
+  double kn = P[RK_P_KN], en2 = P[RK_P_EN2], kt = P[RK_P_KT], mu = P[RK_P_MU], kr = P[RK_P_KR], mur = P[RK_P_MUR];
+  double prev_dn = L.dn_old;
+  if (prev_dn > 0.0) prev_dn = 0.0;
+  double ddn = L.dn - prev_dn;
+  if (ddn > 0.0) fn = -kn * en2 * L.dn;
+  else if (ddn < 0.0) fn = fn + -kn * ddn;
+  if (fn < 0.0) fn = 0.0;
+  V3 vt = L.vel - dot(L.vel, L.n) * L.n;
+  ft = ft + kt * (s.dt * vt);
+  double thr = fabs(mu * fn);
+  double ft2 = dot(ft, ft);
+  if (ft2 > 0.0 && ft2 > thr * thr) ft = ft * (thr / sqrt(ft2));
+  mom = mom + (kr * (L.wj - L.wi)) * s.dt;
+  V3 branch;
+  if (L.i_driven) {
+    branch = L.cpos - L.xj;
+    double r = dot(branch, L.wj) / dot(L.wj, L.wj);
+    branch = branch - r * L.wj;
+  } else {
+    branch = L.cpos - L.xi;
+    double r = dot(branch, L.wi) / dot(L.wi, L.wi);
+    branch = branch - r * L.wi;
+  }
+  double thm = fabs(mur * sqrt(norm2(branch)) * fn);
+  double m2 = dot(mom, mom);
+  if (m2 > 0.0 && m2 > thm * thm) mom = mom * (thm / sqrt(m2));
+}
+
+__device__ __forceinline__ void law_sticked(const Scene& s, const LawIn& L, double& fn, V3& ft, V3& mom) {
+  if (L.bond >= 0) {
+    double kn, kt, kr, fn0, ft0, mom0, power;
+    double dn0 = s.if_dn0[L.bond];
+    bool inner = (L.ci == L.cj);
+    if (s.params_in_interfaces == 1) {
+      const double* q = s.if_par + 8 * (int64_t)L.bond;
+      kn = q[0]; kt = q[1]; kr = q[2]; fn0 = q[3]; ft0 = q[4]; mom0 = q[5]; power = q[6];
+    } else {
+      const double* P = s.table[L.gi * s.ngroup + L.gj].p;
+      if (inner) {
+        kn = P[RK_P_KN_IN]; kt = P[RK_P_KT_IN]; kr = P[RK_P_KR_IN]; fn0 = P[RK_P_FN0_IN]; ft0 = P[RK_P_FT0_IN];
+        mom0 = P[RK_P_MOM0_IN]; power = P[RK_P_POW_IN];
+        dn0 = 0.0;
+      } else {
+        kn = P[RK_P_KN_OUT]; kt = P[RK_P_KT_OUT]; kr = P[RK_P_KR_OUT]; fn0 = P[RK_P_FN0_OUT]; ft0 = P[RK_P_FT0_OUT];
+        mom0 = P[RK_P_MOM0_OUT]; power = P[RK_P_POW_OUT];
+      }
+    }
+    double vn = dot(L.vel, L.n);
+    double fne = -kn * (L.dn - dn0);
+    double fnv = L.damp * vn;
+    fn = fne + fnv;
+    V3 vt = (L.vel - (vn * L.n));
+    ft = ft + kt * (vt * s.dt);
+    V3 ftv = L.damp * vt;
+    ft = ft + ftv;
+    mom = mom + (kr * (L.wj - L.wi)) * s.dt;
+    double yield = pow(sqrt(norm2(ft)) / ft0, power) + pow(sqrt(norm2(mom)) / mom0, power) - fn / fn0 - 1.0;
+    if (yield > 0.0) s.if_break[L.bond] = 1;
+  } else {
+    if (L.dn > 0.0) { fn = 0.0; ft = v3(0, 0, 0); mom = v3(0, 0, 0); return; }
+    const double* P = s.table[L.gi * s.ngroup + L.gj].p;
+    double kn = P[RK_P_KN], kt = P[RK_P_KT], mu = P[RK_P_MU], kr = P[RK_P_KR], mur = P[RK_P_MUR];
+    double vn = dot(L.vel, L.n);
+    double fne = -kn * L.dn;
+    double fnv = L.damp * vn;
+    fn = fne + fnv;
+    if (fn < 0.0) fn = 0.0;
+    V3 vt = L.vel - vn * L.n;
+    ft = ft + kt * (vt * s.dt);
+    double thr = fabs(mu * fn);
+    double ft2 = dot(ft, ft);
+    if (ft2 > 0.0 && ft2 >= thr * thr) ft = ft * (thr / sqrt(ft2));
+    mom = mom + (kr * (L.wj - L.wi)) * s.dt;
+    double thm = fabs(mur * fn);
+    double m2 = dot(mom, mom);
+    if (m2 > 0.0 && m2 >= thm * thm) mom = mom * (thm / sqrt(m2));
+  }
+}
+
+// ----------------------------------------------------------------- K2 ----
+__device__ __forceinline__ V3 gvx(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
+
+__global__ void k_narrow_force(Scene s) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool active = false;
+  if (e < s.ne) {
+    const int i = s.ei[e], j = s.ej[e];
+    const uint32_t ts = s.etsub[e];
+    const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);
+    const double dn_old = s.dn[e];
+    const int bond = s.bond[e];
+    const double* gi = s.gv + 3 * s.gv_ofs[i];
+    const double* gj = s.gv + 3 * s.gv_ofs[j];
+    const double Ri = s.rad[i], Rj = s.rad[j];
+    V3 n = v3(0, 0, 0), cpos = v3(0, 0, 0);
+    double dn = 0.0;
+    bool ok = true;
+    if (type == 0) {  // vertex-vertex
+      V3 a = gvx(gi, isub), b = gvx(gj, jsub);
+      n = a - b;
+      dn = normalize(n) - (Ri + Rj);
+      cpos = a - n * (Ri + 0.5 * dn);
+    } else if (type == 1) {  // vertex-edge
+      const int sj = s.shape[j];
+      const int eo = s.edge_ofs[sj] + jsub;
+      V3 p1 = gvx(gj, s.edges[2 * eo]), p2 = gvx(gj, s.edges[2 * eo + 1]);
+      V3 a = gvx(gi, isub);
+      V3 E = p2 - p1, v = a - p1;
+      double r = dot(v, E) / dot(E, E);
+      if (r <= 0.0 || r >= 1.0) {
+        ok = false;
+      } else {
+        n = a - (p1 + r * E);
+        dn = normalize(n) - (Ri + Rj);
+        cpos = a - n * (Ri + 0.5 * dn);
+      }
+    } else if (type == 2) {  // vertex-face
+      const int sj = s.shape[j];
+      const int fo = s.face_ofs[sj] + jsub;
+      const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
+      const int* fv = s.face_verts + v0;
+      V3 A = gvx(gj, fv[0]), B = gvx(gj, fv[1]), C = gvx(gj, fv[nbv - 1]);
+      V3 a = gvx(gi, isub);
+      V3 v = a - A;
+      V3 v1 = B - A;
+      normalize(v1);
+      V3 v2 = C - A;
+      n = cross(v1, v2);
+      normalize(n);
+      double dist = dot(v, n);
+      if (dist < 0.0) { n = -n; dist = -dist; }
+      V3 P = a - dist * n;
+      int odd = 0;
+      v2 = cross(n, v1);
+      double ori1 = dot(P, v1), ori2 = dot(P, v2);
+      for (int iva = 0; iva < nbv; ++iva) {
+        int ivb = iva + 1;
+        if (ivb == nbv) ivb = 0;
+        V3 pa = gvx(gj, fv[iva]), pb = gvx(gj, fv[ivb]);
+        double pa1 = dot(pa, v1), pb1 = dot(pb, v1), pa2 = dot(pa, v2), pb2 = dot(pb, v2);
+        if ((pa2 < ori2 && pb2 >= ori2) || (pb2 < ori2 && pa2 >= ori2)) {
+          if (pa1 + (ori2 - pa2) / (pb2 - pa2) * (pb1 - pa1) < ori1) odd = 1 - odd;
+        }
+      }
+      if (odd) {
+        dn = dist - (Ri + Rj);
+        cpos = a - n * (Ri + 0.5 * dn);
+      } else {
+        ok = false;
+      }
+    } else {  // edge-edge
+      const int si = s.shape[i], sj = s.shape[j];
+      const int eoi = s.edge_ofs[si] + isub, eoj = s.edge_ofs[sj] + jsub;
+      V3 pi1 = gvx(gi, s.edges[2 * eoi]), pi2 = gvx(gi, s.edges[2 * eoi + 1]);
+      V3 pj1 = gvx(gj, s.edges[2 * eoj]), pj2 = gvx(gj, s.edges[2 * eoj + 1]);
+      V3 Ei = pi2 - pi1, Ej = pj2 - pj1, v = pi1 - pj1;
+      double c = dot(Ei, Ei), d = dot(Ej, Ej), ee = dot(Ei, Ej);
+      double f = (c * d) - (ee * ee);
+      if (fabs(f) > 1.0e-12) {
+        f = 1.0 / f;
+        double a = dot(Ei, v), b = dot(Ej, v);
+        double ss = (ee * b - a * d) * f;
+        double tt = (c * b - ee * a) * f;
+        if (ss <= 0.0 || ss >= 1.0 || tt <= 0.0 || tt >= 1.0) {
+          ok = false;
+        } else {
+          n = (pi1 + ss * Ei) - (pj1 + tt * Ej);
+          dn = normalize(n) - (Ri + Rj);
+          cpos = pi1 + ss * Ei - n * (Ri + 0.5 * dn);
+        }
+      } else {
+        ok = false;
+      }
+    }
+    const V3 xi = ld3(s.pos, i), xj = ld3(s.pos, j);
+    const V3 wi = ld3(s.vrot, i), wj = ld3(s.vrot, j);
+    V3 cvel;
+    double fn;
+    V3 ft, mom;
+    if (ok) {
+      const V3 vi = ld3(s.vel, i), vj = ld3(s.vel, j);
+      cvel = (vj - cross(cpos - xj, wj)) - (vi - cross(cpos - xi, wi));
+      fn = s.fn[e];
+      ft = ld3(s.ft, e);
+      mom = ld3(s.mom, e);
+      if (s.record_geom || bond >= 0) {
+        st3(s.gn, e, n);
+        st3(s.gpos, e, cpos);
+        st3(s.gvel, e, cvel);
+      }
+    } else {  // Interaction::deactivate (Interaction.cpp:123-128)
+      dn = 0.0;
+      fn = 0.0;
+      ft = v3(0, 0, 0);
+      mom = v3(0, 0, 0);
+      if (bond >= 0) {  // a bonded entry stays active with its previous geometry
+        n = ld3(s.gn, e);
+        cpos = ld3(s.gpos, e);
+        cvel = ld3(s.gvel, e);
+      } else {
+        cvel = v3(0, 0, 0);
+      }
+    }
+    active = (dn < 0.0 || bond >= 0);
+    if (active) {
+      LawIn L;
+      L.dn = dn; L.dn_old = ok ? dn_old : 0.0; L.damp = s.damp[e];
+      L.n = n; L.vel = cvel; L.cpos = cpos;
+      L.wi = wi; L.wj = wj; L.xi = xi; L.xj = xj;
+      L.i_driven = i < s.n_driven;
+      L.gi = s.group[i]; L.gj = s.group[j];
+      L.ci = s.cluster[i]; L.cj = s.cluster[j];
+      L.bond = bond;
+      if (s.law == RK_LAW_AVALANCHE) law_avalanche(s, L, fn, ft, mom);
+      else if (s.law == RK_LAW_STICKEDLINKS) law_sticked(s, L, fn, ft, mom);
+      else law_default(s, L, fn, ft, mom);
+      // Rockable::incrementResultants (Rockable.cpp:2752-2789)
+      V3 f = fn * n + ft;
+      V3 Ci = (cpos - xi), Cj = (cpos - xj);
+      st3(s.cf, e, f);
+      st3(s.cmi, e, cross(Ci, f) + mom);
+      st3(s.cmj, e, cross(Cj, -f) - mom);
+    }
+    s.dn[e] = dn;
+    if (active || !ok) {
+      s.fn[e] = fn;
+      st3(s.ft, e, ft);
+      st3(s.mom, e, mom);
+    }
+    s.act[e] = active ? 1 : 0;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, active);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(&s.flags[FLAG_NACTIVE], (unsigned long long)__popc(m));
+}
+
+// ----------------------------------------------------------------- K3 ----
+__device__ __forceinline__ V3 euler_domega(V3 I, V3 w, V3 M) {
+  return v3((M.x - (I.z - I.y) * w.y * w.z) / I.x, (M.y - (I.x - I.z) * w.z * w.x) / I.y,
+            (M.z - (I.y - I.x) * w.x * w.y) / I.z);
+}
+
+__global__ void k_gather_accel(Scene s, int apply_kick) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= s.n) return;
+  const bool driven = b < s.n_driven;
+  V3 F = v3(0, 0, 0), M = v3(0, 0, 0);
+  if (driven) {  // imposed force / moment components (Rockable.cpp:2904-2928)
+    for (int k = 0; k < s.ncontrols; k++) {
+      const Control c = s.controls[k];
+      if (c.body != b) continue;
+      switch (c.type) {
+        case RK_X_FOR: F.x = c.value; break;
+        case RK_Y_FOR: F.y = c.value; break;
+        case RK_Z_FOR: F.z = c.value; break;
+        case RK_XROT_MOM: M.x = c.value; break;
+        case RK_YROT_MOM: M.y = c.value; break;
+        case RK_ZROT_MOM: M.z = c.value; break;
+        case RK_XYZROT_MOM: M = v3(c.vec[0], c.vec[1], c.vec[2]); break;
+        default: break;
+      }
+    }
+  }
+  // Resultants in the serial order of the active entries (key order): the
+  // j-side entries before b's own block, b's block, the remaining j-side.
+  const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
+  int64_t jk = s.jofs[b];
+  const int64_t j1 = s.jofs[b + 1];
+  for (; jk < j1; ++jk) {
+    const int e = s.jlist[jk];
+    if (e >= i0) break;
+    if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
+  }
+  for (int64_t e = i0; e < i1; ++e)
+    if (s.act[e]) { F = F + ld3(s.cf, e); M = M + ld3(s.cmi, e); }
+  for (; jk < j1; ++jk) {
+    const int e = s.jlist[jk];
+    if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
+  }
+  const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
+  const V3 vel = ld3(s.vel, b), vrot = ld3(s.vrot, b);
+  const double mass = s.mass[b];
+  const V3 inertia = ld3(s.inertia, b);
+  const Q4 q = ldq(s.Q, b);
+  if (driven) {
+    V3 acc = v3(0, 0, 0), arot = v3(0, 0, 0);
+    if (s.num_damp > 0.0) {  // Rockable.cpp:3814-3835
+      for (int k = 0; k < s.ncontrols; k++) {
+        const Control c = s.controls[k];
+        if (c.body != b) continue;
+        if (c.type == RK_X_FOR) F.x *= (F.x * vel.x > 0.0) ? fm : fp;
+        else if (c.type == RK_Y_FOR) F.y *= (F.y * vel.y > 0.0) ? fm : fp;
+        else if (c.type == RK_Z_FOR) F.z *= (F.z * vel.z > 0.0) ? fm : fp;
+      }
+    }
+    for (int k = 0; k < s.ncontrols; k++) {  // Rockable.cpp:3448-3507
+      const Control c = s.controls[k];
+      if (c.body != b) continue;
+      switch (c.type) {
+        case RK_X_FOR: acc.x = F.x / mass; break;
+        case RK_Y_FOR: acc.y = F.y / mass; break;
+        case RK_Z_FOR: acc.z = F.z / mass; break;
+        case RK_XROT_MOM: case RK_YROT_MOM: case RK_ZROT_MOM: case RK_XYZROT_MOM: {
+          Q4 qi = qconj(q);
+          V3 w;
+          if (c.type == RK_XROT_MOM) w = v3(vrot.x, 0.0, 0.0);
+          else if (c.type == RK_YROT_MOM) w = v3(0.0, vrot.y, 0.0);
+          else if (c.type == RK_ZROT_MOM) w = v3(0.0, 0.0, vrot.z);
+          else w = vrot;
+          V3 om = qrot(qi, w);
+          V3 Mb = qrot(qi, M);
+          V3 dw = qrot(q, euler_domega(inertia, om, Mb));
+          if (c.type == RK_XROT_MOM) arot.x = dw.x;
+          else if (c.type == RK_YROT_MOM) arot.y = dw.y;
+          else if (c.type == RK_ZROT_MOM) arot.z = dw.z;
+          else arot = dw;
+        } break;
+        default: break;
+      }
+    }
+    V3 v = vel, wr = vrot;
+    if (apply_kick) {  // Rockable.cpp:2084-2117
+      for (int k = 0; k < s.ncontrols; k++) {
+        const Control c = s.controls[k];
+        if (c.body != b) continue;
+        switch (c.type) {
+          case RK_X_FOR: v.x += s.dt_2 * acc.x; break;
+          case RK_Y_FOR: v.y += s.dt_2 * acc.y; break;
+          case RK_Z_FOR: v.z += s.dt_2 * acc.z; break;
+          case RK_XROT_MOM: wr.x += s.dt_2 * arot.x; break;
+          case RK_YROT_MOM: wr.y += s.dt_2 * arot.y; break;
+          case RK_ZROT_MOM: wr.z += s.dt_2 * arot.z; break;
+          case RK_XYZROT_MOM: wr = wr + s.dt_2 * arot; break;
+          default: break;
+        }
+      }
+    }
+    st3(s.acc, b, acc);
+    st3(s.arot, b, arot);
+    st3(s.vel, b, v);
+    st3(s.vrot, b, wr);
+  } else {
+    if (s.num_damp > 0.0) {  // Rockable.cpp:3837-3866
+      double factor = (dot(F, vel) > 0.0) ? fm : fp;
+      F = F * factor;
+      factor = (dot(M, vrot) > 0.0) ? fm : fp;
+      M = M * factor;
+    }
+    V3 acc = vdiv(F, mass) + v3(s.gravity[0], s.gravity[1], s.gravity[2]);
+    Q4 qi = qconj(q);
+    V3 om = qrot(qi, vrot);
+    V3 Mb = qrot(qi, M);
+    V3 arot = qrot(q, euler_domega(inertia, om, Mb));
+    st3(s.acc, b, acc);
+    st3(s.arot, b, arot);
+    if (apply_kick) {
+      st3(s.vel, b, vel + s.dt_2 * acc);
+      st3(s.vrot, b, vrot + s.dt_2 * arot);
+    }
+  }
+  st3(s.force, b, F);
+  st3(s.moment, b, M);
+}
+
+// ----------------------------------------------------------------- K4 ----
+__global__ void k_bond_break(Scene s) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= s.ne) return;
+  int bond = s.bond[e];
+  if (bond < 0 || !s.if_break[bond]) return;
+  s.bond[e] = -1;
+  if (s.dn[e] >= 0.0) {
+    s.fn[e] = 0.0;
+    st3(s.ft, e, v3(0, 0, 0));
+  } else {
+    V3 T = ld3(s.ft, e);
+    double FT = normalize(T);
+    int gi = s.group[s.if_i[bond]], gj = s.group[s.if_j[bond]];
+    double mu = s.table[gi * s.ngroup + gj].p[RK_P_MU];
+    double thr = fabs(mu * s.fn[e]);
+    if (FT > thr) st3(s.ft, e, thr * T);
+  }
+}
+
+__global__ void k_iface_break(Scene s) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= s.nif) return;
+  if (!s.if_break[k]) return;
+  s.if_break[k] = 0;
+  if (!s.if_broken[k]) {
+    s.if_broken[k] = 1;
+    atomicAdd(&s.flags[FLAG_NBROKEN], 1ull);
+    s.flags[FLAG_NEED_UPDATE] = 1ull;
+  }
+}
+
+// ---------------------------------------------------- dynamic NL guard ----
+// Rockable.cpp:1571-1596: accumulated displacement and rotation since the
+// last guard-triggered update; running maxima are kept in the flag block.
+__global__ void k_guard(Scene s) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double t1 = 0.0, t2 = 0.0;
+  if (i < s.n) {
+    V3 dp = ld3(s.dpos, i);
+    Q4 dq = ldq(s.dq, i);
+    if (s.flags[FLAG_GRESET]) {
+      dp = v3(0, 0, 0);
+      dq = q4(1.0, 0.0, 0.0, 0.0);
+    }
+    dp = dp + ld3(s.vel, i) * s.dt;
+    t1 = norm2(dp);
+    qaddscaled(dq, qdot(ldq(s.Q, i), ld3(s.vrot, i)), s.dt);
+    t2 = qangle(dq);
+    st3(s.dpos, i, dp);
+    stq(s.dq, i, dq);
+  }
+  // both are >= 0: the IEEE bit patterns order like the values
+  for (int o = 16; o > 0; o >>= 1) {
+    t1 = fmax(t1, __shfl_xor_sync(0xffffffffu, t1, o));
+    t2 = fmax(t2, __shfl_xor_sync(0xffffffffu, t2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&s.flags[FLAG_GPOS], (unsigned long long)__double_as_longlong(t1));
+    atomicMax(&s.flags[FLAG_GROT], (unsigned long long)__double_as_longlong(t2));
+  }
+}
+
+__global__ void k_guard_finalize(Scene s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  s.flags[FLAG_GRESET] = 0ull;
+  double mp = sqrt(__longlong_as_double((long long)s.flags[FLAG_GPOS]));
+  double mr = __longlong_as_double((long long)s.flags[FLAG_GROT]);
+  if (mp >= s.disp_update || mr >= s.angle_update) {
+    s.flags[FLAG_NEED_UPDATE] = 1ull;
+    s.flags[FLAG_GRESET] = 1ull;
+    s.flags[FLAG_GPOS] = 0ull;
+    s.flags[FLAG_GROT] = 0ull;
+  }
+}
+
+// kinetic energies (Rockable.cpp:3958-3970), two partial sums per block
+__global__ void k_kinetic(Scene s, double* out) {
+  __shared__ double sh[2][256];
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double et = 0.0, er = 0.0;
+  if (i < s.n) {
+    V3 v = ld3(s.vel, i);
+    et = s.mass[i] * dot(v, v);
+    V3 w = qrot(qconj(ldq(s.Q, i)), ld3(s.vrot, i));
+    V3 I = ld3(s.inertia, i);
+    er = I.x * w.x * w.x + I.y * w.y * w.y + I.z * w.z * w.z;
+  }
+  sh[0][threadIdx.x] = et;
+  sh[1][threadIdx.x] = er;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[2 * blockIdx.x] = sh[0][0];
+    out[2 * blockIdx.x + 1] = sh[1][0];
+  }
+}
+
+// ------------------------------------------------------------ launchers ----
+static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int launch_controls_pre(const Scene& s, cudaStream_t st) {
+  if (s.ncontrols == 0 && s.servo_kind == 0) return 0;
+  k_controls_pre<<<1, 32, 0, st>>>(s);
+  return 1;
+}
+int launch_drift(const Scene& s, cudaStream_t st) {
+  int64_t nf = s.n - s.n_driven;
+  if (nf <= 0) return 0;
+  k_drift<<<nblk(nf, 128), 128, 0, st>>>(s);
+  return 1;
+}
+int launch_glob_vertices(const Scene& s, cudaStream_t st) {
+  if (s.nvert <= 0) return 0;
+  k_glob_vertices<<<nblk(s.nvert, 256), 256, 0, st>>>(s);
+  return 1;
+}
+int launch_narrow_force(const Scene& s, cudaStream_t st) {
+  if (s.ne <= 0) return 0;
+  k_narrow_force<<<nblk(s.ne, 128), 128, 0, st>>>(s);
+  return 1;
+}
+int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
+  if (s.n <= 0) return 0;
+  k_gather_accel<<<nblk(s.n, 128), 128, 0, st>>>(s, apply_kick);
+  return 1;
+}
+int launch_breakage(const Scene& s, cudaStream_t st) {
+  if (s.nif <= 0) return 0;
+  int k = 0;
+  if (s.ne > 0) { k_bond_break<<<nblk(s.ne, 256), 256, 0, st>>>(s); k++; }
+  k_iface_break<<<nblk(s.nif, 256), 256, 0, st>>>(s);
+  return k + 1;
+}
+int launch_guard(const Scene& s, cudaStream_t st) {
+  if (s.n <= 0) return 0;
+  k_guard<<<nblk(s.n, 128), 128, 0, st>>>(s);
+  k_guard_finalize<<<1, 32, 0, st>>>(s);
+  return 2;
+}
+int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st) {
+  if (s.n <= 0) return 0;
+  k_kinetic<<<nblk(s.n, 256), 256, 0, st>>>(s, d_out2);
+  return (int)nblk(s.n, 256);
+}
+
+}  // namespace rk

@@ -1,0 +1,290 @@
+"""Seeded synthetic scenes of the benchmark workloads.
+
+Rockable ships no benchmark inputs; these generators build scenes with the
+shapes, sizes and value distributions of the workloads the engine is measured
+on, as numpy arrays ready for the C ABI, and can write them as Rockable
+`.conf` / `.shp` files (Rockable.cpp:440-610, Shape.cpp:130-170 formats) so
+that the reference CPU path reads exactly the same scene.
+
+Grains are convex sphero-polyhedra: the convex hull of k ~ U{8..20} points on
+an ellipsoid, Minkowski-summed with a sphere of radius 5% of the smallest
+semi-axis.  Vertices are expressed in the principal frame of inertia, like
+Rockable's shape library requires (Shape.hpp:60-62).
+"""
+import math
+import os
+
+import numpy as np
+
+SEED = 20261203
+
+
+# ------------------------------------------------------------------ shapes --
+def _hull(points):
+    from scipy.spatial import ConvexHull
+    h = ConvexHull(points)
+    used = np.unique(h.simplices)
+    remap = -np.ones(len(points), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    verts = points[used]
+    tris = remap[h.simplices]
+    # outward orientation
+    c = verts.mean(axis=0)
+    for t in tris:
+        a, b, d = verts[t[0]], verts[t[1]], verts[t[2]]
+        if np.dot(np.cross(b - a, d - a), a - c) < 0:
+            t[1], t[2] = t[2], t[1]
+    return verts, tris
+
+
+def _mass_properties(verts, tris):
+    """Volume, centroid and inertia tensor (unit density) of a closed
+    triangulated polyhedron, by signed tetrahedra from the origin."""
+    V = 0.0
+    C = np.zeros(3)
+    J = np.zeros((3, 3))  # second moments  int x_i x_j dV
+    for t in tris:
+        a, b, c = verts[t[0]], verts[t[1]], verts[t[2]]
+        v = np.dot(a, np.cross(b, c)) / 6.0
+        V += v
+        C += v * (a + b + c) / 4.0
+        s = a + b + c
+        J += v / 20.0 * (np.outer(a, a) + np.outer(b, b) + np.outer(c, c) + np.outer(s, s))
+    C /= V
+    J -= V * np.outer(C, C)
+    inertia = np.trace(J) * np.eye(3) - J
+    return V, C, inertia
+
+
+def hull_shape(rng, name, kmin=8, kmax=20, semi_lo=0.0025, semi_hi=0.0075, rfrac=0.05):
+    """One convex sphero-polyhedron (dict of the Shape fields)."""
+    while True:
+        k = int(rng.integers(kmin, kmax + 1))
+        ax = rng.uniform(semi_lo, semi_hi, 3)
+        d = rng.normal(size=(k, 3))
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        p = d * ax
+        try:
+            verts, tris = _hull(p)
+        except Exception:
+            continue
+        if len(verts) >= 4:
+            break
+    V, C, I = _mass_properties(verts, tris)
+    verts = verts - C
+    w, R = np.linalg.eigh(I)
+    if np.linalg.det(R) < 0:
+        R[:, 0] = -R[:, 0]
+    verts = verts @ R  # coordinates in the principal frame
+    r = rfrac * float(ax.min())
+    # faces: triangles; edges: unique vertex pairs of the triangles
+    edges = set()
+    for t in tris:
+        for a, b in ((t[0], t[1]), (t[1], t[2]), (t[2], t[0])):
+            edges.add((min(a, b), max(a, b)))
+    edges = sorted(edges)
+    area = sum(0.5 * np.linalg.norm(np.cross(verts[t[1]] - verts[t[0]], verts[t[2]] - verts[t[0]])) for t in tris)
+    vol = V + area * r + 4.0 / 3.0 * math.pi * r ** 3  # rounding shell to first order plus the corner sphere
+    i_over_m = w / V
+    lo = verts.min(axis=0) - r
+    hi = verts.max(axis=0) + r
+    return {"name": name, "radius": r, "volume": vol, "I/m": i_over_m, "vertices": verts, "edges": np.array(edges),
+            "faces": [list(map(int, t)) for t in tris], "obb_center": 0.5 * (lo + hi), "obb_extent": 0.5 * (hi - lo),
+            "bound": float(np.max(np.linalg.norm(verts, axis=1)) + r)}
+
+
+def plate_shape(name, half, r):
+    """A square plate (4 vertices, 1 face) in the z = 0 plane, like the wall
+    shapes of Rockable's test inputs."""
+    v = np.array([[half, half, 0.0], [half, -half, 0.0], [-half, -half, 0.0], [-half, half, 0.0]])
+    return {"name": name, "radius": r, "volume": (2 * half) ** 2 * 2 * r,
+            "I/m": np.array([(2 * half) ** 2 / 12.0, (2 * half) ** 2 / 12.0, (2 * half) ** 2 / 6.0]),
+            "vertices": v, "edges": np.array([[0, 1], [0, 3], [1, 2], [2, 3]]), "faces": [[0, 1, 2, 3]],
+            "obb_center": np.zeros(3), "obb_extent": np.array([half + r, half + r, r]), "bound": half * 1.5 + r}
+
+
+def flatten_shapes(shapes):
+    vo, eo, fo, fvo = [0], [0], [0], [0]
+    verts, edges, fverts, rad, obb = [], [], [], [], []
+    for s in shapes:
+        verts.append(np.asarray(s["vertices"], dtype=np.float64))
+        edges.append(np.asarray(s["edges"], dtype=np.int32).reshape(-1, 2))
+        for f in s["faces"]:
+            fverts.extend(f)
+            fvo.append(len(fverts))
+        vo.append(vo[-1] + len(s["vertices"]))
+        eo.append(eo[-1] + len(s["edges"]))
+        fo.append(fo[-1] + len(s["faces"]))
+        rad.append(s["radius"])
+        obb.extend(list(s["obb_center"]) + [1, 0, 0, 0, 1, 0, 0, 0, 1] + list(s["obb_extent"]))
+    return {"vert_ofs": np.array(vo, np.int32), "vertices": np.concatenate(verts).ravel(),
+            "edge_ofs": np.array(eo, np.int32), "edges": np.concatenate(edges).ravel().astype(np.int32),
+            "face_ofs": np.array(fo, np.int32), "face_vofs": np.array(fvo, np.int32),
+            "face_verts": np.array(fverts, np.int32), "radius": np.array(rad), "obb": np.array(obb, np.float64)}
+
+
+def random_quaternions(rng, n):
+    """Uniform rotations (Shoemake)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    q = np.stack([np.sqrt(u1) * np.cos(2 * np.pi * u3), np.sqrt(1 - u1) * np.sin(2 * np.pi * u2),
+                  np.sqrt(1 - u1) * np.cos(2 * np.pi * u2), np.sqrt(u1) * np.sin(2 * np.pi * u3)], axis=1)
+    return q / np.linalg.norm(q, axis=1)[:, None]
+
+
+# ------------------------------------------------------------------ scenes --
+def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2700.0, kn=1e6, kt=1e6,
+                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), fill=None):
+    """Granular column collapse: n hull grains (axes U[0.5, 1.5] cm, i.e.
+    semi-axes U[0.25, 0.75] cm) on a jittered lattice in a 0.5 x 0.5 x 1.5 m
+    column above a rigid floor plate (the only driven body); the column's side
+    walls are released at t = 0, so they are not part of the scene."""
+    rng = np.random.default_rng(seed)
+    shapes = [plate_shape("FLOOR", 1.5, 0.005)]
+    shapes += [hull_shape(rng, "G%05d" % k) for k in range(nshapes)]
+    bound = max(s["bound"] for s in shapes[1:])
+    spacing = 2.0 * bound * 1.01
+    nx = int(column[0] / spacing)
+    ny = int(column[1] / spacing)
+    nz_needed = int(math.ceil(n / (nx * ny)))
+    nz = max(nz_needed, int(column[2] / spacing))
+    sites = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    sites = sites[np.argsort(sites[:, 2], kind="stable")]
+    if fill is None:
+        pick = np.sort(rng.choice(len(sites), n, replace=False)) if len(sites) > n else np.arange(n)
+    else:
+        pick = np.arange(n)
+    sites = sites[pick]
+    pos = (sites + 0.5) * spacing
+    pos[:, 0] -= 0.5 * nx * spacing
+    pos[:, 1] -= 0.5 * ny * spacing
+    pos[:, 2] += 0.006
+    shape_of = rng.integers(1, nshapes + 1, n)
+    Q = random_quaternions(rng, n)
+    return _assemble(shapes, [np.zeros(3)], [np.array([1.0, 0, 0, 0])], pos, Q, shape_of, density, law, kn, kt, en2,
+                     mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bound, dVerlet=0.1 * bound,
+                     interVerlet=100 * dt, name="column_collapse_%d" % n)
+
+
+def sphero_cube_box(n_side=8, seed=SEED, dt=1e-6):
+    """512 sphero-cubes (side 1 mm, rounding 0.1 mm, density 2700) on an 8x8x8
+    lattice of 1.5 mm spacing with uniform-random orientations, in a rigid box
+    of 6 plates; Default law kn = 1e6 N/m, e_n^2 = 0.25, mu = 0.4."""
+    rng = np.random.default_rng(seed)
+    h = 0.4e-3
+    r = 0.1e-3
+    v = np.array([[sx * h, sy * h, sz * h] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)])
+    tris = []
+    quads = [[0, 1, 3, 2], [4, 6, 7, 5], [0, 4, 5, 1], [2, 3, 7, 6], [0, 2, 6, 4], [1, 5, 7, 3]]
+    edges = sorted({(min(a, b), max(a, b)) for q in quads for a, b in zip(q, q[1:] + q[:1])})
+    side = 2 * h + 2 * r
+    vol = (2 * h) ** 3 + 6 * (2 * h) ** 2 * r + 3 * math.pi * r * r * (2 * h) + 4.0 / 3.0 * math.pi * r ** 3
+    cube = {"name": "CUBE", "radius": r, "volume": vol, "I/m": np.full(3, side * side / 6.0), "vertices": v,
+            "edges": np.array(edges), "faces": quads, "obb_center": np.zeros(3),
+            "obb_extent": np.full(3, h + r), "bound": math.sqrt(3) * h + r}
+    bound = math.sqrt(3) * h + r
+    sp = max(1.5e-3, 2.0 * bound * 1.01)  # 1.5 sides, widened so that rotated cubes cannot overlap
+    L = n_side * sp + 2e-4
+    wall = plate_shape("WALL", 0.5 * L + 1e-3, 0.1e-3)
+    shapes = [wall, cube]
+    c = 0.5 * L
+    wpos = [np.array([c, c, 0.0]), np.array([c, c, L]), np.array([c, 0.0, c]), np.array([c, L, c]),
+            np.array([0.0, c, c]), np.array([L, c, c])]
+    s2 = math.sqrt(0.5)
+    wq = [np.array([1.0, 0, 0, 0]), np.array([1.0, 0, 0, 0]), np.array([s2, -s2, 0, 0]), np.array([s2, s2, 0, 0]),
+          np.array([s2, 0, -s2, 0]), np.array([s2, 0, s2, 0])]
+    g = (np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), np.arange(n_side), indexing="ij"), -1)
+         .reshape(-1, 3) + 0.5) * sp + 1e-4
+    Q = random_quaternions(rng, len(g))
+    return _assemble(shapes, wpos, wq, g, Q, np.ones(len(g), np.int64), 2700.0, "Default", 1e6, 1e6, 0.25, 0.4, dt,
+                     gravity=(0.0, 0.0, -9.81), DVerlet=0.2e-3, dVerlet=0.1e-3, interVerlet=1e-4,
+                     name="sphero_cubes_%d" % len(g), wall_shape=0)
+
+
+def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, en2, mu, dt, gravity, DVerlet,
+              dVerlet, interVerlet, name, wall_shape=0):
+    nd = len(wall_pos)
+    n = nd + len(pos)
+    shape = np.concatenate([np.full(nd, wall_shape), shape_of]).astype(np.int32)
+    P = np.concatenate([np.array(wall_pos), pos])
+    Qa = np.concatenate([np.array(wall_Q), Q])
+    group = np.concatenate([np.ones(nd), np.zeros(len(pos))]).astype(np.int32)
+    vol = np.array([shapes[s]["volume"] for s in shape])
+    mass = vol * density
+    im = np.array([shapes[s]["I/m"] for s in shape])
+    tab = law_table(kn=kn, kt=kt, en2=en2, mu=mu)
+    return {"name": name, "shapes": shapes, "shape_tables": flatten_shapes(shapes), "n_driven": nd,
+            "bodies": {"pos": P, "vel": np.zeros((n, 3)), "acc": np.zeros((n, 3)), "Q": Qa,
+                       "vrot": np.zeros((n, 3)), "arot": np.zeros((n, 3)), "homothety": np.ones(n), "mass": mass,
+                       "inertia": im * mass[:, None], "shape": shape, "group": group,
+                       "cluster": np.zeros(n, np.int32)},
+            "density": {0: density, 1: density}, "law": law, "ngroup": 2, "table": tab, "dt": dt,
+            "gravity": gravity, "DVerlet": DVerlet, "dVerlet": dVerlet, "interVerlet": interVerlet,
+            "params": {"kn": kn, "kt": kt, "en2": en2, "mu": mu}}
+
+
+def law_table(kn, kt, en2, mu, kr=0.0, mur=0.0, ngroup=2):
+    """Parameter table in the RK_P_* slot order (include/rk_gpu.h)."""
+    t = np.zeros((22, ngroup, ngroup))
+    t[0] = kn
+    t[1] = en2
+    t[2] = kt
+    t[3] = mu
+    t[4] = kr
+    t[5] = mur
+    return t.ravel()
+
+
+# -------------------------------------------------------------- conf files --
+def _f(x):
+    return "%.16e" % x
+
+
+def write_conf(scene, directory, conf_name="input.conf", shape_name="shapes.shp", tmax=None):
+    """Write the scene as a Rockable conf + shape library."""
+    os.makedirs(directory, exist_ok=True)
+    with open(os.path.join(directory, shape_name), "w") as f:
+        for s in scene["shapes"]:
+            f.write("<\nname %s\nradius %s\npreCompDone y\nvolume %s\n" % (s["name"], _f(s["radius"]), _f(s["volume"])))
+            f.write("I/m %s\n" % " ".join(_f(x) for x in s["I/m"]))
+            f.write("obb.extent %s\nobb.center %s\n" % (" ".join(_f(x) for x in s["obb_extent"]),
+                                                        " ".join(_f(x) for x in s["obb_center"])))
+            f.write("obb.e1 1 0 0\nobb.e2 0 1 0\nobb.e3 0 0 1\nOBBtreeLevel 0\n")
+            f.write("nv %d\n" % len(s["vertices"]))
+            for v in s["vertices"]:
+                f.write("%s\n" % " ".join(_f(x) for x in v))
+            f.write("ne %d\n" % len(s["edges"]))
+            for e in s["edges"]:
+                f.write("%d %d\n" % (e[0], e[1]))
+            f.write("nf %d\n" % len(s["faces"]))
+            for fc in s["faces"]:
+                f.write("%d %s\n" % (len(fc), " ".join(str(x) for x in fc)))
+            f.write(">\n")
+    b = scene["bodies"]
+    p = scene["params"]
+    dt = scene["dt"]
+    lines = ["Rockable 29-11-2018", "AddOrRemoveInteractions bruteForce", "UpdateNL linkCells",
+             "forceLaw %s" % scene["law"], "t 0", "tmax %s" % (tmax if tmax is not None else 1.0), "dt %r" % dt,
+             "interVerlet %r" % scene["interVerlet"], "interConf 1", "DVerlet %r" % scene["DVerlet"],
+             "dVerlet %r" % scene["dVerlet"]]
+    for g, d in scene["density"].items():
+        lines.append("density %d %r" % (g, d))
+    lines.append("gravity %r %r %r" % tuple(scene["gravity"]))
+    for g1 in range(2):
+        for g2 in range(g1, 2):
+            lines += ["knContact %d %d %r" % (g1, g2, p["kn"]), "en2Contact %d %d %r" % (g1, g2, p["en2"]),
+                      "ktContact %d %d %r" % (g1, g2, p["kt"]), "muContact %d %d %r" % (g1, g2, p["mu"]),
+                      "krContact %d %d 0" % (g1, g2), "murContact %d %d 0" % (g1, g2)]
+    bound = max(s["bound"] for s in scene["shapes"][scene["n_driven"] and 1:])
+    cs = 2.0 * bound + scene["DVerlet"]
+    lines += ["cellMinSizes %r %r %r" % (cs, cs, cs), "nDriven %d" % scene["n_driven"],
+              "shapeFile %s" % shape_name, "precision 16", "Particles %d" % len(b["mass"])]
+    for i in range(len(b["mass"])):
+        nm = scene["shapes"][b["shape"][i]]["name"]
+        vals = list(b["pos"][i]) + list(b["vel"][i]) + list(b["acc"][i]) + list(b["Q"][i]) + list(b["vrot"][i]) + \
+            list(b["arot"][i])
+        lines.append("%s %d %d %s %s" % (nm, b["group"][i], b["cluster"][i], _f(b["homothety"][i]),
+                                         " ".join(_f(x) for x in vals)))
+    lines += ["Interactions 0", "Interfaces 0", ""]
+    with open(os.path.join(directory, conf_name), "w") as f:
+        f.write("\n".join(lines))
+    return os.path.join(directory, conf_name)
