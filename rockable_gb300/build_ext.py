@@ -63,9 +63,35 @@ def build(verbose=False):
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
         open(stamp, "w").write(out + "\n")
+    build_host(out)
     if verbose:
         print("built", out)
     return out
+
+
+def build_host(gpu_lib):
+    """librk_host.so (C++ host: conf I/O and plugin API over the C ABI) and the
+    rockable-gb300 command-line runner."""
+    hsrc = os.path.join(HERE, "host")
+    cxx = shutil.which("g++") or "g++"
+    host = os.path.join(LIBDIR, "librk_host.so")
+    stamp = os.path.join(BUILD, "librk_host.so.stamp")
+    srcs = [os.path.join(hsrc, "rk_host.cpp")]
+    deps = srcs + [os.path.join(hsrc, "rk_host.hpp"), os.path.join(HERE, "..", "include", "rk_gpu.h"), gpu_lib]
+    if not os.path.exists(stamp) or any(os.path.getmtime(d) > os.path.getmtime(stamp) for d in deps):
+        cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-o", host] + srcs + \
+              ["-L" + LIBDIR, "-lrk_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host build failed:\n%s\n%s" % (r.stdout, r.stderr))
+        cli = os.path.join(LIBDIR, "rockable-gb300")
+        cmd = [cxx, "-O2", "-std=c++17", "-o", cli, os.path.join(hsrc, "rk_run.cpp"), "-L" + LIBDIR, "-lrk_host",
+               "-lrk_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("runner build failed:\n%s\n%s" % (r.stdout, r.stderr))
+        open(stamp, "w").write(host + "\n")
+    return host
 
 
 if __name__ == "__main__":

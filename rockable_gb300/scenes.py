@@ -132,36 +132,65 @@ def random_quaternions(rng, n):
 
 
 # ------------------------------------------------------------------ scenes --
+def deposit(rng, radii, half_x, half_y, z0, gap=1e-5):
+    """Loose random packing by ballistic deposition: each grain, in the given
+    order, drops vertically at a random (x, y) in the column and stops on the
+    floor or on the first bounding sphere it meets (no rolling)."""
+    rmax = float(np.max(radii))
+    cs = 2.0 * rmax
+    nx = max(1, int(2 * half_x / cs))
+    ny = max(1, int(2 * half_y / cs))
+    cap = 64
+    cells = np.zeros((nx, ny, cap, 4))  # x y z r of the grains of each column cell
+    count = np.zeros((nx, ny), dtype=np.int64)
+    top = np.zeros((nx, ny))
+    pos = np.zeros((len(radii), 3))
+    for k, r in enumerate(radii):
+        x = rng.uniform(-half_x + r, half_x - r)
+        y = rng.uniform(-half_y + r, half_y - r)
+        cx = min(nx - 1, int((x + half_x) / cs))
+        cy = min(ny - 1, int((y + half_y) / cs))
+        z = z0 + r
+        x0, x1, y0, y1 = max(cx - 1, 0), min(cx + 2, nx), max(cy - 1, 0), min(cy + 2, ny)
+        blk = cells[x0:x1, y0:y1]
+        cnt = count[x0:x1, y0:y1]
+        mask = np.arange(cap)[None, None, :] < cnt[:, :, None]
+        c = blk[mask]
+        if len(c):
+            d2 = (c[:, 0] - x) ** 2 + (c[:, 1] - y) ** 2
+            rr = (c[:, 3] + r + gap) ** 2
+            hit = d2 < rr
+            if hit.any():
+                z = max(z, float(np.max(c[hit, 2] + np.sqrt(rr[hit] - d2[hit]))))
+        pos[k] = (x, y, z)
+        if count[cx, cy] == cap:  # keep the highest grains of a cell only
+            lo = int(np.argmin(cells[cx, cy, :, 2]))
+            cells[cx, cy, lo] = (x, y, z, r)
+        else:
+            cells[cx, cy, count[cx, cy]] = (x, y, z, r)
+            count[cx, cy] += 1
+    return pos
+
+
 def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2700.0, kn=1e6, kt=1e6,
-                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), fill=None):
+                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), pack=1.0):
     """Granular column collapse: n hull grains (axes U[0.5, 1.5] cm, i.e.
-    semi-axes U[0.25, 0.75] cm) on a jittered lattice in a 0.5 x 0.5 x 1.5 m
-    column above a rigid floor plate (the only driven body); the column's side
-    walls are released at t = 0, so they are not part of the scene."""
+    semi-axes U[0.25, 0.75] cm), loosely packed by ballistic deposition in a
+    0.5 x 0.5 m column above a rigid floor plate (the only driven body); the
+    column's side walls are released at t = 0, so they are not part of the
+    scene.  With pack < 1 the deposition uses bounding spheres shrunk by that
+    factor, so that the hulls interpenetrate slightly; relax() then pushes
+    them apart into a dense, contact-rich pile."""
     rng = np.random.default_rng(seed)
     shapes = [plate_shape("FLOOR", 1.5, 0.005)]
     shapes += [hull_shape(rng, "G%05d" % k) for k in range(nshapes)]
-    bound = max(s["bound"] for s in shapes[1:])
-    spacing = 2.0 * bound * 1.01
-    nx = int(column[0] / spacing)
-    ny = int(column[1] / spacing)
-    nz_needed = int(math.ceil(n / (nx * ny)))
-    nz = max(nz_needed, int(column[2] / spacing))
-    sites = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
-    sites = sites[np.argsort(sites[:, 2], kind="stable")]
-    if fill is None:
-        pick = np.sort(rng.choice(len(sites), n, replace=False)) if len(sites) > n else np.arange(n)
-    else:
-        pick = np.arange(n)
-    sites = sites[pick]
-    pos = (sites + 0.5) * spacing
-    pos[:, 0] -= 0.5 * nx * spacing
-    pos[:, 1] -= 0.5 * ny * spacing
-    pos[:, 2] += 0.006
+    bound = np.array([s["bound"] for s in shapes])
     shape_of = rng.integers(1, nshapes + 1, n)
+    pos = deposit(rng, pack * bound[shape_of], 0.5 * column[0], 0.5 * column[1], 0.005 + 1e-5)
     Q = random_quaternions(rng, n)
+    bmax = float(bound[1:].max())
     return _assemble(shapes, [np.zeros(3)], [np.array([1.0, 0, 0, 0])], pos, Q, shape_of, density, law, kn, kt, en2,
-                     mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bound, dVerlet=0.1 * bound,
+                     mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax,
                      interVerlet=100 * dt, name="column_collapse_%d" % n)
 
 
@@ -220,6 +249,54 @@ def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, 
             "density": {0: density, 1: density}, "law": law, "ngroup": 2, "table": tab, "dt": dt,
             "gravity": gravity, "DVerlet": DVerlet, "dVerlet": dVerlet, "interVerlet": interVerlet,
             "params": {"kn": kn, "kt": kt, "en2": en2, "mu": mu}}
+
+
+def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=0, report=None):
+    """Compact a freshly deposited pile on the GPU: Avalanche contacts at a
+    soft stiffness, boosted gravity and numerical damping, large time step.
+    Returns the GpuScene, switched afterwards to the scene's own parameters
+    (the Avalanche law's incremental normal force carries the settled contact
+    forces across the change of stiffness)."""
+    from .abi import GpuScene, RK_LAW
+    g = GpuScene(device=device)
+    g.upload_shapes(scene["shape_tables"])
+    g.upload_bodies(scene["bodies"], scene["n_driven"])
+    p = scene["params"]
+    grav = tuple(gboost * x for x in scene["gravity"])
+    g.set_params(t=0.0, dt=dt, gravity=grav, DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
+                 interVerlet=10 * dt, interVerletC=0.0, law=RK_LAW["Avalanche"], ngroup=scene["ngroup"],
+                 table=law_table(kn=kn, kt=kn, en2=p["en2"], mu=p["mu"]), numerical_damping=damping)
+    g.update_nl()
+    done = 0
+    while done < steps:
+        k = min(500, steps - done)
+        g.step(k)
+        done += k
+        if report is not None:
+            st = g.stats()
+            report.append((done, st["n_entries"], st["n_active"], st["e_trans"]))
+    set_scene_params(g, scene, t=done * dt)
+    return g
+
+
+def set_scene_params(g, scene, t=0.0, numerical_damping=0.0):
+    from .abi import RK_LAW
+    g.set_params(t=t, dt=scene["dt"], gravity=scene["gravity"], DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
+                 interVerlet=scene["interVerlet"], interVerletC=0.0, law=RK_LAW[scene["law"]],
+                 ngroup=scene["ngroup"], table=scene["table"], numerical_damping=numerical_damping)
+
+
+def scene_from_gpu(scene, g):
+    """The scene with the bodies and the neighbour list of a running engine
+    (for writing a conf that the CPU path can load)."""
+    out = dict(scene)
+    st = g.bodies()
+    b = dict(scene["bodies"])
+    for k in ["pos", "vel", "acc", "Q", "vrot", "arot"]:
+        b[k] = st[k]
+    out["bodies"] = b
+    out["entries"] = g.entries(geometry=True)
+    return out
 
 
 def law_table(kn, kt, en2, mu, kr=0.0, mur=0.0, ngroup=2):
@@ -284,7 +361,18 @@ def write_conf(scene, directory, conf_name="input.conf", shape_name="shapes.shp"
             list(b["arot"][i])
         lines.append("%s %d %d %s %s" % (nm, b["group"][i], b["cluster"][i], _f(b["homothety"][i]),
                                          " ".join(_f(x) for x in vals)))
-    lines += ["Interactions 0", "Interfaces 0", ""]
+    e = scene.get("entries")
+    if e is None:
+        lines += ["Interactions 0"]
+    else:  # active entries with their history, like Rockable::saveConf
+        act = np.nonzero((e["dn"] < 0.0) | (e["bond"] >= 0))[0]
+        lines.append("Interactions %d" % len(act))
+        for k in act:
+            vals = list(e["n"][k]) + [e["dn"][k]] + list(e["pos"][k]) + list(e["vel"][k]) + [e["fn"][k]] + \
+                list(e["ft"][k]) + list(e["mom"][k]) + [e["damp"][k]]
+            lines.append("%d %d %d %d %d %s" % (e["i"][k], e["j"][k], e["type"][k], e["isub"][k], e["jsub"][k],
+                                                " ".join(_f(x) for x in vals)))
+    lines += ["Interfaces 0", ""]
     with open(os.path.join(directory, conf_name), "w") as f:
         f.write("\n".join(lines))
     return os.path.join(directory, conf_name)
