@@ -207,9 +207,18 @@ def main():
         dist.barrier()
     g.synchronize()
     clocks.start()
+    nvtx = None
+    try:
+        import torch
+        nvtx = torch.cuda.nvtx
+        nvtx.range_push("timed")
+    except Exception:
+        nvtx = None
     t0 = time.perf_counter()
     rep = g.step(a.steps)
     wall = time.perf_counter() - t0
+    if nvtx:
+        nvtx.range_pop()
     ms, launches = g.last_step_timing()
     ck = clocks.stop()
     if dist:
@@ -220,8 +229,9 @@ def main():
     value = ws * nfree * a.steps / (ms / 1000.0)
     st = g.stats()
     # ---- per-phase profile (outside the timed region)
+    nprof = max(1, min(a.steps, 120))
     g.set_profiling(True)
-    g.step(min(50, a.steps))
+    g.step(nprof)
     prof = g.profile()
     g.set_profiling(False)
     nphase = prof["narrow_force"]
@@ -269,7 +279,8 @@ def main():
                             "peak_source": src, "bytes_per_entry": 140, "entries": int(C),
                             "ms_per_launch": t_narrow},
                "setup": {"settle_s": t_settle, "settle_log": settle_log},
-               "phases_ms_per_step": {k: v[0] / max(1, min(50, a.steps)) for k, v in prof.items()},
+               "phases_ms_per_step": {k: v[0] / nprof for k, v in prof.items()},
+               "phases_launches": {k: v[1] for k, v in prof.items()},
                "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()

@@ -196,6 +196,11 @@ int rk_set_params(rk_ctx* ctx, const rk_params* p);
 int rk_upload_entries(rk_ctx* ctx, const rk_entries* e);
 int rk_upload_interfaces(rk_ctx* ctx, const rk_interfaces* f);
 int rk_set_controls(rk_ctx* ctx, const rk_control* c, int32_t n, const rk_servo* servo);
+/* Select the arithmetic of the narrow phase and force laws for the next
+ * steps: RK_FORM_FP64 (bit-identical to the reference CPU path) or
+ * RK_FORM_MIXED (FP32 on body-relative coordinates, FP64 for positions, the
+ * overlap dn and the integration).  No reference counterpart. */
+int rk_set_form(rk_ctx* ctx, int form);
 /* When on, every step also stores each entry's contact normal, point and
  * relative velocity (needed to write a conf file); off by default. */
 int rk_set_record_geometry(rk_ctx* ctx, int on);

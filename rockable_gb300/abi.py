@@ -89,6 +89,7 @@ SIGNATURES = {
     "rk_upload_interfaces": (C.c_int, [P, C.POINTER(RkInterfaces)]),
     "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
     "rk_set_record_geometry": (C.c_int, [P, C.c_int]),
+    "rk_set_form": (C.c_int, [P, C.c_int]),
     "rk_accelerations": (C.c_int, [P]),
     "rk_update_nl": (C.c_int, [P]),
     "rk_step": (C.c_int, [P, I64, C.POINTER(RkStepReport)]),
@@ -220,6 +221,9 @@ class GpuScene:
                 sv.walls[d] = int(servo["walls"][d])
             sv.pressure = float(servo["pressure"])
         self._chk(self.L.rk_set_controls(self.h, arr, n, C.byref(sv)), "rk_set_controls")
+
+    def set_form(self, form):
+        self._chk(self.L.rk_set_form(self.h, int(form)), "rk_set_form")
 
     def set_record_geometry(self, on=True):
         self._chk(self.L.rk_set_record_geometry(self.h, 1 if on else 0), "rk_set_record_geometry")

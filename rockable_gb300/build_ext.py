@@ -24,6 +24,7 @@ UNITS = {
     "rk_step.cu": ["--fmad=false"],
     "rk_nl.cu": ["--fmad=false"],
     "rk_api.cu": ["--fmad=false"],
+    "rk_mixed.cu": [],
 }
 
 

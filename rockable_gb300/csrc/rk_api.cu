@@ -191,7 +191,7 @@ int build_index(Ctx& c) {
   }
   k_jofs2<<<nblk(N + 1, 256), 256, 0, c.stream>>>(w.jkeys, ne, N, s.jofs);
   CK(cudaGetLastError());
-  return 0;
+  return heavy_list(c);
 }
 
 int read_flags(Ctx& c) {
@@ -220,7 +220,7 @@ int rk_create(rk_ctx** out, const rk_config* cfg) {
     delete x;
     return RK_ERR_CUDA;
   }
-  if (c.form != RK_FORM_FP64) {
+  if (c.form != RK_FORM_FP64 && c.form != RK_FORM_MIXED) {
     delete x;
     return RK_ERR_UNSUPPORTED;
   }
@@ -260,6 +260,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.gv); dfree(s.bobb); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jlist);
+  dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
   dfree(s.if_break); dfree(s.if_ofs); dfree(s.flags);
   free_entrybuf(c.eb[0]);
@@ -287,6 +288,8 @@ int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
   const int ns = sh->nshapes;
   const int nv = sh->vert_ofs[ns], ne = sh->edge_ofs[ns], nf = sh->face_ofs[ns], nfv = sh->face_vofs[nf];
   c.shape_nv.assign(ns, 0);
+  c.shape_ne.assign(ns, 0);
+  c.shape_nf.assign(ns, 0);
   for (int k = 0; k < ns; k++) {
     int v = sh->vert_ofs[k + 1] - sh->vert_ofs[k];
     int e = sh->edge_ofs[k + 1] - sh->edge_ofs[k];
@@ -294,6 +297,8 @@ int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
     if (v <= 0 || v > 64) return fail(c, RK_ERR_CAPACITY, "a shape has no vertex or more than 64 vertices");
     if (e >= kMaxSub || f >= kMaxSub) return fail(c, RK_ERR_CAPACITY, "a shape has more than 1023 edges or faces");
     c.shape_nv[k] = v;
+    c.shape_ne[k] = e;
+    c.shape_nf[k] = f;
   }
   for (int f = 0; f < nf; f++)
     if (sh->face_vofs[f + 1] - sh->face_vofs[f] < 3) return fail(c, RK_ERR_ARG, "a face has fewer than 3 vertices");
@@ -327,6 +332,11 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
     rad[i] = b->homothety[i] * c.shape_radius[sh];  // Particle::MinkowskiRadius (Particle.cpp:71)
   }
   const int64_t nv = gv_ofs[n];
+  std::vector<int64_t> sph_ofs(n + 1, 0);
+  for (int64_t i = 0; i < n; i++) {
+    int sh = b->shape[i];
+    sph_ofs[i + 1] = sph_ofs[i] + c.shape_nv[sh] + c.shape_ne[sh] + c.shape_nf[sh];
+  }
   std::vector<int> gv_body(nv);
   for (int64_t i = 0; i < n; i++)
     for (int64_t k = gv_ofs[i]; k < gv_ofs[i + 1]; k++) gv_body[k] = (int)i;
@@ -347,8 +357,12 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.dpos, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.dq, (const double*)nullptr, 4 * n)) ||
       (rc = dupload(c, s.iofs, (const int64_t*)nullptr, n + 1)) ||
       (rc = dupload(c, s.jofs, (const int64_t*)nullptr, n + 1)) ||
-      (rc = dupload(c, s.if_ofs, (const int64_t*)nullptr, n + 1)))
+      (rc = dupload(c, s.if_ofs, (const int64_t*)nullptr, n + 1)) ||
+      (rc = dupload(c, s.sph_ofs, sph_ofs.data(), n + 1)) || (rc = dalloc(c, s.sph, sph_ofs[n])) ||
+      (rc = dupload(c, s.is_heavy, (const uint8_t*)nullptr, n)) || (rc = dalloc(c, s.heavy, n)))
     return rc;
+  s.nheavy = 0;
+  if (!c.w.counter) CK(cudaMalloc(&c.w.counter, 64));
   // deltaQ starts as the identity quaternion
   std::vector<double> dq(4 * n, 0.0);
   for (int64_t i = 0; i < n; i++) dq[4 * i] = 1.0;
@@ -515,6 +529,13 @@ int rk_set_controls(rk_ctx* x, const rk_control* cs, int32_t n, const rk_servo* 
   return RK_OK;
 }
 
+int rk_set_form(rk_ctx* x, int form) {
+  if (!x) return RK_ERR_ARG;
+  if (form != RK_FORM_FP64 && form != RK_FORM_MIXED) return fail(x->c, RK_ERR_UNSUPPORTED, "unknown form");
+  x->c.form = form;
+  return RK_OK;
+}
+
 int rk_set_record_geometry(rk_ctx* x, int on) {
   if (!x) return RK_ERR_ARG;
   x->c.s.record_geom = on ? 1 : 0;
@@ -537,7 +558,9 @@ int rk_accelerations(rk_ctx* x) {
   Scene& s = c.s;
   CK(cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream));
   launch_glob_vertices(s, c.stream);
-  launch_narrow_force(s, c.stream);
+  if (c.form == RK_FORM_MIXED) launch_narrow_force_mixed(s, c.stream);
+  else launch_narrow_force(s, c.stream);
+  launch_gather_heavy(s, c.stream);
   launch_gather_accel(s, 0, c.stream);
   launch_breakage(s, c.stream);
   CK(cudaGetLastError());
@@ -594,8 +617,9 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
     mark(0, false); phase(0, launch_controls_pre(s, c.stream));
     mark(1, false); phase(1, launch_drift(s, c.stream));
     mark(2, false); phase(2, launch_glob_vertices(s, c.stream));
-    mark(3, false); phase(3, launch_narrow_force(s, c.stream));
-    mark(4, false); phase(4, launch_gather_accel(s, 1, c.stream));
+    mark(3, false);
+    phase(3, c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream));
+    mark(4, false); phase(4, launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream));
     mark(5, false); phase(5, launch_breakage(s, c.stream));
     bool need = false;
     if (need_flags) {

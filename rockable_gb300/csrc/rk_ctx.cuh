@@ -55,6 +55,7 @@ struct Ctx {
   std::vector<Control> controls;
   std::vector<int> shape_nv;  // vertices per shape
   std::vector<double> shape_radius;
+  std::vector<int> shape_ne, shape_nf;
   bool have_shapes = false, have_bodies = false, have_params = false;
   // loop bookkeeping (Rockable::integrate)
   double t = 0.0, interVerlet = 0.01, interVerletC = 0.0;
@@ -75,6 +76,7 @@ struct Ctx {
 };
 
 int rebuild_nl(Ctx& c);
+int heavy_list(Ctx& c);
 int ensure_entry_capacity(Ctx& c, int which, int64_t n);
 void bind_entries(Ctx& c);
 

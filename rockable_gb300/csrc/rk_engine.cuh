@@ -26,6 +26,7 @@ namespace rk {
 constexpr int kMaxSub = 1024;       // sub-element index limit of the sort key
 constexpr int kMaxBody = 1 << 21;   // body index limit of the sort key
 constexpr int kMaskWords = 2;       // vertex cull mask words per half-pair (<= 64 vertices)
+constexpr int kHeavy = 64;          // entries above which a body's resultant is summed by a block
 
 __host__ __device__ __forceinline__ uint64_t entry_key(uint32_t i, uint32_t j, uint32_t t, uint32_t isub,
                                                        uint32_t jsub) {
@@ -105,6 +106,11 @@ struct Scene {
   int64_t* iofs;  // n+1
   int64_t* jofs;  // n+1
   int* jlist;     // ne
+  int* heavy;     // bodies whose entry count exceeds kHeavy (summed by a block each)
+  int nheavy;
+  uint8_t* is_heavy;  // n
+  float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
+  int64_t* sph_ofs;   // n+1
   // ---- interfaces
   int64_t nif;
   int *if_i, *if_j;
@@ -127,7 +133,9 @@ int launch_controls_pre(const Scene& s, cudaStream_t st);
 int launch_drift(const Scene& s, cudaStream_t st);
 int launch_glob_vertices(const Scene& s, cudaStream_t st);
 int launch_narrow_force(const Scene& s, cudaStream_t st);
+int launch_narrow_force_mixed(const Scene& s, cudaStream_t st);
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st);
+int launch_gather_heavy(const Scene& s, cudaStream_t st);
 int launch_breakage(const Scene& s, cudaStream_t st);
 int launch_guard(const Scene& s, cudaStream_t st);
 int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);

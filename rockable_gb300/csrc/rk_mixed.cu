@@ -1,0 +1,299 @@
+// rk_mixed.cu -- narrow phase and force laws of the mixed-precision form.
+//
+// Same inputs, outputs and semantics as k_narrow_force (rk_step.cu: update of
+// Interaction.cpp:143-326, ForceLaw_*.cpp laws, contributions of
+// Rockable.cpp:2752-2789), with the arithmetic split by what it needs:
+//   FP64  vertex positions, the separation vector of the two sub-elements and
+//         its length (hence dn), the face normal of a vertex-face contact
+//         (FP32 reciprocal-sqrt seed refined by two FP64 Newton steps), the
+//         history dn and the Avalanche normal-force increment;
+//   FP32  everything measured relative to a body centre or a face vertex:
+//         edge / segment parameters, the point-in-polygon test, the contact
+//         point, the relative velocity, the tangential force and rolling
+//         moment, and the force / moment contributions.
+// An overlap dn is a small difference of lengths of the order of the
+// particle size, which FP32 cannot resolve; all the other quantities are well
+// conditioned.  Compiled with fused multiply-adds allowed.
+#include "../../include/rk_gpu.h"
+#include "rk_engine.cuh"
+
+namespace rk {
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) {
+  F3 r;
+  r.x = x; r.y = y; r.z = z;
+  return r;
+}
+__device__ __forceinline__ F3 tof(V3 a) { return f3((float)a.x, (float)a.y, (float)a.z); }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 operator-(F3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ F3 operator*(float s, F3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float dotf(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 crossf(F3 a, F3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+__device__ __forceinline__ V3 ld3m(const double* a, int64_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
+__device__ __forceinline__ void st3m(double* a, int64_t k, F3 v) {
+  a[3 * k] = (double)v.x;
+  a[3 * k + 1] = (double)v.y;
+  a[3 * k + 2] = (double)v.z;
+}
+__device__ __forceinline__ V3 gvm(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
+
+// |d| in FP64 from an FP32 reciprocal-sqrt seed and two Newton steps
+__device__ __forceinline__ double len64(V3 d, double& inv) {
+  double s = d.x * d.x + d.y * d.y + d.z * d.z;
+  double y = (double)rsqrtf((float)s);
+  y = y * (1.5 - 0.5 * s * y * y);
+  y = y * (1.5 - 0.5 * s * y * y);
+  inv = y;
+  return s * y;
+}
+
+__global__ void k_narrow_force_mixed(Scene s) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool active = false;
+  if (e < s.ne) {
+    const int i = s.ei[e], j = s.ej[e];
+    const uint32_t ts = s.etsub[e];
+    const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);
+    const double dn_old = s.dn[e];
+    const int bond = s.bond[e];
+    const double* gi = s.gv + 3 * s.gv_ofs[i];
+    const double* gj = s.gv + 3 * s.gv_ofs[j];
+    const double Ri = s.rad[i], Rj = s.rad[j];
+    const V3 xi = ld3m(s.pos, i), xj = ld3m(s.pos, j);
+    double dn = 0.0;
+    F3 n = f3(0, 0, 0), ci = f3(0, 0, 0);  // normal, contact point relative to x_i
+    bool ok = true;
+    if (type == 0) {
+      V3 a = gvm(gi, isub), b = gvm(gj, jsub);
+      V3 d = a - b;
+      double inv;
+      double L = len64(d, inv);
+      dn = L - (Ri + Rj);
+      n = tof(d * inv);
+      ci = tof(a - xi) - (float)(Ri + 0.5 * dn) * n;
+    } else if (type == 1) {
+      const int sj = s.shape[j];
+      const int eo = s.edge_ofs[sj] + jsub;
+      V3 p1 = gvm(gj, s.edges[2 * eo]), p2 = gvm(gj, s.edges[2 * eo + 1]);
+      V3 a = gvm(gi, isub);
+      V3 E = p2 - p1, w = a - p1;
+      F3 Ef = tof(E), wf = tof(w);
+      float r = dotf(wf, Ef) / dotf(Ef, Ef);
+      if (r <= 0.f || r >= 1.f) {
+        ok = false;
+      } else {
+        V3 d = w - (double)r * E;
+        double inv;
+        double L = len64(d, inv);
+        dn = L - (Ri + Rj);
+        n = tof(d * inv);
+        ci = tof(a - xi) - (float)(Ri + 0.5 * dn) * n;
+      }
+    } else if (type == 2) {
+      const int sj = s.shape[j];
+      const int fo = s.face_ofs[sj] + jsub;
+      const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
+      const int* fv = s.face_verts + v0;
+      V3 A = gvm(gj, fv[0]), B = gvm(gj, fv[1]), C = gvm(gj, fv[nbv - 1]);
+      V3 a = gvm(gi, isub);
+      V3 w = a - A;
+      V3 nn = cross(B - A, C - A);
+      double inv;
+      len64(nn, inv);
+      nn = nn * inv;
+      double dist = dot(w, nn);
+      if (dist < 0.0) { nn = -nn; dist = -dist; }
+      // crossing-number test in FP32, relative to the face vertex A
+      F3 nf = tof(nn);
+      F3 v1 = tof(B - A);
+      v1 = rsqrtf(dotf(v1, v1)) * v1;
+      F3 v2 = crossf(nf, v1);
+      F3 P = tof(w - dist * nn);
+      float ori1 = dotf(P, v1), ori2 = dotf(P, v2);
+      int odd = 0;
+      for (int iva = 0; iva < nbv; ++iva) {
+        int ivb = iva + 1;
+        if (ivb == nbv) ivb = 0;
+        F3 pa = tof(gvm(gj, fv[iva]) - A), pb = tof(gvm(gj, fv[ivb]) - A);
+        float pa1 = dotf(pa, v1), pb1 = dotf(pb, v1), pa2 = dotf(pa, v2), pb2 = dotf(pb, v2);
+        if ((pa2 < ori2 && pb2 >= ori2) || (pb2 < ori2 && pa2 >= ori2)) {
+          if (pa1 + (ori2 - pa2) / (pb2 - pa2) * (pb1 - pa1) < ori1) odd = 1 - odd;
+        }
+      }
+      if (odd) {
+        dn = dist - (Ri + Rj);
+        n = nf;
+        ci = tof(a - xi) - (float)(Ri + 0.5 * dn) * n;
+      } else {
+        ok = false;
+      }
+    } else {
+      const int si = s.shape[i], sj = s.shape[j];
+      const int eoi = s.edge_ofs[si] + isub, eoj = s.edge_ofs[sj] + jsub;
+      V3 pi1 = gvm(gi, s.edges[2 * eoi]), pi2 = gvm(gi, s.edges[2 * eoi + 1]);
+      V3 pj1 = gvm(gj, s.edges[2 * eoj]), pj2 = gvm(gj, s.edges[2 * eoj + 1]);
+      V3 Ei = pi2 - pi1, Ej = pj2 - pj1, w = pi1 - pj1;
+      F3 Eif = tof(Ei), Ejf = tof(Ej), wf = tof(w);
+      float c = dotf(Eif, Eif), d = dotf(Ejf, Ejf), ee = dotf(Eif, Ejf);
+      float f = (c * d) - (ee * ee);
+      if (fabsf(f) > 1.0e-12f) {
+        f = 1.0f / f;
+        float a = dotf(Eif, wf), b = dotf(Ejf, wf);
+        float ss = (ee * b - a * d) * f;
+        float tt = (c * b - ee * a) * f;
+        if (ss <= 0.f || ss >= 1.f || tt <= 0.f || tt >= 1.f) {
+          ok = false;
+        } else {
+          V3 dd = (w + (double)ss * Ei) - (double)tt * Ej;
+          double inv;
+          double L = len64(dd, inv);
+          dn = L - (Ri + Rj);
+          n = tof(dd * inv);
+          ci = tof((pi1 - xi) + (double)ss * Ei) - (float)(Ri + 0.5 * dn) * n;
+        }
+      } else {
+        ok = false;
+      }
+    }
+    const F3 dx = tof(xj - xi);
+    const F3 wi = tof(ld3m(s.vrot, i)), wj = tof(ld3m(s.vrot, j));
+    F3 cj = ci - dx;
+    F3 cvel;
+    double fn;
+    F3 ft, mom;
+    if (ok) {
+      const F3 dv = tof(ld3m(s.vel, j) - ld3m(s.vel, i));
+      cvel = (dv - crossf(cj, wj)) + crossf(ci, wi);
+      fn = s.fn[e];
+      ft = tof(ld3m(s.ft, e));
+      mom = tof(ld3m(s.mom, e));
+      if (s.record_geom || bond >= 0) {
+        st3m(s.gn, e, n);
+        st3m(s.gpos, e, tof(xi) + ci);
+        st3m(s.gvel, e, cvel);
+      }
+    } else {
+      dn = 0.0;
+      fn = 0.0;
+      ft = f3(0, 0, 0);
+      mom = f3(0, 0, 0);
+      if (bond >= 0) {
+        n = tof(ld3m(s.gn, e));
+        ci = tof(ld3m(s.gpos, e) - xi);
+        cj = ci - dx;
+        cvel = tof(ld3m(s.gvel, e));
+      } else {
+        cvel = f3(0, 0, 0);
+      }
+    }
+    active = (dn < 0.0 || bond >= 0);
+    if (active) {
+      const double* P = s.table[s.group[i] * s.ngroup + s.group[j]].p;
+      const float dt = (float)s.dt;
+      const float damp = (float)s.damp[e];
+      const F3 dw = wj - wi;
+      if (s.law == RK_LAW_STICKEDLINKS && bond >= 0) {
+        float kn, kt, kr, fn0, ft0, mom0, power;
+        double dn0 = s.if_dn0[bond];
+        if (s.params_in_interfaces == 1) {
+          const double* q = s.if_par + 8 * (int64_t)bond;
+          kn = (float)q[0]; kt = (float)q[1]; kr = (float)q[2]; fn0 = (float)q[3]; ft0 = (float)q[4];
+          mom0 = (float)q[5]; power = (float)q[6];
+        } else if (s.cluster[i] == s.cluster[j]) {
+          kn = (float)P[RK_P_KN_IN]; kt = (float)P[RK_P_KT_IN]; kr = (float)P[RK_P_KR_IN]; fn0 = (float)P[RK_P_FN0_IN];
+          ft0 = (float)P[RK_P_FT0_IN]; mom0 = (float)P[RK_P_MOM0_IN]; power = (float)P[RK_P_POW_IN];
+          dn0 = 0.0;
+        } else {
+          kn = (float)P[RK_P_KN_OUT]; kt = (float)P[RK_P_KT_OUT]; kr = (float)P[RK_P_KR_OUT];
+          fn0 = (float)P[RK_P_FN0_OUT]; ft0 = (float)P[RK_P_FT0_OUT]; mom0 = (float)P[RK_P_MOM0_OUT];
+          power = (float)P[RK_P_POW_OUT];
+        }
+        float vn = dotf(cvel, n);
+        fn = -(double)kn * (dn - dn0) + (double)(damp * vn);
+        F3 vt = cvel - vn * n;
+        ft = ft + (kt * dt) * vt;
+        ft = ft + damp * vt;
+        mom = mom + (kr * dt) * dw;
+        float yield = powf(sqrtf(dotf(ft, ft)) / ft0, power) + powf(sqrtf(dotf(mom, mom)) / mom0, power) -
+                      (float)fn / fn0 - 1.0f;
+        if (yield > 0.f) s.if_break[bond] = 1;
+      } else if (dn > 0.0) {
+        fn = 0.0;
+        ft = f3(0, 0, 0);
+        mom = f3(0, 0, 0);
+      } else if (s.law == RK_LAW_AVALANCHE) {
+        const float kn = (float)P[RK_P_KN], en2 = (float)P[RK_P_EN2], kt = (float)P[RK_P_KT];
+        const float mu = (float)P[RK_P_MU], kr = (float)P[RK_P_KR], mur = (float)P[RK_P_MUR];
+        double prev_dn = ok ? dn_old : 0.0;
+        if (prev_dn > 0.0) prev_dn = 0.0;
+        double ddn = dn - prev_dn;
+        if (ddn > 0.0) fn = -(double)(kn * en2) * dn;
+        else if (ddn < 0.0) fn = fn - (double)kn * ddn;
+        if (fn < 0.0) fn = 0.0;
+        F3 vt = cvel - dotf(cvel, n) * n;
+        ft = ft + (kt * dt) * vt;
+        float thr = fabsf(mu * (float)fn);
+        float ft2 = dotf(ft, ft);
+        if (ft2 > 0.f && ft2 > thr * thr) ft = (thr * rsqrtf(ft2)) * ft;
+        mom = mom + (kr * dt) * dw;
+        F3 br;
+        F3 w0;
+        if (i < s.n_driven) { br = cj; w0 = wj; }
+        else { br = ci; w0 = wi; }
+        float r = dotf(br, w0) / dotf(w0, w0);
+        br = br - r * w0;
+        float thm = fabsf(mur * sqrtf(dotf(br, br)) * (float)fn);
+        float m2 = dotf(mom, mom);
+        if (m2 > 0.f && m2 > thm * thm) mom = (thm * rsqrtf(m2)) * mom;
+      } else {  // Default law, and the contact branch of StickedLinks
+        const float kn = (float)P[RK_P_KN], kt = (float)P[RK_P_KT], mu = (float)P[RK_P_MU];
+        const float kr = (float)P[RK_P_KR], mur = (float)P[RK_P_MUR];
+        const bool sticked = s.law == RK_LAW_STICKEDLINKS;
+        float vn = dotf(cvel, n);
+        double fne = -(double)kn * dn;
+        fn = fne + (double)(damp * vn);
+        if (fn < 0.0) fn = 0.0;
+        F3 vt = cvel - vn * n;
+        ft = ft + (kt * dt) * vt;
+        float thr = fabsf(mu * (float)(sticked ? fn : fne));
+        float ft2 = dotf(ft, ft);
+        if (ft2 > 0.f && ft2 >= thr * thr) ft = (thr * rsqrtf(ft2)) * ft;
+        if (sticked || kr > 0.f) {
+          mom = mom + (kr * dt) * dw;
+          float thm = fabsf(mur * (float)fn);
+          float m2 = dotf(mom, mom);
+          if (m2 > 0.f && m2 >= thm * thm) mom = (thm * rsqrtf(m2)) * mom;
+        }
+      }
+      F3 f = (float)fn * n + ft;
+      st3m(s.cf, e, f);
+      st3m(s.cmi, e, crossf(ci, f) + mom);
+      st3m(s.cmj, e, crossf(cj, -f) - mom);
+    }
+    s.dn[e] = dn;
+    if (active || !ok) {
+      s.fn[e] = fn;
+      st3m(s.ft, e, ft);
+      st3m(s.mom, e, mom);
+    }
+    s.act[e] = active ? 1 : 0;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, active);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(&s.flags[FLAG_NACTIVE], (unsigned long long)__popc(m));
+}
+
+int launch_narrow_force_mixed(const Scene& s, cudaStream_t st) {
+  if (s.ne <= 0) return 0;
+  k_narrow_force_mixed<<<(unsigned)((s.ne + 127) / 128), 128, 0, st>>>(s);
+  return 1;
+}
+
+}  // namespace rk

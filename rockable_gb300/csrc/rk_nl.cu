@@ -79,6 +79,46 @@ __global__ void k_body_obb(Scene s) {
   }
 }
 
+// Bounding spheres of every sub-element (vertices, edges, faces) in world
+// coordinates, as floats with the radius rounded up: the conservative filter
+// in front of the FP64 NEAR predicates.
+__global__ void k_spheres(Scene s) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= s.n) return;
+  const int sh = s.shape[b];
+  const double* g = s.gv + 3 * s.gv_ofs[b];
+  float4* out = s.sph + s.sph_ofs[b];
+  const int nv = s.vert_ofs[sh + 1] - s.vert_ofs[sh];
+  const int e0 = s.edge_ofs[sh], ne = s.edge_ofs[sh + 1] - e0;
+  const int f0 = s.face_ofs[sh], nf = s.face_ofs[sh + 1] - f0;
+  for (int v = 0; v < nv; v++) out[v] = make_float4((float)g[3 * v], (float)g[3 * v + 1], (float)g[3 * v + 2], 0.f);
+  for (int e = 0; e < ne; e++) {
+    V3 a = g3(g, s.edges[2 * (e0 + e)]), c = g3(g, s.edges[2 * (e0 + e) + 1]);
+    V3 m = 0.5 * (a + c);
+    double h = 0.5 * sqrt(norm2(c - a));
+    out[nv + e] = make_float4((float)m.x, (float)m.y, (float)m.z, __double2float_ru(h));
+  }
+  for (int f = 0; f < nf; f++) {
+    const int v0 = s.face_vofs[f0 + f], k = s.face_vofs[f0 + f + 1] - v0;
+    V3 c = v3(0, 0, 0);
+    for (int q = 0; q < k; q++) c = c + g3(g, s.face_verts[v0 + q]);
+    c = (1.0 / k) * c;
+    double r2 = 0.0;
+    for (int q = 0; q < k; q++) r2 = fmax(r2, norm2(g3(g, s.face_verts[v0 + q]) - c));
+    out[nv + ne + f] = make_float4((float)c.x, (float)c.y, (float)c.z, __double2float_ru(sqrt(r2)));
+  }
+}
+
+// bodies whose resultant is summed by a block (see k_gather_heavy)
+__global__ void k_heavy(Scene s, unsigned long long* count) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= s.n) return;
+  int64_t c = (s.iofs[b + 1] - s.iofs[b]) + (s.jofs[b + 1] - s.jofs[b]);
+  bool h = c > kHeavy;
+  s.is_heavy[b] = h ? 1 : 0;
+  if (h) s.heavy[atomicAdd(count, 1ull)] = (int)b;
+}
+
 __device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
   // unbroken interface (i, j) stored under its first body (Rockable.cpp:1637-1641)
   int64_t lo = s.if_ofs[i], hi = s.if_ofs[i + 1];
@@ -255,6 +295,18 @@ __global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* 
   } else {
     for (int w = 0; w < kMaskWords; w++) m[w] = mask[kMaskWords * h + w];
   }
+  // conservative float filter: a candidate whose bounding spheres are
+  // farther apart than the NEAR distance allows cannot be NEAR
+  const float4* sb = s.sph + s.sph_ofs[b];
+  const float4* sp = s.sph + s.sph_ofs[p];
+  const float sum = (float)(P.Rb + P.Rp + P.dmax);
+  auto far = [&](float4 a, float4 c, float extent) {
+    float dx = a.x - c.x, dy = a.y - c.y, dz = a.z - c.z;
+    float lim = sum + extent;
+    lim = lim + 1e-4f * lim + 2e-6f;
+    return dx * dx + dy * dy + dz * dz > lim * lim;
+  };
+  const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
   int64_t c = 0;
   uint64_t* o = (MODE == 1) ? out + ofs[h] : nullptr;
   auto emit = [&](int t, int i1, int j1) {
@@ -265,20 +317,28 @@ __global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* 
     for (int v = 0; v < nvb; v++)
       if (m[v >> 5] >> (v & 31) & 1u)
         for (int w = 0; w < nvp; w++)
-          if (near_vv(P, v, w)) emit(0, v, w);
+          if (!far(sb[v], sp[w], 0.f) && near_vv(P, v, w)) emit(0, v, w);
   }
   for (int v = 0; v < nvb; v++)
     if (m[v >> 5] >> (v & 31) & 1u)
-      for (int e = 0; e < nep; e++)
-        if (near_ve(s, P, v, e)) emit(1, v, e);
+      for (int e = 0; e < nep; e++) {
+        const float4 se = sp[nvp + e];
+        if (!far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e)) emit(1, v, e);
+      }
   for (int v = 0; v < nvb; v++)
     if (m[v >> 5] >> (v & 31) & 1u)
-      for (int f = 0; f < nfp; f++)
-        if (near_vf(s, P, v, f)) emit(2, v, f);
+      for (int f = 0; f < nfp; f++) {
+        const float4 sf = sp[nvp + nep + f];
+        if (!far(sb[v], sf, sf.w) && near_vf(s, P, v, f)) emit(2, v, f);
+      }
   if (b < p) {
-    for (int e = 0; e < neb; e++)
-      for (int e2 = 0; e2 < nep; e2++)
-        if (near_ee(s, P, e, e2)) emit(3, e, e2);
+    for (int e = 0; e < neb; e++) {
+      const float4 s1 = sb[nvb + e];
+      for (int e2 = 0; e2 < nep; e2++) {
+        const float4 s2 = sp[nvp + e2];
+        if (!far(s1, s2, s1.w + s2.w) && near_ee(s, P, e, e2)) emit(3, e, e2);
+      }
+    }
   }
   if (MODE == 0) cnt[h] = c;
 }
@@ -460,7 +520,8 @@ int rebuild_nl(Ctx& c) {
   const int64_t N = s.n;
   if (N <= 0) return 0;
   k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
-  c.kernels++;
+  k_spheres<<<nblk(N, 128), 128, 0, st>>>(s);
+  c.kernels += 2;
   // ---- pairs
   if (w.pair_cap < 16 * N + 1024) {
     int64_t nc = 16 * N + 1024;
@@ -580,6 +641,18 @@ int rebuild_nl(Ctx& c) {
   k_jofs<<<nblk(N + 1, 256), 256, 0, st>>>(w.jkeys, nf, N, s.jofs);
   c.kernels++;
   RKCHK(cudaGetLastError());
+  return heavy_list(c);
+}
+
+int heavy_list(Ctx& c) {
+  Scene& s = c.s;
+  RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 8, c.stream));
+  k_heavy<<<nblk(s.n, 256), 256, 0, c.stream>>>(s, c.w.counter + 1);
+  c.kernels++;
+  unsigned long long nh = 0;
+  RKCHK(cudaMemcpyAsync(&nh, c.w.counter + 1, 8, cudaMemcpyDeviceToHost, c.stream));
+  RKCHK(cudaStreamSynchronize(c.stream));
+  s.nheavy = (int)nh;
   return 0;
 }
 

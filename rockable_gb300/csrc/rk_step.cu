@@ -418,42 +418,115 @@ __device__ __forceinline__ V3 euler_domega(V3 I, V3 w, V3 M) {
             (M.z - (I.y - I.x) * w.x * w.y) / I.z);
 }
 
+// imposed force / moment components of a driven body (Rockable.cpp:2904-2928)
+__device__ __forceinline__ void init_resultant(const Scene& s, int64_t b, V3& F, V3& M) {
+  F = v3(0, 0, 0);
+  M = v3(0, 0, 0);
+  if (b >= s.n_driven) return;
+  for (int k = 0; k < s.ncontrols; k++) {
+    const Control c = s.controls[k];
+    if (c.body != b) continue;
+    switch (c.type) {
+      case RK_X_FOR: F.x = c.value; break;
+      case RK_Y_FOR: F.y = c.value; break;
+      case RK_Z_FOR: F.z = c.value; break;
+      case RK_XROT_MOM: M.x = c.value; break;
+      case RK_YROT_MOM: M.y = c.value; break;
+      case RK_ZROT_MOM: M.z = c.value; break;
+      case RK_XYZROT_MOM: M = v3(c.vec[0], c.vec[1], c.vec[2]); break;
+      default: break;
+    }
+  }
+}
+
+// Bodies with many entries (walls, floors): a block loads a chunk of the
+// body's entries in the serial order in parallel, then one thread adds the
+// chunk in that order -- the same sums as the one-thread loop, without its
+// memory latency.
+constexpr int kHeavyChunk = 256;
+__global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s) {
+  __shared__ double sf[kHeavyChunk][3], sm[kHeavyChunk][3];
+  __shared__ int sgn[kHeavyChunk];
+  __shared__ int64_t split;
+  const int b = s.heavy[blockIdx.x];
+  const int t = threadIdx.x;
+  const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
+  const int64_t j0 = s.jofs[b], j1 = s.jofs[b + 1];
+  if (t == 0) {  // first j-side slot whose entry follows b's own block
+    int64_t lo = j0, hi = j1;
+    while (lo < hi) {
+      int64_t m = (lo + hi) >> 1;
+      if (s.jlist[m] < i0) lo = m + 1;
+      else hi = m;
+    }
+    split = lo;
+  }
+  __syncthreads();
+  const int64_t nA = split - j0, nB = i1 - i0, nC = j1 - split;
+  const int64_t L = nA + nB + nC;
+  V3 F, M;
+  if (t == 0) init_resultant(s, b, F, M);
+  for (int64_t c0 = 0; c0 < L; c0 += kHeavyChunk) {
+    const int64_t p = c0 + t;
+    int sign = 0;
+    if (p < L) {
+      int64_t e;
+      bool jside;
+      if (p < nA) { e = s.jlist[j0 + p]; jside = true; }
+      else if (p < nA + nB) { e = i0 + (p - nA); jside = false; }
+      else { e = s.jlist[split + (p - nA - nB)]; jside = true; }
+      if (s.act[e]) {
+        sign = jside ? -1 : 1;
+        V3 f = ld3(s.cf, e), m = jside ? ld3(s.cmj, e) : ld3(s.cmi, e);
+        sf[t][0] = f.x; sf[t][1] = f.y; sf[t][2] = f.z;
+        sm[t][0] = m.x; sm[t][1] = m.y; sm[t][2] = m.z;
+      }
+    }
+    sgn[t] = sign;
+    __syncthreads();
+    if (t == 0) {
+      const int nk = (int)min((int64_t)kHeavyChunk, L - c0);
+      for (int k = 0; k < nk; k++) {
+        if (sgn[k] == 0) continue;
+        V3 f = v3(sf[k][0], sf[k][1], sf[k][2]);
+        F = sgn[k] > 0 ? F + f : F - f;
+        M = M + v3(sm[k][0], sm[k][1], sm[k][2]);
+      }
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    st3(s.force, b, F);
+    st3(s.moment, b, M);
+  }
+}
+
 __global__ void k_gather_accel(Scene s, int apply_kick) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
   const bool driven = b < s.n_driven;
-  V3 F = v3(0, 0, 0), M = v3(0, 0, 0);
-  if (driven) {  // imposed force / moment components (Rockable.cpp:2904-2928)
-    for (int k = 0; k < s.ncontrols; k++) {
-      const Control c = s.controls[k];
-      if (c.body != b) continue;
-      switch (c.type) {
-        case RK_X_FOR: F.x = c.value; break;
-        case RK_Y_FOR: F.y = c.value; break;
-        case RK_Z_FOR: F.z = c.value; break;
-        case RK_XROT_MOM: M.x = c.value; break;
-        case RK_YROT_MOM: M.y = c.value; break;
-        case RK_ZROT_MOM: M.z = c.value; break;
-        case RK_XYZROT_MOM: M = v3(c.vec[0], c.vec[1], c.vec[2]); break;
-        default: break;
-      }
+  V3 F, M;
+  if (s.is_heavy[b]) {  // summed by k_gather_heavy, in the same order
+    F = ld3(s.force, b);
+    M = ld3(s.moment, b);
+  } else {
+    init_resultant(s, b, F, M);
+    // Resultants in the serial order of the active entries (key order): the
+    // j-side entries before b's own block, b's block, the remaining j-side.
+    const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
+    int64_t jk = s.jofs[b];
+    const int64_t j1 = s.jofs[b + 1];
+    for (; jk < j1; ++jk) {
+      const int e = s.jlist[jk];
+      if (e >= i0) break;
+      if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
     }
-  }
-  // Resultants in the serial order of the active entries (key order): the
-  // j-side entries before b's own block, b's block, the remaining j-side.
-  const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
-  int64_t jk = s.jofs[b];
-  const int64_t j1 = s.jofs[b + 1];
-  for (; jk < j1; ++jk) {
-    const int e = s.jlist[jk];
-    if (e >= i0) break;
-    if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
-  }
-  for (int64_t e = i0; e < i1; ++e)
-    if (s.act[e]) { F = F + ld3(s.cf, e); M = M + ld3(s.cmi, e); }
-  for (; jk < j1; ++jk) {
-    const int e = s.jlist[jk];
-    if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
+    for (int64_t e = i0; e < i1; ++e)
+      if (s.act[e]) { F = F + ld3(s.cf, e); M = M + ld3(s.cmi, e); }
+    for (; jk < j1; ++jk) {
+      const int e = s.jlist[jk];
+      if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
+    }
   }
   const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
   const V3 vel = ld3(s.vel, b), vrot = ld3(s.vrot, b);
@@ -671,6 +744,11 @@ int launch_narrow_force(const Scene& s, cudaStream_t st) {
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
   if (s.n <= 0) return 0;
   k_gather_accel<<<nblk(s.n, 128), 128, 0, st>>>(s, apply_kick);
+  return 1;
+}
+int launch_gather_heavy(const Scene& s, cudaStream_t st) {
+  if (s.nheavy <= 0) return 0;
+  k_gather_heavy<<<s.nheavy, kHeavyChunk, 0, st>>>(s);
   return 1;
 }
 int launch_breakage(const Scene& s, cudaStream_t st) {
