@@ -201,6 +201,14 @@ int rk_set_controls(rk_ctx* ctx, const rk_control* c, int32_t n, const rk_servo*
  * RK_FORM_MIXED (FP32 on body-relative coordinates, FP64 for positions, the
  * overlap dn and the integration).  No reference counterpart. */
 int rk_set_form(rk_ctx* ctx, int form);
+/* Broad phase of the NL rebuild: 0 automatic (all pairs up to 4096 bodies,
+ * grid above), 1 all pairs (Rockable's UpdateNL bruteForce), 2 uniform grid
+ * (the role of UpdateNL linkCells).  Both visit exactly the same pairs. */
+int rk_set_broadphase(rk_ctx* ctx, int mode);
+/* Several independent scenes in one context: scene_of[b] for every body
+ * (NULL = one scene).  Bodies of different scenes never interact; every
+ * kernel launch covers all scenes.  No reference counterpart. */
+int rk_set_scenes(rk_ctx* ctx, const int32_t* scene_of);
 /* When on, every step also stores each entry's contact normal, point and
  * relative velocity (needed to write a conf file); off by default. */
 int rk_set_record_geometry(rk_ctx* ctx, int on);
@@ -229,11 +237,53 @@ int rk_get_stats(rk_ctx* ctx, rk_stats* out);
 /* Device time (ms) of the last rk_step call, measured with CUDA events on the
  * context's stream, and the number of kernels it launched. */
 int rk_last_step_timing(const rk_ctx* ctx, double* ms, int64_t* kernels);
+/* Stable LSD radix sort of n 64-bit keys in device memory on bits
+ * [lo_bit, hi_bit), in place, on `stream` (a cudaStream_t, NULL = default).
+ * The primitive the neighbour-list rebuild orders its keys with (the
+ * lexicographic key order of Interaction.hpp:106-122, and the j-side list);
+ * temporary memory is allocated and freed by the call. */
+int rk_sort_keys(uint64_t* keys, int64_t n, int lo_bit, int hi_bit, void* stream);
 /* Per-phase device time: when on, rk_step brackets each phase with CUDA
  * events on the context stream (adds one event pair per phase and step).
  * Phases: 0 controls, 1 drift, 2 global vertices, 3 narrow phase + law,
  * 4 resultants + accelerations, 5 breakage, 6 NL rebuild, 7 guard. */
 #define RK_NPHASE 8
+
+/* Learned Verlet skin (no reference counterpart; replaces the fixed
+ * interVerlet / dVerlet schedule and the dynamic guard of Rockable.cpp:
+ * 1571-1596 while enabled).  An exact bound on every body's point motion
+ * since the last rebuild forces a rebuild when it reaches dVerlet / 2; between
+ * forced rebuilds, a 16-64-64-2 MLP (FP16, trained online on the run's own
+ * displacement and churn history) predicts the next window's displacement
+ * rate, from which the skin (dVerlet, DVerlet = ratio * dVerlet) and the
+ * rebuild interval are chosen by minimising the measured step + rebuild cost. */
+typedef struct rk_skin_config {
+  int32_t enabled;
+  int32_t use_mlp;        /* 0: predict the next window from the last one only */
+  double skin_min, skin_max;
+  double dverlet_ratio;   /* DVerlet / dVerlet */
+  int32_t interval_min, interval_max;
+  double learning_rate;
+  int32_t train_steps;    /* optimiser steps per rebuild */
+  uint64_t seed;
+} rk_skin_config;
+typedef struct rk_skin_stats {
+  int64_t rebuilds, forced, scheduled;
+  double skin;            /* current dVerlet */
+  int64_t interval;       /* current scheduled interval (steps) */
+  double last_rate;       /* observed max displacement per step, last window */
+  double predicted_rate;  /* prediction for the current window */
+  double loss;            /* last training loss */
+} rk_skin_stats;
+int rk_set_skin(rk_ctx* ctx, const rk_skin_config* cfg);
+int rk_get_skin_stats(rk_ctx* ctx, rk_skin_stats* out);
+/* Direct access to the network (tests: gradient checks against a CPU model).
+ * Parameters: W1[64][16] b1[64] W2[64][64] b2[64] W3[2][64] b3[2]. */
+int rk_mlp_num_params(void);
+int rk_mlp_set_params(rk_ctx* ctx, const float* params);
+int rk_mlp_get_params(rk_ctx* ctx, float* params);
+int rk_mlp_forward(rk_ctx* ctx, const float* x, float* y);
+int rk_mlp_gradient(rk_ctx* ctx, const float* X, const float* T, int32_t nbatch, float* grad, float* loss);
 int rk_set_profiling(rk_ctx* ctx, int on);
 int rk_get_profile(const rk_ctx* ctx, double* ms, int64_t* launches);
 

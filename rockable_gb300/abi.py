@@ -66,6 +66,17 @@ class RkServo(C.Structure):
     _fields_ = [("kind", C.c_int32), ("icontr", C.c_int32), ("walls", C.c_int32 * 6), ("pressure", C.c_double)]
 
 
+class RkSkinConfig(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("use_mlp", C.c_int32), ("skin_min", C.c_double), ("skin_max", C.c_double),
+                ("dverlet_ratio", C.c_double), ("interval_min", C.c_int32), ("interval_max", C.c_int32),
+                ("learning_rate", C.c_double), ("train_steps", C.c_int32), ("seed", C.c_uint64)]
+
+
+class RkSkinStats(C.Structure):
+    _fields_ = [("rebuilds", I64), ("forced", I64), ("scheduled", I64), ("skin", C.c_double), ("interval", I64),
+                ("last_rate", C.c_double), ("predicted_rate", C.c_double), ("loss", C.c_double)]
+
+
 class RkStepReport(C.Structure):
     _fields_ = [("steps_done", I64), ("nl_updates", I64), ("n_entries", I64), ("n_active", I64),
                 ("n_broken", I64), ("t", C.c_double)]
@@ -90,6 +101,8 @@ SIGNATURES = {
     "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
     "rk_set_record_geometry": (C.c_int, [P, C.c_int]),
     "rk_set_form": (C.c_int, [P, C.c_int]),
+    "rk_set_broadphase": (C.c_int, [P, C.c_int]),
+    "rk_set_scenes": (C.c_int, [P, P]),
     "rk_accelerations": (C.c_int, [P]),
     "rk_update_nl": (C.c_int, [P]),
     "rk_step": (C.c_int, [P, I64, C.POINTER(RkStepReport)]),
@@ -105,6 +118,14 @@ SIGNATURES = {
     "rk_upload_kinematics": (C.c_int, [P] * 7),
     "rk_set_profiling": (C.c_int, [P, C.c_int]),
     "rk_get_profile": (C.c_int, [P, P, P]),
+    "rk_sort_keys": (C.c_int, [P, I64, C.c_int, C.c_int, P]),
+    "rk_set_skin": (C.c_int, [P, C.POINTER(RkSkinConfig)]),
+    "rk_get_skin_stats": (C.c_int, [P, C.POINTER(RkSkinStats)]),
+    "rk_mlp_num_params": (C.c_int, []),
+    "rk_mlp_set_params": (C.c_int, [P, P]),
+    "rk_mlp_get_params": (C.c_int, [P, P]),
+    "rk_mlp_forward": (C.c_int, [P, P, P]),
+    "rk_mlp_gradient": (C.c_int, [P, P, P, C.c_int32, P, P]),
 }
 
 _lib = None
@@ -222,6 +243,14 @@ class GpuScene:
             sv.pressure = float(servo["pressure"])
         self._chk(self.L.rk_set_controls(self.h, arr, n, C.byref(sv)), "rk_set_controls")
 
+    def set_broadphase(self, mode):
+        self._chk(self.L.rk_set_broadphase(self.h, int(mode)), "rk_set_broadphase")
+
+    def set_scenes(self, scene_of):
+        a = None if scene_of is None else _c(scene_of, np.int32)
+        self._keep.append(a)
+        self._chk(self.L.rk_set_scenes(self.h, _p(a)), "rk_set_scenes")
+
     def set_form(self, form):
         self._chk(self.L.rk_set_form(self.h, int(form)), "rk_set_form")
 
@@ -256,6 +285,43 @@ class GpuScene:
 
     def set_profiling(self, on=True):
         self._chk(self.L.rk_set_profiling(self.h, 1 if on else 0), "rk_set_profiling")
+
+    def set_skin(self, enabled=True, use_mlp=True, skin_min=1e-5, skin_max=1e-3, dverlet_ratio=2.0,
+                 interval_min=5, interval_max=1000, learning_rate=3e-3, train_steps=2, seed=1):
+        cfg = RkSkinConfig(1 if enabled else 0, 1 if use_mlp else 0, skin_min, skin_max, dverlet_ratio, interval_min,
+                           interval_max, learning_rate, train_steps, seed)
+        self._chk(self.L.rk_set_skin(self.h, C.byref(cfg)), "rk_set_skin")
+
+    def skin_stats(self):
+        st = RkSkinStats()
+        self._chk(self.L.rk_get_skin_stats(self.h, C.byref(st)), "rk_get_skin_stats")
+        return {k: getattr(st, k) for k, _ in RkSkinStats._fields_}
+
+    def mlp_num_params(self):
+        return self.L.rk_mlp_num_params()
+
+    def mlp_set_params(self, p):
+        p = _c(p, np.float32)
+        self._chk(self.L.rk_mlp_set_params(self.h, _p(p)), "rk_mlp_set_params")
+
+    def mlp_get_params(self):
+        p = np.zeros(self.mlp_num_params(), np.float32)
+        self._chk(self.L.rk_mlp_get_params(self.h, _p(p)), "rk_mlp_get_params")
+        return p
+
+    def mlp_forward(self, x):
+        x = _c(x, np.float32)
+        y = np.zeros(2, np.float32)
+        self._chk(self.L.rk_mlp_forward(self.h, _p(x), _p(y)), "rk_mlp_forward")
+        return y
+
+    def mlp_gradient(self, X, T):
+        X = _c(X, np.float32)
+        T = _c(T, np.float32)
+        g = np.zeros(self.mlp_num_params(), np.float32)
+        loss = np.zeros(1, np.float32)
+        self._chk(self.L.rk_mlp_gradient(self.h, _p(X), _p(T), len(X), _p(g), _p(loss)), "rk_mlp_gradient")
+        return g, float(loss[0])
 
     PHASES = ["controls", "drift", "glob_vertices", "narrow_force", "gather_accel", "breakage", "nl_rebuild", "guard"]
 

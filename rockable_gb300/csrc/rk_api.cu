@@ -203,6 +203,173 @@ int read_flags(Ctx& c) {
 
 }  // namespace
 
+
+// Resultants of driven bodies that feed no state are summed on demand, from
+// the contributions of the last narrow phase (before they are overwritten or
+// re-ordered by a rebuild).
+static void settle_lazy_forces(Ctx& c) {
+  if (c.forces_stale) {
+    c.kernels += launch_gather_heavy_lazy(c.s, c.stream);
+    c.forces_stale = false;
+  }
+}
+
+// ------------------------------------------------------------ learned skin ----
+static double to_f(unsigned int bits) {
+  float f;
+  std::memcpy(&f, &bits, 4);
+  return (double)f;
+}
+
+static int skin_train(Ctx& c) {
+  Skin& k = c.skin;
+  const int nb = (int)std::min<size_t>(k.rx.size(), (size_t)mlp_max_batch());
+  if (nb < 8) return 0;
+  std::vector<float> X(16 * nb), T(2 * nb);
+  for (int i = 0; i < nb; i++) {
+    for (int q = 0; q < 16; q++) X[16 * i + q] = k.rx[i][q];
+    T[2 * i] = k.ry[i][0];
+    T[2 * i + 1] = k.ry[i][1];
+  }
+  CK(cudaMemcpyAsync(k.X, X.data(), X.size() * 4, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(k.T, T.data(), T.size() * 4, cudaMemcpyHostToDevice, c.stream));
+  for (int it = 0; it < std::max(1, k.cfg.train_steps); it++) {
+    launch_mlp_grad(k.w, k.X, k.T, nb, k.grad, k.loss, c.stream);
+    launch_mlp_adam(k.master, k.w, k.m, k.v, k.grad, (float)k.cfg.learning_rate, ++k.adam_step, c.stream);
+    c.kernels += 2;
+  }
+  float l = 0.f;
+  CK(cudaMemcpyAsync(&l, k.loss, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  k.last_loss = l;
+  return 0;
+}
+
+static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
+  Skin& k = c.skin;
+  Scene& s = c.s;
+  const double N = (double)std::max<int64_t>(1, s.n - s.n_driven);
+  const double ref = k.cfg.skin_max;
+  const double rate = dmax / (double)std::max<int64_t>(1, k.since);
+  const int64_t ne0 = s.ne;
+  const double active = (double)c.h_flags[FLAG_NACTIVE];
+  if (k.since > 0) {  // measured cost of the window
+    float ms = 0.f;
+    CK(cudaEventRecord(k.eb, c.stream));
+    CK(cudaEventSynchronize(k.eb));
+    CK(cudaEventElapsedTime(&ms, k.ea, k.eb));
+    double per = ms / (double)k.since;
+    k.step_ms = k.step_ms > 0 ? 0.7 * k.step_ms + 0.3 * per : per;
+  }
+  k.last_rate = rate;
+  for (int q = 3; q > 0; q--) k.rates[q] = k.rates[q - 1];
+  k.rates[0] = rate;
+  auto lg = [](double x) { return (float)std::log10(std::max(x, 1e-30)); };
+  std::array<float, 16> f{};
+  f[0] = lg(rate / ref);
+  f[1] = lg(k.rates[1] / ref);
+  f[2] = lg(k.rates[2] / ref);
+  f[3] = lg(k.rates[3] / ref);
+  f[4] = lg(vmax * s.dt / ref);
+  f[5] = (float)(active / N);
+  f[6] = (float)((double)ne0 / (N * 50.0));
+  f[7] = lg(k.skin / ref);
+  f[8] = (float)(std::log10((double)k.since + 1.0) / 3.0);
+  f[9] = forced ? 1.f : 0.f;
+  f[10] = (float)std::min(1.0, k.pred_churn);
+  f[11] = lg(k.step_ms + 1e-3);
+  f[12] = lg(k.rebuild_ms + 1e-3);
+  f[13] = (float)std::max(-3.0, std::min(3.0, std::log10(std::max(rate, 1e-30) / std::max(k.rates[1], 1e-30))));
+  f[14] = 1.f;
+  f[15] = 0.f;
+  // prediction of the next window's displacement rate
+  double u = rate, churn = k.pred_churn;
+  if (k.cfg.use_mlp && k.rx.size() >= 8) {
+    float y[2];
+    CK(cudaMemcpyAsync(k.io, f.data(), 64, cudaMemcpyHostToDevice, c.stream));
+    launch_mlp_infer(k.w, k.io, k.io + 16, c.stream);
+    c.kernels++;
+    CK(cudaMemcpyAsync(y, k.io + 16, 8, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    u = std::pow(10.0, (double)y[0]) * ref;
+    churn = std::pow(10.0, (double)y[1]);
+  }
+  if (!(u > 0.0) || !std::isfinite(u)) u = std::max(rate, 1e-30);
+  k.pred_rate = u;
+  // skin and interval minimising the measured step + rebuild cost
+  const double margin = 1.3;
+  const double C = (double)std::max<int64_t>(1, ne0), A = std::min(active, C);
+  const double te = k.step_ms > 0 ? k.step_ms / C : 1e-6;
+  const double R = k.rebuild_ms > 0 ? k.rebuild_ms : 100.0 * te * C;
+  double best = 1e300, best_s = k.skin;
+  int64_t best_k = k.interval;
+  for (int m = -4; m <= 4; m++) {
+    double sk = std::min(k.cfg.skin_max, std::max(k.cfg.skin_min, k.skin * std::pow(2.0, 0.5 * m)));
+    double kk = std::floor(0.5 * sk / std::max(u * margin * (1.0 + churn), 1e-30));
+    int64_t ki = (int64_t)std::max<double>(k.cfg.interval_min, std::min<double>(k.cfg.interval_max, kk));
+    double Cs = A + (C - A) * (sk / std::max(k.skin, 1e-30));
+    double J = te * Cs + R / (double)ki;
+    if (J < best) { best = J; best_s = sk; best_k = ki; }
+  }
+  k.skin = best_s;
+  k.interval = best_k;
+  s.dVerlet = k.skin;
+  s.DVerlet = k.cfg.dverlet_ratio * k.skin;
+  settle_lazy_forces(c);
+  // the rebuild itself, timed
+  float rms = 0.f;
+  CK(cudaEventRecord(k.ea, c.stream));
+  int rc = rebuild_nl(c);
+  if (rc) return rc;
+  CK(cudaEventRecord(k.eb, c.stream));
+  CK(cudaEventSynchronize(k.eb));
+  CK(cudaEventElapsedTime(&rms, k.ea, k.eb));
+  k.rebuild_ms = k.rebuild_ms > 0 ? 0.7 * k.rebuild_ms + 0.3 * rms : rms;
+  c.nl_updates++;
+  k.rebuilds++;
+  if (forced) k.forced++;
+  else k.scheduled++;
+  const double churn_obs = std::fabs((double)s.ne - (double)ne0) / std::max(1.0, (double)ne0);
+  k.pred_churn = churn_obs;
+  // training sample: the previous window's features -> this window's outcome
+  if (k.have_prev) {
+    std::array<float, 2> y{lg(rate / ref), lg(churn_obs + 1e-4)};
+    if (k.rx.size() < (size_t)mlp_max_batch()) {
+      k.rx.push_back(k.feat_prev);
+      k.ry.push_back(y);
+    } else {
+      k.rx[k.rhead] = k.feat_prev;
+      k.ry[k.rhead] = y;
+      k.rhead = (k.rhead + 1) % k.rx.size();
+    }
+  }
+  k.feat_prev = f;
+  k.have_prev = true;
+  if (k.cfg.use_mlp && (rc = skin_train(c))) return rc;
+  launch_skin_snapshot(s, k.ref_pos, k.ref_q, c.stream);
+  c.kernels++;
+  CK(cudaMemsetAsync(s.flags + FLAG_NEED_UPDATE, 0, sizeof(unsigned long long), c.stream));
+  k.since = 0;
+  CK(cudaEventRecord(k.ea, c.stream));
+  return 0;
+}
+
+int skin_after_step(Ctx& c) {
+  Skin& k = c.skin;
+  Scene& s = c.s;
+  CK(cudaMemsetAsync(k.d_guard, 0, 8, c.stream));
+  c.kernels += launch_skin_guard(s, k.ref_pos, k.ref_q, k.rsw, k.d_guard, c.stream);
+  CK(cudaMemcpyAsync(k.h_guard, k.d_guard, 8, cudaMemcpyDeviceToHost, c.stream));
+  int rc;
+  if ((rc = read_flags(c))) return rc;
+  k.since++;
+  const double dmax = to_f(k.h_guard[0]), vmax = to_f(k.h_guard[1]);
+  const bool forced = dmax >= 0.5 * k.skin;
+  const bool need = c.h_flags[FLAG_NEED_UPDATE] != 0ull;
+  if (forced || need || k.since >= k.interval) return skin_rebuild(c, dmax, vmax, forced);
+  return 0;
+}
+
 extern "C" {
 
 int rk_abi_version(void) { return RK_ABI_VERSION; }
@@ -260,7 +427,8 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.gv); dfree(s.bobb); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jlist);
-  dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs);
+  dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.heavy_lazy); dfree(s.bnd);
+  dfree(s.needres); dfree(s.scene_of);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
   dfree(s.if_break); dfree(s.if_ofs); dfree(s.flags);
   free_entrybuf(c.eb[0]);
@@ -268,8 +436,18 @@ void rk_destroy(rk_ctx* x) {
   NLWork& w = c.w;
   dfree(w.pairs); dfree(w.hp); dfree(w.hp_tmp); dfree(w.hp_cnt); dfree(w.hp_mask); dfree(w.cand); dfree(w.cand_src);
   dfree(w.flag); dfree(w.stale); dfree(w.stale_src); dfree(w.fkey); dfree(w.fsrc); dfree(w.jkeys); dfree(w.jtmp);
-  dfree(w.tmp); dfree(w.counter);
+  dfree(w.tmp); dfree(w.counter); dfree(w.gkeys); dfree(w.gtmp); dfree(w.gover); dfree(w.gis_over);
+  if (w.gstat) cudaFree(w.gstat);
   dfree(c.d_ke);
+  {
+    Skin& k = c.skin;
+    dfree(k.ref_pos); dfree(k.ref_q); dfree(k.rsw); dfree(k.d_guard); dfree(k.master); dfree(k.m); dfree(k.v);
+    dfree(k.grad); dfree(k.loss); dfree(k.X); dfree(k.T); dfree(k.io);
+    if (k.w) cudaFree(k.w);
+    if (k.h_guard) cudaFreeHost(k.h_guard);
+    if (k.ea) cudaEventDestroy(k.ea);
+    if (k.eb) cudaEventDestroy(k.eb);
+  }
   for (int k = 0; k < 2 * RK_NPHASE; k++)
     if (c.pev[k]) cudaEventDestroy(c.pev[k]);
   if (c.h_flags) cudaFreeHost(c.h_flags);
@@ -300,6 +478,12 @@ int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
     c.shape_ne[k] = e;
     c.shape_nf[k] = f;
   }
+  c.shape_vmax.assign(ns, 0.0);
+  for (int k = 0; k < ns; k++)
+    for (int v = sh->vert_ofs[k]; v < sh->vert_ofs[k + 1]; v++) {
+      const double* p = sh->vertices + 3 * (int64_t)v;
+      c.shape_vmax[k] = std::max(c.shape_vmax[k], std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]));
+    }
   for (int f = 0; f < nf; f++)
     if (sh->face_vofs[f + 1] - sh->face_vofs[f] < 3) return fail(c, RK_ERR_ARG, "a face has fewer than 3 vertices");
   Scene& s = c.s;
@@ -359,9 +543,15 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.jofs, (const int64_t*)nullptr, n + 1)) ||
       (rc = dupload(c, s.if_ofs, (const int64_t*)nullptr, n + 1)) ||
       (rc = dupload(c, s.sph_ofs, sph_ofs.data(), n + 1)) || (rc = dalloc(c, s.sph, sph_ofs[n])) ||
-      (rc = dupload(c, s.is_heavy, (const uint8_t*)nullptr, n)) || (rc = dalloc(c, s.heavy, n)))
+      (rc = dupload(c, s.is_heavy, (const uint8_t*)nullptr, n)) || (rc = dalloc(c, s.heavy, n)) ||
+      (rc = dalloc(c, s.heavy_lazy, n)) || (rc = dalloc(c, s.bnd, n)) || (rc = dalloc(c, s.needres, n)))
     return rc;
   s.nheavy = 0;
+  s.nheavy_lazy = 0;
+  dfree(s.scene_of);
+  c.needres_host.assign(n, 1);
+  for (int64_t i = 0; i < b->n_driven; i++) c.needres_host[i] = 0;
+  CK(cudaMemcpyAsync(s.needres, c.needres_host.data(), n, cudaMemcpyHostToDevice, c.stream));
   if (!c.w.counter) CK(cudaMalloc(&c.w.counter, 64));
   // deltaQ starts as the identity quaternion
   std::vector<double> dq(4 * n, 0.0);
@@ -371,6 +561,8 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
   s.n = n;
   s.n_driven = b->n_driven;
   s.nvert = nv;
+  c.body_shape.assign(b->shape, b->shape + n);
+  c.body_hom.assign(b->homothety, b->homothety + n);
   s.ne = 0;
   s.nif = 0;
   c.have_bodies = true;
@@ -511,6 +703,11 @@ int rk_set_controls(rk_ctx* x, const rk_control* cs, int32_t n, const rk_servo* 
   int rc;
   if ((rc = dupload(c, s.controls, v.data(), n))) return rc;
   s.ncontrols = n;
+  for (int64_t i = 0; i < s.n; i++) c.needres_host[i] = i >= s.n_driven ? 1 : 0;
+  for (auto& q : v)
+    if (q.type >= RK_X_FOR && q.type != RK_XYZROT_VEL) c.needres_host[q.body] = 1;
+  CK(cudaMemcpyAsync(s.needres, c.needres_host.data(), s.n, cudaMemcpyHostToDevice, c.stream));
+  if (s.ne > 0 && (rc = heavy_list(c))) return rc;
   s.servo_kind = 0;
   if (servo && servo->kind == 1) {
     if (servo->icontr < 0 || servo->icontr + 5 >= n) return fail(c, RK_ERR_ARG, "servo control index out of range");
@@ -529,6 +726,188 @@ int rk_set_controls(rk_ctx* x, const rk_control* cs, int32_t n, const rk_servo* 
   return RK_OK;
 }
 
+
+static int ready(Ctx& c) {
+  if (!c.have_shapes || !c.have_bodies || !c.have_params)
+    return fail(c, RK_ERR_STATE, "shapes, bodies and parameters must be uploaded first");
+  return 0;
+}
+
+static int skin_alloc(Ctx& c) {
+  Skin& k = c.skin;
+  Scene& s = c.s;
+  const int np = mlp_num_params();
+  int rc;
+  if (!k.ref_pos) {
+    if ((rc = dalloc(c, k.ref_pos, 3 * s.n)) || (rc = dalloc(c, k.ref_q, 4 * s.n)) || (rc = dalloc(c, k.rsw, s.n)) ||
+        (rc = dalloc(c, k.d_guard, 2)) || (rc = dalloc(c, k.master, np)) || (rc = dalloc(c, k.m, np)) ||
+        (rc = dalloc(c, k.v, np)) || (rc = dalloc(c, k.grad, np)) || (rc = dalloc(c, k.loss, 1)) ||
+        (rc = dalloc(c, k.X, 16 * mlp_max_batch())) || (rc = dalloc(c, k.T, 2 * mlp_max_batch())) ||
+        (rc = dalloc(c, k.io, 32)))
+      return rc;
+    char* wbuf = nullptr;
+    CK(cudaMalloc(&wbuf, 2 * (size_t)np));
+    k.w = wbuf;
+    CK(cudaMallocHost(&k.h_guard, 8));
+    CK(cudaEventCreate(&k.ea));
+    CK(cudaEventCreate(&k.eb));
+  }
+  return 0;
+}
+
+int rk_mlp_num_params(void) { return mlp_num_params(); }
+
+int rk_mlp_set_params(rk_ctx* x, const float* p) {
+  if (!x || !p) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies first");
+  int rc;
+  if ((rc = skin_alloc(c))) return rc;
+  Skin& k = c.skin;
+  CK(cudaMemcpyAsync(k.master, p, 4 * (size_t)mlp_num_params(), cudaMemcpyHostToDevice, c.stream));
+  launch_mlp_to_half(k.master, k.w, c.stream);
+  CK(cudaMemsetAsync(k.m, 0, 4 * (size_t)mlp_num_params(), c.stream));
+  CK(cudaMemsetAsync(k.v, 0, 4 * (size_t)mlp_num_params(), c.stream));
+  k.adam_step = 0;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_mlp_get_params(rk_ctx* x, float* p) {
+  if (!x || !p) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  if (!c.skin.master) return fail(c, RK_ERR_STATE, "no network");
+  CK(cudaMemcpyAsync(p, c.skin.master, 4 * (size_t)mlp_num_params(), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_mlp_forward(rk_ctx* x, const float* in, float* out) {
+  if (!x || !in || !out) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  if (!c.skin.master) return fail(c, RK_ERR_STATE, "no network");
+  Skin& k = c.skin;
+  CK(cudaMemcpyAsync(k.io, in, 64, cudaMemcpyHostToDevice, c.stream));
+  launch_mlp_infer(k.w, k.io, k.io + 16, c.stream);
+  CK(cudaMemcpyAsync(out, k.io + 16, 8, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_mlp_gradient(rk_ctx* x, const float* X, const float* T, int32_t nb, float* grad, float* loss) {
+  if (!x || !X || !T || nb <= 0) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  if (!c.skin.master) return fail(c, RK_ERR_STATE, "no network");
+  if (nb > mlp_max_batch()) return fail(c, RK_ERR_CAPACITY, "batch larger than 128");
+  Skin& k = c.skin;
+  CK(cudaMemcpyAsync(k.X, X, 64 * (size_t)nb, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(k.T, T, 8 * (size_t)nb, cudaMemcpyHostToDevice, c.stream));
+  launch_mlp_grad(k.w, k.X, k.T, nb, k.grad, k.loss, c.stream);
+  if (grad) CK(cudaMemcpyAsync(grad, k.grad, 4 * (size_t)mlp_num_params(), cudaMemcpyDeviceToHost, c.stream));
+  if (loss) CK(cudaMemcpyAsync(loss, k.loss, 4, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  CK(cudaGetLastError());
+  return RK_OK;
+}
+
+int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
+  if (!x || !cfg) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  int rc;
+  if ((rc = ready(c))) return rc;
+  Skin& k = c.skin;
+  if (!cfg->enabled) {
+    k.on = false;
+    return RK_OK;
+  }
+  if (!(cfg->skin_min > 0.0) || cfg->skin_max < cfg->skin_min || cfg->interval_min < 1 ||
+      cfg->interval_max < cfg->interval_min || !(cfg->dverlet_ratio >= 1.0))
+    return fail(c, RK_ERR_ARG, "invalid skin configuration");
+  if ((rc = skin_alloc(c))) return rc;
+  Scene& s = c.s;
+  k.cfg = *cfg;
+  // swing radius of every body (largest vertex distance, scaled)
+  std::vector<float> rsw(s.n);
+  for (int64_t b = 0; b < s.n; b++) rsw[b] = (float)(c.body_hom[b] * c.shape_vmax[c.body_shape[b]] * (1.0 + 1e-6));
+  CK(cudaMemcpyAsync(k.rsw, rsw.data(), rsw.size() * 4, cudaMemcpyHostToDevice, c.stream));
+  // network: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from the seed, zero biases
+  const int np = mlp_num_params();
+  std::vector<float> p(np, 0.f);
+  uint64_t st = cfg->seed ? cfg->seed : 0x9E3779B97F4A7C15ull;
+  auto rnd = [&]() {
+    st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+    return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+  };
+  const int layers[3][3] = {{0, 64, 16}, {64 * 16 + 64, 64, 64}, {64 * 16 + 64 + 64 * 64 + 64, 2, 64}};
+  for (auto& L : layers) {
+    double a = 1.0 / std::sqrt((double)L[2]);
+    for (int q = 0; q < L[1] * L[2]; q++) p[L[0] + q] = (float)((2.0 * rnd() - 1.0) * a);
+  }
+  CK(cudaMemcpyAsync(k.master, p.data(), 4 * (size_t)np, cudaMemcpyHostToDevice, c.stream));
+  launch_mlp_to_half(k.master, k.w, c.stream);
+  CK(cudaMemsetAsync(k.m, 0, 4 * (size_t)np, c.stream));
+  CK(cudaMemsetAsync(k.v, 0, 4 * (size_t)np, c.stream));
+  k.adam_step = 0;
+  k.rx.clear();
+  k.ry.clear();
+  k.rhead = 0;
+  k.have_prev = false;
+  k.skin = std::min(cfg->skin_max, std::max(cfg->skin_min, s.dVerlet));
+  k.interval = cfg->interval_min;
+  k.since = 0;
+  k.rebuilds = k.forced = k.scheduled = 0;
+  k.step_ms = k.rebuild_ms = 0.0;
+  for (double& r : k.rates) r = 0.0;
+  s.dVerlet = k.skin;
+  s.DVerlet = cfg->dverlet_ratio * k.skin;
+  k.on = true;
+  // start from a fresh list built with the initial skin
+  launch_glob_vertices(s, c.stream);
+  if ((rc = rebuild_nl(c))) return rc;
+  launch_skin_snapshot(s, k.ref_pos, k.ref_q, c.stream);
+  CK(cudaEventRecord(k.ea, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_get_skin_stats(rk_ctx* x, rk_skin_stats* o) {
+  if (!x || !o) return RK_ERR_ARG;
+  Skin& k = x->c.skin;
+  o->rebuilds = k.rebuilds;
+  o->forced = k.forced;
+  o->scheduled = k.scheduled;
+  o->skin = k.skin;
+  o->interval = k.interval;
+  o->last_rate = k.last_rate;
+  o->predicted_rate = k.pred_rate;
+  o->loss = k.last_loss;
+  return RK_OK;
+}
+
+int rk_set_broadphase(rk_ctx* x, int mode) {
+  if (!x || mode < 0 || mode > 2) return RK_ERR_ARG;
+  x->c.broadphase = mode;
+  return RK_OK;
+}
+
+int rk_set_scenes(rk_ctx* x, const int32_t* scene_of) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies first");
+  Scene& s = c.s;
+  if (!scene_of) {
+    dfree(s.scene_of);
+    return RK_OK;
+  }
+  int rc;
+  if ((rc = dupload(c, s.scene_of, scene_of, s.n))) return rc;
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
 int rk_set_form(rk_ctx* x, int form) {
   if (!x) return RK_ERR_ARG;
   if (form != RK_FORM_FP64 && form != RK_FORM_MIXED) return fail(x->c, RK_ERR_UNSUPPORTED, "unknown form");
@@ -542,11 +921,6 @@ int rk_set_record_geometry(rk_ctx* x, int on) {
   return RK_OK;
 }
 
-static int ready(Ctx& c) {
-  if (!c.have_shapes || !c.have_bodies || !c.have_params)
-    return fail(c, RK_ERR_STATE, "shapes, bodies and parameters must be uploaded first");
-  return 0;
-}
 
 // Rockable::accelerations without a time increment (the load-time step).
 int rk_accelerations(rk_ctx* x) {
@@ -563,6 +937,7 @@ int rk_accelerations(rk_ctx* x) {
   launch_gather_heavy(s, c.stream);
   launch_gather_accel(s, 0, c.stream);
   launch_breakage(s, c.stream);
+  c.forces_stale = s.nheavy_lazy > 0;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c.stream));
   return RK_OK;
@@ -574,6 +949,7 @@ int rk_update_nl(rk_ctx* x) {
   cudaSetDevice(c.device);
   int rc;
   if ((rc = ready(c))) return rc;
+  settle_lazy_forces(c);
   launch_glob_vertices(c.s, c.stream);
   if ((rc = rebuild_nl(c))) return rc;
   c.nl_updates++;
@@ -620,13 +996,20 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
     mark(3, false);
     phase(3, c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream));
     mark(4, false); phase(4, launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream));
+    c.forces_stale = s.nheavy_lazy > 0;
     mark(5, false); phase(5, launch_breakage(s, c.stream));
+    if (c.skin.on) {
+      if ((rc = skin_after_step(c))) return rc;
+      c.steps++;
+      continue;
+    }
     bool need = false;
     if (need_flags) {
       if ((rc = read_flags(c))) return rc;
       need = c.h_flags[FLAG_NEED_UPDATE] != 0ull;
     }
     if (need || c.interVerletC >= c.interVerlet - s.dt_2) {
+      settle_lazy_forces(c);
       mark(6, false);
       int64_t k1 = c.kernels;
       if ((rc = rebuild_nl(c))) return rc;
@@ -676,6 +1059,7 @@ int rk_download_bodies(rk_ctx* x, double* pos, double* vel, double* acc, double*
   Ctx& c = x->c;
   cudaSetDevice(c.device);
   Scene& s = c.s;
+  if (force || moment) settle_lazy_forces(c);
   const size_t n3 = 3 * (size_t)s.n * sizeof(double);
   if (pos) CK(cudaMemcpyAsync(pos, s.pos, n3, cudaMemcpyDeviceToHost, c.stream));
   if (vel) CK(cudaMemcpyAsync(vel, s.vel, n3, cudaMemcpyDeviceToHost, c.stream));
@@ -726,11 +1110,20 @@ int rk_download_entries(rk_ctx* x, int32_t* i, int32_t* j, int32_t* type, int32_
   if (mom) CK(cudaMemcpyAsync(mom, s.mom, d3, cudaMemcpyDeviceToHost, c.stream));
   if (damp) CK(cudaMemcpyAsync(damp, s.damp, d1, cudaMemcpyDeviceToHost, c.stream));
   if (bond) CK(cudaMemcpyAsync(bond, s.bond, i1, cudaMemcpyDeviceToHost, c.stream));
-  if (active) CK(cudaMemcpyAsync(active, s.act, (size_t)ne, cudaMemcpyDeviceToHost, c.stream));
+  std::vector<double> dn_h;
+  std::vector<int32_t> bond_h;
+  if (active) {  // active = dn < 0 or bonded (Rockable.cpp:3005-3029), from the stored history
+    dn_h.resize(ne);
+    bond_h.resize(ne);
+    CK(cudaMemcpyAsync(dn_h.data(), s.dn, d1, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(bond_h.data(), s.bond, i1, cudaMemcpyDeviceToHost, c.stream));
+  }
   if (n) CK(cudaMemcpyAsync(n, s.gn, d3, cudaMemcpyDeviceToHost, c.stream));
   if (pos) CK(cudaMemcpyAsync(pos, s.gpos, d3, cudaMemcpyDeviceToHost, c.stream));
   if (vel) CK(cudaMemcpyAsync(vel, s.gvel, d3, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
+  if (active)
+    for (int64_t e = 0; e < ne; e++) active[e] = (dn_h[e] < 0.0 || bond_h[e] >= 0) ? 1 : 0;
   return RK_OK;
 }
 
@@ -796,6 +1189,24 @@ int rk_upload_kinematics(rk_ctx* x, const double* pos, const double* vel, const 
   if (vrot) CK(cudaMemcpyAsync(s.vrot, vrot, n3, cudaMemcpyHostToDevice, c.stream));
   if (arot) CK(cudaMemcpyAsync(s.arot, arot, n3, cudaMemcpyHostToDevice, c.stream));
   return RK_OK;
+}
+
+int rk_sort_keys(uint64_t* keys, int64_t n, int lo_bit, int hi_bit, void* stream) {
+  if (n < 0 || (n > 0 && !keys) || lo_bit < 0 || hi_bit > 64 || lo_bit >= hi_bit) return RK_ERR_ARG;
+  if (n <= 1) return RK_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint64_t* tmp = nullptr;
+  void* temp = nullptr;
+  if (cudaMalloc(&tmp, (size_t)n * sizeof(uint64_t)) != cudaSuccess) return RK_ERR_CUDA;
+  if (cudaMalloc(&temp, sort_temp_bytes(n)) != cudaSuccess) {
+    cudaFree(tmp);
+    return RK_ERR_CUDA;
+  }
+  radix_sort_u64(keys, tmp, n, lo_bit, hi_bit, temp, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(tmp);
+  cudaFree(temp);
+  return e == cudaSuccess ? RK_OK : RK_ERR_CUDA;
 }
 
 int rk_set_profiling(rk_ctx* x, int on) {

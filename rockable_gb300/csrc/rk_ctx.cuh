@@ -1,6 +1,7 @@
 // rk_ctx.cuh -- host-side context of librk_gpu.so (one scene on one GPU).
 #pragma once
 #include <cstdint>
+#include <array>
 #include <string>
 #include <vector>
 
@@ -39,6 +40,43 @@ struct NLWork {
   uint64_t* jtmp = nullptr;      // fin_cap
   void* tmp = nullptr;           // scan / sort temp
   unsigned long long* counter = nullptr;
+  // grid broad phase
+  int64_t grid_cap = 0;
+  uint64_t* gkeys = nullptr;
+  uint64_t* gtmp = nullptr;
+  int* gover = nullptr;
+  uint8_t* gis_over = nullptr;
+  void* gstat = nullptr;
+};
+
+// Learned-skin state (rk_skin.cu kernels, policy in rk_api.cu).
+struct Skin {
+  rk_skin_config cfg{};
+  bool on = false;
+  double* ref_pos = nullptr;
+  double* ref_q = nullptr;
+  float* rsw = nullptr;
+  unsigned int* d_guard = nullptr;  // [0] max delta bits, [1] max |v| bits
+  unsigned int* h_guard = nullptr;  // pinned
+  // MLP
+  float* master = nullptr;
+  void* w = nullptr;
+  float *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr, *X = nullptr, *T = nullptr, *io = nullptr;
+  int adam_step = 0;
+  std::vector<std::array<float, 16>> rx;
+  std::vector<std::array<float, 2>> ry;
+  size_t rhead = 0;
+  std::array<float, 16> feat_prev{};
+  bool have_prev = false;
+  // window bookkeeping
+  int64_t since = 0, interval = 100;
+  double skin = 0.0;
+  double rates[4] = {0, 0, 0, 0};
+  double last_rate = 0.0, pred_rate = 0.0, pred_churn = 0.0, last_loss = 0.0;
+  int64_t rebuilds = 0, forced = 0, scheduled = 0;
+  double step_ms = 0.0, rebuild_ms = 0.0;  // measured costs (exponential averages)
+  cudaEvent_t ea = nullptr, eb = nullptr;
+  double window_ms = 0.0;
 };
 
 struct Ctx {
@@ -56,6 +94,9 @@ struct Ctx {
   std::vector<int> shape_nv;  // vertices per shape
   std::vector<double> shape_radius;
   std::vector<int> shape_ne, shape_nf;
+  std::vector<double> shape_vmax;      // largest vertex distance from the shape centre
+  std::vector<int> body_shape;
+  std::vector<double> body_hom;
   bool have_shapes = false, have_bodies = false, have_params = false;
   // loop bookkeeping (Rockable::integrate)
   double t = 0.0, interVerlet = 0.01, interVerletC = 0.0;
@@ -73,6 +114,12 @@ struct Ctx {
   cudaEvent_t pev[2 * RK_NPHASE] = {};
   double prof_ms[RK_NPHASE] = {};
   int64_t prof_n[RK_NPHASE] = {};
+  Skin skin;
+  int broadphase = 0;  // 0 automatic, 1 all pairs, 2 grid
+  float last_cell = 0.f;
+  int64_t last_nover = 0;
+  bool forces_stale = false;
+  std::vector<uint8_t> needres_host;
 };
 
 int rebuild_nl(Ctx& c);

@@ -108,7 +108,12 @@ struct Scene {
   int* jlist;     // ne
   int* heavy;     // bodies whose entry count exceeds kHeavy (summed by a block each)
   int nheavy;
-  uint8_t* is_heavy;  // n
+  int* heavy_lazy;    // heavy driven bodies whose resultant feeds no state (summed on demand)
+  int nheavy_lazy;
+  uint8_t* is_heavy;  // n: 1 summed by k_gather_heavy in the step, 2 deferred
+  uint8_t* needres;   // n: 1 when the body's resultant is used by the step (free or force-controlled)
+  float* bnd;         // n: largest distance of a vertex from the body centre (world, rounded up)
+  int* scene_of;      // n: scene index (bodies of different scenes never interact)
   float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
   int64_t* sph_ofs;   // n+1
   // ---- interfaces
@@ -136,9 +141,23 @@ int launch_narrow_force(const Scene& s, cudaStream_t st);
 int launch_narrow_force_mixed(const Scene& s, cudaStream_t st);
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st);
 int launch_gather_heavy(const Scene& s, cudaStream_t st);
+int launch_gather_heavy_lazy(const Scene& s, cudaStream_t st);
 int launch_breakage(const Scene& s, cudaStream_t st);
 int launch_guard(const Scene& s, cudaStream_t st);
 int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);
+
+// learned skin (rk_skin.cu)
+int launch_skin_snapshot(const Scene& s, double* rp, double* rq, cudaStream_t st);
+int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, unsigned int* out,
+                      cudaStream_t st);
+int mlp_num_params();
+int mlp_max_batch();
+void launch_mlp_infer(const void* w, const float* x, float* y, cudaStream_t st);
+void launch_mlp_grad(const void* w, const float* X, const float* T, int nb, float* grad, float* loss,
+                     cudaStream_t st);
+void launch_mlp_adam(float* master, void* w, float* m, float* v, const float* grad, float lr, int step,
+                     cudaStream_t st);
+void launch_mlp_to_half(const float* master, void* w, cudaStream_t st);
 
 // primitives (rk_prims.cu)
 size_t scan_temp_bytes(int64_t n);

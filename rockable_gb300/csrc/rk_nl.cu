@@ -21,6 +21,7 @@
 //   history carry -> i-side offsets and j-side list.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 
 #include "rk_ctx.cuh"
 
@@ -91,7 +92,13 @@ __global__ void k_spheres(Scene s) {
   const int nv = s.vert_ofs[sh + 1] - s.vert_ofs[sh];
   const int e0 = s.edge_ofs[sh], ne = s.edge_ofs[sh + 1] - e0;
   const int f0 = s.face_ofs[sh], nf = s.face_ofs[sh + 1] - f0;
-  for (int v = 0; v < nv; v++) out[v] = make_float4((float)g[3 * v], (float)g[3 * v + 1], (float)g[3 * v + 2], 0.f);
+  double r2 = 0.0;
+  for (int v = 0; v < nv; v++) {
+    out[v] = make_float4((float)g[3 * v], (float)g[3 * v + 1], (float)g[3 * v + 2], 0.f);
+    double dx = g[3 * v] - s.pos[3 * b], dy = g[3 * v + 1] - s.pos[3 * b + 1], dz = g[3 * v + 2] - s.pos[3 * b + 2];
+    r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
+  }
+  s.bnd[b] = __double2float_ru(sqrt(r2));
   for (int e = 0; e < ne; e++) {
     V3 a = g3(g, s.edges[2 * (e0 + e)]), c = g3(g, s.edges[2 * (e0 + e) + 1]);
     V3 m = 0.5 * (a + c);
@@ -100,23 +107,41 @@ __global__ void k_spheres(Scene s) {
   }
   for (int f = 0; f < nf; f++) {
     const int v0 = s.face_vofs[f0 + f], k = s.face_vofs[f0 + f + 1] - v0;
-    V3 c = v3(0, 0, 0);
+    V3 c = v3(0, 0, 0);  // centroid of the face vertices
     for (int q = 0; q < k; q++) c = c + g3(g, s.face_verts[v0 + q]);
     c = (1.0 / k) * c;
-    double r2 = 0.0;
-    for (int q = 0; q < k; q++) r2 = fmax(r2, norm2(g3(g, s.face_verts[v0 + q]) - c));
-    out[nv + ne + f] = make_float4((float)c.x, (float)c.y, (float)c.z, __double2float_ru(sqrt(r2)));
+    double rf2 = 0.0;
+    for (int q = 0; q < k; q++) rf2 = fmax(rf2, norm2(g3(g, s.face_verts[v0 + q]) - c));
+    out[nv + ne + f] = make_float4((float)c.x, (float)c.y, (float)c.z, __double2float_ru(sqrt(rf2)));
   }
 }
 
-// bodies whose resultant is summed by a block (see k_gather_heavy)
+// bodies whose resultant is summed by a block (see k_gather_heavy): in the
+// step when the resultant is used, on demand otherwise
 __global__ void k_heavy(Scene s, unsigned long long* count) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
   int64_t c = (s.iofs[b + 1] - s.iofs[b]) + (s.jofs[b + 1] - s.jofs[b]);
   bool h = c > kHeavy;
-  s.is_heavy[b] = h ? 1 : 0;
-  if (h) s.heavy[atomicAdd(count, 1ull)] = (int)b;
+  uint8_t kind = 0;
+  if (h && s.needres[b]) {
+    kind = 1;
+    s.heavy[atomicAdd(&count[0], 1ull)] = (int)b;
+  } else if (h) {
+    kind = 2;
+    s.heavy_lazy[atomicAdd(&count[1], 1ull)] = (int)b;
+  }
+  s.is_heavy[b] = kind;
+}
+
+__device__ __forceinline__ int64_t lower_bound_u64(const uint64_t* a, int64_t n, uint64_t x) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t m = (lo + hi) >> 1;
+    if (a[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
 }
 
 __device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
@@ -155,6 +180,7 @@ __global__ void k_pairs(Scene s, uint64_t* pairs, int64_t cap, unsigned long lon
           sb[t][2] > a[5])
         continue;
       if (i < s.n_driven && j < s.n_driven) continue;
+      if (s.scene_of && s.scene_of[i] != s.scene_of[j]) continue;
       if (has_iface(s, (int)i, (int)j)) continue;
       Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
       enlarge(oi, 0.5 * s.DVerlet);
@@ -164,6 +190,115 @@ __global__ void k_pairs(Scene s, uint64_t* pairs, int64_t cap, unsigned long lon
       if ((int64_t)k < cap) pairs[k] = ((uint64_t)i << 21) | (uint64_t)j;
     }
   }
+}
+
+
+// ------------------------------------------------------------- grid ----
+// Uniform grid broad phase (the role of Rockable's linkCells,
+// Rockable.cpp:1667-1809): bodies are binned by the centre of their enlarged
+// AABB in cells at least as large as every non-oversized body's AABB, so two
+// boxes that overlap are in the same or adjacent cells; bodies larger than a
+// cell (walls, floors, slopes) are tested against every body of their scene.
+// The pair predicate is the same as the all-pairs one: same pairs found.
+__device__ __forceinline__ bool pair_predicate(const Scene& s, int64_t i, int64_t j) {
+  // i < j
+  if (i < s.n_driven && j < s.n_driven) return false;
+  if (s.scene_of && s.scene_of[i] != s.scene_of[j]) return false;
+  const float* a = s.baabb + 6 * i;
+  const float* b = s.baabb + 6 * j;
+  if (a[0] > b[3] || b[0] > a[3] || a[1] > b[4] || b[1] > a[4] || a[2] > b[5] || b[2] > a[5]) return false;
+  if (has_iface(s, (int)i, (int)j)) return false;
+  Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
+  enlarge(oi, 0.5 * s.DVerlet);
+  enlarge(oj, 0.5 * s.DVerlet);
+  return obb_intersect(oi, oj);
+}
+
+__device__ __forceinline__ float extent_of(const float* bb) {
+  return fmaxf(fmaxf(bb[3] - bb[0], bb[4] - bb[1]), bb[5] - bb[2]);
+}
+
+__global__ void k_grid_sum(Scene s, double* sum) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double e = b < s.n ? (double)extent_of(s.baabb + 6 * b) : 0.0;
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sum, e);
+}
+
+__global__ void k_grid_max(Scene s, float lim, unsigned int* maxbits) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float e = 0.f;
+  if (b < s.n) {
+    e = extent_of(s.baabb + 6 * b);
+    if (!(e <= lim)) e = 0.f;
+  }
+  for (int o = 16; o > 0; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(e));
+}
+
+__device__ __forceinline__ int cell_coord(float x, float inv_cell) {
+  float f = floorf(x * inv_cell) + 8192.f;
+  f = fminf(fmaxf(f, 0.f), 16383.f);
+  return (int)f;
+}
+
+__global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys, int* over,
+                            unsigned long long* nover) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= s.n) return;
+  const float* bb = s.baabb + 6 * b;
+  if (extent_of(bb) > cell) {
+    keys[b] = ~0ull;
+    over[atomicAdd(nover, 1ull)] = (int)b;
+    return;
+  }
+  const int cx = cell_coord(0.5f * (bb[0] + bb[3]), inv_cell), cy = cell_coord(0.5f * (bb[1] + bb[4]), inv_cell),
+            cz = cell_coord(0.5f * (bb[2] + bb[5]), inv_cell);
+  const uint64_t code = ((uint64_t)cx << 28) | ((uint64_t)cy << 14) | (uint64_t)cz;
+  keys[b] = (code << 21) | (uint64_t)b;
+}
+
+__global__ void k_grid_pairs(Scene s, const uint64_t* keys, int64_t nnorm, float inv_cell, uint64_t* pairs,
+                             int64_t cap, unsigned long long* counter) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nnorm) return;
+  const uint64_t key = keys[k];
+  const int64_t i = (int64_t)(key & ((1u << 21) - 1));
+  const uint64_t code = key >> 21;
+  const int cx = (int)(code >> 28), cy = (int)((code >> 14) & 16383), cz = (int)(code & 16383);
+  for (int dx = -1; dx <= 1; dx++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dz = -1; dz <= 1; dz++) {
+        const int x = cx + dx, y = cy + dy, z = cz + dz;
+        if (x < 0 || y < 0 || z < 0 || x > 16383 || y > 16383 || z > 16383) continue;
+        const uint64_t c2 = ((uint64_t)x << 28) | ((uint64_t)y << 14) | (uint64_t)z;
+        int64_t q = lower_bound_u64(keys, nnorm, c2 << 21);
+        for (; q < nnorm && (keys[q] >> 21) == c2; q++) {
+          const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
+          if (j <= i) continue;
+          if (!pair_predicate(s, i, j)) continue;
+          unsigned long long at = atomicAdd(counter, 1ull);
+          if ((int64_t)at < cap) pairs[at] = ((uint64_t)i << 21) | (uint64_t)j;
+        }
+      }
+}
+
+// oversized body o against every body j of its scene (each pair once)
+__global__ void k_over_pairs(Scene s, const int* over, const uint8_t* is_over, uint64_t* pairs, int64_t cap,
+                             unsigned long long* counter) {
+  int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int o = over[blockIdx.y];
+  if (j >= s.n || j == o) return;
+  if (is_over[j] && j < o) return;  // counted from the other oversized body
+  const int64_t i0 = min((int64_t)o, j), j0 = max((int64_t)o, j);
+  if (!pair_predicate(s, i0, j0)) return;
+  unsigned long long at = atomicAdd(counter, 1ull);
+  if ((int64_t)at < cap) pairs[at] = ((uint64_t)i0 << 21) | (uint64_t)j0;
+}
+
+__global__ void k_mark_over(const int* over, int nover, uint8_t* is_over) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nover) is_over[over[k]] = 1;
 }
 
 __global__ void k_half_pairs(const uint64_t* pairs, int64_t np, uint64_t* hp) {
@@ -307,6 +442,32 @@ __global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* 
     return dx * dx + dy * dy + dz * dz > lim * lim;
   };
   const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
+  // two-sided culling: only the sub-elements of one body that can reach the
+  // other body's bounding sphere take part
+  const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
+  const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
+  constexpr int kW = 8;  // up to 256 edges / faces per shape are culled, more are all kept
+  uint32_t mpv[2] = {0u, 0u}, mpe[kW], mpf[kW], mbe[kW];
+  for (int q = 0; q < kW; q++) mpe[q] = mpf[q] = mbe[q] = 0u;
+  for (int w = 0; w < nvp; w++)
+    if (!far(sp[w], cb, cb.w)) mpv[w >> 5] |= 1u << (w & 31);
+  const bool cull_pe = nep <= 32 * kW, cull_pf = nfp <= 32 * kW, cull_be = neb <= 32 * kW;
+  if (cull_pe)
+    for (int e = 0; e < nep; e++) {
+      const float4 se = sp[nvp + e];
+      if (!far(se, cb, cb.w + ve_ext * se.w)) mpe[e >> 5] |= 1u << (e & 31);
+    }
+  if (cull_pf)
+    for (int f = 0; f < nfp; f++) {
+      const float4 sf = sp[nvp + nep + f];
+      if (!far(sf, cb, cb.w + sf.w)) mpf[f >> 5] |= 1u << (f & 31);
+    }
+  if (cull_be && b < p)
+    for (int e = 0; e < neb; e++) {
+      const float4 se = sb[nvb + e];
+      if (!far(se, cp, cp.w + se.w)) mbe[e >> 5] |= 1u << (e & 31);
+    }
+  auto on = [](const uint32_t* mk, bool cull, int k) { return !cull || ((mk[k >> 5] >> (k & 31)) & 1u); };
   int64_t c = 0;
   uint64_t* o = (MODE == 1) ? out + ofs[h] : nullptr;
   auto emit = [&](int t, int i1, int j1) {
@@ -317,24 +478,28 @@ __global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* 
     for (int v = 0; v < nvb; v++)
       if (m[v >> 5] >> (v & 31) & 1u)
         for (int w = 0; w < nvp; w++)
-          if (!far(sb[v], sp[w], 0.f) && near_vv(P, v, w)) emit(0, v, w);
+          if ((mpv[w >> 5] >> (w & 31) & 1u) && !far(sb[v], sp[w], 0.f) && near_vv(P, v, w)) emit(0, v, w);
   }
   for (int v = 0; v < nvb; v++)
     if (m[v >> 5] >> (v & 31) & 1u)
       for (int e = 0; e < nep; e++) {
+        if (!on(mpe, cull_pe, e)) continue;
         const float4 se = sp[nvp + e];
         if (!far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e)) emit(1, v, e);
       }
   for (int v = 0; v < nvb; v++)
     if (m[v >> 5] >> (v & 31) & 1u)
       for (int f = 0; f < nfp; f++) {
+        if (!on(mpf, cull_pf, f)) continue;
         const float4 sf = sp[nvp + nep + f];
         if (!far(sb[v], sf, sf.w) && near_vf(s, P, v, f)) emit(2, v, f);
       }
   if (b < p) {
     for (int e = 0; e < neb; e++) {
+      if (!on(mbe, cull_be, e)) continue;
       const float4 s1 = sb[nvb + e];
       for (int e2 = 0; e2 < nep; e2++) {
+        if (!on(mpe, cull_pe, e2)) continue;
         const float4 s2 = sp[nvp + e2];
         if (!far(s1, s2, s1.w + s2.w) && near_ee(s, P, e, e2)) emit(3, e, e2);
       }
@@ -343,15 +508,6 @@ __global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* 
   if (MODE == 0) cnt[h] = c;
 }
 
-__device__ __forceinline__ int64_t lower_bound_u64(const uint64_t* a, int64_t n, uint64_t x) {
-  int64_t lo = 0, hi = n;
-  while (lo < hi) {
-    int64_t m = (lo + hi) >> 1;
-    if (a[m] < x) lo = m + 1;
-    else hi = m;
-  }
-  return lo;
-}
 
 // Old entries that were not tested this time are kept as they are.
 __global__ void k_stale_flag(const uint64_t* okey, int64_t no, const uint64_t* hp, int64_t nhp, const uint32_t* mask,
@@ -529,22 +685,84 @@ int rebuild_nl(Ctx& c) {
     w.pair_cap = nc;
   }
   if (!w.counter) RKCHK(cudaMalloc(&w.counter, 64));
-  int64_t np = 0;
-  for (int attempt = 0; attempt < 4; attempt++) {
-    RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
-    k_pairs<<<nblk(N, kPairTile), kPairTile, 0, st>>>(s, w.pairs, w.pair_cap, w.counter);
-    c.kernels++;
-    unsigned long long cnt = 0;
-    RKCHK(cudaMemcpyAsync(&cnt, w.counter, 8, cudaMemcpyDeviceToHost, st));
+  int64_t np = -1;
+  bool use_grid = (c.broadphase == 2) || (c.broadphase == 0 && N > 4096);
+  float cell = 0.f;
+  int64_t nover = 0;
+  if (use_grid) {
+    // cell size: the largest extent among bodies not larger than 4x the mean
+    if (w.grid_cap < N) {
+      if ((rc = grow(c, w.gkeys, w.grid_cap, N)) || (rc = grow(c, w.gtmp, w.grid_cap, N)) ||
+          (rc = grow(c, w.gover, w.grid_cap, N)) || (rc = grow(c, w.gis_over, w.grid_cap, N)))
+        return rc;
+      w.grid_cap = N;
+    }
+    if (!w.gstat) RKCHK(cudaMalloc(&w.gstat, 64));
+    RKCHK(cudaMemsetAsync(w.gstat, 0, 64, st));
+    k_grid_sum<<<nblk(N, 256), 256, 0, st>>>(s, (double*)w.gstat);
+    double mean_sum = 0.0;
+    RKCHK(cudaMemcpyAsync(&mean_sum, w.gstat, 8, cudaMemcpyDeviceToHost, st));
     RKCHK(cudaStreamSynchronize(st));
-    np = (int64_t)cnt;
-    if (np <= w.pair_cap) break;
-    int64_t nc = np + np / 2 + 1024;
-    if ((rc = grow(c, w.pairs, w.pair_cap, nc))) return rc;
-    w.pair_cap = nc;
-    np = -1;
+    const float lim = (float)(4.0 * mean_sum / (double)N);
+    k_grid_max<<<nblk(N, 256), 256, 0, st>>>(s, lim, (unsigned int*)((char*)w.gstat + 8));
+    unsigned int mb = 0;
+    RKCHK(cudaMemcpyAsync(&mb, (char*)w.gstat + 8, 4, cudaMemcpyDeviceToHost, st));
+    RKCHK(cudaStreamSynchronize(st));
+    std::memcpy(&cell, &mb, 4);
+    cell *= 1.01f;
+    c.kernels += 2;
+    if (!(cell > 0.f)) use_grid = false;
+  }
+  if (use_grid) {
+    const float inv = 1.0f / cell;
+    RKCHK(cudaMemsetAsync((char*)w.gstat + 16, 0, 8, st));
+    RKCHK(cudaMemsetAsync(w.gis_over, 0, N, st));
+    k_grid_keys<<<nblk(N, 256), 256, 0, st>>>(s, cell, inv, w.gkeys, w.gover, (unsigned long long*)((char*)w.gstat + 16));
+    unsigned long long no_ = 0;
+    RKCHK(cudaMemcpyAsync(&no_, (char*)w.gstat + 16, 8, cudaMemcpyDeviceToHost, st));
+    RKCHK(cudaStreamSynchronize(st));
+    nover = (int64_t)no_;
+    if ((rc = ensure_tmp(c, (int64_t)sort_temp_bytes(N)))) return rc;
+    radix_sort_u64(w.gkeys, w.gtmp, N, 21, 63, w.tmp, st);
+    if (nover > 0) k_mark_over<<<nblk(nover, 256), 256, 0, st>>>(w.gover, (int)nover, w.gis_over);
+    c.kernels += 16;
+    for (int attempt = 0; attempt < 4; attempt++) {
+      RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
+      k_grid_pairs<<<nblk(N - nover, 128), 128, 0, st>>>(s, w.gkeys, N - nover, inv, w.pairs, w.pair_cap, w.counter);
+      if (nover > 0) {
+        dim3 g2(nblk(N, 128), (unsigned)nover);
+        k_over_pairs<<<g2, 128, 0, st>>>(s, w.gover, w.gis_over, w.pairs, w.pair_cap, w.counter);
+      }
+      c.kernels += 2;
+      unsigned long long cnt = 0;
+      RKCHK(cudaMemcpyAsync(&cnt, w.counter, 8, cudaMemcpyDeviceToHost, st));
+      RKCHK(cudaStreamSynchronize(st));
+      np = (int64_t)cnt;
+      if (np <= w.pair_cap) break;
+      int64_t nc = np + np / 2 + 1024;
+      if ((rc = grow(c, w.pairs, w.pair_cap, nc))) return rc;
+      w.pair_cap = nc;
+      np = -1;
+    }
+  } else {
+    for (int attempt = 0; attempt < 4; attempt++) {
+      RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
+      k_pairs<<<nblk(N, kPairTile), kPairTile, 0, st>>>(s, w.pairs, w.pair_cap, w.counter);
+      c.kernels++;
+      unsigned long long cnt = 0;
+      RKCHK(cudaMemcpyAsync(&cnt, w.counter, 8, cudaMemcpyDeviceToHost, st));
+      RKCHK(cudaStreamSynchronize(st));
+      np = (int64_t)cnt;
+      if (np <= w.pair_cap) break;
+      int64_t nc = np + np / 2 + 1024;
+      if ((rc = grow(c, w.pairs, w.pair_cap, nc))) return rc;
+      w.pair_cap = nc;
+      np = -1;
+    }
   }
   if (np < 0) { c.err = "pair buffer kept overflowing"; return RK_ERR_CAPACITY; }
+  c.last_cell = cell;
+  c.last_nover = nover;
   const int64_t nhp = 2 * np;
   if (w.hp_cap < nhp + 1) {
     int64_t nc = nhp + nhp / 2 + 1024;
@@ -646,13 +864,14 @@ int rebuild_nl(Ctx& c) {
 
 int heavy_list(Ctx& c) {
   Scene& s = c.s;
-  RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 8, c.stream));
+  RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 16, c.stream));
   k_heavy<<<nblk(s.n, 256), 256, 0, c.stream>>>(s, c.w.counter + 1);
   c.kernels++;
-  unsigned long long nh = 0;
-  RKCHK(cudaMemcpyAsync(&nh, c.w.counter + 1, 8, cudaMemcpyDeviceToHost, c.stream));
+  unsigned long long nh[2] = {0, 0};
+  RKCHK(cudaMemcpyAsync(nh, c.w.counter + 1, 16, cudaMemcpyDeviceToHost, c.stream));
   RKCHK(cudaStreamSynchronize(c.stream));
-  s.nheavy = (int)nh;
+  s.nheavy = (int)nh[0];
+  s.nheavy_lazy = (int)nh[1];
   return 0;
 }
 

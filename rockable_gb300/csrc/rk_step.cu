@@ -444,11 +444,11 @@ __device__ __forceinline__ void init_resultant(const Scene& s, int64_t b, V3& F,
 // chunk in that order -- the same sums as the one-thread loop, without its
 // memory latency.
 constexpr int kHeavyChunk = 256;
-__global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s) {
+__global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s, const int* list) {
   __shared__ double sf[kHeavyChunk][3], sm[kHeavyChunk][3];
   __shared__ int sgn[kHeavyChunk];
   __shared__ int64_t split;
-  const int b = s.heavy[blockIdx.x];
+  const int b = list[blockIdx.x];
   const int t = threadIdx.x;
   const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
   const int64_t j0 = s.jofs[b], j1 = s.jofs[b + 1];
@@ -506,6 +506,13 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   if (b >= s.n) return;
   const bool driven = b < s.n_driven;
   V3 F, M;
+  if (s.is_heavy[b] == 2) {
+    // a driven body whose resultant feeds no state (no force / moment
+    // control): summed on demand by k_gather_heavy when downloaded
+    st3(s.acc, b, v3(0, 0, 0));
+    st3(s.arot, b, v3(0, 0, 0));
+    return;
+  }
   if (s.is_heavy[b]) {  // summed by k_gather_heavy, in the same order
     F = ld3(s.force, b);
     M = ld3(s.moment, b);
@@ -748,7 +755,12 @@ int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
 }
 int launch_gather_heavy(const Scene& s, cudaStream_t st) {
   if (s.nheavy <= 0) return 0;
-  k_gather_heavy<<<s.nheavy, kHeavyChunk, 0, st>>>(s);
+  k_gather_heavy<<<s.nheavy, kHeavyChunk, 0, st>>>(s, s.heavy);
+  return 1;
+}
+int launch_gather_heavy_lazy(const Scene& s, cudaStream_t st) {
+  if (s.nheavy_lazy <= 0) return 0;
+  k_gather_heavy<<<s.nheavy_lazy, kHeavyChunk, 0, st>>>(s, s.heavy_lazy);
   return 1;
 }
 int launch_breakage(const Scene& s, cudaStream_t st) {

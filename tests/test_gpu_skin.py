@@ -1,0 +1,101 @@
+"""Learned Verlet skin (GPU): the FP16 network's gradients against the CPU
+FP64 model, and the skin policy on a settled pile -- the exact guard keeps the
+contacts of a run that rebuilds every step, and the network's proposals are
+compared with the method without it."""
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(scene):
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene
+    g = GpuScene()
+    g.upload_shapes(scene["shape_tables"])
+    g.upload_bodies(scene["bodies"], scene["n_driven"])
+    scenes.set_scene_params(g, scene)
+    return g
+
+
+def test_mlp_fp16_gradient_matches_cpu_model(gpu_lib):
+    from rockable_gb300 import scenes
+    scene = scenes.sphero_cube_box()
+    g = _engine(scene)
+    rng = np.random.default_rng(7)
+    p = (rng.normal(scale=0.25, size=mlp_ref.NP)).astype(np.float32)
+    g.mlp_set_params(p)
+    X = rng.normal(size=(64, 16)).astype(np.float32)
+    T = rng.normal(size=(64, 2)).astype(np.float32)
+    gg, lg = g.mlp_gradient(X, T)
+    lc, gc = mlp_ref.loss_and_grad(p.astype(np.float64), X, T, half=True)
+    assert abs(lg - lc) <= 1e-3 * abs(lc) + 1e-6
+    scale = np.max(np.abs(gc))
+    assert np.max(np.abs(gg - gc)) <= 5e-3 * scale, np.max(np.abs(gg - gc)) / scale
+    y = g.mlp_forward(X[0])
+    yc, _ = mlp_ref.forward(p.astype(np.float64), X[:1], half=True)
+    assert np.max(np.abs(y - yc[0])) <= 1e-3 * (np.max(np.abs(yc)) + 1e-3)
+
+
+def _pairs(e):
+    act = e["active"]
+    return set(zip(e["i"][act].tolist(), e["j"][act].tolist()))
+
+
+def test_guard_keeps_the_contacts_of_per_step_rebuilds(gpu_lib):
+    from rockable_gb300 import scenes
+    scene = scenes.column_collapse(n=2000, nshapes=64)
+    gs = scenes.settle(scene, steps=1500)
+    src = scenes.scene_from_gpu(scene, gs)
+    gl = _engine(src)
+    gl.upload_entries(src["entries"])
+    gl.set_skin(skin_min=0.02 * scene["dVerlet"], skin_max=2.0 * scene["dVerlet"], interval_min=1,
+                interval_max=200)
+    gr = _engine(src)
+    gr.upload_entries(src["entries"])
+    # reference: rebuild every step with the largest skin
+    import copy
+    sc2 = copy.deepcopy(scene)
+    sc2["interVerlet"] = scene["dt"] * 0.999
+    sc2["dVerlet"] = 2.0 * scene["dVerlet"]
+    sc2["DVerlet"] = 2.0 * sc2["dVerlet"]
+    scenes.set_scene_params(gr, sc2)
+    gr.update_nl()
+    for _ in range(6):
+        gl.step(20)
+        gr.step(20)
+        pl, pr = _pairs(gl.entries()), _pairs(gr.entries())
+        missing = pr - pl
+        assert len(missing) <= max(1, len(pr) // 1000), (len(missing), len(pr))
+    st = gl.skin_stats()
+    assert st["rebuilds"] >= 1
+
+
+def test_learned_skin_against_the_method_without_it(gpu_lib):
+    """Same settled pile, 600 steps: fixed interval (plain), guard + last-window
+    predictor, guard + trained network.  Prints rebuilds and device time."""
+    from rockable_gb300 import scenes
+    scene = scenes.column_collapse(n=3000, nshapes=64)
+    gs = scenes.settle(scene, steps=1500)
+    src = scenes.scene_from_gpu(scene, gs)
+    res = {}
+    for name in ["plain", "naive", "mlp"]:
+        g = _engine(src)
+        g.upload_entries(src["entries"])
+        if name != "plain":
+            g.set_skin(use_mlp=(name == "mlp"), skin_min=0.05 * scene["dVerlet"], skin_max=4.0 * scene["dVerlet"],
+                       interval_min=2, interval_max=400, seed=11)
+        else:
+            g.update_nl()
+        r = g.step(600)
+        ms, _ = g.last_step_timing()
+        sk = g.skin_stats() if name != "plain" else {}
+        res[name] = {"ms": ms, "nl_updates": r["nl_updates"], "active": r["n_active"], "entries": r["n_entries"],
+                     "skin": sk}
+        g.close()
+    print("learned skin comparison:", res)
+    for name in ["naive", "mlp"]:
+        assert res[name]["nl_updates"] >= 1
+        assert abs(res[name]["active"] - res["plain"]["active"]) <= 0.05 * res["plain"]["active"] + 5
