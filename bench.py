@@ -48,6 +48,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle-steps", type=int, default=4000)
+    ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin",
+                    help="comma list of the forms to time (the last one is the headline)")
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes of the batched slope workload (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--batch-settle", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -152,6 +158,74 @@ def cpu_baseline(scene, budget_s):
                 steps, o.n, el)}
 
 
+def batched_workload(a, dev):
+    """Many independent slope scenes (N ~ U{200..5000} grains each, slopes
+    25-45 degrees, Default law) in ONE engine context: every launch covers all
+    scenes, each step's launches replay as one CUDA graph.  Reports the
+    aggregate particle-steps/s, and each scene's own step time when it runs
+    alone in a context of its own (the spread, and the sum that batching
+    replaces)."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene
+    t0 = time.perf_counter()
+    bt = scenes.slope_batch(nscenes=a.batch_scenes)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g = scenes.settle(bt, steps=a.batch_settle, dt=5e-6, kn=bt["params"]["kn"], gboost=10.0, damping=0.5,
+                      device=dev, law="Default")
+    src = scenes.scene_from_gpu(bt, g)
+    g.close()
+    t_settle = time.perf_counter() - t0
+    nfree = int(sum(bt["free_per_scene"]))
+
+    def engine(sc, entries=None):
+        e = GpuScene(device=dev)
+        e.upload_shapes(sc["shape_tables"])
+        e.upload_bodies(sc["bodies"], sc["n_driven"])
+        if sc.get("scene_of") is not None:
+            e.set_scenes(sc["scene_of"])
+        scenes.set_scene_params(e, sc)
+        if entries is not None:
+            e.upload_entries(entries)
+        else:
+            e.update_nl()
+        e.set_graphs(True)
+        return e
+
+    e = engine(src, src["entries"])
+    e.step(max(3, a.warmup))
+    clocks = Clocks()
+    e.synchronize()
+    clocks.start()
+    rep = e.step(a.batch_steps)
+    ms, launches = e.last_step_timing()
+    ck = clocks.stop()
+    st = e.stats()
+    gst = e.graph_stats()
+    e.close()
+    solo = []
+    for k in range(len(bt["free_per_scene"])):
+        part = scenes.part_of(src, k)
+        p = engine(part)
+        p.step(3)
+        p.step(a.batch_steps)
+        pms, _ = p.last_step_timing()
+        solo.append(pms / a.batch_steps)
+        p.close()
+    solo = np.array(solo)
+    return {"workload": bt["name"], "scenes": len(solo), "free_bodies": nfree, "bodies": int(len(bt["scene_of"])),
+            "law": "Default", "form": "plain FP64, step graphs", "steps": a.batch_steps,
+            "value": nfree * a.batch_steps / (ms / 1000.0), "unit": "particle-steps/s",
+            "ms_per_step": ms / a.batch_steps, "gpu_launches": int(launches), "graph": gst,
+            "entries": int(st["n_entries"]), "active": int(st["n_active"]), "nl_rebuilds_in_timed": int(rep["nl_updates"]),
+            "clocks": ck,
+            "solo_ms_per_step": {"min": float(solo.min()), "median": float(np.median(solo)),
+                                 "p90": float(np.percentile(solo, 90)), "max": float(solo.max()),
+                                 "sum": float(solo.sum())},
+            "batched_vs_solo_sum": float(solo.sum() / (ms / a.batch_steps)),
+            "setup_s": {"generate": t_gen, "settle": t_settle}}
+
+
 def run_reference(a, rank):
     if rank != 0:
         return
@@ -199,47 +273,91 @@ def main():
         g.upload_bodies(b, scene["n_driven"])
         scenes.set_scene_params(g, scene)
     t_settle = time.perf_counter() - t_settle
-    g.update_nl()
-    g.step(a.warmup)
-    # ---- timed region (device-resident state)
-    clocks = Clocks()
-    if dist:
-        dist.barrier()
-    g.synchronize()
-    clocks.start()
-    nvtx = None
-    try:
-        import torch
-        nvtx = torch.cuda.nvtx
-        nvtx.range_push("timed")
-    except Exception:
+    # the settled state S every form starts from
+    src = scenes.scene_from_gpu(scene, g) if a.scene == "column" else None
+    g.close()
+    from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
+
+    def engine(form):
+        e = GpuScene(device=dev, form=form)
+        e.upload_shapes(scene["shape_tables"])
+        e.upload_bodies(src["bodies"] if src else b, scene["n_driven"])
+        scenes.set_scene_params(e, scene)
+        if src:
+            e.upload_entries(src["entries"])
+        return e
+
+    def timed(e, steps, label):
+        clocks = Clocks()
+        if dist:
+            dist.barrier()
+        e.synchronize()
+        clocks.start()
         nvtx = None
-    t0 = time.perf_counter()
-    rep = g.step(a.steps)
-    wall = time.perf_counter() - t0
-    if nvtx:
-        nvtx.range_pop()
-    ms, launches = g.last_step_timing()
-    ck = clocks.stop()
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * nfree * a.steps / (ms / 1000.0)
-    st = g.stats()
-    # ---- per-phase profile (outside the timed region)
-    nprof = max(1, min(a.steps, 120))
-    g.set_profiling(True)
-    g.step(nprof)
-    prof = g.profile()
-    g.set_profiling(False)
+        try:
+            import torch
+            nvtx = torch.cuda.nvtx
+            nvtx.range_push("timed_" + label)
+        except Exception:
+            nvtx = None
+        t0 = time.perf_counter()
+        rep = e.step(steps)
+        wall = time.perf_counter() - t0
+        if nvtx:
+            nvtx.range_pop()
+        ms, launches = e.last_step_timing()
+        ck = clocks.stop()
+        if dist:
+            import torch
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return {"ms": ms, "launches": launches, "wall": wall, "rep": rep, "clocks": ck,
+                "value": ws * nfree * steps / (ms / 1000.0)}
+
+    def profile(e, n):
+        e.set_profiling(True)
+        e.step(n)
+        p = e.profile()
+        e.set_profiling(False)
+        return p
+
+    forms = {}
+    dmin = scene["dVerlet"]
+    known = {"plain_fp64": (RK_FORM_FP64, False), "mixed": (RK_FORM_MIXED, False),
+             "mixed_learned_skin": (RK_FORM_MIXED, True)}
+    order = [f.strip() for f in a.forms.split(",") if f.strip()]
+    for label in order:
+        form, skin = known[label]
+        e = engine(form)
+        if skin:
+            e.set_skin(use_mlp=True, skin_min=0.1 * dmin, skin_max=4.0 * dmin, dverlet_ratio=2.0, interval_min=2,
+                       interval_max=1000, seed=3)
+        else:
+            e.update_nl()
+        e.step(a.warmup)
+        r = timed(e, a.steps, label)
+        st = e.stats()
+        nprof = max(1, min(a.steps, 120))
+        prof = profile(e, nprof)
+        r.update({"entries": st["n_entries"], "active": st["n_active"], "prof": prof, "nprof": nprof,
+                  "skin": e.skin_stats() if skin else None})
+        forms[label] = r
+        if label != order[-1]:
+            e.close()
+        else:
+            g = e
+    head = forms[order[-1]]
+    ms, launches, wall, rep, ck, value = (head["ms"], head["launches"], head["wall"], head["rep"], head["clocks"],
+                                          head["value"])
+    prof, nprof = head["prof"], head["nprof"]
     nphase = prof["narrow_force"]
     t_narrow = nphase[0] / max(nphase[1], 1)  # ms per launch
-    C = st["n_entries"]
-    hbm, src = peaks()
+    C = head["entries"]
+    hbm, src_peak = peaks()
     achieved = 140.0 * C / (t_narrow / 1000.0) / 1e9 if t_narrow > 0 else None
-    # ---- e2e through the C ABI with host-owned state
+    st = {"n_entries": C, "n_active": head["active"]}
+    # ---- e2e through the C ABI with host-owned state (headline form)
     e2e = None
     if not a.no_e2e:
         hb = {k: pinned((N, 4 if k == "Q" else 3)) for k in ["pos", "vel", "acc", "Q", "vrot", "arot"]}
@@ -252,36 +370,48 @@ def main():
         for _ in range(k_e2e):
             g.upload_kinematics(hb["pos"], hb["vel"], hb["acc"], hb["Q"], hb["vrot"], hb["arot"])
             g.step(1)
-            out = g.bodies()
+            out_b = g.bodies()
             for k in hb:
-                hb[k][...] = out[k]
+                hb[k][...] = out_b[k]
         el = time.perf_counter() - t0
         e2e = {"value": ws * nfree * k_e2e / el, "unit": "particle-steps/s",
                "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 25 * 8),
                "steps": k_e2e, "note": "every step: kinematics H2D from pinned host, rk_step, full body state D2H"}
+    batched = None
+    if rank == 0 and a.batch_scenes > 0:
+        batched = batched_workload(a, dev)
     cpu = None
     if rank == 0 and not a.no_cpu:
-        cpu = cpu_baseline(scenes.scene_from_gpu(scene, g), a.cpu_seconds)
+        cpu = cpu_baseline(src if src else scene, a.cpu_seconds)
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, rockable_gb300.scenes)",
-               "form": "plain FP64 (bit-identical to the reference CPU arithmetic)",
+               "vs_baseline": None, "dtype": "f64+f32 (mixed form; plain form is f64)",
+               "data": "synthetic (seeded generator, rockable_gb300.scenes)",
+               "form": "mixed precision + learned skin (headline); plain FP64 and mixed without skin alongside",
+               "forms": {k: {"value": v["value"], "ms_per_step": v["ms"] / a.steps, "entries": v["entries"],
+                             "active": v["active"], "nl_rebuilds_in_timed": v["rep"]["nl_updates"],
+                             "gpu_launches": v["launches"], "skin": v["skin"],
+                             "phases_ms_per_step": {q: w[0] / v["nprof"] for q, w in v["prof"].items()}}
+                         for k, v in forms.items()},
+               "headline_form": order[-1],
+               "headline_vs_plain": (head["value"] / forms["plain_fp64"]["value"]) if "plain_fp64" in forms else None,
                "config": {"workload": scene["name"], "law": scene["law"], "bodies": N, "free_bodies": nfree,
                           "entries": int(C), "active": int(st["n_active"]),
                           "nl_rebuilds_in_timed": int(rep["nl_updates"]), "dt": scene["dt"],
                           "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
-                          "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if C * 240 > 129e6 else
-                          "working set below L2 size", "parallelism": "replicas" if ws > 1 else "single GPU"},
+                          "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if C * 240 + N * 600 > 129e6 else
+                          "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
+                          "parallelism": "replicas" if ws > 1 else "single GPU"},
                "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
                "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
                             "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": None,
-                            "peak_source": src, "bytes_per_entry": 140, "entries": int(C),
+                            "peak_source": src_peak, "bytes_per_entry": 140, "entries": int(C),
                             "ms_per_launch": t_narrow},
                "setup": {"settle_s": t_settle, "settle_log": settle_log},
                "phases_ms_per_step": {k: v[0] / nprof for k, v in prof.items()},
                "phases_launches": {k: v[1] for k, v in prof.items()},
-               "e2e": e2e, "cpu_baseline": cpu}
+               "e2e": e2e, "cpu_baseline": cpu, "batched": batched}
         print(json.dumps(out), flush=True)
     g.close()
     if dist:

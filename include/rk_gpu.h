@@ -209,6 +209,13 @@ int rk_set_broadphase(rk_ctx* ctx, int mode);
  * (NULL = one scene).  Bodies of different scenes never interact; every
  * kernel launch covers all scenes.  No reference counterpart. */
 int rk_set_scenes(rk_ctx* ctx, const int32_t* scene_of);
+/* When on (off by default), rk_step replays each step's launches as one CUDA
+ * graph captured on the context stream, re-captured after a neighbour-list
+ * rebuild or a parameter change; per-phase profiling turns it off.  Results
+ * are identical to the launch-by-launch path.  No reference counterpart. */
+int rk_set_graphs(rk_ctx* ctx, int on);
+/* Number of step-graph captures and replays since the context was created. */
+int rk_get_graph_stats(const rk_ctx* ctx, int64_t* captures, int64_t* replays);
 /* When on, every step also stores each entry's contact normal, point and
  * relative velocity (needed to write a conf file); off by default. */
 int rk_set_record_geometry(rk_ctx* ctx, int on);

@@ -103,6 +103,8 @@ SIGNATURES = {
     "rk_set_form": (C.c_int, [P, C.c_int]),
     "rk_set_broadphase": (C.c_int, [P, C.c_int]),
     "rk_set_scenes": (C.c_int, [P, P]),
+    "rk_set_graphs": (C.c_int, [P, C.c_int]),
+    "rk_get_graph_stats": (C.c_int, [P, P, P]),
     "rk_accelerations": (C.c_int, [P]),
     "rk_update_nl": (C.c_int, [P]),
     "rk_step": (C.c_int, [P, I64, C.POINTER(RkStepReport)]),
@@ -245,6 +247,14 @@ class GpuScene:
 
     def set_broadphase(self, mode):
         self._chk(self.L.rk_set_broadphase(self.h, int(mode)), "rk_set_broadphase")
+
+    def set_graphs(self, on=True):
+        self._chk(self.L.rk_set_graphs(self.h, int(bool(on))), "rk_set_graphs")
+
+    def graph_stats(self):
+        a, b = C.c_int64(0), C.c_int64(0)
+        self._chk(self.L.rk_get_graph_stats(self.h, C.byref(a), C.byref(b)), "rk_get_graph_stats")
+        return {"captures": a.value, "replays": b.value}
 
     def set_scenes(self, scene_of):
         a = None if scene_of is None else _c(scene_of, np.int32)

@@ -354,6 +354,70 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   return 0;
 }
 
+// The launches of one step body (flag reset, controls, drift, global
+// vertices, narrow phase + law, resultants + accelerations, breakage) as one
+// CUDA graph: captured on the context stream the first time and whenever the
+// scene description the kernels receive by value has changed since (a
+// rebuild swaps the entry buffers, a parameter call changes scalars), then
+// replayed.  Same kernels, same arguments, same order as the launch-by-launch
+// path, so the results are identical.
+static int step_launches(Ctx& c) {
+  Scene& s = c.s;
+  int n = 0;
+  n += launch_controls_pre(s, c.stream);
+  n += launch_drift(s, c.stream);
+  n += launch_glob_vertices(s, c.stream);
+  n += c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream);
+  n += launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream);
+  n += launch_breakage(s, c.stream);
+  return n;
+}
+
+static int step_graph(Ctx& c) {
+  Scene& s = c.s;
+  const bool stale = !c.gexec || c.gform != c.form || std::memcmp(&c.gscene, &s, sizeof(Scene)) != 0;
+  if (stale) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream);
+    int n = step_launches(c);
+    cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      c.err = std::string("step graph capture: ") + cudaGetErrorString(e);
+      return RK_ERR_CUDA;
+    }
+    bool updated = false;
+    if (c.gexec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(c.gexec, g, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(c.gexec);
+        c.gexec = nullptr;
+      }
+    }
+    if (!updated) {
+      e = cudaGraphInstantiate(&c.gexec, g, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        c.gexec = nullptr;
+        c.err = std::string("step graph instantiation: ") + cudaGetErrorString(e);
+        return RK_ERR_CUDA;
+      }
+    }
+    cudaGraphDestroy(g);
+    std::memcpy(&c.gscene, &s, sizeof(Scene));  // byte copy: the comparison above is bytewise
+    c.gform = c.form;
+    c.glaunched = n;
+    c.graph_captures++;
+  }
+  CK(cudaGraphLaunch(c.gexec, c.stream));
+  c.graph_replays++;
+  c.kernels += c.glaunched;
+  return RK_OK;
+}
+
 int skin_after_step(Ctx& c) {
   Skin& k = c.skin;
   Scene& s = c.s;
@@ -419,6 +483,7 @@ void rk_destroy(rk_ctx* x) {
   Ctx& c = x->c;
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.gexec) cudaGraphExecDestroy(c.gexec);
   Scene& s = c.s;
   dfree(s.vert_ofs); dfree(s.edge_ofs); dfree(s.edges); dfree(s.face_ofs); dfree(s.face_vofs); dfree(s.face_verts);
   dfree(s.svert); dfree(s.sradius); dfree(s.sobb);
@@ -908,6 +973,19 @@ int rk_set_scenes(rk_ctx* x, const int32_t* scene_of) {
   return RK_OK;
 }
 
+int rk_set_graphs(rk_ctx* x, int on) {
+  if (!x) return RK_ERR_ARG;
+  x->c.use_graphs = on ? 1 : 0;
+  return RK_OK;
+}
+
+int rk_get_graph_stats(const rk_ctx* x, int64_t* captures, int64_t* replays) {
+  if (!x) return RK_ERR_ARG;
+  if (captures) *captures = x->c.graph_captures;
+  if (replays) *replays = x->c.graph_replays;
+  return RK_OK;
+}
+
 int rk_set_form(rk_ctx* x, int form) {
   if (!x) return RK_ERR_ARG;
   if (form != RK_FORM_FP64 && form != RK_FORM_MIXED) return fail(x->c, RK_ERR_UNSUPPORTED, "unknown form");
@@ -973,7 +1051,12 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
   for (int64_t it = 0; it < nsteps; it++) {
     c.t += s.dt;
     c.interVerletC += s.dt;
-    CK(cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream));
+    const bool graphed = c.use_graphs && !c.profiling;
+    if (graphed) {
+      if ((rc = step_graph(c))) return rc;
+    } else {
+      CK(cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream));
+    }
     int ph = 0;
     auto mark = [&](int phase, bool end) {
       if (c.profiling) cudaEventRecord(c.pev[2 * phase + (end ? 1 : 0)], c.stream);
@@ -990,14 +1073,16 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
         c.prof_n[p] += launched;
       }
     };
-    mark(0, false); phase(0, launch_controls_pre(s, c.stream));
-    mark(1, false); phase(1, launch_drift(s, c.stream));
-    mark(2, false); phase(2, launch_glob_vertices(s, c.stream));
-    mark(3, false);
-    phase(3, c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream));
-    mark(4, false); phase(4, launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream));
+    if (!graphed) {
+      mark(0, false); phase(0, launch_controls_pre(s, c.stream));
+      mark(1, false); phase(1, launch_drift(s, c.stream));
+      mark(2, false); phase(2, launch_glob_vertices(s, c.stream));
+      mark(3, false);
+      phase(3, c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream));
+      mark(4, false); phase(4, launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream));
+      mark(5, false); phase(5, launch_breakage(s, c.stream));
+    }
     c.forces_stale = s.nheavy_lazy > 0;
-    mark(5, false); phase(5, launch_breakage(s, c.stream));
     if (c.skin.on) {
       if ((rc = skin_after_step(c))) return rc;
       c.steps++;

@@ -120,6 +120,13 @@ struct Ctx {
   int64_t last_nover = 0;
   bool forces_stale = false;
   std::vector<uint8_t> needres_host;
+  // CUDA graph of one step's launches (re-captured when the scene changes)
+  int use_graphs = 0;
+  cudaGraphExec_t gexec = nullptr;
+  Scene gscene{};       // the scene the graph was captured with
+  int gform = -1;
+  int glaunched = 0;    // kernels per replay
+  int64_t graph_captures = 0, graph_replays = 0;
 };
 
 int rebuild_nl(Ctx& c);

@@ -236,10 +236,31 @@ __global__ void k_grid_max(Scene s, float lim, unsigned int* maxbits) {
   if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(e));
 }
 
-__device__ __forceinline__ int cell_coord(float x, float inv_cell) {
-  float f = floorf(x * inv_cell) + 8192.f;
-  f = fminf(fmaxf(f, 0.f), 16383.f);
-  return (int)f;
+// Cell code of the sort key (42 bits above the 21 body bits).  One scene:
+// 14 bits per axis.  Several scenes: the scene index (mod 512) in the top 9
+// bits and 11 bits per axis, so bodies of different scenes that share a
+// region of space fall in different cells.  Coordinates are clamped at the
+// edges of the range; clamping keeps neighbouring cells neighbours, so the
+// search stays conservative (far bodies only share a cell, filtered later).
+// The largest coordinate stays one below all-ones so that no cell code equals
+// the all-ones key that sorts the oversized bodies last.
+struct CellFormat {
+  int bits, off, max;  // per-axis bits, offset of cell 0, largest coordinate
+  bool batched;
+};
+__device__ __forceinline__ CellFormat cell_format(const Scene& s) {
+  return s.scene_of ? CellFormat{11, 1024, 2046, true} : CellFormat{14, 8192, 16382, false};
+}
+
+__device__ __forceinline__ int cell_coord(float x, float inv_cell, const CellFormat& f) {
+  float v = floorf(x * inv_cell) + (float)f.off;
+  v = fminf(fmaxf(v, 0.f), (float)f.max);
+  return (int)v;
+}
+
+__device__ __forceinline__ uint64_t cell_code(uint64_t scene, int x, int y, int z, const CellFormat& f) {
+  const uint64_t c = ((uint64_t)x << (2 * f.bits)) | ((uint64_t)y << f.bits) | (uint64_t)z;
+  return f.batched ? ((scene & 511u) << 33) | c : c;
 }
 
 __global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys, int* over,
@@ -252,26 +273,30 @@ __global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys,
     over[atomicAdd(nover, 1ull)] = (int)b;
     return;
   }
-  const int cx = cell_coord(0.5f * (bb[0] + bb[3]), inv_cell), cy = cell_coord(0.5f * (bb[1] + bb[4]), inv_cell),
-            cz = cell_coord(0.5f * (bb[2] + bb[5]), inv_cell);
-  const uint64_t code = ((uint64_t)cx << 28) | ((uint64_t)cy << 14) | (uint64_t)cz;
-  keys[b] = (code << 21) | (uint64_t)b;
+  const CellFormat f = cell_format(s);
+  const int cx = cell_coord(0.5f * (bb[0] + bb[3]), inv_cell, f), cy = cell_coord(0.5f * (bb[1] + bb[4]), inv_cell, f),
+            cz = cell_coord(0.5f * (bb[2] + bb[5]), inv_cell, f);
+  const uint64_t scene = f.batched ? (uint64_t)(uint32_t)s.scene_of[b] : 0u;
+  keys[b] = (cell_code(scene, cx, cy, cz, f) << 21) | (uint64_t)b;
 }
 
 __global__ void k_grid_pairs(Scene s, const uint64_t* keys, int64_t nnorm, float inv_cell, uint64_t* pairs,
                              int64_t cap, unsigned long long* counter) {
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= nnorm) return;
+  const CellFormat f = cell_format(s);
   const uint64_t key = keys[k];
   const int64_t i = (int64_t)(key & ((1u << 21) - 1));
   const uint64_t code = key >> 21;
-  const int cx = (int)(code >> 28), cy = (int)((code >> 14) & 16383), cz = (int)(code & 16383);
+  const uint64_t amask = (1u << f.bits) - 1u;
+  const uint64_t scene = f.batched ? (code >> 33) : 0u;
+  const int cx = (int)((code >> (2 * f.bits)) & amask), cy = (int)((code >> f.bits) & amask), cz = (int)(code & amask);
   for (int dx = -1; dx <= 1; dx++)
     for (int dy = -1; dy <= 1; dy++)
       for (int dz = -1; dz <= 1; dz++) {
         const int x = cx + dx, y = cy + dy, z = cz + dz;
-        if (x < 0 || y < 0 || z < 0 || x > 16383 || y > 16383 || z > 16383) continue;
-        const uint64_t c2 = ((uint64_t)x << 28) | ((uint64_t)y << 14) | (uint64_t)z;
+        if (x < 0 || y < 0 || z < 0 || x > f.max || y > f.max || z > f.max) continue;
+        const uint64_t c2 = cell_code(scene, x, y, z, f);
         int64_t q = lower_bound_u64(keys, nnorm, c2 << 21);
         for (; q < nnorm && (keys[q] >> 21) == c2; q++) {
           const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));

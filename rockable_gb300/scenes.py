@@ -229,6 +229,130 @@ def sphero_cube_box(n_side=8, seed=SEED, dt=1e-6):
                      name="sphero_cubes_%d" % len(g), wall_shape=0)
 
 
+def _qmul(a, b):
+    """Hamilton product of quaternions stored (w, x, y, z), broadcast over rows."""
+    aw, ax, ay, az = np.moveaxis(np.asarray(a, np.float64), -1, 0)
+    bw, bx, by, bz = np.moveaxis(np.asarray(b, np.float64), -1, 0)
+    return np.stack([aw * bw - ax * bx - ay * by - az * bz, aw * bx + ax * bw + ay * bz - az * by,
+                     aw * by - ax * bz + ay * bw + az * bx, aw * bz + ax * by - ay * bx + az * bw], -1)
+
+
+def tilt(scene, theta):
+    """The scene rotated by theta (radians) about the y axis through the
+    origin: positions, orientations and all body vectors (a slope of angle
+    theta when the scene was built on a horizontal floor)."""
+    c, s_ = math.cos(theta), math.sin(theta)
+    R = np.array([[c, 0.0, s_], [0.0, 1.0, 0.0], [-s_, 0.0, c]])
+    q = np.array([math.cos(0.5 * theta), 0.0, math.sin(0.5 * theta), 0.0])
+    out = dict(scene)
+    b = dict(scene["bodies"])
+    for k in ["pos", "vel", "acc", "vrot", "arot"]:
+        b[k] = np.asarray(b[k]) @ R.T
+    Qn = _qmul(q[None, :], b["Q"])
+    b["Q"] = Qn / np.linalg.norm(Qn, axis=1)[:, None]
+    out["bodies"] = b
+    out.pop("entries", None)
+    return out
+
+
+def batch(parts, name=None):
+    """Several independent scenes as one: the driven bodies of every part
+    first (part order), then the free bodies of every part (part order), so
+    that each part keeps the relative order of its bodies.  Returns the
+    combined scene with `scene_of` (part index of every body) and
+    `index_of` (per part: new index of each of its bodies).  The parts must
+    share their parameters (law, table, dt, gravity, Verlet distances); they
+    share one shape list when they hold the same list object."""
+    p0 = parts[0]
+    for p in parts[1:]:
+        for k in ["law", "dt", "DVerlet", "dVerlet", "interVerlet", "ngroup"]:
+            assert p[k] == p0[k], k
+        assert tuple(p["gravity"]) == tuple(p0["gravity"])
+        assert np.array_equal(p["table"], p0["table"])
+    shared = all(p["shapes"] is p0["shapes"] for p in parts)
+    shapes, sofs = (list(p0["shapes"]), [0] * len(parts)) if shared else ([], [])
+    if not shared:
+        for p in parts:
+            sofs.append(len(shapes))
+            shapes.extend(p["shapes"])
+    nds = [p["n_driven"] for p in parts]
+    ns = [len(p["bodies"]["mass"]) for p in parts]
+    ND = sum(nds)
+    index_of, dstart, fstart = [], 0, ND
+    for nd, n in zip(nds, ns):
+        idx = np.empty(n, np.int64)
+        idx[:nd] = dstart + np.arange(nd)
+        idx[nd:] = fstart + np.arange(n - nd)
+        dstart += nd
+        fstart += n - nd
+        index_of.append(idx)
+    N = fstart
+    keys = list(p0["bodies"].keys())
+    bodies = {}
+    for k in keys:
+        a0 = np.asarray(p0["bodies"][k])
+        out = np.zeros((N,) + a0.shape[1:], a0.dtype)
+        for p, idx, so in zip(parts, index_of, sofs):
+            v = np.asarray(p["bodies"][k])
+            out[idx] = v + so if k == "shape" else v
+        bodies[k] = out
+    scene_of = np.zeros(N, np.int32)
+    for s_, idx in enumerate(index_of):
+        scene_of[idx] = s_
+    out = dict(p0)
+    out.pop("entries", None)
+    out.update({"name": name or "batch_%d" % len(parts), "shapes": shapes, "n_driven": ND, "bodies": bodies,
+                "shape_tables": p0["shape_tables"] if shared else flatten_shapes(shapes), "scene_of": scene_of,
+                "index_of": index_of, "free_per_scene": [n - nd for n, nd in zip(ns, nds)]})
+    return out
+
+
+def part_of(batched, k):
+    """Part k of a scene built by batch(), as a scene of its own (shared
+    shape list, the part's bodies in their original order)."""
+    idx = batched["index_of"][k]
+    out = dict(batched)
+    for key in ["scene_of", "index_of", "free_per_scene", "slope_deg", "entries"]:
+        out.pop(key, None)
+    out["bodies"] = {key: np.asarray(v)[idx] for key, v in batched["bodies"].items()}
+    out["n_driven"] = int(np.sum(idx < batched["n_driven"]))
+    out["name"] = "%s_part%d" % (batched["name"], k)
+    return out
+
+
+def slope_batch(nscenes=256, seed=SEED, nmin=200, nmax=5000, nshapes=256, density=2700.0, kn=1e6, kt=1e6,
+                en2=0.25, mu=0.4, dt=1e-6):
+    """Many independent slope scenes: scene k draws N_k ~ U{nmin..nmax} hull
+    grains and a slope angle U[25, 45] degrees from the generator seeded
+    seed + 1 + k; its grains are deposited ballistically on a square patch of
+    a rigid plate (about 8 layers), and the plate and the pile are tilted by
+    the slope angle (gravity stays vertical).  Default law.  All scenes share
+    one shape library (a plate and nshapes grain shapes)."""
+    rng = np.random.default_rng(seed)
+    shapes = [plate_shape("SLOPE", 0.5, 0.005)]
+    shapes += [hull_shape(rng, "B%04d" % k) for k in range(nshapes)]
+    bound = np.array([s["bound"] for s in shapes])
+    bmax = float(bound[1:].max())
+    parts, angles = [], []
+    for k in range(nscenes):
+        rs = np.random.default_rng(seed + 1 + k)
+        n = int(rs.integers(nmin, nmax + 1))
+        theta = math.radians(float(rs.uniform(25.0, 45.0)))
+        shape_of = rs.integers(1, nshapes + 1, n)
+        half = 0.5 * math.sqrt(n / 8.0) * 0.0125
+        pos = deposit(rs, bound[shape_of], half, half, 0.005 + 1e-5)
+        Q = random_quaternions(rs, n)
+        sc = _assemble(shapes, [np.zeros(3)], [np.array([1.0, 0, 0, 0])], pos, Q, shape_of, density, "Default", kn,
+                       kt, en2, mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax,
+                       interVerlet=100 * dt, name="slope_%d" % k)
+        sc["shapes"] = shapes
+        parts.append(tilt(sc, theta))
+        angles.append(math.degrees(theta))
+    out = batch(parts, name="slope_batch_%d" % nscenes)
+    out["slope_deg"] = angles
+    return out
+
+
 def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, en2, mu, dt, gravity, DVerlet,
               dVerlet, interVerlet, name, wall_shape=0):
     nd = len(wall_pos)
@@ -251,9 +375,10 @@ def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, 
             "params": {"kn": kn, "kt": kt, "en2": en2, "mu": mu}}
 
 
-def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=0, report=None):
-    """Compact a freshly deposited pile on the GPU: Avalanche contacts at a
-    soft stiffness, boosted gravity and numerical damping, large time step.
+def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=0, report=None, law="Avalanche"):
+    """Compact a freshly deposited pile on the GPU: contacts of the given law
+    (Avalanche by default) at a soft stiffness, boosted gravity and numerical
+    damping, large time step.
     Returns the GpuScene, switched afterwards to the scene's own parameters
     (the Avalanche law's incremental normal force carries the settled contact
     forces across the change of stiffness)."""
@@ -261,10 +386,12 @@ def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=
     g = GpuScene(device=device)
     g.upload_shapes(scene["shape_tables"])
     g.upload_bodies(scene["bodies"], scene["n_driven"])
+    if scene.get("scene_of") is not None:
+        g.set_scenes(scene["scene_of"])
     p = scene["params"]
     grav = tuple(gboost * x for x in scene["gravity"])
     g.set_params(t=0.0, dt=dt, gravity=grav, DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
-                 interVerlet=10 * dt, interVerletC=0.0, law=RK_LAW["Avalanche"], ngroup=scene["ngroup"],
+                 interVerlet=10 * dt, interVerletC=0.0, law=RK_LAW[law], ngroup=scene["ngroup"],
                  table=law_table(kn=kn, kt=kn, en2=p["en2"], mu=p["mu"]), numerical_damping=damping)
     g.update_nl()
     done = 0

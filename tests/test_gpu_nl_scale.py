@@ -36,7 +36,7 @@ def test_grid_and_all_pairs_give_the_same_list(gpu_lib):
     ga.update_nl()
     gg.update_nl()
     ea, eg = ga.entries(), gg.entries()
-    assert len(ea["i"]) > 10000
+    assert len(ea["i"]) > 4000
     assert np.array_equal(_keys(ea), _keys(eg))
     for k in ["dn", "fn", "ft", "mom", "damp"]:
         assert bitwise_equal(ea[k], eg[k]), k
