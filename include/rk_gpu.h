@@ -250,6 +250,17 @@ int rk_last_step_timing(const rk_ctx* ctx, double* ms, int64_t* kernels);
  * lexicographic key order of Interaction.hpp:106-122, and the j-side list);
  * temporary memory is allocated and freed by the call. */
 int rk_sort_keys(uint64_t* keys, int64_t n, int lo_bit, int hi_bit, void* stream);
+/* rk_sort_keys without any allocation; it has no counterpart in the reference.
+ * For callers that cannot allocate device memory (an allocator that already
+ * holds the device's memory, a serving loop with a footprint fixed at start-up,
+ * streams that cannot take cudaFree's device-wide synchronisation).  The
+ * temporary buffers are one static device array of about 4.5 MB shared by all
+ * calls: n is limited to 524288 keys (RK_ERR_CAPACITY beyond), calls that
+ * overlap on the GPU race on that array and must be ordered by the caller, and
+ * the first call on each device looks up the array's address (make it before
+ * any stream capture begins).  Asynchronous on `stream`: unlike rk_sort_keys
+ * it does not synchronise. */
+int rk_sort_keys_noalloc(uint64_t* keys, int64_t n, int lo_bit, int hi_bit, void* stream);
 /* Per-phase device time: when on, rk_step brackets each phase with CUDA
  * events on the context stream (adds one event pair per phase and step).
  * Phases: 0 controls, 1 drift, 2 global vertices, 3 narrow phase + law,

@@ -121,6 +121,7 @@ SIGNATURES = {
     "rk_set_profiling": (C.c_int, [P, C.c_int]),
     "rk_get_profile": (C.c_int, [P, P, P]),
     "rk_sort_keys": (C.c_int, [P, I64, C.c_int, C.c_int, P]),
+    "rk_sort_keys_noalloc": (C.c_int, [P, I64, C.c_int, C.c_int, P]),
     "rk_set_skin": (C.c_int, [P, C.POINTER(RkSkinConfig)]),
     "rk_get_skin_stats": (C.c_int, [P, C.POINTER(RkSkinStats)]),
     "rk_mlp_num_params": (C.c_int, []),

@@ -26,6 +26,7 @@ UNITS = {
     "rk_api.cu": ["--fmad=false"],
     "rk_mixed.cu": [],
     "rk_skin.cu": [],
+    "rk_noalloc.cu": [],
 }
 
 
