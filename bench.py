@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched slope workload (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=100)
-    ap.add_argument("--batch-settle", type=int, default=2000)
+    ap.add_argument("--batch-settle", type=int, default=4000)
     return ap.parse_args()
 
 
@@ -158,6 +158,14 @@ def cpu_baseline(scene, budget_s):
                 steps, o.n, el)}
 
 
+def _nvtx():
+    try:
+        import torch
+        return torch.cuda.nvtx
+    except Exception:
+        return None
+
+
 def batched_workload(a, dev):
     """Many independent slope scenes (N ~ U{200..5000} grains each, slopes
     25-45 degrees, Default law) in ONE engine context: every launch covers all
@@ -171,8 +179,8 @@ def batched_workload(a, dev):
     bt = scenes.slope_batch(nscenes=a.batch_scenes)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
-    g = scenes.settle(bt, steps=a.batch_settle, dt=5e-6, kn=bt["params"]["kn"], gboost=10.0, damping=0.5,
-                      device=dev, law="Default")
+    g = scenes.settle(bt, steps=a.batch_settle, dt=5e-6, kn=bt["params"]["kn"], gboost=20.0, damping=0.5,
+                      device=dev, law="Default", rebuild_every=40)
     src = scenes.scene_from_gpu(bt, g)
     g.close()
     t_settle = time.perf_counter() - t0
@@ -197,11 +205,19 @@ def batched_workload(a, dev):
     clocks = Clocks()
     e.synchronize()
     clocks.start()
+    nvtx = _nvtx()
+    if nvtx:
+        nvtx.range_push("timed_batch")
     rep = e.step(a.batch_steps)
+    if nvtx:
+        nvtx.range_pop()
     ms, launches = e.last_step_timing()
     ck = clocks.stop()
     st = e.stats()
     gst = e.graph_stats()
+    e.set_profiling(True)
+    e.step(a.batch_steps)
+    prof = e.profile()
     e.close()
     solo = []
     for k in range(len(bt["free_per_scene"])):
@@ -223,6 +239,7 @@ def batched_workload(a, dev):
                                  "p90": float(np.percentile(solo, 90)), "max": float(solo.max()),
                                  "sum": float(solo.sum())},
             "batched_vs_solo_sum": float(solo.sum() / (ms / a.batch_steps)),
+            "phases_ms_per_step": {q: w[0] / a.batch_steps for q, w in prof.items()},
             "setup_s": {"generate": t_gen, "settle": t_settle}}
 
 

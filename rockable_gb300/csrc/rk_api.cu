@@ -296,19 +296,26 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   }
   if (!(u > 0.0) || !std::isfinite(u)) u = std::max(rate, 1e-30);
   k.pred_rate = u;
-  // skin and interval minimising the measured step + rebuild cost
-  const double margin = 1.3;
+  // skin and interval minimising the predicted cost per step.  Entries grow
+  // faster than the skin (more sub-element pairs come within reach): the
+  // non-active entries are scaled by (skin ratio)^1.6, the power measured on
+  // the hull-grain piles.  Half of the step time (the per-body kernels) and
+  // 30% of the rebuild time (broad phase, sorts) do not depend on the list
+  // size; the rest scales with it.  The interval is the number of steps the
+  // predicted displacement rate takes to use half the skin (with a margin),
+  // which is also when the exact guard would force the rebuild.
+  const double margin = 1.3, alpha = 1.6;
   const double C = (double)std::max<int64_t>(1, ne0), A = std::min(active, C);
-  const double te = k.step_ms > 0 ? k.step_ms / C : 1e-6;
-  const double R = k.rebuild_ms > 0 ? k.rebuild_ms : 100.0 * te * C;
+  const double T = k.step_ms > 0 ? k.step_ms : 1e-3 * C / 1e5;
+  const double R = k.rebuild_ms > 0 ? k.rebuild_ms : 20.0 * T;
   double best = 1e300, best_s = k.skin;
   int64_t best_k = k.interval;
   for (int m = -4; m <= 4; m++) {
-    double sk = std::min(k.cfg.skin_max, std::max(k.cfg.skin_min, k.skin * std::pow(2.0, 0.5 * m)));
+    double sk = std::min(k.cfg.skin_max, std::max(k.cfg.skin_min, k.skin * std::pow(2.0, 0.25 * m)));
     double kk = std::floor(0.5 * sk / std::max(u * margin * (1.0 + churn), 1e-30));
     int64_t ki = (int64_t)std::max<double>(k.cfg.interval_min, std::min<double>(k.cfg.interval_max, kk));
-    double Cs = A + (C - A) * (sk / std::max(k.skin, 1e-30));
-    double J = te * Cs + R / (double)ki;
+    double ratio = (A + (C - A) * std::pow(sk / std::max(k.skin, 1e-30), alpha)) / C;
+    double J = T * (0.5 + 0.5 * ratio) + R * (0.3 + 0.7 * ratio) / (double)ki;
     if (J < best) { best = J; best_s = sk; best_k = ki; }
   }
   k.skin = best_s;
@@ -499,7 +506,7 @@ void rk_destroy(rk_ctx* x) {
   free_entrybuf(c.eb[0]);
   free_entrybuf(c.eb[1]);
   NLWork& w = c.w;
-  dfree(w.pairs); dfree(w.hp); dfree(w.hp_tmp); dfree(w.hp_cnt); dfree(w.hp_mask); dfree(w.cand); dfree(w.cand_src);
+  dfree(w.pairs); dfree(w.hp); dfree(w.hp_tmp); dfree(w.hp_mask); dfree(w.cand); dfree(w.cand_tmp);
   dfree(w.flag); dfree(w.stale); dfree(w.stale_src); dfree(w.fkey); dfree(w.fsrc); dfree(w.jkeys); dfree(w.jtmp);
   dfree(w.tmp); dfree(w.counter); dfree(w.gkeys); dfree(w.gtmp); dfree(w.gover); dfree(w.gis_over);
   if (w.gstat) cudaFree(w.gstat);

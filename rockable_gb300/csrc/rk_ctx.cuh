@@ -27,10 +27,10 @@ struct NLWork {
   uint64_t* pairs = nullptr;     // pair_cap
   uint64_t* hp = nullptr;        // hp_cap (half-pair keys owner<<21 | partner)
   uint64_t* hp_tmp = nullptr;    // hp_cap
-  int64_t* hp_cnt = nullptr;     // hp_cap + 1
   uint32_t* hp_mask = nullptr;   // kMaskWords * hp_cap
   uint64_t* cand = nullptr;      // cand_cap new entry keys
-  int64_t* cand_src = nullptr;   // cand_cap
+  uint64_t* cand_tmp = nullptr;  // cand_cap (sort)
+  int64_t cand_hint = 0;         // candidates found by the previous rebuild
   int64_t* flag = nullptr;       // old_cap + 1
   uint64_t* stale = nullptr;     // old_cap
   int64_t* stale_src = nullptr;  // old_cap

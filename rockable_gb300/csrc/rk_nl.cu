@@ -14,9 +14,9 @@
 // enlarged boxes, so both options map onto this exact pair predicate.
 //
 // Pipeline (all on the context stream, a few host reads of counts):
-//   body_obb -> all-pairs AABB filter + FP64 SAT -> half-pairs (both
-//   directions, radix-sorted) -> per half-pair candidate count / cull mask ->
-//   scan -> candidate write (keys in sorted order per half-pair) -> old-entry
+//   body_obb -> pairs (all-pairs AABB filter or uniform grid, then the FP64
+//   SAT) -> half-pairs (both directions, radix-sorted) -> candidates (one
+//   warp per half-pair: cull mask, NEAR keys appended) -> key sort -> old-entry
 //   classification and order-preserving compaction -> merge by key ->
 //   history carry -> i-side offsets and j-side list.
 #include <algorithm>
@@ -414,123 +414,187 @@ __device__ __forceinline__ bool near_ee(const Scene& s, const PairView& P, int e
   return false;
 }
 
-// Candidates of one half-pair (owner b -> partner p), in key order.
-// MODE 0 counts (and records the vertex cull mask), MODE 1 writes keys.
-template <int MODE>
-__global__ void k_candidates(Scene s, const uint64_t* hp, int64_t nhp, int64_t* cnt, uint32_t* mask,
-                             const int64_t* ofs, uint64_t* out) {
-  int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (h >= nhp) return;
-  const uint64_t key = hp[h];
-  const int b = (int)(key >> 21), p = (int)(key & ((1u << 21) - 1));
-  PairView P;
-  P.gb = s.gv + 3 * s.gv_ofs[b];
-  P.gp = s.gv + 3 * s.gv_ofs[p];
-  P.sb = s.shape[b];
-  P.sp = s.shape[p];
-  P.Rb = s.rad[b];
-  P.Rp = s.rad[p];
-  P.dmax = s.dVerlet;
-  const int nvb = s.vert_ofs[P.sb + 1] - s.vert_ofs[P.sb];
-  const int nvp = s.vert_ofs[P.sp + 1] - s.vert_ofs[P.sp];
-  const int neb = s.edge_ofs[P.sb + 1] - s.edge_ofs[P.sb];
-  const int nep = s.edge_ofs[P.sp + 1] - s.edge_ofs[P.sp];
-  const int nfp = s.face_ofs[P.sp + 1] - s.face_ofs[P.sp];
-  uint32_t m[kMaskWords];
-  if (MODE == 0) {
-    Obb op = load_obb(s.bobb + 15 * p);
-    enlarge(op, P.dmax);
-    for (int w = 0; w < kMaskWords; w++) m[w] = 0u;
-    for (int v = 0; v < nvb; v++) {
-      Obb sub;
-      sub.c = g3(P.gb, v);
-      sub.e0 = v3(1, 0, 0);
-      sub.e1 = v3(0, 1, 0);
-      sub.e2 = v3(0, 0, 1);
-      double r = P.Rb + P.dmax;
-      sub.ext = v3(r, r, r);
-      if (obb_intersect(op, sub)) m[v >> 5] |= 1u << (v & 31);
-    }
-    for (int w = 0; w < kMaskWords; w++) mask[kMaskWords * h + w] = m[w];
-  } else {
-    for (int w = 0; w < kMaskWords; w++) m[w] = mask[kMaskWords * h + w];
+// Candidate sub-contacts of the half-pairs: one warp per half-pair (owner b
+// -> partner p).  The lanes first compute, in parallel, the owner vertices
+// that pass the OBB cull (FP64 SAT of the vertex cube against p's box
+// enlarged by dVerlet; this mask also tells the old-entry pass which
+// candidates were tested) and the sub-elements of each body that a
+// conservative float bounding-sphere test leaves within reach of the other
+// body; those index lists go to shared memory.  The lanes then sweep the
+// products of the lists 32 candidates at a time: float sphere prefilter,
+// then the FP64 NEAR predicate, and the survivors are appended with one
+// atomic per warp and ballot.  Appending leaves the keys unordered; they are
+// sorted afterwards.  The float tests only skip candidates that cannot be
+// NEAR, so the NEAR set is exactly the one of testing every candidate.
+constexpr int kCandWarps = 4;  // warps per block
+
+struct CandLists {
+  uint16_t bv[64], pv[64];                   // owner / partner vertices
+  uint16_t be[kMaxSub], pe[kMaxSub], pf[kMaxSub];  // owner edges, partner edges and faces
+};
+
+// Indices k < n with pred(k), in increasing order, written by the warp.
+template <class Pred>
+__device__ __forceinline__ int warp_list(uint16_t* list, int n, int lane, Pred pred) {
+  int cnt = 0;
+  for (int base = 0; base < n; base += 32) {
+    const int k = base + lane;
+    const bool ok = k < n && pred(k);
+    const unsigned bal = __ballot_sync(0xffffffffu, ok);
+    if (ok) list[cnt + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)k;
+    cnt += __popc(bal);
   }
-  // conservative float filter: a candidate whose bounding spheres are
-  // farther apart than the NEAR distance allows cannot be NEAR
-  const float4* sb = s.sph + s.sph_ofs[b];
-  const float4* sp = s.sph + s.sph_ofs[p];
-  const float sum = (float)(P.Rb + P.Rp + P.dmax);
-  auto far = [&](float4 a, float4 c, float extent) {
-    float dx = a.x - c.x, dy = a.y - c.y, dz = a.z - c.z;
-    float lim = sum + extent;
-    lim = lim + 1e-4f * lim + 2e-6f;
-    return dx * dx + dy * dy + dz * dz > lim * lim;
-  };
-  const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
-  // two-sided culling: only the sub-elements of one body that can reach the
-  // other body's bounding sphere take part
-  const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
-  const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
-  constexpr int kW = 8;  // up to 256 edges / faces per shape are culled, more are all kept
-  uint32_t mpv[2] = {0u, 0u}, mpe[kW], mpf[kW], mbe[kW];
-  for (int q = 0; q < kW; q++) mpe[q] = mpf[q] = mbe[q] = 0u;
-  for (int w = 0; w < nvp; w++)
-    if (!far(sp[w], cb, cb.w)) mpv[w >> 5] |= 1u << (w & 31);
-  const bool cull_pe = nep <= 32 * kW, cull_pf = nfp <= 32 * kW, cull_be = neb <= 32 * kW;
-  if (cull_pe)
-    for (int e = 0; e < nep; e++) {
+  __syncwarp();
+  return cnt;
+}
+
+__device__ __forceinline__ void warp_emit(bool ok, uint64_t key, int lane, uint64_t* out, int64_t cap,
+                                          unsigned long long* counter) {
+  const unsigned bal = __ballot_sync(0xffffffffu, ok);
+  if (!bal) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(counter, (unsigned long long)__popc(bal));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (ok) {
+    const unsigned long long at = base + __popc(bal & ((1u << lane) - 1u));
+    if ((int64_t)at < cap) out[at] = key;
+  }
+}
+
+__global__ void __launch_bounds__(32 * kCandWarps)
+k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t* out, int64_t cap,
+             unsigned long long* counter) {
+  __shared__ CandLists lists[kCandWarps];
+  const int lane = threadIdx.x & 31;
+  CandLists& L = lists[threadIdx.x >> 5];
+  const int64_t stride = (int64_t)gridDim.x * kCandWarps;
+  for (int64_t h = (int64_t)blockIdx.x * kCandWarps + (threadIdx.x >> 5); h < nhp; h += stride) {
+    __syncwarp();  // the previous half-pair's lists have been read
+    const uint64_t key = hp[h];
+    const int b = (int)(key >> 21), p = (int)(key & ((1u << 21) - 1));
+    PairView P;
+    P.gb = s.gv + 3 * s.gv_ofs[b];
+    P.gp = s.gv + 3 * s.gv_ofs[p];
+    P.sb = s.shape[b];
+    P.sp = s.shape[p];
+    P.Rb = s.rad[b];
+    P.Rp = s.rad[p];
+    P.dmax = s.dVerlet;
+    const int nvb = s.vert_ofs[P.sb + 1] - s.vert_ofs[P.sb];
+    const int nvp = s.vert_ofs[P.sp + 1] - s.vert_ofs[P.sp];
+    const int neb = s.edge_ofs[P.sb + 1] - s.edge_ofs[P.sb];
+    const int nep = s.edge_ofs[P.sp + 1] - s.edge_ofs[P.sp];
+    const int nfp = s.face_ofs[P.sp + 1] - s.face_ofs[P.sp];
+    // owner-vertex cull (Rockable.cpp:1385-1391): the vertex cube against
+    // the partner's OBB enlarged by dVerlet
+    uint32_t m0, m1;
+    {
+      Obb op = load_obb(s.bobb + 15 * p);
+      enlarge(op, P.dmax);
+      const double r = P.Rb + P.dmax;
+      bool hit0 = false, hit1 = false;
+      for (int half = 0; half < 2; half++) {
+        const int v = lane + 32 * half;
+        if (v < nvb) {
+          Obb sub;
+          sub.c = g3(P.gb, v);
+          sub.e0 = v3(1, 0, 0);
+          sub.e1 = v3(0, 1, 0);
+          sub.e2 = v3(0, 0, 1);
+          sub.ext = v3(r, r, r);
+          const bool hit = obb_intersect(op, sub);
+          if (half == 0) hit0 = hit;
+          else hit1 = hit;
+        }
+      }
+      m0 = __ballot_sync(0xffffffffu, hit0);
+      m1 = __ballot_sync(0xffffffffu, hit1);
+    }
+    if (lane == 0) {
+      mask[kMaskWords * h] = m0;
+      mask[kMaskWords * h + 1] = m1;
+    }
+    // conservative float filter: a candidate whose bounding spheres are
+    // farther apart than the NEAR distance allows cannot be NEAR
+    const float4* sb = s.sph + s.sph_ofs[b];
+    const float4* sp = s.sph + s.sph_ofs[p];
+    const float sum = (float)(P.Rb + P.Rp + P.dmax);
+    auto far = [&](float4 a, float4 c, float extent) {
+      float dx = a.x - c.x, dy = a.y - c.y, dz = a.z - c.z;
+      float lim = sum + extent;
+      lim = lim + 1e-4f * lim + 2e-6f;
+      return dx * dx + dy * dy + dz * dz > lim * lim;
+    };
+    const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
+    const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
+    const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
+    const bool lower = b < p;  // vertex-vertex and edge-edge pairs are tested in the i < j direction only
+    const int nbv = warp_list(L.bv, nvb, lane, [&](int v) { return (((v < 32 ? m0 : m1) >> (v & 31)) & 1u) != 0u; });
+    const int npv = lower ? warp_list(L.pv, nvp, lane, [&](int w) { return !far(sp[w], cb, cb.w); }) : 0;
+    const int npe = warp_list(L.pe, nep, lane, [&](int e) {
       const float4 se = sp[nvp + e];
-      if (!far(se, cb, cb.w + ve_ext * se.w)) mpe[e >> 5] |= 1u << (e & 31);
-    }
-  if (cull_pf)
-    for (int f = 0; f < nfp; f++) {
+      return !far(se, cb, cb.w + ve_ext * se.w);
+    });
+    const int npf = warp_list(L.pf, nfp, lane, [&](int f) {
       const float4 sf = sp[nvp + nep + f];
-      if (!far(sf, cb, cb.w + sf.w)) mpf[f >> 5] |= 1u << (f & 31);
-    }
-  if (cull_be && b < p)
-    for (int e = 0; e < neb; e++) {
+      return !far(sf, cb, cb.w + sf.w);
+    });
+    const int nbe = lower ? warp_list(L.be, neb, lane, [&](int e) {
       const float4 se = sb[nvb + e];
-      if (!far(se, cp, cp.w + se.w)) mbe[e >> 5] |= 1u << (e & 31);
+      return !far(se, cp, cp.w + se.w);
+    }) : 0;
+    // vertex-vertex
+    for (int base = 0, tot = nbv * npv; base < tot; base += 32) {
+      const int c = base + lane;
+      bool ok = false;
+      int v = 0, w = 0;
+      if (c < tot) {
+        v = L.bv[c / npv];
+        w = L.pv[c % npv];
+        ok = !far(sb[v], sp[w], 0.f) && near_vv(P, v, w);
+      }
+      warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 0u, (uint32_t)v, (uint32_t)w), lane, out, cap, counter);
     }
-  auto on = [](const uint32_t* mk, bool cull, int k) { return !cull || ((mk[k >> 5] >> (k & 31)) & 1u); };
-  int64_t c = 0;
-  uint64_t* o = (MODE == 1) ? out + ofs[h] : nullptr;
-  auto emit = [&](int t, int i1, int j1) {
-    if (MODE == 1) o[c] = entry_key((uint32_t)b, (uint32_t)p, (uint32_t)t, (uint32_t)i1, (uint32_t)j1);
-    c++;
-  };
-  if (b < p) {
-    for (int v = 0; v < nvb; v++)
-      if (m[v >> 5] >> (v & 31) & 1u)
-        for (int w = 0; w < nvp; w++)
-          if ((mpv[w >> 5] >> (w & 31) & 1u) && !far(sb[v], sp[w], 0.f) && near_vv(P, v, w)) emit(0, v, w);
-  }
-  for (int v = 0; v < nvb; v++)
-    if (m[v >> 5] >> (v & 31) & 1u)
-      for (int e = 0; e < nep; e++) {
-        if (!on(mpe, cull_pe, e)) continue;
+    // vertex-edge
+    for (int base = 0, tot = nbv * npe; base < tot; base += 32) {
+      const int c = base + lane;
+      bool ok = false;
+      int v = 0, e = 0;
+      if (c < tot) {
+        v = L.bv[c / npe];
+        e = L.pe[c % npe];
         const float4 se = sp[nvp + e];
-        if (!far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e)) emit(1, v, e);
+        ok = !far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e);
       }
-  for (int v = 0; v < nvb; v++)
-    if (m[v >> 5] >> (v & 31) & 1u)
-      for (int f = 0; f < nfp; f++) {
-        if (!on(mpf, cull_pf, f)) continue;
+      warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 1u, (uint32_t)v, (uint32_t)e), lane, out, cap, counter);
+    }
+    // vertex-face
+    for (int base = 0, tot = nbv * npf; base < tot; base += 32) {
+      const int c = base + lane;
+      bool ok = false;
+      int v = 0, f = 0;
+      if (c < tot) {
+        v = L.bv[c / npf];
+        f = L.pf[c % npf];
         const float4 sf = sp[nvp + nep + f];
-        if (!far(sb[v], sf, sf.w) && near_vf(s, P, v, f)) emit(2, v, f);
+        ok = !far(sb[v], sf, sf.w) && near_vf(s, P, v, f);
       }
-  if (b < p) {
-    for (int e = 0; e < neb; e++) {
-      if (!on(mbe, cull_be, e)) continue;
-      const float4 s1 = sb[nvb + e];
-      for (int e2 = 0; e2 < nep; e2++) {
-        if (!on(mpe, cull_pe, e2)) continue;
-        const float4 s2 = sp[nvp + e2];
-        if (!far(s1, s2, s1.w + s2.w) && near_ee(s, P, e, e2)) emit(3, e, e2);
+      warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 2u, (uint32_t)v, (uint32_t)f), lane, out, cap, counter);
+    }
+    // edge-edge
+    for (int base = 0, tot = nbe * npe; base < tot; base += 32) {
+      const int c = base + lane;
+      bool ok = false;
+      int e1 = 0, e2 = 0;
+      if (c < tot) {
+        e1 = L.be[c / npe];
+        e2 = L.pe[c % npe];
+        const float4 s1 = sb[nvb + e1], s2 = sp[nvp + e2];
+        ok = !far(s1, s2, s1.w + s2.w) && near_ee(s, P, e1, e2);
       }
+      warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 3u, (uint32_t)e1, (uint32_t)e2), lane, out, cap, counter);
     }
   }
-  if (MODE == 0) cnt[h] = c;
 }
 
 
@@ -793,14 +857,12 @@ int rebuild_nl(Ctx& c) {
     int64_t nc = nhp + nhp / 2 + 1024;
     if ((rc = grow(c, w.hp, w.hp_cap, nc))) return rc;
     if ((rc = grow(c, w.hp_tmp, w.hp_cap, nc))) return rc;
-    if ((rc = grow(c, w.hp_cnt, w.hp_cap, nc + 1))) return rc;
     if ((rc = grow(c, w.hp_mask, w.hp_cap, kMaskWords * nc))) return rc;
     w.hp_cap = nc;
   }
   const EntryBuf& ob = c.eb[c.cur];
   const int64_t no = s.ne;
-  int64_t need_tmp = (int64_t)std::max(std::max(sort_temp_bytes(nhp), scan_temp_bytes(nhp + 1)),
-                                       scan_temp_bytes(no + 1));
+  int64_t need_tmp = (int64_t)std::max(sort_temp_bytes(nhp), scan_temp_bytes(no + 1));
   if ((rc = ensure_tmp(c, need_tmp))) return rc;
   if (np > 0) {
     k_half_pairs<<<nblk(np, 256), 256, 0, st>>>(w.pairs, np, w.hp);
@@ -808,23 +870,37 @@ int rebuild_nl(Ctx& c) {
     radix_sort_u64(w.hp, w.hp_tmp, nhp, 0, 48, w.tmp, st);
     c.kernels += 13;
   }
-  // ---- candidates: count, scan, write
+  // ---- candidates: appended by one warp per half-pair, then sorted by key
   int64_t ncand = 0;
   if (nhp > 0) {
-    k_candidates<0><<<nblk(nhp, 64), 64, 0, st>>>(s, w.hp, nhp, w.hp_cnt, w.hp_mask, nullptr, nullptr);
-    RKCHK(cudaMemsetAsync(w.hp_cnt + nhp, 0, sizeof(int64_t), st));
-    exclusive_scan_i64(w.hp_cnt, w.hp_cnt, nhp + 1, w.tmp, st);
-    c.kernels += 3;
-    ncand = read_i64(c, w.hp_cnt + nhp);
-  }
-  if (w.cand_cap < ncand + 1) {
-    int64_t nc = ncand + ncand / 2 + 1024;
-    if ((rc = grow(c, w.cand, w.cand_cap, nc))) return rc;
-    w.cand_cap = nc;
-  }
-  if (ncand > 0) {
-    k_candidates<1><<<nblk(nhp, 64), 64, 0, st>>>(s, w.hp, nhp, nullptr, w.hp_mask, w.hp_cnt, w.cand);
-    c.kernels++;
+    const int64_t want = std::max<int64_t>(w.cand_hint, 4 * nhp) + 1024;
+    if (w.cand_cap < want) {
+      int64_t nc = want + want / 4;
+      if ((rc = grow(c, w.cand, w.cand_cap, nc)) || (rc = grow(c, w.cand_tmp, w.cand_cap, nc))) return rc;
+      w.cand_cap = nc;
+    }
+    const unsigned grid = (unsigned)std::min<int64_t>((nhp + kCandWarps - 1) / kCandWarps, 152 * 16);
+    for (int attempt = 0; attempt < 4; attempt++) {
+      RKCHK(cudaMemsetAsync(w.counter + 3, 0, 8, st));
+      k_candidates<<<grid, 32 * kCandWarps, 0, st>>>(s, w.hp, nhp, w.hp_mask, w.cand, w.cand_cap, w.counter + 3);
+      c.kernels++;
+      unsigned long long cnt = 0;
+      RKCHK(cudaMemcpyAsync(&cnt, w.counter + 3, 8, cudaMemcpyDeviceToHost, st));
+      RKCHK(cudaStreamSynchronize(st));
+      ncand = (int64_t)cnt;
+      if (ncand <= w.cand_cap) break;
+      int64_t nc = ncand + ncand / 4 + 1024;
+      if ((rc = grow(c, w.cand, w.cand_cap, nc)) || (rc = grow(c, w.cand_tmp, w.cand_cap, nc))) return rc;
+      w.cand_cap = nc;
+      ncand = -1;
+    }
+    if (ncand < 0) { c.err = "candidate buffer kept overflowing"; return RK_ERR_CAPACITY; }
+    w.cand_hint = ncand + ncand / 8;
+    if (ncand > 1) {
+      if ((rc = ensure_tmp(c, (int64_t)sort_temp_bytes(ncand)))) return rc;
+      radix_sort_u64(w.cand, w.cand_tmp, ncand, 0, 64, w.tmp, st);
+      c.kernels += 25;
+    }
   }
   // ---- old entries kept untouched
   if (w.old_cap < no + 1) {

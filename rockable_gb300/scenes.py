@@ -375,7 +375,8 @@ def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, 
             "params": {"kn": kn, "kt": kt, "en2": en2, "mu": mu}}
 
 
-def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=0, report=None, law="Avalanche"):
+def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=0, report=None, law="Avalanche",
+           rebuild_every=10):
     """Compact a freshly deposited pile on the GPU: contacts of the given law
     (Avalanche by default) at a soft stiffness, boosted gravity and numerical
     damping, large time step.
@@ -391,7 +392,7 @@ def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=
     p = scene["params"]
     grav = tuple(gboost * x for x in scene["gravity"])
     g.set_params(t=0.0, dt=dt, gravity=grav, DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
-                 interVerlet=10 * dt, interVerletC=0.0, law=RK_LAW[law], ngroup=scene["ngroup"],
+                 interVerlet=rebuild_every * dt, interVerletC=0.0, law=RK_LAW[law], ngroup=scene["ngroup"],
                  table=law_table(kn=kn, kt=kn, en2=p["en2"], mu=p["mu"]), numerical_damping=damping)
     g.update_nl()
     done = 0

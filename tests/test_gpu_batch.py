@@ -51,7 +51,7 @@ def test_graph_replay_is_bitwise_identical(form, gpu_lib):
 def test_batched_scenes_match_each_scene_alone(gpu_lib):
     from rockable_gb300 import scenes
     bt = scenes.slope_batch(nscenes=4, nmin=300, nmax=1500, nshapes=32)
-    gs = scenes.settle(bt, steps=1500, dt=5e-6, kn=bt["params"]["kn"], gboost=10.0, damping=0.5, law="Default")
+    gs = scenes.settle(bt, steps=2000, dt=5e-6, kn=bt["params"]["kn"], gboost=20.0, damping=0.5, law="Default")
     bt = scenes.scene_from_gpu(bt, gs)
     gs.close()
     whole = _engine(bt, graphs=True)
