@@ -34,6 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
+TUNE_STEPS = 8  # untimed block-size tuning steps before the warm-up (rk_set_autotune, 2 rounds)
 
 
 def parse():
@@ -53,7 +54,7 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched slope workload (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=100)
-    ap.add_argument("--batch-settle", type=int, default=4000)
+    ap.add_argument("--batch-settle", type=int, default=3000)
     return ap.parse_args()
 
 
@@ -179,8 +180,7 @@ def batched_workload(a, dev):
     bt = scenes.slope_batch(nscenes=a.batch_scenes)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
-    g = scenes.settle(bt, steps=a.batch_settle, dt=5e-6, kn=bt["params"]["kn"], gboost=20.0, damping=0.5,
-                      device=dev, law="Default", rebuild_every=40)
+    g = scenes.settle(bt, steps=a.batch_settle, device=dev, rebuild_every=10, relax_steps=a.batch_settle // 3)
     src = scenes.scene_from_gpu(bt, g)
     g.close()
     t_settle = time.perf_counter() - t0
@@ -201,6 +201,8 @@ def batched_workload(a, dev):
         return e
 
     e = engine(src, src["entries"])
+    e.autotune(2)
+    e.step(TUNE_STEPS)
     e.step(max(3, a.warmup))
     clocks = Clocks()
     e.synchronize()
@@ -215,6 +217,7 @@ def batched_workload(a, dev):
     ck = clocks.stop()
     st = e.stats()
     gst = e.graph_stats()
+    bsz = e.block_sizes()
     e.set_profiling(True)
     e.step(a.batch_steps)
     prof = e.profile()
@@ -233,6 +236,7 @@ def batched_workload(a, dev):
             "law": "Default", "form": "plain FP64, step graphs", "steps": a.batch_steps,
             "value": nfree * a.batch_steps / (ms / 1000.0), "unit": "particle-steps/s",
             "ms_per_step": ms / a.batch_steps, "gpu_launches": int(launches), "graph": gst,
+            "block_sizes": bsz,
             "entries": int(st["n_entries"]), "active": int(st["n_active"]), "nl_rebuilds_in_timed": int(rep["nl_updates"]),
             "clocks": ck,
             "solo_ms_per_step": {"min": float(solo.min()), "median": float(np.median(solo)),
@@ -243,22 +247,57 @@ def batched_workload(a, dev):
             "setup_s": {"generate": t_gen, "settle": t_settle}}
 
 
+def reference_input(a):
+    """The benchmark's input state for the CPU arm: the same seeded scene,
+    settled the same way when a GPU is present (input preparation only,
+    outside the timed region), else the freshly deposited pile."""
+    from rockable_gb300 import scenes
+    scene = make_scene(a)
+    if a.scene != "column":
+        return scene, "lattice as generated"
+    try:
+        import torch
+        have_gpu = torch.cuda.is_available()
+    except Exception:
+        have_gpu = False
+    if not have_gpu:
+        return scene, "deposited pile (no GPU to settle it)"
+    g = scenes.settle(scene, steps=a.settle_steps)
+    src = scenes.scene_from_gpu(scene, g)
+    g.close()
+    return src, "pile settled by the same generator (%d steps), not timed" % a.settle_steps
+
+
 def run_reference(a, rank):
+    """The reference's CPU path (the oracle: restatement of the reference
+    step loop, OpenMP over all host threads) on the same workload: W warm-up
+    steps, then exactly K timed steps."""
     if rank != 0:
         return
-    scene = make_scene(a)
-    reps = []
-    for _ in range(max(1, a.warmup and 1)):
-        pass
-    r = cpu_baseline(scene, a.cpu_seconds)
-    value = r["value"]
+    from oracle import oracle
+    from rockable_gb300 import scenes
+    src, how = reference_input(a)
+    oracle.build()
+    d = tempfile.mkdtemp(prefix="rk_ref_")
+    o = oracle.Oracle(scenes.write_conf(src, d))
+    o.update_nl()
+    nfree = o.n - o.n_driven
+    o.run(max(0, a.warmup))
+    t0 = time.perf_counter()
+    o.run(a.steps)
+    el = time.perf_counter() - t0
+    value = nfree * a.steps / el
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = "%d timed steps after %d warm-up steps of the %d-body scene (%s), %.1f s" % (
+        a.steps, a.warmup, o.n, how, el)
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": a.gpus, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "impl": "reference",
-           "config": {"workload": scene["name"], "law": scene["law"], "bodies": int(len(scene["bodies"]["mass"]))},
-           "cpu_baseline": r, "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
-                                      "d2h_bytes_per_step": 0}}
-    out["ms_per_step"] = 1000.0 * (len(scene["bodies"]["mass"]) - scene["n_driven"]) / value
+           "warmup": a.warmup, "ms_per_step": 1000.0 * el / max(1, a.steps), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+           "impl": "reference",
+           "config": {"workload": src["name"], "law": src["law"], "bodies": int(o.n), "free_bodies": int(nfree)},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -302,6 +341,7 @@ def main():
         scenes.set_scene_params(e, scene)
         if src:
             e.upload_entries(src["entries"])
+        e.set_graphs(True)
         return e
 
     def timed(e, steps, label):
@@ -352,13 +392,15 @@ def main():
                        interval_max=1000, seed=3)
         else:
             e.update_nl()
+        e.autotune(2)
+        e.step(TUNE_STEPS)
         e.step(a.warmup)
         r = timed(e, a.steps, label)
         st = e.stats()
         nprof = max(1, min(a.steps, 120))
         prof = profile(e, nprof)
         r.update({"entries": st["n_entries"], "active": st["n_active"], "prof": prof, "nprof": nprof,
-                  "skin": e.skin_stats() if skin else None})
+                  "skin": e.skin_stats() if skin else None, "block_sizes": e.block_sizes()})
         forms[label] = r
         if label != order[-1]:
             e.close()
@@ -408,7 +450,7 @@ def main():
                "form": "mixed precision + learned skin (headline); plain FP64 and mixed without skin alongside",
                "forms": {k: {"value": v["value"], "ms_per_step": v["ms"] / a.steps, "entries": v["entries"],
                              "active": v["active"], "nl_rebuilds_in_timed": v["rep"]["nl_updates"],
-                             "gpu_launches": v["launches"], "skin": v["skin"],
+                             "gpu_launches": v["launches"], "skin": v["skin"], "block_sizes": v["block_sizes"],
                              "phases_ms_per_step": {q: w[0] / v["nprof"] for q, w in v["prof"].items()}}
                          for k, v in forms.items()},
                "headline_form": order[-1],
@@ -419,7 +461,8 @@ def main():
                           "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
                           "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if C * 240 + N * 600 > 129e6 else
                           "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
-                          "parallelism": "replicas" if ws > 1 else "single GPU"},
+                          "parallelism": "replicas" if ws > 1 else "single GPU",
+                          "setup_before_warmup": "%d untimed block-size tuning steps; step graphs on" % TUNE_STEPS},
                "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
                "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
                             "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": None,

@@ -216,6 +216,14 @@ int rk_set_scenes(rk_ctx* ctx, const int32_t* scene_of);
 int rk_set_graphs(rk_ctx* ctx, int on);
 /* Number of step-graph captures and replays since the context was created. */
 int rk_get_graph_stats(const rk_ctx* ctx, int64_t* captures, int64_t* replays);
+/* Block-size autotuner: the next 4 * rounds steps run the narrow phase, the
+ * resultants, the global vertices and the drift with block sizes 64, 128,
+ * 256 and 512 in turn, timed with events; each kernel then keeps its fastest
+ * size.  These kernels give the same results at any block size, so the
+ * tuning steps are ordinary steps.  No reference counterpart. */
+int rk_set_autotune(rk_ctx* ctx, int rounds);
+/* Current block sizes of those four kernels, in that order. */
+int rk_get_block_sizes(const rk_ctx* ctx, int32_t* tpb);
 /* When on, every step also stores each entry's contact normal, point and
  * relative velocity (needed to write a conf file); off by default. */
 int rk_set_record_geometry(rk_ctx* ctx, int on);
@@ -284,6 +292,9 @@ typedef struct rk_skin_config {
   double learning_rate;
   int32_t train_steps;    /* optimiser steps per rebuild */
   uint64_t seed;
+  double partial_fraction;  /* a forced update refreshes only the bodies near their guard
+                               limit when they are at most this fraction of all bodies
+                               (0: every update is a full rebuild) */
 } rk_skin_config;
 typedef struct rk_skin_stats {
   int64_t rebuilds, forced, scheduled;
@@ -292,6 +303,8 @@ typedef struct rk_skin_stats {
   double last_rate;       /* observed max displacement per step, last window */
   double predicted_rate;  /* prediction for the current window */
   double loss;            /* last training loss */
+  int64_t partial;        /* partial refreshes */
+  int64_t partial_bodies; /* bodies refreshed by them, summed */
 } rk_skin_stats;
 int rk_set_skin(rk_ctx* ctx, const rk_skin_config* cfg);
 int rk_get_skin_stats(rk_ctx* ctx, rk_skin_stats* out);

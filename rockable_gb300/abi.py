@@ -69,12 +69,14 @@ class RkServo(C.Structure):
 class RkSkinConfig(C.Structure):
     _fields_ = [("enabled", C.c_int32), ("use_mlp", C.c_int32), ("skin_min", C.c_double), ("skin_max", C.c_double),
                 ("dverlet_ratio", C.c_double), ("interval_min", C.c_int32), ("interval_max", C.c_int32),
-                ("learning_rate", C.c_double), ("train_steps", C.c_int32), ("seed", C.c_uint64)]
+                ("learning_rate", C.c_double), ("train_steps", C.c_int32), ("seed", C.c_uint64),
+                ("partial_fraction", C.c_double)]
 
 
 class RkSkinStats(C.Structure):
     _fields_ = [("rebuilds", I64), ("forced", I64), ("scheduled", I64), ("skin", C.c_double), ("interval", I64),
-                ("last_rate", C.c_double), ("predicted_rate", C.c_double), ("loss", C.c_double)]
+                ("last_rate", C.c_double), ("predicted_rate", C.c_double), ("loss", C.c_double),
+                ("partial", I64), ("partial_bodies", I64)]
 
 
 class RkStepReport(C.Structure):
@@ -104,6 +106,8 @@ SIGNATURES = {
     "rk_set_broadphase": (C.c_int, [P, C.c_int]),
     "rk_set_scenes": (C.c_int, [P, P]),
     "rk_set_graphs": (C.c_int, [P, C.c_int]),
+    "rk_set_autotune": (C.c_int, [P, C.c_int]),
+    "rk_get_block_sizes": (C.c_int, [P, P]),
     "rk_get_graph_stats": (C.c_int, [P, P, P]),
     "rk_accelerations": (C.c_int, [P]),
     "rk_update_nl": (C.c_int, [P]),
@@ -257,6 +261,14 @@ class GpuScene:
         self._chk(self.L.rk_get_graph_stats(self.h, C.byref(a), C.byref(b)), "rk_get_graph_stats")
         return {"captures": a.value, "replays": b.value}
 
+    def autotune(self, rounds=2):
+        self._chk(self.L.rk_set_autotune(self.h, int(rounds)), "rk_set_autotune")
+
+    def block_sizes(self):
+        a = (C.c_int32 * 4)()
+        self._chk(self.L.rk_get_block_sizes(self.h, a), "rk_get_block_sizes")
+        return {"narrow": a[0], "resultants": a[1], "global_vertices": a[2], "drift": a[3]}
+
     def set_scenes(self, scene_of):
         a = None if scene_of is None else _c(scene_of, np.int32)
         self._keep.append(a)
@@ -298,9 +310,9 @@ class GpuScene:
         self._chk(self.L.rk_set_profiling(self.h, 1 if on else 0), "rk_set_profiling")
 
     def set_skin(self, enabled=True, use_mlp=True, skin_min=1e-5, skin_max=1e-3, dverlet_ratio=2.0,
-                 interval_min=5, interval_max=1000, learning_rate=3e-3, train_steps=2, seed=1):
+                 interval_min=5, interval_max=1000, learning_rate=3e-3, train_steps=2, seed=1, partial_fraction=0.2):
         cfg = RkSkinConfig(1 if enabled else 0, 1 if use_mlp else 0, skin_min, skin_max, dverlet_ratio, interval_min,
-                           interval_max, learning_rate, train_steps, seed)
+                           interval_max, learning_rate, train_steps, seed, partial_fraction)
         self._chk(self.L.rk_set_skin(self.h, C.byref(cfg)), "rk_set_skin")
 
     def skin_stats(self):

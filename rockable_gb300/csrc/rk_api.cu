@@ -245,12 +245,41 @@ static int skin_train(Ctx& c) {
   return 0;
 }
 
+// time = fixed + per_entry * size, by least squares over the samples when
+// their sizes differ by more than 5 %, else half fixed / half proportional
+static void fit_cost(const std::vector<std::array<double, 2>>& smp, double& fixed, double& per) {
+  const size_t n = smp.size();
+  if (n == 0) { fixed = per = 0.0; return; }
+  double sx = 0, sy = 0, lo = smp[0][0], hi = smp[0][0];
+  for (auto& q : smp) { sx += q[0]; sy += q[1]; lo = std::min(lo, q[0]); hi = std::max(hi, q[0]); }
+  const double mx = sx / n, my = sy / n;
+  if (n >= 3 && hi > 1.05 * lo) {
+    double sxx = 0, sxy = 0;
+    for (auto& q : smp) { sxx += (q[0] - mx) * (q[0] - mx); sxy += (q[0] - mx) * (q[1] - my); }
+    per = std::max(0.0, sxy / sxx);
+    fixed = std::max(0.0, my - per * mx);
+    if (fixed == 0.0) per = my / std::max(mx, 1.0);
+  } else {
+    fixed = 0.5 * my;
+    per = 0.5 * my / std::max(mx, 1.0);
+  }
+}
+static void push_sample(std::vector<std::array<double, 2>>& v, double size, double ms) {
+  if (v.size() >= 16) v.erase(v.begin());
+  v.push_back({size, ms});
+}
+
 static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   Skin& k = c.skin;
   Scene& s = c.s;
   const double N = (double)std::max<int64_t>(1, s.n - s.n_driven);
   const double ref = k.cfg.skin_max;
-  const double rate = dmax / (double)std::max<int64_t>(1, k.since);
+  // displacement rate that sets the next full rebuild: the largest body's
+  // without partial refreshes; with them (the fastest bodies are refreshed on
+  // their own), twice the mean over all bodies
+  const double rate_max = dmax / (double)std::max<int64_t>(1, k.since);
+  const double rate_bulk = 2.0 * k.dsum / (N * (double)std::max<int64_t>(1, k.since));
+  const double rate = k.cfg.partial_fraction > 0.0 ? std::max(rate_bulk, 1e-30) : rate_max;
   const int64_t ne0 = s.ne;
   const double active = (double)c.h_flags[FLAG_NACTIVE];
   if (k.since > 0) {  // measured cost of the window
@@ -260,6 +289,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
     CK(cudaEventElapsedTime(&ms, k.ea, k.eb));
     double per = ms / (double)k.since;
     k.step_ms = k.step_ms > 0 ? 0.7 * k.step_ms + 0.3 * per : per;
+    push_sample(k.step_samples, (double)s.ne, per);
   }
   k.last_rate = rate;
   for (int q = 3; q > 0; q--) k.rates[q] = k.rates[q - 1];
@@ -281,7 +311,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   f[12] = lg(k.rebuild_ms + 1e-3);
   f[13] = (float)std::max(-3.0, std::min(3.0, std::log10(std::max(rate, 1e-30) / std::max(k.rates[1], 1e-30))));
   f[14] = 1.f;
-  f[15] = 0.f;
+  f[15] = (float)std::max(-3.0, std::min(3.0, std::log10(std::max(rate_max, 1e-30) / std::max(rate, 1e-30))));
   // prediction of the next window's displacement rate
   double u = rate, churn = k.pred_churn;
   if (k.cfg.use_mlp && k.rx.size() >= 8) {
@@ -299,23 +329,26 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   // skin and interval minimising the predicted cost per step.  Entries grow
   // faster than the skin (more sub-element pairs come within reach): the
   // non-active entries are scaled by (skin ratio)^1.6, the power measured on
-  // the hull-grain piles.  Half of the step time (the per-body kernels) and
-  // 30% of the rebuild time (broad phase, sorts) do not depend on the list
-  // size; the rest scales with it.  The interval is the number of steps the
-  // predicted displacement rate takes to use half the skin (with a margin),
-  // which is also when the exact guard would force the rebuild.
+  // the hull-grain piles.  Step and full-rebuild times are the measured
+  // fixed + per-entry costs (least squares over recent windows).  The
+  // interval is the number of steps the predicted displacement rate takes to
+  // use half the skin (with a margin), which is also when the exact guard
+  // would force the rebuild.
   const double margin = 1.3, alpha = 1.6;
   const double C = (double)std::max<int64_t>(1, ne0), A = std::min(active, C);
-  const double T = k.step_ms > 0 ? k.step_ms : 1e-3 * C / 1e5;
-  const double R = k.rebuild_ms > 0 ? k.rebuild_ms : 20.0 * T;
+  double t0, t1, r0, r1;
+  fit_cost(k.step_samples, t0, t1);
+  fit_cost(k.rebuild_samples, r0, r1);
+  if (k.step_samples.empty()) { t0 = 0.05; t1 = 1e-6; }
+  if (k.rebuild_samples.empty()) { r0 = 1.0; r1 = 2e-5; }
   double best = 1e300, best_s = k.skin;
   int64_t best_k = k.interval;
   for (int m = -4; m <= 4; m++) {
     double sk = std::min(k.cfg.skin_max, std::max(k.cfg.skin_min, k.skin * std::pow(2.0, 0.25 * m)));
     double kk = std::floor(0.5 * sk / std::max(u * margin * (1.0 + churn), 1e-30));
     int64_t ki = (int64_t)std::max<double>(k.cfg.interval_min, std::min<double>(k.cfg.interval_max, kk));
-    double ratio = (A + (C - A) * std::pow(sk / std::max(k.skin, 1e-30), alpha)) / C;
-    double J = T * (0.5 + 0.5 * ratio) + R * (0.3 + 0.7 * ratio) / (double)ki;
+    double Cs = A + (C - A) * std::pow(sk / std::max(k.skin, 1e-30), alpha);
+    double J = (t0 + t1 * Cs) + (r0 + r1 * Cs) / (double)ki;
     if (J < best) { best = J; best_s = sk; best_k = ki; }
   }
   k.skin = best_s;
@@ -332,6 +365,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   CK(cudaEventSynchronize(k.eb));
   CK(cudaEventElapsedTime(&rms, k.ea, k.eb));
   k.rebuild_ms = k.rebuild_ms > 0 ? 0.7 * k.rebuild_ms + 0.3 * rms : rms;
+  push_sample(k.rebuild_samples, (double)s.ne, rms);
   c.nl_updates++;
   k.rebuilds++;
   if (forced) k.forced++;
@@ -353,10 +387,10 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   k.feat_prev = f;
   k.have_prev = true;
   if (k.cfg.use_mlp && (rc = skin_train(c))) return rc;
-  launch_skin_snapshot(s, k.ref_pos, k.ref_q, c.stream);
-  c.kernels++;
+  c.kernels += launch_skin_reset(s, nullptr, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
   CK(cudaMemsetAsync(s.flags + FLAG_NEED_UPDATE, 0, sizeof(unsigned long long), c.stream));
   k.since = 0;
+  k.partial_since_global = 0;
   CK(cudaEventRecord(k.ea, c.stream));
   return 0;
 }
@@ -378,6 +412,52 @@ static int step_launches(Ctx& c) {
   n += launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream);
   n += launch_breakage(s, c.stream);
   return n;
+}
+
+// Online block-size tuning: during the first steps after rk_set_autotune,
+// step k launches the four tuned kernels (narrow phase, resultants, global
+// vertices, drift) with candidate block size k mod 4, timed with events;
+// then each kernel keeps its fastest size.  Every thread of these kernels
+// works on its own entry, body or vertex (ordered sums included), so the
+// block size changes no result and the tuning steps are ordinary steps.
+static const int kTuneCand[4] = {64, 128, 256, 512};
+
+static int tune_step(Ctx& c) {
+  Scene& s = c.s;
+  const int64_t done = c.tune_total - c.tune_left;
+  const int ci = (int)(done % 4);
+  for (int k = 0; k < 4; k++) s.tpb[k] = std::min(kTuneCand[ci], max_tpb(k, c.form == RK_FORM_MIXED));
+  cudaStream_t st = c.stream;
+  int n = launch_controls_pre(s, st);
+  CK(cudaEventRecord(c.tev[0], st));
+  n += launch_drift(s, st);
+  CK(cudaEventRecord(c.tev[1], st));
+  n += launch_glob_vertices(s, st);
+  CK(cudaEventRecord(c.tev[2], st));
+  n += c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, st) : launch_narrow_force(s, st);
+  CK(cudaEventRecord(c.tev[3], st));
+  n += launch_gather_heavy(s, st);
+  CK(cudaEventRecord(c.tev[4], st));
+  n += launch_gather_accel(s, 1, st);
+  CK(cudaEventRecord(c.tev[5], st));
+  n += launch_breakage(s, st);
+  c.kernels += n;
+  CK(cudaEventSynchronize(c.tev[5]));
+  float ms[4] = {0, 0, 0, 0};
+  cudaEventElapsedTime(&ms[3], c.tev[0], c.tev[1]);  // drift
+  cudaEventElapsedTime(&ms[2], c.tev[1], c.tev[2]);  // global vertices
+  cudaEventElapsedTime(&ms[0], c.tev[2], c.tev[3]);  // narrow phase
+  cudaEventElapsedTime(&ms[1], c.tev[4], c.tev[5]);  // resultants
+  for (int k = 0; k < 4; k++) c.tune_ms[k][ci] += ms[k];
+  if (--c.tune_left == 0) {
+    for (int k = 0; k < 4; k++) {
+      int best = 1;
+      for (int q = 0; q < 4; q++)
+        if (c.tune_ms[k][q] < c.tune_ms[k][best]) best = q;
+      s.tpb[k] = std::min(kTuneCand[best], max_tpb(k, c.form == RK_FORM_MIXED));
+    }
+  }
+  return RK_OK;
 }
 
 static int step_graph(Ctx& c) {
@@ -425,19 +505,48 @@ static int step_graph(Ctx& c) {
   return RK_OK;
 }
 
+// Partial refresh of the flagged bodies (see rk_skin.cu): the neighbour
+// list restricted to their pairs, and their snapshots reset.
+static int skin_partial(Ctx& c, int64_t nflag) {
+  Skin& k = c.skin;
+  Scene& s = c.s;
+  settle_lazy_forces(c);
+  int rc = rebuild_nl(c, k.flag);
+  if (rc) return rc;
+  c.kernels += launch_skin_reset(s, k.flag, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
+  c.nl_updates++;
+  k.partial++;
+  k.partial_bodies += nflag;
+  k.partial_since_global++;
+  return 0;
+}
+
 int skin_after_step(Ctx& c) {
   Skin& k = c.skin;
   Scene& s = c.s;
-  CK(cudaMemsetAsync(k.d_guard, 0, 8, c.stream));
-  c.kernels += launch_skin_guard(s, k.ref_pos, k.ref_q, k.rsw, k.d_guard, c.stream);
-  CK(cudaMemcpyAsync(k.h_guard, k.d_guard, 8, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemsetAsync(k.d_guard, 0, 32, c.stream));
+  // bodies past half of their budget are refreshed together with the one
+  // that reached it
+  const float flag_at = (float)(0.25 * k.skin);
+  c.kernels += launch_skin_guard(s, k.ref_pos, k.ref_q, k.rsw, k.maxd, k.path, flag_at, k.flag, k.d_guard, c.stream);
+  CK(cudaMemcpyAsync(k.h_guard, k.d_guard, 32, cudaMemcpyDeviceToHost, c.stream));
   int rc;
   if ((rc = read_flags(c))) return rc;
   k.since++;
-  const double dmax = to_f(k.h_guard[0]), vmax = to_f(k.h_guard[1]);
-  const bool forced = dmax >= 0.5 * k.skin;
+  const double dmax = to_f(k.h_guard[0]), vmax = to_f(k.h_guard[1]), gmax = to_f(k.h_guard[2]);
+  const int64_t nflag = (int64_t)k.h_guard[3];
+  double dsum = 0.0;
+  std::memcpy(&dsum, k.h_guard + 4, sizeof dsum);
+  k.dsum = dsum;
+  const double crit = k.partial_since_global > 0 ? gmax : dmax;
+  const bool forced = crit >= 0.5 * k.skin;
   const bool need = c.h_flags[FLAG_NEED_UPDATE] != 0ull;
-  if (forced || need || k.since >= k.interval) return skin_rebuild(c, dmax, vmax, forced);
+  if (need || k.since >= k.interval) return skin_rebuild(c, dmax, vmax, false);
+  if (forced) {
+    if (k.cfg.partial_fraction > 0.0 && nflag > 0 && (double)nflag <= k.cfg.partial_fraction * (double)s.n)
+      return skin_partial(c, nflag);
+    return skin_rebuild(c, dmax, vmax, true);
+  }
   return 0;
 }
 
@@ -491,6 +600,8 @@ void rk_destroy(rk_ctx* x) {
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.gexec) cudaGraphExecDestroy(c.gexec);
+  for (int k = 0; k < 8; k++)
+    if (c.tev[k]) cudaEventDestroy(c.tev[k]);
   Scene& s = c.s;
   dfree(s.vert_ofs); dfree(s.edge_ofs); dfree(s.edges); dfree(s.face_ofs); dfree(s.face_vofs); dfree(s.face_verts);
   dfree(s.svert); dfree(s.sradius); dfree(s.sobb);
@@ -498,7 +609,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.shape); dfree(s.group); dfree(s.cluster);
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.gv); dfree(s.bobb); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
-  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jlist);
+  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.heavy_lazy); dfree(s.bnd);
   dfree(s.needres); dfree(s.scene_of);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
@@ -514,6 +625,7 @@ void rk_destroy(rk_ctx* x) {
   {
     Skin& k = c.skin;
     dfree(k.ref_pos); dfree(k.ref_q); dfree(k.rsw); dfree(k.d_guard); dfree(k.master); dfree(k.m); dfree(k.v);
+    dfree(k.maxd); dfree(k.path); dfree(k.flag);
     dfree(k.grad); dfree(k.loss); dfree(k.X); dfree(k.T); dfree(k.io);
     if (k.w) cudaFree(k.w);
     if (k.h_guard) cudaFreeHost(k.h_guard);
@@ -579,6 +691,11 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
   if (!c.have_shapes) return fail(c, RK_ERR_STATE, "upload the shapes before the bodies");
   if (b->n >= kMaxBody) return fail(c, RK_ERR_CAPACITY, "more than 2^21 - 1 bodies");
   const int64_t n = b->n;
+  // new bodies: the learned skin (per-body guard state) starts again with rk_set_skin
+  c.skin.on = false;
+  c.s.sk_path = nullptr;
+  c.s.sk_rsw = nullptr;
+  c.s.near_geometric = 0;
   std::vector<int64_t> gv_ofs(n + 1, 0);
   std::vector<double> rad(n);
   for (int64_t i = 0; i < n; i++) {
@@ -613,6 +730,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.dpos, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.dq, (const double*)nullptr, 4 * n)) ||
       (rc = dupload(c, s.iofs, (const int64_t*)nullptr, n + 1)) ||
       (rc = dupload(c, s.jofs, (const int64_t*)nullptr, n + 1)) ||
+      (rc = dupload(c, s.jsplit, (const int64_t*)nullptr, n)) ||
       (rc = dupload(c, s.if_ofs, (const int64_t*)nullptr, n + 1)) ||
       (rc = dupload(c, s.sph_ofs, sph_ofs.data(), n + 1)) || (rc = dalloc(c, s.sph, sph_ofs[n])) ||
       (rc = dupload(c, s.is_heavy, (const uint8_t*)nullptr, n)) || (rc = dalloc(c, s.heavy, n)) ||
@@ -810,9 +928,19 @@ static int skin_alloc(Ctx& c) {
   Scene& s = c.s;
   const int np = mlp_num_params();
   int rc;
-  if (!k.ref_pos) {
+  if (k.ref_pos && k.nalloc < s.n) {  // bodies re-uploaded with a larger count
+    dfree(k.ref_pos); dfree(k.ref_q); dfree(k.rsw); dfree(k.maxd); dfree(k.path); dfree(k.flag);
+    k.ref_pos = nullptr;
     if ((rc = dalloc(c, k.ref_pos, 3 * s.n)) || (rc = dalloc(c, k.ref_q, 4 * s.n)) || (rc = dalloc(c, k.rsw, s.n)) ||
-        (rc = dalloc(c, k.d_guard, 2)) || (rc = dalloc(c, k.master, np)) || (rc = dalloc(c, k.m, np)) ||
+        (rc = dalloc(c, k.maxd, s.n)) || (rc = dalloc(c, k.path, s.n)) || (rc = dalloc(c, k.flag, s.n)))
+      return rc;
+    k.nalloc = s.n;
+  }
+  if (!k.ref_pos) {
+    k.nalloc = s.n;
+    if ((rc = dalloc(c, k.ref_pos, 3 * s.n)) || (rc = dalloc(c, k.ref_q, 4 * s.n)) || (rc = dalloc(c, k.rsw, s.n)) ||
+        (rc = dalloc(c, k.d_guard, 8)) || (rc = dalloc(c, k.maxd, s.n)) || (rc = dalloc(c, k.path, s.n)) ||
+        (rc = dalloc(c, k.flag, s.n)) || (rc = dalloc(c, k.master, np)) || (rc = dalloc(c, k.m, np)) ||
         (rc = dalloc(c, k.v, np)) || (rc = dalloc(c, k.grad, np)) || (rc = dalloc(c, k.loss, 1)) ||
         (rc = dalloc(c, k.X, 16 * mlp_max_batch())) || (rc = dalloc(c, k.T, 2 * mlp_max_batch())) ||
         (rc = dalloc(c, k.io, 32)))
@@ -820,7 +948,7 @@ static int skin_alloc(Ctx& c) {
     char* wbuf = nullptr;
     CK(cudaMalloc(&wbuf, 2 * (size_t)np));
     k.w = wbuf;
-    CK(cudaMallocHost(&k.h_guard, 8));
+    CK(cudaMallocHost(&k.h_guard, 32));
     CK(cudaEventCreate(&k.ea));
     CK(cudaEventCreate(&k.eb));
   }
@@ -892,10 +1020,14 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   Skin& k = c.skin;
   if (!cfg->enabled) {
     k.on = false;
+    c.s.sk_path = nullptr;
+    c.s.sk_rsw = nullptr;
+    c.s.near_geometric = 0;
     return RK_OK;
   }
   if (!(cfg->skin_min > 0.0) || cfg->skin_max < cfg->skin_min || cfg->interval_min < 1 ||
-      cfg->interval_max < cfg->interval_min || !(cfg->dverlet_ratio >= 1.0))
+      cfg->interval_max < cfg->interval_min || !(cfg->dverlet_ratio >= 1.0) || !(cfg->partial_fraction >= 0.0) ||
+      cfg->partial_fraction > 1.0)
     return fail(c, RK_ERR_ARG, "invalid skin configuration");
   if ((rc = skin_alloc(c))) return rc;
   Scene& s = c.s;
@@ -930,15 +1062,22 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   k.interval = cfg->interval_min;
   k.since = 0;
   k.rebuilds = k.forced = k.scheduled = 0;
+  k.partial = k.partial_bodies = k.partial_since_global = 0;
+  k.rebuild_samples.clear();
+  k.step_samples.clear();
+  k.dsum = 0.0;
   k.step_ms = k.rebuild_ms = 0.0;
   for (double& r : k.rates) r = 0.0;
   s.dVerlet = k.skin;
   s.DVerlet = cfg->dverlet_ratio * k.skin;
   k.on = true;
+  s.sk_path = k.path;
+  s.sk_rsw = k.rsw;
+  s.near_geometric = 1;
   // start from a fresh list built with the initial skin
   launch_glob_vertices(s, c.stream);
   if ((rc = rebuild_nl(c))) return rc;
-  launch_skin_snapshot(s, k.ref_pos, k.ref_q, c.stream);
+  launch_skin_reset(s, nullptr, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
   CK(cudaEventRecord(k.ea, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   return RK_OK;
@@ -955,6 +1094,8 @@ int rk_get_skin_stats(rk_ctx* x, rk_skin_stats* o) {
   o->last_rate = k.last_rate;
   o->predicted_rate = k.pred_rate;
   o->loss = k.last_loss;
+  o->partial = k.partial;
+  o->partial_bodies = k.partial_bodies;
   return RK_OK;
 }
 
@@ -977,6 +1118,25 @@ int rk_set_scenes(rk_ctx* x, const int32_t* scene_of) {
   int rc;
   if ((rc = dupload(c, s.scene_of, scene_of, s.n))) return rc;
   CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
+int rk_set_autotune(rk_ctx* x, int rounds) {
+  if (!x || rounds < 0) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  for (int k = 0; k < 8; k++)
+    if (!c.tev[k]) CK(cudaEventCreate(&c.tev[k]));
+  for (auto& row : c.tune_ms)
+    for (double& v : row) v = 0.0;
+  c.tune_total = c.tune_left = 4 * (int64_t)rounds;
+  return RK_OK;
+}
+
+int rk_get_block_sizes(const rk_ctx* x, int32_t* tpb) {
+  if (!x || !tpb) return RK_ERR_ARG;
+  const int def[4] = {128, 128, 256, 128};
+  for (int k = 0; k < 4; k++) tpb[k] = x->c.s.tpb[k] > 0 ? x->c.s.tpb[k] : def[k];
   return RK_OK;
 }
 
@@ -1058,7 +1218,8 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
   for (int64_t it = 0; it < nsteps; it++) {
     c.t += s.dt;
     c.interVerletC += s.dt;
-    const bool graphed = c.use_graphs && !c.profiling;
+    const bool tuning = c.tune_left > 0 && !c.profiling;
+    const bool graphed = c.use_graphs && !c.profiling && !tuning;
     if (graphed) {
       if ((rc = step_graph(c))) return rc;
     } else {
@@ -1080,7 +1241,9 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
         c.prof_n[p] += launched;
       }
     };
-    if (!graphed) {
+    if (tuning) {
+      if ((rc = tune_step(c))) return rc;
+    } else if (!graphed) {
       mark(0, false); phase(0, launch_controls_pre(s, c.stream));
       mark(1, false); phase(1, launch_drift(s, c.stream));
       mark(2, false); phase(2, launch_glob_vertices(s, c.stream));

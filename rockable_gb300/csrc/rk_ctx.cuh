@@ -56,8 +56,14 @@ struct Skin {
   double* ref_pos = nullptr;
   double* ref_q = nullptr;
   float* rsw = nullptr;
-  unsigned int* d_guard = nullptr;  // [0] max delta bits, [1] max |v| bits
+  int64_t nalloc = 0;               // bodies the per-body arrays hold
+  float* maxd = nullptr;            // n: largest delta since the body's last refresh
+  float* path = nullptr;            // n: path-length bound since the body's last refresh
+  uint8_t* flag = nullptr;          // n: bodies due for a partial refresh
+  unsigned int* d_guard = nullptr;  // guard reductions (see k_skin_guard)
   unsigned int* h_guard = nullptr;  // pinned
+  int64_t partial = 0, partial_bodies = 0, partial_since_global = 0, since_global = 0;
+  double dsum = 0.0;                // sum of delta over bodies at the last step
   // MLP
   float* master = nullptr;
   void* w = nullptr;
@@ -75,6 +81,9 @@ struct Skin {
   double last_rate = 0.0, pred_rate = 0.0, pred_churn = 0.0, last_loss = 0.0;
   int64_t rebuilds = 0, forced = 0, scheduled = 0;
   double step_ms = 0.0, rebuild_ms = 0.0;  // measured costs (exponential averages)
+  // recent (list size, time) samples of full rebuilds and of window steps,
+  // fitted by least squares to time = fixed + per_entry * size
+  std::vector<std::array<double, 2>> rebuild_samples, step_samples;
   cudaEvent_t ea = nullptr, eb = nullptr;
   double window_ms = 0.0;
 };
@@ -120,6 +129,10 @@ struct Ctx {
   int64_t last_nover = 0;
   bool forces_stale = false;
   std::vector<uint8_t> needres_host;
+  // block-size autotuner of the step kernels (results do not depend on it)
+  int64_t tune_left = 0, tune_total = 0;
+  double tune_ms[4][4] = {};
+  cudaEvent_t tev[8] = {};
   // CUDA graph of one step's launches (re-captured when the scene changes)
   int use_graphs = 0;
   cudaGraphExec_t gexec = nullptr;
@@ -129,7 +142,9 @@ struct Ctx {
   int64_t graph_captures = 0, graph_replays = 0;
 };
 
-int rebuild_nl(Ctx& c);
+// Neighbour-list update; with `only` (device flags per body), only the pairs
+// with at least one flagged body are visited (partial refresh).
+int rebuild_nl(Ctx& c, const uint8_t* only = nullptr);
 int heavy_list(Ctx& c);
 int ensure_entry_capacity(Ctx& c, int which, int64_t n);
 void bind_entries(Ctx& c);

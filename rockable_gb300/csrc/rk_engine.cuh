@@ -105,6 +105,7 @@ struct Scene {
   int record_geom;
   int64_t* iofs;  // n+1
   int64_t* jofs;  // n+1
+  int64_t* jsplit;  // n: first j-side slot of body b whose entry follows b's own block
   int* jlist;     // ne
   int* heavy;     // bodies whose entry count exceeds kHeavy (summed by a block each)
   int nheavy;
@@ -114,6 +115,10 @@ struct Scene {
   uint8_t* needres;   // n: 1 when the body's resultant is used by the step (free or force-controlled)
   float* bnd;         // n: largest distance of a vertex from the body centre (world, rounded up)
   int* scene_of;      // n: scene index (bodies of different scenes never interact)
+  int near_geometric;  // 1: distance-only NEAR tests in the rebuild (learned skin), 0: Rockable's predicates
+  int tpb[4];         // threads per block of the narrow phase, resultants, global vertices, drift (0: default)
+  float* sk_path;     // n: path-length bound of each free body since its last refresh (learned skin), or null
+  const float* sk_rsw;  // n: swing radius (largest vertex distance from the centre), with sk_path
   float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
   int64_t* sph_ofs;   // n+1
   // ---- interfaces
@@ -131,7 +136,7 @@ struct Scene {
 };
 
 enum { FLAG_NEED_UPDATE = 0, FLAG_NACTIVE = 1, FLAG_NBROKEN = 2, FLAG_GPOS = 3, FLAG_GROT = 4, FLAG_GRESET = 5,
-       FLAG_ERROR = 6, FLAG_COUNT = 8 };
+       FLAG_ERROR = 6, FLAG_NONFINITE = 7, FLAG_COUNT = 8 };  // [7]: 1 + index of a body with non-finite state
 
 // step kernels (rk_step.cu)
 int launch_controls_pre(const Scene& s, cudaStream_t st);
@@ -145,11 +150,14 @@ int launch_gather_heavy_lazy(const Scene& s, cudaStream_t st);
 int launch_breakage(const Scene& s, cudaStream_t st);
 int launch_guard(const Scene& s, cudaStream_t st);
 int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);
+int max_tpb(int which, int form_mixed);
+cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a);
 
 // learned skin (rk_skin.cu)
-int launch_skin_snapshot(const Scene& s, double* rp, double* rq, cudaStream_t st);
-int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, unsigned int* out,
+int launch_skin_reset(const Scene& s, const uint8_t* only, double* rp, double* rq, float* maxd, float* path,
                       cudaStream_t st);
+int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, float* maxd,
+                      const float* path, float flag_at, uint8_t* flag, unsigned int* out, cudaStream_t st);
 int mlp_num_params();
 int mlp_max_batch();
 void launch_mlp_infer(const void* w, const float* x, float* y, cudaStream_t st);

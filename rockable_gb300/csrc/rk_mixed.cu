@@ -292,8 +292,10 @@ __global__ void k_narrow_force_mixed(Scene s) {
 
 int launch_narrow_force_mixed(const Scene& s, cudaStream_t st) {
   if (s.ne <= 0) return 0;
-  k_narrow_force_mixed<<<(unsigned)((s.ne + 127) / 128), 128, 0, st>>>(s);
+  const int t = s.tpb[0] > 0 ? s.tpb[0] : 128;
+  k_narrow_force_mixed<<<(unsigned)((s.ne + t - 1) / t), t, 0, st>>>(s);
   return 1;
 }
+cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a) { return cudaFuncGetAttributes(a, k_narrow_force_mixed); }
 
 }  // namespace rk

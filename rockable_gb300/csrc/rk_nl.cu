@@ -72,6 +72,8 @@ __global__ void k_body_obb(Scene s) {
                         ex * fabs(o.e0.y) + ey * fabs(o.e1.y) + ez * fabs(o.e2.y),
                         ex * fabs(o.e0.z) + ey * fabs(o.e1.z) + ez * fabs(o.e2.z)};
   const double c[3] = {o.c.x, o.c.y, o.c.z};
+  if (!isfinite(c[0] + c[1] + c[2] + hw[0] + hw[1] + hw[2]))
+    atomicMax(s.flags + FLAG_NONFINITE, (unsigned long long)b + 1ull);
   float* bb = s.baabb + 6 * b;
   for (int k = 0; k < 3; k++) {
     double m = 1e-6 * (hw[k] + fabs(c[k])) + 1e-12;  // slack covering the SAT epsilon
@@ -122,6 +124,16 @@ __global__ void k_heavy(Scene s, unsigned long long* count) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
   int64_t c = (s.iofs[b + 1] - s.iofs[b]) + (s.jofs[b + 1] - s.jofs[b]);
+  {  // split of the j-side list around b's own block (entry indices ascend in it)
+    const int64_t i0 = s.iofs[b];
+    int64_t lo = s.jofs[b], hi = s.jofs[b + 1];
+    while (lo < hi) {
+      const int64_t m = (lo + hi) >> 1;
+      if (s.jlist[m] < i0) lo = m + 1;
+      else hi = m;
+    }
+    s.jsplit[b] = lo;
+  }
   bool h = c > kHeavy;
   uint8_t kind = 0;
   if (h && s.needres[b]) {
@@ -158,7 +170,7 @@ __device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
 // All-pairs broad phase: float AABB filter (tiled through shared memory),
 // then eligibility and the FP64 SAT of the enlarged OBBs.
 constexpr int kPairTile = 128;
-__global__ void k_pairs(Scene s, uint64_t* pairs, int64_t cap, unsigned long long* counter) {
+__global__ void k_pairs(Scene s, const uint8_t* only, uint64_t* pairs, int64_t cap, unsigned long long* counter) {
   __shared__ float sb[kPairTile][6];
   const int64_t i = blockIdx.x * (int64_t)kPairTile + threadIdx.x;
   const bool vi = i < s.n;
@@ -180,6 +192,7 @@ __global__ void k_pairs(Scene s, uint64_t* pairs, int64_t cap, unsigned long lon
           sb[t][2] > a[5])
         continue;
       if (i < s.n_driven && j < s.n_driven) continue;
+      if (only && !only[i] && !only[j]) continue;
       if (s.scene_of && s.scene_of[i] != s.scene_of[j]) continue;
       if (has_iface(s, (int)i, (int)j)) continue;
       Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
@@ -280,13 +293,16 @@ __global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys,
   keys[b] = (cell_code(scene, cx, cy, cz, f) << 21) | (uint64_t)b;
 }
 
-__global__ void k_grid_pairs(Scene s, const uint64_t* keys, int64_t nnorm, float inv_cell, uint64_t* pairs,
-                             int64_t cap, unsigned long long* counter) {
+// With `only` (a partial refresh), body i enumerates its pairs when it is
+// flagged, with every neighbour that is not flagged or has a larger index.
+__global__ void k_grid_pairs(Scene s, const uint8_t* only, const uint64_t* keys, int64_t nnorm, float inv_cell,
+                             uint64_t* pairs, int64_t cap, unsigned long long* counter) {
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= nnorm) return;
   const CellFormat f = cell_format(s);
   const uint64_t key = keys[k];
   const int64_t i = (int64_t)(key & ((1u << 21) - 1));
+  if (only && !only[i]) return;
   const uint64_t code = key >> 21;
   const uint64_t amask = (1u << f.bits) - 1u;
   const uint64_t scene = f.batched ? (code >> 33) : 0u;
@@ -300,21 +316,23 @@ __global__ void k_grid_pairs(Scene s, const uint64_t* keys, int64_t nnorm, float
         int64_t q = lower_bound_u64(keys, nnorm, c2 << 21);
         for (; q < nnorm && (keys[q] >> 21) == c2; q++) {
           const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
-          if (j <= i) continue;
-          if (!pair_predicate(s, i, j)) continue;
+          if (only ? (j == i || (only[j] && j < i)) : (j <= i)) continue;
+          const int64_t lo = min(i, j), hi = max(i, j);
+          if (!pair_predicate(s, lo, hi)) continue;
           unsigned long long at = atomicAdd(counter, 1ull);
-          if ((int64_t)at < cap) pairs[at] = ((uint64_t)i << 21) | (uint64_t)j;
+          if ((int64_t)at < cap) pairs[at] = ((uint64_t)lo << 21) | (uint64_t)hi;
         }
       }
 }
 
 // oversized body o against every body j of its scene (each pair once)
-__global__ void k_over_pairs(Scene s, const int* over, const uint8_t* is_over, uint64_t* pairs, int64_t cap,
-                             unsigned long long* counter) {
+__global__ void k_over_pairs(Scene s, const uint8_t* only, const int* over, const uint8_t* is_over, uint64_t* pairs,
+                             int64_t cap, unsigned long long* counter) {
   int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int o = over[blockIdx.y];
   if (j >= s.n || j == o) return;
   if (is_over[j] && j < o) return;  // counted from the other oversized body
+  if (only && !only[o] && !only[j]) return;
   const int64_t i0 = min((int64_t)o, j), j0 = max((int64_t)o, j);
   if (!pair_predicate(s, i0, j0)) return;
   unsigned long long at = atomicAdd(counter, 1ull);
@@ -414,6 +432,100 @@ __device__ __forceinline__ bool near_ee(const Scene& s, const PairView& P, int e
   return false;
 }
 
+// ------------------------------------------ geometric NEAR (skin mode) ----
+// Distance-only tests on float coordinates (the vertex spheres' centres are
+// the vertices): vertex-vertex, vertex-segment, vertex-polygon and
+// segment-segment distances against R_b + R_p + dVerlet plus a rounding
+// margin.  Rockable's NEAR predicates also require the projection of a
+// vertex inside the face, or the closest points inside both edges, so a
+// sub-contact can start to touch after an arbitrarily small sliding motion;
+// with distances only, every sub-contact that touches now was within
+// dVerlet of touching at its last test whenever the motion since is below
+// dVerlet -- what makes the learned-skin guard exact.  Used only with the
+// learned skin; the plain and mixed forms keep the reference predicates.
+struct G3 {
+  float x, y, z;
+};
+__device__ __forceinline__ G3 gsub(G3 a, G3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ G3 gmad(G3 a, float t, G3 d) { return {a.x + t * d.x, a.y + t * d.y, a.z + t * d.z}; }
+__device__ __forceinline__ float gdot(G3 a, G3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ G3 gcross(G3 a, G3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ G3 gpt(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ float clamp01(float t) { return fminf(fmaxf(t, 0.f), 1.f); }
+
+__device__ __forceinline__ float pt_seg_d2(G3 p, G3 a, G3 b) {
+  const G3 ab = gsub(b, a), ap = gsub(p, a);
+  const float l2 = gdot(ab, ab);
+  const float t = l2 > 0.f ? clamp01(gdot(ap, ab) / l2) : 0.f;
+  const G3 d = gmad(ap, -t, ab);
+  return gdot(d, d);
+}
+
+// squared distance of two segments: the closest-point parameters minimise
+// |p1 + s d1 - p2 - t d2| over [0,1]^2 (interior stationary point, else the
+// best clamped edge of the square)
+__device__ __forceinline__ float seg_seg_d2(G3 p1, G3 q1, G3 p2, G3 q2) {
+  const G3 d1 = gsub(q1, p1), d2 = gsub(q2, p2), r = gsub(p1, p2);
+  const float a = gdot(d1, d1), e = gdot(d2, d2), f = gdot(d2, r), c = gdot(d1, r), b = gdot(d1, d2);
+  float s = 0.f, t = 0.f;
+  if (a <= 1e-30f && e <= 1e-30f) {
+    s = t = 0.f;
+  } else if (a <= 1e-30f) {
+    t = clamp01(f / e);
+  } else if (e <= 1e-30f) {
+    s = clamp01(-c / a);
+  } else {
+    const float den = a * e - b * b;
+    s = den > 0.f ? clamp01((b * f - c * e) / den) : 0.f;
+    t = (b * s + f) / e;
+    if (t < 0.f) {
+      t = 0.f;
+      s = clamp01(-c / a);
+    } else if (t > 1.f) {
+      t = 1.f;
+      s = clamp01((b - c) / a);
+    }
+  }
+  const G3 w = gsub(gmad(p1, s, d1), gmad(p2, t, d2));
+  return gdot(w, w);
+}
+
+// squared distance of a point to a planar polygon (vertices in order)
+__device__ __forceinline__ float pt_poly_d2(const Scene& s, const float4* sp, int sh, int f, G3 p) {
+  const int fo = s.face_ofs[sh] + f;
+  const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
+  const int* fv = s.face_verts + v0;
+  const G3 A = gpt(sp[fv[0]]), B = gpt(sp[fv[1]]), C = gpt(sp[fv[nbv - 1]]);
+  G3 n = gcross(gsub(B, A), gsub(C, A));
+  const float nn = gdot(n, n);
+  float best = 3.0e38f;
+  if (nn > 0.f) {
+    const float inv = rsqrtf(nn);
+    n = {n.x * inv, n.y * inv, n.z * inv};
+    const float dist = gdot(gsub(p, A), n);
+    // crossing number of the projection, in the plane
+    const G3 u = gsub(B, A);
+    const float iu = rsqrtf(fmaxf(gdot(u, u), 1e-30f));
+    const G3 e1 = {u.x * iu, u.y * iu, u.z * iu};
+    const G3 e2 = gcross(n, e1);
+    const G3 q = gsub(p, A);
+    const float o1 = gdot(q, e1), o2 = gdot(q, e2);
+    int odd = 0;
+    for (int k = 0; k < nbv; k++) {
+      const G3 pa = gsub(gpt(sp[fv[k]]), A), pb = gsub(gpt(sp[fv[k + 1 == nbv ? 0 : k + 1]]), A);
+      const float a1 = gdot(pa, e1), b1 = gdot(pb, e1), a2 = gdot(pa, e2), b2 = gdot(pb, e2);
+      if ((a2 < o2 && b2 >= o2) || (b2 < o2 && a2 >= o2))
+        if (a1 + (o2 - a2) / (b2 - a2) * (b1 - a1) < o1) odd = 1 - odd;
+    }
+    if (odd) best = dist * dist;
+  }
+  for (int k = 0; k < nbv; k++)
+    best = fminf(best, pt_seg_d2(p, gpt(sp[fv[k]]), gpt(sp[fv[k + 1 == nbv ? 0 : k + 1]])));
+  return best;
+}
+
 // Candidate sub-contacts of the half-pairs: one warp per half-pair (owner b
 // -> partner p).  The lanes first compute, in parallel, the owner vertices
 // that pass the OBB cull (FP64 SAT of the vertex cube against p's box
@@ -461,6 +573,7 @@ __device__ __forceinline__ void warp_emit(bool ok, uint64_t key, int lane, uint6
   }
 }
 
+template <bool GEOM>
 __global__ void __launch_bounds__(32 * kCandWarps)
 k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t* out, int64_t cap,
              unsigned long long* counter) {
@@ -528,6 +641,12 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
     const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
     const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
+    // geometric tests: limit with a margin for the float rounding of
+    // coordinates of magnitude up to `mag`
+    const float mag = fmaxf(fmaxf(fmaxf(fabsf(cb.x), fabsf(cb.y)), fabsf(cb.z)) + cb.w,
+                            fmaxf(fmaxf(fabsf(cp.x), fabsf(cp.y)), fabsf(cp.z)) + cp.w);
+    const float glim = sum + 1e-4f * sum + 1e-6f * mag + 1e-9f;
+    const float glim2 = glim * glim;
     const bool lower = b < p;  // vertex-vertex and edge-edge pairs are tested in the i < j direction only
     const int nbv = warp_list(L.bv, nvb, lane, [&](int v) { return (((v < 32 ? m0 : m1) >> (v & 31)) & 1u) != 0u; });
     const int npv = lower ? warp_list(L.pv, nvp, lane, [&](int w) { return !far(sp[w], cb, cb.w); }) : 0;
@@ -551,7 +670,12 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
       if (c < tot) {
         v = L.bv[c / npv];
         w = L.pv[c % npv];
-        ok = !far(sb[v], sp[w], 0.f) && near_vv(P, v, w);
+        if (GEOM) {
+          const G3 d = gsub(gpt(sb[v]), gpt(sp[w]));
+          ok = gdot(d, d) <= glim2;
+        } else {
+          ok = !far(sb[v], sp[w], 0.f) && near_vv(P, v, w);
+        }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 0u, (uint32_t)v, (uint32_t)w), lane, out, cap, counter);
     }
@@ -564,7 +688,13 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         v = L.bv[c / npe];
         e = L.pe[c % npe];
         const float4 se = sp[nvp + e];
-        ok = !far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e);
+        if (GEOM) {
+          const int eo = s.edge_ofs[P.sp] + e;
+          ok = !far(sb[v], se, se.w) &&
+               pt_seg_d2(gpt(sb[v]), gpt(sp[s.edges[2 * eo]]), gpt(sp[s.edges[2 * eo + 1]])) <= glim2;
+        } else {
+          ok = !far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e);
+        }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 1u, (uint32_t)v, (uint32_t)e), lane, out, cap, counter);
     }
@@ -577,7 +707,8 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         v = L.bv[c / npf];
         f = L.pf[c % npf];
         const float4 sf = sp[nvp + nep + f];
-        ok = !far(sb[v], sf, sf.w) && near_vf(s, P, v, f);
+        if (GEOM) ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2;
+        else ok = !far(sb[v], sf, sf.w) && near_vf(s, P, v, f);
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 2u, (uint32_t)v, (uint32_t)f), lane, out, cap, counter);
     }
@@ -590,7 +721,14 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         e1 = L.be[c / npe];
         e2 = L.pe[c % npe];
         const float4 s1 = sb[nvb + e1], s2 = sp[nvp + e2];
-        ok = !far(s1, s2, s1.w + s2.w) && near_ee(s, P, e1, e2);
+        if (GEOM) {
+          const int ob = s.edge_ofs[P.sb] + e1, op = s.edge_ofs[P.sp] + e2;
+          ok = !far(s1, s2, s1.w + s2.w) &&
+               seg_seg_d2(gpt(sb[s.edges[2 * ob]]), gpt(sb[s.edges[2 * ob + 1]]), gpt(sp[s.edges[2 * op]]),
+                          gpt(sp[s.edges[2 * op + 1]])) <= glim2;
+        } else {
+          ok = !far(s1, s2, s1.w + s2.w) && near_ee(s, P, e1, e2);
+        }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 3u, (uint32_t)e1, (uint32_t)e2), lane, out, cap, counter);
     }
@@ -757,16 +895,27 @@ static int64_t read_i64(Ctx& c, const int64_t* d) {
   return v;
 }
 
-int rebuild_nl(Ctx& c) {
+int rebuild_nl(Ctx& c, const uint8_t* only) {
   Scene& s = c.s;
   NLWork& w = c.w;
   cudaStream_t st = c.stream;
   int rc;
   const int64_t N = s.n;
   if (N <= 0) return 0;
+  RKCHK(cudaMemsetAsync(s.flags + FLAG_NONFINITE, 0, sizeof(unsigned long long), st));
   k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
   k_spheres<<<nblk(N, 128), 128, 0, st>>>(s);
   c.kernels += 2;
+  {  // a body whose state is no longer finite: stop here, loudly
+    unsigned long long bad = 0;
+    RKCHK(cudaMemcpyAsync(&bad, s.flags + FLAG_NONFINITE, sizeof bad, cudaMemcpyDeviceToHost, st));
+    RKCHK(cudaStreamSynchronize(st));
+    if (bad) {
+      c.err = "non-finite position or orientation of body " + std::to_string(bad - 1) +
+              " (unstable time step or exploding contact?)";
+      return RK_ERR_NUMERIC;
+    }
+  }
   // ---- pairs
   if (w.pair_cap < 16 * N + 1024) {
     int64_t nc = 16 * N + 1024;
@@ -817,10 +966,11 @@ int rebuild_nl(Ctx& c) {
     c.kernels += 16;
     for (int attempt = 0; attempt < 4; attempt++) {
       RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
-      k_grid_pairs<<<nblk(N - nover, 128), 128, 0, st>>>(s, w.gkeys, N - nover, inv, w.pairs, w.pair_cap, w.counter);
+      k_grid_pairs<<<nblk(N - nover, 128), 128, 0, st>>>(s, only, w.gkeys, N - nover, inv, w.pairs, w.pair_cap,
+                                                          w.counter);
       if (nover > 0) {
         dim3 g2(nblk(N, 128), (unsigned)nover);
-        k_over_pairs<<<g2, 128, 0, st>>>(s, w.gover, w.gis_over, w.pairs, w.pair_cap, w.counter);
+        k_over_pairs<<<g2, 128, 0, st>>>(s, only, w.gover, w.gis_over, w.pairs, w.pair_cap, w.counter);
       }
       c.kernels += 2;
       unsigned long long cnt = 0;
@@ -836,7 +986,7 @@ int rebuild_nl(Ctx& c) {
   } else {
     for (int attempt = 0; attempt < 4; attempt++) {
       RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
-      k_pairs<<<nblk(N, kPairTile), kPairTile, 0, st>>>(s, w.pairs, w.pair_cap, w.counter);
+      k_pairs<<<nblk(N, kPairTile), kPairTile, 0, st>>>(s, only, w.pairs, w.pair_cap, w.counter);
       c.kernels++;
       unsigned long long cnt = 0;
       RKCHK(cudaMemcpyAsync(&cnt, w.counter, 8, cudaMemcpyDeviceToHost, st));
@@ -882,7 +1032,11 @@ int rebuild_nl(Ctx& c) {
     const unsigned grid = (unsigned)std::min<int64_t>((nhp + kCandWarps - 1) / kCandWarps, 152 * 16);
     for (int attempt = 0; attempt < 4; attempt++) {
       RKCHK(cudaMemsetAsync(w.counter + 3, 0, 8, st));
-      k_candidates<<<grid, 32 * kCandWarps, 0, st>>>(s, w.hp, nhp, w.hp_mask, w.cand, w.cand_cap, w.counter + 3);
+      if (s.near_geometric)
+        k_candidates<true><<<grid, 32 * kCandWarps, 0, st>>>(s, w.hp, nhp, w.hp_mask, w.cand, w.cand_cap, w.counter + 3);
+      else
+        k_candidates<false><<<grid, 32 * kCandWarps, 0, st>>>(s, w.hp, nhp, w.hp_mask, w.cand, w.cand_cap,
+                                                              w.counter + 3);
       c.kernels++;
       unsigned long long cnt = 0;
       RKCHK(cudaMemcpyAsync(&cnt, w.counter + 3, 8, cudaMemcpyDeviceToHost, st));

@@ -9,7 +9,7 @@
 // (theta_b the rotation angle between Q_b0 and Q_b, rsw_b the largest vertex
 // distance from the centre).  Two sub-elements can only have come closer by
 // delta_i + delta_j, so while max_b delta_b < dVerlet / 2 every sub-contact
-// that was not NEAR at the rebuild is still separated, and a rebuild is
+// that was not NEAR at the rebuild is still separated, and a refresh is
 // forced as soon as the bound reaches dVerlet / 2.
 //
 // The MLP runs in FP16 storage with FP32 accumulation, trained by one CTA
@@ -22,19 +22,38 @@
 namespace rk {
 
 // ---------------------------------------------------------------- guard ----
-__global__ void k_skin_snapshot(Scene s, double* ref_pos, double* ref_q) {
+// Partial refresh: when only a few bodies have used up their budget, only
+// their pairs are refreshed (the neighbour-list rebuild restricted to pairs
+// with at least one flagged body) and only their snapshots are reset.  A
+// pair (i, j) is then last tested at T_ij = the later of the two bodies'
+// last refreshes, and the motion of i since T_ij is no longer bounded by
+// delta_i (measured from i's own refresh, possibly earlier).  Two monotone
+// bounds still hold for any T_ij after i's refresh:
+//   path_i   = the accumulated per-step motion (drift kernel), and
+//   2 maxd_i = twice the largest delta_i seen since i's refresh
+// (|x(now) - x(T)| <= delta(now) + delta(T)).  So once a partial refresh has
+// happened, g_b = min(path_b, 2 maxd_b) < dVerlet / 2 for every body keeps
+// every missed sub-contact separated; before it, max delta_b suffices.
+__global__ void k_skin_reset(Scene s, const uint8_t* only, double* ref_pos, double* ref_q, float* maxd, float* path) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
+  if (only && !only[b]) return;
   for (int d = 0; d < 3; d++) ref_pos[3 * b + d] = s.pos[3 * b + d];
   for (int d = 0; d < 4; d++) ref_q[4 * b + d] = s.Q[4 * b + d];
+  maxd[b] = 0.f;
+  path[b] = 0.f;
 }
 
-// out[0]: max delta (float bits, atomicMax); out[1]: max |v| (float bits)
-__global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q, const float* rsw,
-                             unsigned int* out) {
+// Guard of every body after a step.  out (zeroed before): [0] max delta,
+// [1] max |v| of the free bodies, [2] max g (float bits, atomicMax),
+// [3] number of flagged bodies (g >= flag_at), [4..5] sum of delta (double).
+__global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q, const float* rsw, float* maxd,
+                             const float* path, float flag_at, uint8_t* flag, unsigned int* out) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  float dmax = 0.f, vmax = 0.f;
-  if (b >= s.n_driven && b < s.n) {
+  float dmax = 0.f, vmax = 0.f, gmax = 0.f;
+  double dsum = 0.0;
+  unsigned nflag = 0;
+  if (b < s.n) {
     double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
            dz = s.pos[3 * b + 2] - ref_pos[3 * b + 2];
     // rotation angle between ref_q and Q: 2 acos(|<q0, q>|)
@@ -44,26 +63,44 @@ __global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q
     double ang = 2.0 * acos(c);
     double delta = sqrt(dx * dx + dy * dy + dz * dz) + ang * (double)rsw[b];
     dmax = (float)(delta * (1.0 + 1e-6)) + 1e-12f;
-    double vx = s.vel[3 * b], vy = s.vel[3 * b + 1], vz = s.vel[3 * b + 2];
-    vmax = (float)sqrt(vx * vx + vy * vy + vz * vz);
+    dsum = delta;
+    const float md = fmaxf(maxd[b], dmax);
+    maxd[b] = md;
+    // driven bodies are moved by their controls, not by the drift: no path
+    const float pth = b >= s.n_driven ? path[b] : INFINITY;
+    gmax = fminf(pth, 2.f * md);
+    const bool f = gmax >= flag_at;
+    flag[b] = f ? 1 : 0;
+    nflag = f ? 1u : 0u;
+    if (b >= s.n_driven) {
+      double vx = s.vel[3 * b], vy = s.vel[3 * b + 1], vz = s.vel[3 * b + 2];
+      vmax = (float)sqrt(vx * vx + vy * vy + vz * vz);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    gmax = fmaxf(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+    dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+    nflag += __shfl_xor_sync(0xffffffffu, nflag, o);
   }
   if ((threadIdx.x & 31) == 0) {
     atomicMax(&out[0], __float_as_uint(dmax));
     atomicMax(&out[1], __float_as_uint(vmax));
+    atomicMax(&out[2], __float_as_uint(gmax));
+    if (nflag) atomicAdd(&out[3], nflag);
+    atomicAdd(reinterpret_cast<double*>(out + 4), dsum);
   }
 }
 
-int launch_skin_snapshot(const Scene& s, double* rp, double* rq, cudaStream_t st) {
-  k_skin_snapshot<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, rp, rq);
+int launch_skin_reset(const Scene& s, const uint8_t* only, double* rp, double* rq, float* maxd, float* path,
+                      cudaStream_t st) {
+  k_skin_reset<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, only, rp, rq, maxd, path);
   return 1;
 }
-int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, unsigned int* out,
-                      cudaStream_t st) {
-  k_skin_guard<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, rp, rq, rsw, out);
+int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, float* maxd,
+                      const float* path, float flag_at, uint8_t* flag, unsigned int* out, cudaStream_t st) {
+  k_skin_guard<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, rp, rq, rsw, maxd, path, flag_at, flag, out);
   return 1;
 }
 

@@ -115,12 +115,23 @@ __global__ void k_drift(Scene s) {
   V3 p = ld3(s.pos, i), v = ld3(s.vel, i), a = ld3(s.acc, i);
   V3 w = ld3(s.vrot, i), al = ld3(s.arot, i);
   Q4 q = ldq(s.Q, i);
-  p = p + (s.dt * v + s.dt2_2 * a);
+  const Q4 q0 = q;
+  const V3 dx = s.dt * v + s.dt2_2 * a;
+  p = p + dx;
   v = v + s.dt_2 * a;
   qaddscaled(q, qdot(q, w), s.dt);
   qaddscaled(q, qddot(q, w, al), s.dt2_2);
   qnormalize(q);
   w = w + s.dt_2 * al;
+  if (s.sk_path) {
+    // learned-skin path bound: |dx| plus the rotation angle of the step
+    // (at most 2c(1 + c) for the chord c = |q - q0| of unit quaternions)
+    // times the swing radius, rounded up
+    const double cx = q.s - q0.s, cy = q.v.x - q0.v.x, cz = q.v.y - q0.v.y, cw = q.v.z - q0.v.z;
+    const double c = sqrt(cx * cx + cy * cy + cz * cz + cw * cw);
+    const double inc = sqrt(dx.x * dx.x + dx.y * dx.y + dx.z * dx.z) + 2.0 * c * (1.0 + c) * (double)s.sk_rsw[i];
+    s.sk_path[i] += (float)(inc * (1.0 + 1e-5)) + 1e-12f;
+  }
   st3(s.pos, i, p);
   st3(s.vel, i, v);
   stq(s.Q, i, q);
@@ -520,19 +531,41 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
     init_resultant(s, b, F, M);
     // Resultants in the serial order of the active entries (key order): the
     // j-side entries before b's own block, b's block, the remaining j-side.
+    // Four positions of that sequence are loaded together, then added in
+    // order (same sums, a quarter of the dependent load chains).
     const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
-    int64_t jk = s.jofs[b];
-    const int64_t j1 = s.jofs[b + 1];
-    for (; jk < j1; ++jk) {
-      const int e = s.jlist[jk];
-      if (e >= i0) break;
-      if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
-    }
-    for (int64_t e = i0; e < i1; ++e)
-      if (s.act[e]) { F = F + ld3(s.cf, e); M = M + ld3(s.cmi, e); }
-    for (; jk < j1; ++jk) {
-      const int e = s.jlist[jk];
-      if (s.act[e]) { F = F - ld3(s.cf, e); M = M + ld3(s.cmj, e); }
+    const int64_t j0 = s.jofs[b], j1 = s.jofs[b + 1], js = s.jsplit[b];
+    const int64_t nA = js - j0, nAB = nA + (i1 - i0), L = nAB + (j1 - js);
+    for (int64_t p0 = 0; p0 < L; p0 += 4) {
+      int64_t e[4];
+      bool jside[4], on[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int64_t p = p0 + u;
+        on[u] = p < L;
+        jside[u] = p < nA || p >= nAB;
+        e[u] = !on[u] ? 0 : (p < nA ? (int64_t)s.jlist[j0 + p] : (p < nAB ? i0 + (p - nA) : (int64_t)s.jlist[js + (p - nAB)]));
+      }
+      bool a[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) a[u] = on[u] && s.act[e[u]];
+      V3 f[4], m[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (a[u]) {
+          f[u] = ld3(s.cf, e[u]);
+          m[u] = jside[u] ? ld3(s.cmj, e[u]) : ld3(s.cmi, e[u]);
+        } else {
+          f[u] = v3(0, 0, 0);
+          m[u] = v3(0, 0, 0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (!a[u]) continue;
+        F = jside[u] ? F - f[u] : F + f[u];
+        M = M + m[u];
+      }
     }
   }
   const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
@@ -732,26 +765,43 @@ int launch_controls_pre(const Scene& s, cudaStream_t st) {
   k_controls_pre<<<1, 32, 0, st>>>(s);
   return 1;
 }
+static inline int tpb_or(const Scene& s, int k, int d) { return s.tpb[k] > 0 ? s.tpb[k] : d; }
+
 int launch_drift(const Scene& s, cudaStream_t st) {
   int64_t nf = s.n - s.n_driven;
   if (nf <= 0) return 0;
-  k_drift<<<nblk(nf, 128), 128, 0, st>>>(s);
+  const int t = tpb_or(s, 3, 128);
+  k_drift<<<nblk(nf, t), t, 0, st>>>(s);
   return 1;
 }
 int launch_glob_vertices(const Scene& s, cudaStream_t st) {
   if (s.nvert <= 0) return 0;
-  k_glob_vertices<<<nblk(s.nvert, 256), 256, 0, st>>>(s);
+  const int t = tpb_or(s, 2, 256);
+  k_glob_vertices<<<nblk(s.nvert, t), t, 0, st>>>(s);
   return 1;
 }
 int launch_narrow_force(const Scene& s, cudaStream_t st) {
   if (s.ne <= 0) return 0;
-  k_narrow_force<<<nblk(s.ne, 128), 128, 0, st>>>(s);
+  const int t = tpb_or(s, 0, 128);
+  k_narrow_force<<<nblk(s.ne, t), t, 0, st>>>(s);
   return 1;
 }
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
   if (s.n <= 0) return 0;
-  k_gather_accel<<<nblk(s.n, 128), 128, 0, st>>>(s, apply_kick);
+  const int t = tpb_or(s, 1, 128);
+  k_gather_accel<<<nblk(s.n, t), t, 0, st>>>(s, apply_kick);
   return 1;
+}
+
+// Largest block each tuned kernel can be launched with (register limit).
+int max_tpb(int which, int form_mixed) {
+  cudaFuncAttributes a{};
+  cudaError_t e = cudaSuccess;
+  if (which == 0) e = form_mixed ? narrow_mixed_attributes(&a) : cudaFuncGetAttributes(&a, k_narrow_force);
+  else if (which == 1) e = cudaFuncGetAttributes(&a, k_gather_accel);
+  else if (which == 2) e = cudaFuncGetAttributes(&a, k_glob_vertices);
+  else e = cudaFuncGetAttributes(&a, k_drift);
+  return e == cudaSuccess ? a.maxThreadsPerBlock : 128;
 }
 int launch_gather_heavy(const Scene& s, cudaStream_t st) {
   if (s.nheavy <= 0) return 0;

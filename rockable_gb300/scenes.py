@@ -376,13 +376,15 @@ def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, 
 
 
 def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=0, report=None, law="Avalanche",
-           rebuild_every=10):
+           rebuild_every=10, relax_steps=0):
     """Compact a freshly deposited pile on the GPU: contacts of the given law
     (Avalanche by default) at a soft stiffness, boosted gravity and numerical
     damping, large time step.
     Returns the GpuScene, switched afterwards to the scene's own parameters
     (the Avalanche law's incremental normal force carries the settled contact
-    forces across the change of stiffness)."""
+    forces across the change of stiffness).  With relax_steps, the pile then
+    relaxes under plain gravity with the same soft contacts, which shrinks the
+    overlaps before a law without force history (Default) takes over."""
     from .abi import GpuScene, RK_LAW
     g = GpuScene(device=device)
     g.upload_shapes(scene["shape_tables"])
@@ -403,6 +405,13 @@ def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=
         if report is not None:
             st = g.stats()
             report.append((done, st["n_entries"], st["n_active"], st["e_trans"]))
+    if relax_steps > 0:
+        g.set_params(t=done * dt, dt=dt, gravity=tuple(scene["gravity"]), DVerlet=scene["DVerlet"],
+                     dVerlet=scene["dVerlet"], interVerlet=rebuild_every * dt, interVerletC=0.0, law=RK_LAW[law],
+                     ngroup=scene["ngroup"], table=law_table(kn=kn, kt=kn, en2=p["en2"], mu=p["mu"]),
+                     numerical_damping=damping)
+        g.step(relax_steps)
+        done += relax_steps
     set_scene_params(g, scene, t=done * dt)
     return g
 

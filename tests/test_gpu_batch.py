@@ -51,7 +51,7 @@ def test_graph_replay_is_bitwise_identical(form, gpu_lib):
 def test_batched_scenes_match_each_scene_alone(gpu_lib):
     from rockable_gb300 import scenes
     bt = scenes.slope_batch(nscenes=4, nmin=300, nmax=1500, nshapes=32)
-    gs = scenes.settle(bt, steps=2000, dt=5e-6, kn=bt["params"]["kn"], gboost=20.0, damping=0.5, law="Default")
+    gs = scenes.settle(bt, steps=2000, relax_steps=600)
     bt = scenes.scene_from_gpu(bt, gs)
     gs.close()
     whole = _engine(bt, graphs=True)
@@ -71,3 +71,24 @@ def test_batched_scenes_match_each_scene_alone(gpu_lib):
         total_entries += g.stats()["n_entries"]
         g.close()
     assert total_entries == st["n_entries"]
+
+
+def test_autotuned_block_sizes_change_no_result(gpu_lib):
+    from rockable_gb300 import scenes
+    scene = scenes.column_collapse(n=3000, nshapes=64)
+    gs = scenes.settle(scene, steps=800)
+    src = scenes.scene_from_gpu(scene, gs)
+    gs.close()
+    for form in [0, 1]:
+        a = _engine(src, form, src["entries"])
+        b = _engine(src, form, src["entries"], graphs=True)
+        b.autotune(2)
+        a.step(230)
+        b.step(230)
+        tpb = b.block_sizes()
+        assert all(v in (64, 128, 256, 512) for v in tpb.values()), tpb
+        ba, bb = a.bodies(), b.bodies()
+        for k in ["pos", "vel", "Q", "vrot", "force", "moment"]:
+            assert bitwise_equal(ba[k], bb[k]), (form, k)
+        a.close()
+        b.close()

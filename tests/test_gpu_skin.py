@@ -99,3 +99,51 @@ def test_learned_skin_against_the_method_without_it(gpu_lib):
     for name in ["naive", "mlp"]:
         assert res[name]["nl_updates"] >= 1
         assert abs(res[name]["active"] - res["plain"]["active"]) <= 0.05 * res["plain"]["active"] + 5
+
+
+def _keys(e):
+    return set(zip(e["i"].tolist(), e["j"].tolist(), e["type"].tolist(), e["isub"].tolist(), e["jsub"].tolist()))
+
+
+@pytest.mark.parametrize("partial_fraction", [0.0, 0.2])
+def test_every_touching_subcontact_is_in_the_skin_list(partial_fraction, gpu_lib):
+    """Exactness of the guard, with and without partial refreshes: from the
+    skin engine's own state after each chunk of steps, a fresh list built
+    with a vanishing skin (the sub-contacts that touch or overlap now) must be
+    contained in the skin engine's list."""
+    import copy
+    from rockable_gb300 import scenes
+    scene = scenes.column_collapse(n=2000, nshapes=64)
+    gs = scenes.settle(scene, steps=1500)
+    src = scenes.scene_from_gpu(scene, gs)
+    gs.close()
+    gl = _engine(src)
+    gl.upload_entries(src["entries"])
+    gl.set_skin(use_mlp=False, skin_min=0.05 * scene["dVerlet"], skin_max=2.0 * scene["dVerlet"], interval_min=1,
+                interval_max=400, partial_fraction=partial_fraction)
+    tight = copy.deepcopy(scene)
+    tight["dVerlet"] = 1e-12
+    tight["DVerlet"] = 2e-12
+    touching_seen = 0
+    for _ in range(8):
+        gl.step(25)
+        now = dict(src)
+        b = dict(src["bodies"])
+        st = gl.bodies()
+        for k in ["pos", "vel", "acc", "Q", "vrot", "arot"]:
+            b[k] = st[k]
+        now["bodies"] = b
+        gt = _engine(now)
+        scenes.set_scene_params(gt, tight)
+        gt.update_nl()
+        touching = _keys(gt.entries())
+        gt.close()
+        listed = _keys(gl.entries())
+        missing = touching - listed
+        assert not missing, (len(missing), sorted(missing)[:5])
+        touching_seen += len(touching)
+    assert touching_seen > 0
+    sk = gl.skin_stats()
+    print("skin stats (partial_fraction=%g):" % partial_fraction, sk)
+    if partial_fraction > 0:
+        assert sk["partial"] >= 1
