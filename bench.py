@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle-steps", type=int, default=4000)
-    ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin",
+    ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact,mixed_learned_skin",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched slope workload (0: skip it)")
@@ -381,15 +381,16 @@ def main():
 
     forms = {}
     dmin = scene["dVerlet"]
-    known = {"plain_fp64": (RK_FORM_FP64, False), "mixed": (RK_FORM_MIXED, False),
-             "mixed_learned_skin": (RK_FORM_MIXED, True)}
+    # skin: None (fixed interVerlet), "ref" (learned skin, Rockable's NEAR tests), "exact" (distance-only)
+    known = {"plain_fp64": (RK_FORM_FP64, None), "mixed": (RK_FORM_MIXED, None),
+             "mixed_learned_skin": (RK_FORM_MIXED, "ref"), "mixed_learned_skin_exact": (RK_FORM_MIXED, "exact")}
     order = [f.strip() for f in a.forms.split(",") if f.strip()]
     for label in order:
         form, skin = known[label]
         e = engine(form)
         if skin:
             e.set_skin(use_mlp=True, skin_min=0.1 * dmin, skin_max=4.0 * dmin, dverlet_ratio=2.0, interval_min=2,
-                       interval_max=1000, seed=3)
+                       interval_max=1000, seed=3, exact_contacts=(skin == "exact"))
         else:
             e.update_nl()
         e.autotune(2)

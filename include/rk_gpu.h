@@ -295,6 +295,10 @@ typedef struct rk_skin_config {
   double partial_fraction;  /* a forced update refreshes only the bodies near their guard
                                limit when they are at most this fraction of all bodies
                                (0: every update is a full rebuild) */
+  int32_t exact_contacts;   /* 1: distance-only NEAR tests, so every sub-contact that touches
+                               is listed (more entries); 0: Rockable's NEAR tests, whose
+                               projection conditions can list a sliding vertex-face or
+                               edge-edge contact one refresh late, like the fixed schedule */
 } rk_skin_config;
 typedef struct rk_skin_stats {
   int64_t rebuilds, forced, scheduled;

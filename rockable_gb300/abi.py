@@ -70,7 +70,7 @@ class RkSkinConfig(C.Structure):
     _fields_ = [("enabled", C.c_int32), ("use_mlp", C.c_int32), ("skin_min", C.c_double), ("skin_max", C.c_double),
                 ("dverlet_ratio", C.c_double), ("interval_min", C.c_int32), ("interval_max", C.c_int32),
                 ("learning_rate", C.c_double), ("train_steps", C.c_int32), ("seed", C.c_uint64),
-                ("partial_fraction", C.c_double)]
+                ("partial_fraction", C.c_double), ("exact_contacts", C.c_int32)]
 
 
 class RkSkinStats(C.Structure):
@@ -310,9 +310,10 @@ class GpuScene:
         self._chk(self.L.rk_set_profiling(self.h, 1 if on else 0), "rk_set_profiling")
 
     def set_skin(self, enabled=True, use_mlp=True, skin_min=1e-5, skin_max=1e-3, dverlet_ratio=2.0,
-                 interval_min=5, interval_max=1000, learning_rate=3e-3, train_steps=2, seed=1, partial_fraction=0.2):
+                 interval_min=5, interval_max=1000, learning_rate=3e-3, train_steps=2, seed=1, partial_fraction=0.2,
+                 exact_contacts=True):
         cfg = RkSkinConfig(1 if enabled else 0, 1 if use_mlp else 0, skin_min, skin_max, dverlet_ratio, interval_min,
-                           interval_max, learning_rate, train_steps, seed, partial_fraction)
+                           interval_max, learning_rate, train_steps, seed, partial_fraction, 1 if exact_contacts else 0)
         self._chk(self.L.rk_set_skin(self.h, C.byref(cfg)), "rk_set_skin")
 
     def skin_stats(self):

@@ -94,7 +94,7 @@ int ensure_entry_capacity(Ctx& c, int which, int64_t n) {
     int64_t cap = std::max<int64_t>(n + n / 2, 1024);
     Scene& s = c.s;
     if ((rc = dalloc(c, s.act, cap)) || (rc = dalloc(c, s.cf, 3 * cap)) || (rc = dalloc(c, s.cmi, 3 * cap)) ||
-        (rc = dalloc(c, s.cmj, 3 * cap)) || (rc = dalloc(c, s.jlist, cap)))
+        (rc = dalloc(c, s.cmj, 3 * cap)) || (rc = dalloc(c, s.jlist, cap)) || (rc = dalloc(c, s.nperm, cap)))
       return rc;
     c.contrib_cap = cap;
   }
@@ -609,7 +609,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.shape); dfree(s.group); dfree(s.cluster);
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.gv); dfree(s.bobb); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
-  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist);
+  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.heavy_lazy); dfree(s.bnd);
   dfree(s.needres); dfree(s.scene_of);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
@@ -1073,7 +1073,7 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   k.on = true;
   s.sk_path = k.path;
   s.sk_rsw = k.rsw;
-  s.near_geometric = 1;
+  s.near_geometric = cfg->exact_contacts ? 1 : 0;
   // start from a fresh list built with the initial skin
   launch_glob_vertices(s, c.stream);
   if ((rc = rebuild_nl(c))) return rc;

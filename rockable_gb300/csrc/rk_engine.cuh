@@ -107,6 +107,7 @@ struct Scene {
   int64_t* jofs;  // n+1
   int64_t* jsplit;  // n: first j-side slot of body b whose entry follows b's own block
   int* jlist;     // ne
+  int* nperm;     // ne: entries grouped by sub-contact type (the narrow phase's thread order)
   int* heavy;     // bodies whose entry count exceeds kHeavy (summed by a block each)
   int nheavy;
   int* heavy_lazy;    // heavy driven bodies whose resultant feeds no state (summed on demand)

@@ -56,9 +56,12 @@ __device__ __forceinline__ double len64(V3 d, double& inv) {
 }
 
 __global__ void k_narrow_force_mixed(Scene s) {
-  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // threads follow the entries grouped by sub-contact type (fewer divergent
+  // branches per warp); every entry is computed on its own
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool active = false;
-  if (e < s.ne) {
+  if (k < s.ne) {
+    const int64_t e = s.nperm[k];
     const int i = s.ei[e], j = s.ej[e];
     const uint32_t ts = s.etsub[e];
     const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);

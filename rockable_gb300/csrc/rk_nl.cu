@@ -307,22 +307,24 @@ __global__ void k_grid_pairs(Scene s, const uint8_t* only, const uint64_t* keys,
   const uint64_t amask = (1u << f.bits) - 1u;
   const uint64_t scene = f.batched ? (code >> 33) : 0u;
   const int cx = (int)((code >> (2 * f.bits)) & amask), cy = (int)((code >> f.bits) & amask), cz = (int)(code & amask);
+  // z is the lowest field of the cell code: the three cells (x, y, z-1..z+1)
+  // of a neighbour column are one contiguous key range
+  const int z0 = max(cz - 1, 0), z1 = min(cz + 1, f.max);
   for (int dx = -1; dx <= 1; dx++)
-    for (int dy = -1; dy <= 1; dy++)
-      for (int dz = -1; dz <= 1; dz++) {
-        const int x = cx + dx, y = cy + dy, z = cz + dz;
-        if (x < 0 || y < 0 || z < 0 || x > f.max || y > f.max || z > f.max) continue;
-        const uint64_t c2 = cell_code(scene, x, y, z, f);
-        int64_t q = lower_bound_u64(keys, nnorm, c2 << 21);
-        for (; q < nnorm && (keys[q] >> 21) == c2; q++) {
-          const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
-          if (only ? (j == i || (only[j] && j < i)) : (j <= i)) continue;
-          const int64_t lo = min(i, j), hi = max(i, j);
-          if (!pair_predicate(s, lo, hi)) continue;
-          unsigned long long at = atomicAdd(counter, 1ull);
-          if ((int64_t)at < cap) pairs[at] = ((uint64_t)lo << 21) | (uint64_t)hi;
-        }
+    for (int dy = -1; dy <= 1; dy++) {
+      const int x = cx + dx, y = cy + dy;
+      if (x < 0 || y < 0 || x > f.max || y > f.max) continue;
+      const uint64_t first = cell_code(scene, x, y, z0, f) << 21;
+      const uint64_t last = cell_code(scene, x, y, z1, f);
+      for (int64_t q = lower_bound_u64(keys, nnorm, first); q < nnorm && (keys[q] >> 21) <= last; q++) {
+        const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
+        if (only ? (j == i || (only[j] && j < i)) : (j <= i)) continue;
+        const int64_t lo = min(i, j), hi = max(i, j);
+        if (!pair_predicate(s, lo, hi)) continue;
+        unsigned long long at = atomicAdd(counter, 1ull);
+        if ((int64_t)at < cap) pairs[at] = ((uint64_t)lo << 21) | (uint64_t)hi;
       }
+    }
 }
 
 // oversized body o against every body j of its scene (each pair once)
@@ -1117,8 +1119,41 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   return heavy_list(c);
 }
 
+__global__ void k_type_keys(const uint32_t* etsub, int64_t ne, uint64_t* keys) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  keys[e] = ((uint64_t)tsub_type(etsub[e]) << 40) | (uint64_t)e;
+}
+__global__ void k_type_perm(const uint64_t* keys, int64_t ne, int* perm) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= ne) return;
+  perm[k] = (int)(keys[k] & ((1ull << 40) - 1));
+}
+
+// Order in which the narrow phase visits the entries: by sub-contact type,
+// entry order within a type (after the index build; uses its scratch).
+static int entry_order(Ctx& c) {
+  Scene& s = c.s;
+  NLWork& w = c.w;
+  const int64_t ne = s.ne;
+  if (ne <= 0) return 0;
+  if (w.fin_cap < ne || w.tmp_bytes < (int64_t)sort_temp_bytes(ne)) {
+    c.err = "entry order: scratch smaller than the neighbour list";
+    return RK_ERR_STATE;
+  }
+  k_type_keys<<<nblk(ne, 256), 256, 0, c.stream>>>(s.etsub, ne, w.jkeys);
+  radix_sort_u64(w.jkeys, w.jtmp, ne, 40, 42, w.tmp, c.stream);
+  k_type_perm<<<nblk(ne, 256), 256, 0, c.stream>>>(w.jkeys, ne, s.nperm);
+  c.kernels += 5;
+  return 0;
+}
+
 int heavy_list(Ctx& c) {
   Scene& s = c.s;
+  {
+    const int rc = entry_order(c);
+    if (rc) return rc;
+  }
   RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 16, c.stream));
   k_heavy<<<nblk(s.n, 256), 256, 0, c.stream>>>(s, c.w.counter + 1);
   c.kernels++;

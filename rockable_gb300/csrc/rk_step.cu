@@ -271,9 +271,12 @@ __device__ __forceinline__ void law_sticked(const Scene& s, const LawIn& L, doub
 __device__ __forceinline__ V3 gvx(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
 
 __global__ void k_narrow_force(Scene s) {
-  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // threads follow the entries grouped by sub-contact type (fewer divergent
+  // branches per warp); every entry is computed on its own
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool active = false;
-  if (e < s.ne) {
+  if (k < s.ne) {
+    const int64_t e = s.nperm[k];
     const int i = s.ei[e], j = s.ej[e];
     const uint32_t ts = s.etsub[e];
     const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);
