@@ -35,6 +35,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
 TUNE_STEPS = 8  # untimed block-size tuning steps before the warm-up (rk_set_autotune, 2 rounds)
+NCU_NARROW_MIXED_BYTES_PER_ENTRY = 22.877e6 / 183166  # ncu, 50k-grain column, mixed form (124.9 B)
 
 
 def parse():
@@ -416,6 +417,10 @@ def main():
     C = head["entries"]
     hbm, src_peak = peaks()
     achieved = 140.0 * C / (t_narrow / 1000.0) / 1e9 if t_narrow > 0 else None
+    # DRAM bytes per entry of k_narrow_force_mixed, from one ncu capture of the
+    # 50k-grain column (dram__bytes_read.sum + dram__bytes_write.sum per launch /
+    # entries); the same kernel serves the mixed and learned-skin forms
+    traffic = NCU_NARROW_MIXED_BYTES_PER_ENTRY * C
     st = {"n_entries": C, "n_active": head["active"]}
     # ---- e2e through the C ABI with host-owned state (headline form)
     e2e = None
@@ -430,13 +435,12 @@ def main():
         for _ in range(k_e2e):
             g.upload_kinematics(hb["pos"], hb["vel"], hb["acc"], hb["Q"], hb["vrot"], hb["arot"])
             g.step(1)
-            out_b = g.bodies()
-            for k in hb:
-                hb[k][...] = out_b[k]
+            g.bodies(out=hb)
         el = time.perf_counter() - t0
         e2e = {"value": ws * nfree * k_e2e / el, "unit": "particle-steps/s",
-               "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 25 * 8),
-               "steps": k_e2e, "note": "every step: kinematics H2D from pinned host, rk_step, full body state D2H"}
+               "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8),
+               "steps": k_e2e, "note": "every step: kinematics (pos, vel, acc, Q, vrot, arot) H2D from pinned host, "
+                                       "rk_step(1), the same fields D2H into the pinned buffers"}
     batched = None
     if rank == 0 and a.batch_scenes > 0:
         batched = batched_workload(a, dev)
@@ -466,7 +470,10 @@ def main():
                           "setup_before_warmup": "%d untimed block-size tuning steps; step graphs on" % TUNE_STEPS},
                "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
                "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
-                            "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                            "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                            "traffic_note": "bytes per launch: ncu DRAM bytes per entry of this kernel (column, "
+                                            "mixed form) x this form's entries",
+                            "limiter": "FP64 pipe (ncu: 73% busy in the narrow phase, 81% in the global vertices)",
                             "peak_source": src_peak, "bytes_per_entry": 140, "entries": int(C),
                             "ms_per_launch": t_narrow},
                "setup": {"settle_s": t_settle, "settle_log": settle_log},

@@ -364,13 +364,20 @@ class GpuScene:
     def n_entries(self):
         return self.L.rk_num_entries(self.h)
 
-    def bodies(self):
+    def bodies(self, out=None):
+        """Body state as float64 arrays; with `out` (a dict of C-contiguous
+        float64 arrays, e.g. pinned buffers), only the fields it holds are
+        downloaded, into those arrays."""
         n = self.n
-        out = {k: np.zeros((n, 3)) for k in ["pos", "vel", "acc", "vrot", "arot", "force", "moment"]}
-        out["Q"] = np.zeros((n, 4))
-        self._chk(self.L.rk_download_bodies(self.h, *[_p(out[k]) for k in ["pos", "vel", "acc", "Q", "vrot", "arot",
-                                                                           "force", "moment"]]),
-                  "rk_download_bodies")
+        names = ["pos", "vel", "acc", "Q", "vrot", "arot", "force", "moment"]
+        if out is None:
+            out = {k: np.zeros((n, 4 if k == "Q" else 3)) for k in names}
+        for k, v in out.items():
+            if k not in names or v.dtype != np.float64 or not v.flags["C_CONTIGUOUS"] or v.size != n * (
+                    4 if k == "Q" else 3):
+                raise ValueError("bodies(out=...): %s must be a C-contiguous float64 array of %d x %d" % (
+                    k, n, 4 if k == "Q" else 3))
+        self._chk(self.L.rk_download_bodies(self.h, *[_p(out.get(k)) for k in names]), "rk_download_bodies")
         return out
 
     def entries(self, geometry=False):

@@ -214,6 +214,14 @@ static void settle_lazy_forces(Ctx& c) {
   }
 }
 
+// Before a neighbour-list update inside rk_step: the deferred resultants
+// must be summed from the current list only when no step of this call
+// follows (a step recomputes every contribution of the new list, and the
+// resultants it leaves are the ones a download must see).
+static void settle_before_update(Ctx& c) {
+  if (!c.more_steps_follow) settle_lazy_forces(c);
+}
+
 // ------------------------------------------------------------ learned skin ----
 static double to_f(unsigned int bits) {
   float f;
@@ -245,30 +253,6 @@ static int skin_train(Ctx& c) {
   return 0;
 }
 
-// time = fixed + per_entry * size, by least squares over the samples when
-// their sizes differ by more than 5 %, else half fixed / half proportional
-static void fit_cost(const std::vector<std::array<double, 2>>& smp, double& fixed, double& per) {
-  const size_t n = smp.size();
-  if (n == 0) { fixed = per = 0.0; return; }
-  double sx = 0, sy = 0, lo = smp[0][0], hi = smp[0][0];
-  for (auto& q : smp) { sx += q[0]; sy += q[1]; lo = std::min(lo, q[0]); hi = std::max(hi, q[0]); }
-  const double mx = sx / n, my = sy / n;
-  if (n >= 3 && hi > 1.05 * lo) {
-    double sxx = 0, sxy = 0;
-    for (auto& q : smp) { sxx += (q[0] - mx) * (q[0] - mx); sxy += (q[0] - mx) * (q[1] - my); }
-    per = std::max(0.0, sxy / sxx);
-    fixed = std::max(0.0, my - per * mx);
-    if (fixed == 0.0) per = my / std::max(mx, 1.0);
-  } else {
-    fixed = 0.5 * my;
-    per = 0.5 * my / std::max(mx, 1.0);
-  }
-}
-static void push_sample(std::vector<std::array<double, 2>>& v, double size, double ms) {
-  if (v.size() >= 16) v.erase(v.begin());
-  v.push_back({size, ms});
-}
-
 static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   Skin& k = c.skin;
   Scene& s = c.s;
@@ -276,10 +260,25 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   const double ref = k.cfg.skin_max;
   // displacement rate that sets the next full rebuild: the largest body's
   // without partial refreshes; with them (the fastest bodies are refreshed on
-  // their own), twice the mean over all bodies
+  // their own), the 80th percentile of the bodies' guard values
   const double rate_max = dmax / (double)std::max<int64_t>(1, k.since);
-  const double rate_bulk = 2.0 * k.dsum / (N * (double)std::max<int64_t>(1, k.since));
-  const double rate = k.cfg.partial_fraction > 0.0 ? std::max(rate_bulk, 1e-30) : rate_max;
+  double rate = rate_max;
+  if (k.cfg.partial_fraction > 0.0) {
+    unsigned int h[64];
+    CK(cudaMemsetAsync(k.d_hist, 0, sizeof h, c.stream));
+    c.kernels += launch_skin_hist(s, k.ref_pos, k.ref_q, k.rsw, (float)k.skin, k.d_hist, c.stream);
+    CK(cudaMemcpyAsync(h, k.d_hist, sizeof h, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    const double want = 0.8 * (double)s.n;
+    double acc = 0.0;
+    int bin = 63;
+    for (int q = 0; q < 64; q++) {
+      acc += h[q];
+      if (acc >= want) { bin = q; break; }
+    }
+    const double d80 = k.skin * std::pow(2.0, (bin + 1) / 4.0 - 14.0);  // upper edge of the bin
+    rate = std::max(d80 / (double)std::max<int64_t>(1, k.since), 1e-30);
+  }
   const int64_t ne0 = s.ne;
   const double active = (double)c.h_flags[FLAG_NACTIVE];
   if (k.since > 0) {  // measured cost of the window
@@ -289,7 +288,6 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
     CK(cudaEventElapsedTime(&ms, k.ea, k.eb));
     double per = ms / (double)k.since;
     k.step_ms = k.step_ms > 0 ? 0.7 * k.step_ms + 0.3 * per : per;
-    push_sample(k.step_samples, (double)s.ne, per);
   }
   k.last_rate = rate;
   for (int q = 3; q > 0; q--) k.rates[q] = k.rates[q - 1];
@@ -329,43 +327,47 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   // skin and interval minimising the predicted cost per step.  Entries grow
   // faster than the skin (more sub-element pairs come within reach): the
   // non-active entries are scaled by (skin ratio)^1.6, the power measured on
-  // the hull-grain piles.  Step and full-rebuild times are the measured
-  // fixed + per-entry costs (least squares over recent windows).  The
-  // interval is the number of steps the predicted displacement rate takes to
-  // use half the skin (with a margin), which is also when the exact guard
-  // would force the rebuild.
+  // the hull-grain piles.  The step time is measured over the last window
+  // (40 % of it, the narrow phase, scales with the list); the last full
+  // rebuild is timed in two parts, the broad phase (70 % fixed) and the
+  // candidates-to-index part (proportional to the list).  The interval is
+  // the number of steps the predicted displacement rate takes to use half
+  // the skin (with a margin), which is also when the guard would force it.
   const double margin = 1.3, alpha = 1.6;
   const double C = (double)std::max<int64_t>(1, ne0), A = std::min(active, C);
-  double t0, t1, r0, r1;
-  fit_cost(k.step_samples, t0, t1);
-  fit_cost(k.rebuild_samples, r0, r1);
-  if (k.step_samples.empty()) { t0 = 0.05; t1 = 1e-6; }
-  if (k.rebuild_samples.empty()) { r0 = 1.0; r1 = 2e-5; }
+  const double T = k.step_ms > 0 ? k.step_ms : 0.2;
+  const double Rbp = k.rebuild_bp_ms > 0 ? k.rebuild_bp_ms : 2.0;
+  const double Rvar = k.rebuild_var_ms > 0 ? k.rebuild_var_ms : 2.0;
   double best = 1e300, best_s = k.skin;
   int64_t best_k = k.interval;
   for (int m = -4; m <= 4; m++) {
     double sk = std::min(k.cfg.skin_max, std::max(k.cfg.skin_min, k.skin * std::pow(2.0, 0.25 * m)));
     double kk = std::floor(0.5 * sk / std::max(u * margin * (1.0 + churn), 1e-30));
     int64_t ki = (int64_t)std::max<double>(k.cfg.interval_min, std::min<double>(k.cfg.interval_max, kk));
-    double Cs = A + (C - A) * std::pow(sk / std::max(k.skin, 1e-30), alpha);
-    double J = (t0 + t1 * Cs) + (r0 + r1 * Cs) / (double)ki;
+    double ratio = (A + (C - A) * std::pow(sk / std::max(k.skin, 1e-30), alpha)) / C;
+    double J = T * (0.6 + 0.4 * ratio) + (Rbp * (0.7 + 0.3 * ratio) + Rvar * ratio) / (double)ki;
     if (J < best) { best = J; best_s = sk; best_k = ki; }
   }
   k.skin = best_s;
   k.interval = best_k;
   s.dVerlet = k.skin;
   s.DVerlet = k.cfg.dverlet_ratio * k.skin;
-  settle_lazy_forces(c);
+  settle_before_update(c);
   // the rebuild itself, timed
-  float rms = 0.f;
+  float rms = 0.f, rbp = 0.f;
+  if (!c.w.split) CK(cudaEventCreate(&c.w.split));
   CK(cudaEventRecord(k.ea, c.stream));
+  c.w.timing_split = true;
   int rc = rebuild_nl(c);
+  c.w.timing_split = false;
   if (rc) return rc;
   CK(cudaEventRecord(k.eb, c.stream));
   CK(cudaEventSynchronize(k.eb));
   CK(cudaEventElapsedTime(&rms, k.ea, k.eb));
+  CK(cudaEventElapsedTime(&rbp, k.ea, c.w.split));
+  k.rebuild_bp_ms = rbp;
+  k.rebuild_var_ms = std::max(0.0, (double)rms - (double)rbp);
   k.rebuild_ms = k.rebuild_ms > 0 ? 0.7 * k.rebuild_ms + 0.3 * rms : rms;
-  push_sample(k.rebuild_samples, (double)s.ne, rms);
   c.nl_updates++;
   k.rebuilds++;
   if (forced) k.forced++;
@@ -510,7 +512,7 @@ static int step_graph(Ctx& c) {
 static int skin_partial(Ctx& c, int64_t nflag) {
   Skin& k = c.skin;
   Scene& s = c.s;
-  settle_lazy_forces(c);
+  settle_before_update(c);
   int rc = rebuild_nl(c, k.flag);
   if (rc) return rc;
   c.kernels += launch_skin_reset(s, k.flag, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
@@ -610,7 +612,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.gv); dfree(s.bobb); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm);
-  dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.heavy_lazy); dfree(s.bnd);
+  dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
   dfree(s.needres); dfree(s.scene_of);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
   dfree(s.if_break); dfree(s.if_ofs); dfree(s.flags);
@@ -621,11 +623,12 @@ void rk_destroy(rk_ctx* x) {
   dfree(w.flag); dfree(w.stale); dfree(w.stale_src); dfree(w.fkey); dfree(w.fsrc); dfree(w.jkeys); dfree(w.jtmp);
   dfree(w.tmp); dfree(w.counter); dfree(w.gkeys); dfree(w.gtmp); dfree(w.gover); dfree(w.gis_over);
   if (w.gstat) cudaFree(w.gstat);
+  if (w.split) cudaEventDestroy(w.split);
   dfree(c.d_ke);
   {
     Skin& k = c.skin;
     dfree(k.ref_pos); dfree(k.ref_q); dfree(k.rsw); dfree(k.d_guard); dfree(k.master); dfree(k.m); dfree(k.v);
-    dfree(k.maxd); dfree(k.path); dfree(k.flag);
+    dfree(k.maxd); dfree(k.path); dfree(k.flag); dfree(k.d_hist);
     dfree(k.grad); dfree(k.loss); dfree(k.X); dfree(k.T); dfree(k.io);
     if (k.w) cudaFree(k.w);
     if (k.h_guard) cudaFreeHost(k.h_guard);
@@ -710,6 +713,10 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
     int sh = b->shape[i];
     sph_ofs[i + 1] = sph_ofs[i] + c.shape_nv[sh] + c.shape_ne[sh] + c.shape_nf[sh];
   }
+  c.nsph = sph_ofs[n];
+  std::vector<int> sph_body(std::max<int64_t>(sph_ofs[n], 1));
+  for (int64_t i = 0; i < n; i++)
+    for (int64_t k = sph_ofs[i]; k < sph_ofs[i + 1]; k++) sph_body[k] = (int)i;
   std::vector<int> gv_body(nv);
   for (int64_t i = 0; i < n; i++)
     for (int64_t k = gv_ofs[i]; k < gv_ofs[i + 1]; k++) gv_body[k] = (int)i;
@@ -733,6 +740,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.jsplit, (const int64_t*)nullptr, n)) ||
       (rc = dupload(c, s.if_ofs, (const int64_t*)nullptr, n + 1)) ||
       (rc = dupload(c, s.sph_ofs, sph_ofs.data(), n + 1)) || (rc = dalloc(c, s.sph, sph_ofs[n])) ||
+      (rc = dupload(c, s.sph_body, sph_body.data(), std::max<int64_t>(sph_ofs[n], 1))) ||
       (rc = dupload(c, s.is_heavy, (const uint8_t*)nullptr, n)) || (rc = dalloc(c, s.heavy, n)) ||
       (rc = dalloc(c, s.heavy_lazy, n)) || (rc = dalloc(c, s.bnd, n)) || (rc = dalloc(c, s.needres, n)))
     return rc;
@@ -939,7 +947,8 @@ static int skin_alloc(Ctx& c) {
   if (!k.ref_pos) {
     k.nalloc = s.n;
     if ((rc = dalloc(c, k.ref_pos, 3 * s.n)) || (rc = dalloc(c, k.ref_q, 4 * s.n)) || (rc = dalloc(c, k.rsw, s.n)) ||
-        (rc = dalloc(c, k.d_guard, 8)) || (rc = dalloc(c, k.maxd, s.n)) || (rc = dalloc(c, k.path, s.n)) ||
+        (rc = dalloc(c, k.d_guard, 8)) || (rc = dalloc(c, k.d_hist, 64)) || (rc = dalloc(c, k.maxd, s.n)) ||
+        (rc = dalloc(c, k.path, s.n)) ||
         (rc = dalloc(c, k.flag, s.n)) || (rc = dalloc(c, k.master, np)) || (rc = dalloc(c, k.m, np)) ||
         (rc = dalloc(c, k.v, np)) || (rc = dalloc(c, k.grad, np)) || (rc = dalloc(c, k.loss, 1)) ||
         (rc = dalloc(c, k.X, 16 * mlp_max_batch())) || (rc = dalloc(c, k.T, 2 * mlp_max_batch())) ||
@@ -1063,8 +1072,7 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   k.since = 0;
   k.rebuilds = k.forced = k.scheduled = 0;
   k.partial = k.partial_bodies = k.partial_since_global = 0;
-  k.rebuild_samples.clear();
-  k.step_samples.clear();
+  k.rebuild_bp_ms = k.rebuild_var_ms = 0.0;
   k.dsum = 0.0;
   k.step_ms = k.rebuild_ms = 0.0;
   for (double& r : k.rates) r = 0.0;
@@ -1218,6 +1226,7 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
   for (int64_t it = 0; it < nsteps; it++) {
     c.t += s.dt;
     c.interVerletC += s.dt;
+    c.more_steps_follow = it + 1 < nsteps;
     const bool tuning = c.tune_left > 0 && !c.profiling;
     const bool graphed = c.use_graphs && !c.profiling && !tuning;
     if (graphed) {
@@ -1264,7 +1273,7 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
       need = c.h_flags[FLAG_NEED_UPDATE] != 0ull;
     }
     if (need || c.interVerletC >= c.interVerlet - s.dt_2) {
-      settle_lazy_forces(c);
+      settle_before_update(c);
       mark(6, false);
       int64_t k1 = c.kernels;
       if ((rc = rebuild_nl(c))) return rc;
@@ -1278,6 +1287,7 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
     if (s.dynamic_nl) { mark(7, false); phase(7, launch_guard(s, c.stream)); }
     c.steps++;
   }
+  c.more_steps_follow = false;
   CK(cudaEventRecord(c.ev1, c.stream));
   CK(cudaGetLastError());
   CK(cudaEventSynchronize(c.ev1));

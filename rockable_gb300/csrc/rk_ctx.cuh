@@ -23,6 +23,8 @@ struct EntryBuf {
 
 // Scratch of the neighbour-list rebuild, grown on demand.
 struct NLWork {
+  cudaEvent_t split = nullptr;   // recorded after the pairs (when timing_split)
+  bool timing_split = false;
   int64_t pair_cap = 0, hp_cap = 0, cand_cap = 0, old_cap = 0, fin_cap = 0, tmp_bytes = 0;
   uint64_t* pairs = nullptr;     // pair_cap
   uint64_t* hp = nullptr;        // hp_cap (half-pair keys owner<<21 | partner)
@@ -81,9 +83,8 @@ struct Skin {
   double last_rate = 0.0, pred_rate = 0.0, pred_churn = 0.0, last_loss = 0.0;
   int64_t rebuilds = 0, forced = 0, scheduled = 0;
   double step_ms = 0.0, rebuild_ms = 0.0;  // measured costs (exponential averages)
-  // recent (list size, time) samples of full rebuilds and of window steps,
-  // fitted by least squares to time = fixed + per_entry * size
-  std::vector<std::array<double, 2>> rebuild_samples, step_samples;
+  unsigned int* d_hist = nullptr;   // 64 bins (k_skin_hist)
+  double rebuild_bp_ms = 0.0, rebuild_var_ms = 0.0;  // last full rebuild: broad phase, the rest
   cudaEvent_t ea = nullptr, eb = nullptr;
   double window_ms = 0.0;
 };
@@ -128,6 +129,8 @@ struct Ctx {
   float last_cell = 0.f;
   int64_t last_nover = 0;
   bool forces_stale = false;
+  bool more_steps_follow = false;  // inside rk_step, before its last step
+  int64_t nsph = 0;                // sub-element spheres of all bodies
   std::vector<uint8_t> needres_host;
   // block-size autotuner of the step kernels (results do not depend on it)
   int64_t tune_left = 0, tune_total = 0;

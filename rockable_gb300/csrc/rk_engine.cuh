@@ -122,6 +122,7 @@ struct Scene {
   const float* sk_rsw;  // n: swing radius (largest vertex distance from the centre), with sk_path
   float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
   int64_t* sph_ofs;   // n+1
+  int* sph_body;      // body of every sphere
   // ---- interfaces
   int64_t nif;
   int *if_i, *if_j;
@@ -155,6 +156,8 @@ int max_tpb(int which, int form_mixed);
 cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a);
 
 // learned skin (rk_skin.cu)
+int launch_skin_hist(const Scene& s, const double* rp, const double* rq, const float* rsw, float unit,
+                     unsigned int* hist, cudaStream_t st);
 int launch_skin_reset(const Scene& s, const uint8_t* only, double* rp, double* rq, float* maxd, float* path,
                       cudaStream_t st);
 int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, float* maxd,

@@ -85,36 +85,37 @@ __global__ void k_body_obb(Scene s) {
 // Bounding spheres of every sub-element (vertices, edges, faces) in world
 // coordinates, as floats with the radius rounded up: the conservative filter
 // in front of the FP64 NEAR predicates.
-__global__ void k_spheres(Scene s) {
-  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (b >= s.n) return;
+__global__ void k_spheres(Scene s, int64_t nsph) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nsph) return;
+  const int b = s.sph_body[k];
+  const int local = (int)(k - s.sph_ofs[b]);
   const int sh = s.shape[b];
   const double* g = s.gv + 3 * s.gv_ofs[b];
-  float4* out = s.sph + s.sph_ofs[b];
   const int nv = s.vert_ofs[sh + 1] - s.vert_ofs[sh];
   const int e0 = s.edge_ofs[sh], ne = s.edge_ofs[sh + 1] - e0;
-  const int f0 = s.face_ofs[sh], nf = s.face_ofs[sh + 1] - f0;
-  double r2 = 0.0;
-  for (int v = 0; v < nv; v++) {
-    out[v] = make_float4((float)g[3 * v], (float)g[3 * v + 1], (float)g[3 * v + 2], 0.f);
-    double dx = g[3 * v] - s.pos[3 * b], dy = g[3 * v + 1] - s.pos[3 * b + 1], dz = g[3 * v + 2] - s.pos[3 * b + 2];
-    r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
-  }
-  s.bnd[b] = __double2float_ru(sqrt(r2));
-  for (int e = 0; e < ne; e++) {
+  const int f0 = s.face_ofs[sh];
+  if (local < nv) {  // vertex: its position; the body bound is the largest vertex distance
+    const int v = local;
+    s.sph[k] = make_float4((float)g[3 * v], (float)g[3 * v + 1], (float)g[3 * v + 2], 0.f);
+    const double dx = g[3 * v] - s.pos[3 * b], dy = g[3 * v + 1] - s.pos[3 * b + 1], dz = g[3 * v + 2] - s.pos[3 * b + 2];
+    const float d = __double2float_ru(sqrt(dx * dx + dy * dy + dz * dz));
+    atomicMax(reinterpret_cast<unsigned int*>(s.bnd) + b, __float_as_uint(d));  // non-negative floats order as their bits
+  } else if (local < nv + ne) {  // edge: midpoint, half length
+    const int e = local - nv;
     V3 a = g3(g, s.edges[2 * (e0 + e)]), c = g3(g, s.edges[2 * (e0 + e) + 1]);
     V3 m = 0.5 * (a + c);
     double h = 0.5 * sqrt(norm2(c - a));
-    out[nv + e] = make_float4((float)m.x, (float)m.y, (float)m.z, __double2float_ru(h));
-  }
-  for (int f = 0; f < nf; f++) {
-    const int v0 = s.face_vofs[f0 + f], k = s.face_vofs[f0 + f + 1] - v0;
-    V3 c = v3(0, 0, 0);  // centroid of the face vertices
-    for (int q = 0; q < k; q++) c = c + g3(g, s.face_verts[v0 + q]);
-    c = (1.0 / k) * c;
+    s.sph[k] = make_float4((float)m.x, (float)m.y, (float)m.z, __double2float_ru(h));
+  } else {  // face: centroid of its vertices, largest vertex distance
+    const int f = local - nv - ne;
+    const int v0 = s.face_vofs[f0 + f], cnt = s.face_vofs[f0 + f + 1] - v0;
+    V3 c = v3(0, 0, 0);
+    for (int q = 0; q < cnt; q++) c = c + g3(g, s.face_verts[v0 + q]);
+    c = (1.0 / cnt) * c;
     double rf2 = 0.0;
-    for (int q = 0; q < k; q++) rf2 = fmax(rf2, norm2(g3(g, s.face_verts[v0 + q]) - c));
-    out[nv + ne + f] = make_float4((float)c.x, (float)c.y, (float)c.z, __double2float_ru(sqrt(rf2)));
+    for (int q = 0; q < cnt; q++) rf2 = fmax(rf2, norm2(g3(g, s.face_verts[v0 + q]) - c));
+    s.sph[k] = make_float4((float)c.x, (float)c.y, (float)c.z, __double2float_ru(sqrt(rf2)));
   }
 }
 
@@ -601,9 +602,32 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     const int nep = s.edge_ofs[P.sp + 1] - s.edge_ofs[P.sp];
     const int nfp = s.face_ofs[P.sp + 1] - s.face_ofs[P.sp];
     // owner-vertex cull (Rockable.cpp:1385-1391): the vertex cube against
-    // the partner's OBB enlarged by dVerlet
+    // the partner's OBB enlarged by dVerlet.  With the distance-only tests a
+    // conservative float test does (a vertex out of reach of the partner's
+    // bounding sphere), since an untested candidate only keeps its old entry.
     uint32_t m0, m1;
-    {
+    if (GEOM) {
+      const float4* sbv = s.sph + s.sph_ofs[b];
+      const float4 cpp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
+      const float reach = (float)(P.Rb + P.Rp + P.dmax);
+      bool hit0 = false, hit1 = false;
+      for (int half = 0; half < 2; half++) {
+        const int v = lane + 32 * half;
+        if (v < nvb) {
+          const float4 a = sbv[v];
+          const float dx = a.x - cpp.x, dy = a.y - cpp.y, dz = a.z - cpp.z;
+          const float mg = fmaxf(fmaxf(fmaxf(fabsf(cpp.x), fabsf(cpp.y)), fabsf(cpp.z)) + cpp.w,
+                                 fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)));
+          float lim = reach + cpp.w;
+          lim = lim + 1e-4f * lim + 1e-6f * mg + 2e-6f;
+          const bool hit = dx * dx + dy * dy + dz * dz <= lim * lim;
+          if (half == 0) hit0 = hit;
+          else hit1 = hit;
+        }
+      }
+      m0 = __ballot_sync(0xffffffffu, hit0);
+      m1 = __ballot_sync(0xffffffffu, hit1);
+    } else {
       Obb op = load_obb(s.bobb + 15 * p);
       enlarge(op, P.dmax);
       const double r = P.Rb + P.dmax;
@@ -634,20 +658,21 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     const float4* sb = s.sph + s.sph_ofs[b];
     const float4* sp = s.sph + s.sph_ofs[p];
     const float sum = (float)(P.Rb + P.Rp + P.dmax);
+    const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
+    const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
+    // margin for the float rounding of coordinates of magnitude up to `mag`
+    // (about 16 ulps of it) on top of a relative 1e-4
+    const float mag = fmaxf(fmaxf(fmaxf(fabsf(cb.x), fabsf(cb.y)), fabsf(cb.z)) + cb.w,
+                            fmaxf(fmaxf(fabsf(cp.x), fabsf(cp.y)), fabsf(cp.z)) + cp.w);
+    const float slack = 1e-6f * mag + 2e-6f;
     auto far = [&](float4 a, float4 c, float extent) {
       float dx = a.x - c.x, dy = a.y - c.y, dz = a.z - c.z;
       float lim = sum + extent;
-      lim = lim + 1e-4f * lim + 2e-6f;
+      lim = lim + 1e-4f * lim + slack;
       return dx * dx + dy * dy + dz * dz > lim * lim;
     };
     const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
-    const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
-    const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
-    // geometric tests: limit with a margin for the float rounding of
-    // coordinates of magnitude up to `mag`
-    const float mag = fmaxf(fmaxf(fmaxf(fabsf(cb.x), fabsf(cb.y)), fabsf(cb.z)) + cb.w,
-                            fmaxf(fmaxf(fabsf(cp.x), fabsf(cp.y)), fabsf(cp.z)) + cp.w);
-    const float glim = sum + 1e-4f * sum + 1e-6f * mag + 1e-9f;
+    const float glim = sum + 1e-4f * sum + slack;
     const float glim2 = glim * glim;
     const bool lower = b < p;  // vertex-vertex and edge-edge pairs are tested in the i < j direction only
     const int nbv = warp_list(L.bv, nvb, lane, [&](int v) { return (((v < 32 ? m0 : m1) >> (v & 31)) & 1u) != 0u; });
@@ -906,7 +931,9 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   if (N <= 0) return 0;
   RKCHK(cudaMemsetAsync(s.flags + FLAG_NONFINITE, 0, sizeof(unsigned long long), st));
   k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
-  k_spheres<<<nblk(N, 128), 128, 0, st>>>(s);
+  const int64_t nsph = c.nsph;
+  RKCHK(cudaMemsetAsync(s.bnd, 0, (size_t)N * sizeof(float), st));
+  if (nsph > 0) k_spheres<<<nblk(nsph, 256), 256, 0, st>>>(s, nsph);
   c.kernels += 2;
   {  // a body whose state is no longer finite: stop here, loudly
     unsigned long long bad = 0;
@@ -1004,6 +1031,7 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   if (np < 0) { c.err = "pair buffer kept overflowing"; return RK_ERR_CAPACITY; }
   c.last_cell = cell;
   c.last_nover = nover;
+  if (w.timing_split && w.split) RKCHK(cudaEventRecord(w.split, st));
   const int64_t nhp = 2 * np;
   if (w.hp_cap < nhp + 1) {
     int64_t nc = nhp + nhp / 2 + 1024;

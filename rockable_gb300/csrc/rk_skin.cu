@@ -6,8 +6,8 @@
 // (Rockable.cpp:1571-1596).  Here the guard is exact: the motion of any point
 // of body b since the last rebuild is bounded by
 //     delta_b = |x_b - x_b0| + theta_b * rsw_b
-// (theta_b the rotation angle between Q_b0 and Q_b, rsw_b the largest vertex
-// distance from the centre).  Two sub-elements can only have come closer by
+// (theta_b a bound of the rotation angle between Q_b0 and Q_b, rsw_b the
+// largest vertex distance from the centre).  Two sub-elements can only have come closer by
 // delta_i + delta_j, so while max_b delta_b < dVerlet / 2 every sub-contact
 // that was not NEAR at the rebuild is still separated, and a refresh is
 // forced as soon as the bound reaches dVerlet / 2.
@@ -34,6 +34,49 @@ namespace rk {
 // (|x(now) - x(T)| <= delta(now) + delta(T)).  So once a partial refresh has
 // happened, g_b = min(path_b, 2 maxd_b) < dVerlet / 2 for every body keeps
 // every missed sub-contact separated; before it, max delta_b suffices.
+// Upper bound of the rotation angle between two unit quaternions: with c
+// the shorter of the chords |q - q0| and |q + q0|, the angle is
+// 4 asin(c / 2) <= 2 c (1 + c).
+__device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
+  double m2 = 0.0, p2 = 0.0;
+  for (int d = 0; d < 4; d++) {
+    const double m = q[d] - q0[d], p = q[d] + q0[d];
+    m2 += m * m;
+    p2 += p * p;
+  }
+  const double c = sqrt(fmin(m2, p2));
+  return 2.0 * c * (1.0 + c);
+}
+
+// Histogram of delta_b over the bodies in quarter-octave bins of
+// log2(delta / unit), bins 0..63 covering 2^-14 .. 2^2 units (the skin's
+// displacement-rate percentile at a full rebuild).
+__global__ void k_skin_hist(Scene s, const double* ref_pos, const double* ref_q, const float* rsw, float unit,
+                            unsigned int* hist) {
+  __shared__ unsigned int h[64];
+  if (threadIdx.x < 64) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b < s.n) {
+    const double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
+                 dz = s.pos[3 * b + 2] - ref_pos[3 * b + 2];
+    const float delta =
+        (float)(sqrt(dx * dx + dy * dy + dz * dz) + rot_bound(s.Q + 4 * b, ref_q + 4 * b) * (double)rsw[b]);
+    int bin = 0;
+    if (delta > 0.f) bin = (int)floorf(4.f * (log2f(delta / unit) + 14.f));
+    bin = min(max(bin, 0), 63);
+    atomicAdd(&h[bin], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < 64 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+int launch_skin_hist(const Scene& s, const double* rp, const double* rq, const float* rsw, float unit,
+                     unsigned int* hist, cudaStream_t st) {
+  k_skin_hist<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, rp, rq, rsw, unit, hist);
+  return 1;
+}
+
 __global__ void k_skin_reset(Scene s, const uint8_t* only, double* ref_pos, double* ref_q, float* maxd, float* path) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
@@ -56,12 +99,7 @@ __global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q
   if (b < s.n) {
     double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
            dz = s.pos[3 * b + 2] - ref_pos[3 * b + 2];
-    // rotation angle between ref_q and Q: 2 acos(|<q0, q>|)
-    double c = fabs(s.Q[4 * b] * ref_q[4 * b] + s.Q[4 * b + 1] * ref_q[4 * b + 1] + s.Q[4 * b + 2] * ref_q[4 * b + 2] +
-                    s.Q[4 * b + 3] * ref_q[4 * b + 3]);
-    c = fmin(c, 1.0);
-    double ang = 2.0 * acos(c);
-    double delta = sqrt(dx * dx + dy * dy + dz * dz) + ang * (double)rsw[b];
+    double delta = sqrt(dx * dx + dy * dy + dz * dz) + rot_bound(s.Q + 4 * b, ref_q + 4 * b) * (double)rsw[b];
     dmax = (float)(delta * (1.0 + 1e-6)) + 1e-12f;
     dsum = delta;
     const float md = fmaxf(maxd[b], dmax);
