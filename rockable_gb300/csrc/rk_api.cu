@@ -327,15 +327,22 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   // skin and interval minimising the predicted cost per step.  Entries grow
   // faster than the skin (more sub-element pairs come within reach): the
   // non-active entries are scaled by (skin ratio)^1.6, the power measured on
-  // the hull-grain piles.  The step time is measured over the last window
-  // (40 % of it, the narrow phase, scales with the list); the last full
-  // rebuild is timed in two parts, the broad phase (70 % fixed) and the
-  // candidates-to-index part (proportional to the list).  The interval is
+  // the hull-grain piles.  The step time is measured over the last window,
+  // with the narrow phase (timed by events, proportional to the list) apart;
+  // the last full rebuild is timed in two parts, the broad phase (70 %
+  // fixed) and the candidates-to-index part (proportional to the list); the
+  // partial refreshes of the window are counted and timed.  The interval is
   // the number of steps the predicted displacement rate takes to use half
   // the skin (with a margin), which is also when the guard would force it.
   const double margin = 1.3, alpha = 1.6;
   const double C = (double)std::max<int64_t>(1, ne0), A = std::min(active, C);
-  const double T = k.step_ms > 0 ? k.step_ms : 0.2;
+  // partial refreshes of the window: their rate grows as the skin shrinks
+  // (the fast bodies use it up sooner); their time is part of the window's
+  // step time and is taken out of it
+  const double P = (double)k.partial_in_window / (double)std::max<int64_t>(1, k.since);
+  const double Rp = k.partial_ms;
+  const double T = std::max(0.0, (k.step_ms > 0 ? k.step_ms : 0.2) - P * Rp);
+  const double Tn = k.narrow_cnt > 0 ? std::min(T, k.narrow_acc / (double)k.narrow_cnt) : 0.4 * T;
   const double Rbp = k.rebuild_bp_ms > 0 ? k.rebuild_bp_ms : 2.0;
   const double Rvar = k.rebuild_var_ms > 0 ? k.rebuild_var_ms : 2.0;
   double best = 1e300, best_s = k.skin;
@@ -345,7 +352,8 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
     double kk = std::floor(0.5 * sk / std::max(u * margin * (1.0 + churn), 1e-30));
     int64_t ki = (int64_t)std::max<double>(k.cfg.interval_min, std::min<double>(k.cfg.interval_max, kk));
     double ratio = (A + (C - A) * std::pow(sk / std::max(k.skin, 1e-30), alpha)) / C;
-    double J = T * (0.6 + 0.4 * ratio) + (Rbp * (0.7 + 0.3 * ratio) + Rvar * ratio) / (double)ki;
+    double J = (T - Tn) + Tn * ratio + (Rbp * (0.7 + 0.3 * ratio) + Rvar * ratio) / (double)ki +
+               P * (k.skin / sk) * Rp;
     if (J < best) { best = J; best_s = sk; best_k = ki; }
   }
   k.skin = best_s;
@@ -393,6 +401,9 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   CK(cudaMemsetAsync(s.flags + FLAG_NEED_UPDATE, 0, sizeof(unsigned long long), c.stream));
   k.since = 0;
   k.partial_since_global = 0;
+  k.narrow_acc = 0.0;
+  k.narrow_cnt = 0;
+  k.partial_in_window = 0;
   CK(cudaEventRecord(k.ea, c.stream));
   return 0;
 }
@@ -410,7 +421,10 @@ static int step_launches(Ctx& c) {
   n += launch_controls_pre(s, c.stream);
   n += launch_drift(s, c.stream);
   n += launch_glob_vertices(s, c.stream);
+  const bool timed = c.skin.on && c.skin.nev[0];  // the skin's cost model wants the narrow-phase time
+  if (timed) cudaEventRecord(c.skin.nev[0], c.stream);
   n += c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream);
+  if (timed) cudaEventRecord(c.skin.nev[1], c.stream);
   n += launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream);
   n += launch_breakage(s, c.stream);
   return n;
@@ -502,6 +516,7 @@ static int step_graph(Ctx& c) {
     c.graph_captures++;
   }
   CK(cudaGraphLaunch(c.gexec, c.stream));
+  c.skin.narrow_timed = c.skin.on && c.skin.nev[0];
   c.graph_replays++;
   c.kernels += c.glaunched;
   return RK_OK;
@@ -513,9 +528,16 @@ static int skin_partial(Ctx& c, int64_t nflag) {
   Skin& k = c.skin;
   Scene& s = c.s;
   settle_before_update(c);
+  CK(cudaEventRecord(k.pa, c.stream));
   int rc = rebuild_nl(c, k.flag);
   if (rc) return rc;
   c.kernels += launch_skin_reset(s, k.flag, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
+  CK(cudaEventRecord(k.pb, c.stream));
+  CK(cudaEventSynchronize(k.pb));
+  float pms = 0.f;
+  CK(cudaEventElapsedTime(&pms, k.pa, k.pb));
+  k.partial_ms = k.partial_ms > 0 ? 0.7 * k.partial_ms + 0.3 * pms : pms;
+  k.partial_in_window++;
   c.nl_updates++;
   k.partial++;
   k.partial_bodies += nflag;
@@ -534,6 +556,16 @@ int skin_after_step(Ctx& c) {
   CK(cudaMemcpyAsync(k.h_guard, k.d_guard, 32, cudaMemcpyDeviceToHost, c.stream));
   int rc;
   if ((rc = read_flags(c))) return rc;
+  if (k.narrow_timed) {
+    float nms = 0.f;
+    if (cudaEventElapsedTime(&nms, k.nev[0], k.nev[1]) == cudaSuccess) {
+      k.narrow_acc += nms;
+      k.narrow_cnt++;
+    } else {
+      cudaGetLastError();  // not timed this step: the model falls back to its default share
+    }
+    k.narrow_timed = false;
+  }
   k.since++;
   const double dmax = to_f(k.h_guard[0]), vmax = to_f(k.h_guard[1]), gmax = to_f(k.h_guard[2]);
   const int64_t nflag = (int64_t)k.h_guard[3];
@@ -633,6 +665,8 @@ void rk_destroy(rk_ctx* x) {
     if (k.w) cudaFree(k.w);
     if (k.h_guard) cudaFreeHost(k.h_guard);
     if (k.ea) cudaEventDestroy(k.ea);
+    for (cudaEvent_t e : {k.nev[0], k.nev[1], k.pa, k.pb})
+      if (e) cudaEventDestroy(e);
     if (k.eb) cudaEventDestroy(k.eb);
   }
   for (int k = 0; k < 2 * RK_NPHASE; k++)
@@ -1078,6 +1112,10 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   for (double& r : k.rates) r = 0.0;
   s.dVerlet = k.skin;
   s.DVerlet = cfg->dverlet_ratio * k.skin;
+  for (cudaEvent_t* e : {&k.nev[0], &k.nev[1], &k.pa, &k.pb})
+    if (!*e) CK(cudaEventCreate(e));
+  k.narrow_acc = k.partial_ms = 0.0;
+  k.narrow_cnt = k.partial_in_window = 0;
   k.on = true;
   s.sk_path = k.path;
   s.sk_rsw = k.rsw;
@@ -1257,7 +1295,11 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
       mark(1, false); phase(1, launch_drift(s, c.stream));
       mark(2, false); phase(2, launch_glob_vertices(s, c.stream));
       mark(3, false);
+      const bool ntimed = c.skin.on && c.skin.nev[0];
+      if (ntimed) cudaEventRecord(c.skin.nev[0], c.stream);
       phase(3, c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream));
+      if (ntimed) cudaEventRecord(c.skin.nev[1], c.stream);
+      c.skin.narrow_timed = ntimed;
       mark(4, false); phase(4, launch_gather_heavy(s, c.stream) + launch_gather_accel(s, 1, c.stream));
       mark(5, false); phase(5, launch_breakage(s, c.stream));
     }

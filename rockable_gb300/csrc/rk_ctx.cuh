@@ -65,6 +65,12 @@ struct Skin {
   unsigned int* d_guard = nullptr;  // guard reductions (see k_skin_guard)
   unsigned int* h_guard = nullptr;  // pinned
   int64_t partial = 0, partial_bodies = 0, partial_since_global = 0, since_global = 0;
+  // measured in the current window: narrow-phase time per step (events
+  // around its launch, in the step graph too) and partial-refresh cost
+  double narrow_acc = 0.0, partial_ms = 0.0;
+  int64_t narrow_cnt = 0, partial_in_window = 0;
+  cudaEvent_t nev[2] = {nullptr, nullptr}, pa = nullptr, pb = nullptr;
+  bool narrow_timed = false;
   double dsum = 0.0;                // sum of delta over bodies at the last step
   // MLP
   float* master = nullptr;
