@@ -311,7 +311,12 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   f[14] = 1.f;
   f[15] = (float)std::max(-3.0, std::min(3.0, std::log10(std::max(rate_max, 1e-30) / std::max(rate, 1e-30))));
   // prediction of the next window's displacement rate
-  double u = rate, churn = k.pred_churn;
+  // The network predicts corrections to the method without it, as log10
+  // ratios: next rate / this window's rate, next churn / the last observed
+  // churn.  Its output layer starts at zero, so it starts as that method
+  // and departs from it only as far as its training supports.
+  const double churn_base = k.pred_churn;
+  double u = rate, churn = churn_base;
   if (k.cfg.use_mlp && k.rx.size() >= 8) {
     float y[2];
     CK(cudaMemcpyAsync(k.io, f.data(), 64, cudaMemcpyHostToDevice, c.stream));
@@ -319,8 +324,10 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
     c.kernels++;
     CK(cudaMemcpyAsync(y, k.io + 16, 8, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
-    u = std::pow(10.0, (double)y[0]) * ref;
-    churn = std::pow(10.0, (double)y[1]);
+    const double r0 = std::max(-2.0, std::min(2.0, (double)y[0]));
+    const double r1 = std::max(-2.0, std::min(2.0, (double)y[1]));
+    u = rate * std::pow(10.0, r0);
+    churn = std::max(0.0, (churn_base + 1e-4) * std::pow(10.0, r1) - 1e-4);
   }
   if (!(u > 0.0) || !std::isfinite(u)) u = std::max(rate, 1e-30);
   k.pred_rate = u;
@@ -384,7 +391,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   k.pred_churn = churn_obs;
   // training sample: the previous window's features -> this window's outcome
   if (k.have_prev) {
-    std::array<float, 2> y{lg(rate / ref), lg(churn_obs + 1e-4)};
+    std::array<float, 2> y{lg(rate / ref) - k.feat_prev[0], lg(churn_obs + 1e-4) - lg(k.churn_base_prev + 1e-4)};
     if (k.rx.size() < (size_t)mlp_max_batch()) {
       k.rx.push_back(k.feat_prev);
       k.ry.push_back(y);
@@ -395,6 +402,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
     }
   }
   k.feat_prev = f;
+  k.churn_base_prev = churn_base;
   k.have_prev = true;
   if (k.cfg.use_mlp && (rc = skin_train(c))) return rc;
   c.kernels += launch_skin_reset(s, nullptr, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
@@ -1087,9 +1095,10 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
     st ^= st << 13; st ^= st >> 7; st ^= st << 17;
     return (double)(st >> 11) * (1.0 / 9007199254740992.0);
   };
+  // (the output layer starts at zero: see the prediction in skin_rebuild)
   const int layers[3][3] = {{0, 64, 16}, {64 * 16 + 64, 64, 64}, {64 * 16 + 64 + 64 * 64 + 64, 2, 64}};
   for (auto& L : layers) {
-    double a = 1.0 / std::sqrt((double)L[2]);
+    double a = L[1] == 2 ? 0.0 : 1.0 / std::sqrt((double)L[2]);
     for (int q = 0; q < L[1] * L[2]; q++) p[L[0] + q] = (float)((2.0 * rnd() - 1.0) * a);
   }
   CK(cudaMemcpyAsync(k.master, p.data(), 4 * (size_t)np, cudaMemcpyHostToDevice, c.stream));

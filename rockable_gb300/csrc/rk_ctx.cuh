@@ -81,6 +81,7 @@ struct Skin {
   std::vector<std::array<float, 2>> ry;
   size_t rhead = 0;
   std::array<float, 16> feat_prev{};
+  double churn_base_prev = 0.0;  // churn the previous prediction was relative to
   bool have_prev = false;
   // window bookkeeping
   int64_t since = 0, interval = 100;
