@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle-steps", type=int, default=4000)
+    ap.add_argument("--relax-steps", type=int, default=3000,
+                    help="steps at 1 g (soft contacts, damped) after settling, walls still in place")
+    ap.add_argument("--collapse-steps", type=int, default=10000,
+                    help="untimed steps of the collapse after the walls are removed")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact,mixed_learned_skin",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--batch-scenes", type=int, default=256,
@@ -248,6 +252,32 @@ def batched_workload(a, dev):
             "setup_s": {"generate": t_gen, "settle": t_settle}}
 
 
+def prepare_column(a, dev=0, report=None):
+    """The column-collapse state every timed run starts from: the seeded
+    deposit is settled inside four side walls (soft contacts, gravity x 20,
+    numerical damping), relaxed at 1 g, the walls are removed (t = 0 of the
+    collapse) and the collapse develops for --collapse-steps steps at the
+    benchmark parameters (mixed form, not timed)."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene, RK_FORM_MIXED
+    scene = scenes.column_collapse(n=a.n, walls=True)
+    g = scenes.settle(scene, steps=a.settle_steps, device=dev, report=report, relax_steps=a.relax_steps)
+    src = scenes.scene_from_gpu(scene, g)
+    g.close()
+    src = scenes.drop_bodies(src, scene["walls"])
+    if a.collapse_steps > 0:
+        e = GpuScene(device=dev, form=RK_FORM_MIXED)
+        e.upload_shapes(src["shape_tables"])
+        e.upload_bodies(src["bodies"], src["n_driven"])
+        scenes.set_scene_params(e, src)
+        e.upload_entries(src["entries"])
+        e.set_graphs(True)
+        e.step(a.collapse_steps)
+        src = scenes.scene_from_gpu(src, e)
+        e.close()
+    return src
+
+
 def reference_input(a):
     """The benchmark's input state for the CPU arm: the same seeded scene,
     settled the same way when a GPU is present (input preparation only,
@@ -263,10 +293,8 @@ def reference_input(a):
         have_gpu = False
     if not have_gpu:
         return scene, "deposited pile (no GPU to settle it)"
-    g = scenes.settle(scene, steps=a.settle_steps)
-    src = scenes.scene_from_gpu(scene, g)
-    g.close()
-    return src, "pile settled by the same generator (%d steps), not timed" % a.settle_steps
+    return prepare_column(a), ("the benchmark state: pile settled in walls by the same generator, walls "
+                               "released, %d collapse steps; prepared on the GPU, not timed" % a.collapse_steps)
 
 
 def run_reference(a, rank):
@@ -315,24 +343,19 @@ def main():
         dist.barrier()
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_LAW
-    scene = make_scene(a)
-    b = scene["bodies"]
-    N = len(b["mass"])
-    nfree = N - scene["n_driven"]
     dev = int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0
     settle_log = []
     t_settle = time.perf_counter()
     if a.scene == "column":
-        g = scenes.settle(scene, steps=a.settle_steps, device=dev, report=settle_log)
+        src = prepare_column(a, dev, settle_log)  # the state S every form starts from
+        scene = src
     else:
-        g = GpuScene(device=dev)
-        g.upload_shapes(scene["shape_tables"])
-        g.upload_bodies(b, scene["n_driven"])
-        scenes.set_scene_params(g, scene)
+        scene = make_scene(a)
+        src = None
     t_settle = time.perf_counter() - t_settle
-    # the settled state S every form starts from
-    src = scenes.scene_from_gpu(scene, g) if a.scene == "column" else None
-    g.close()
+    b = scene["bodies"]
+    N = len(b["mass"])
+    nfree = N - scene["n_driven"]
     from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
 
     def engine(form):
@@ -467,7 +490,11 @@ def main():
                           "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if C * 240 + N * 600 > 129e6 else
                           "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
                           "parallelism": "replicas" if ws > 1 else "single GPU",
-                          "setup_before_warmup": "%d untimed block-size tuning steps; step graphs on" % TUNE_STEPS},
+                          "setup_before_warmup": "%d untimed block-size tuning steps; step graphs on" % TUNE_STEPS,
+                          "state": ("pile settled inside 4 walls (%d steps at 20 g + %d at 1 g, soft contacts), "
+                                    "walls removed, %d collapse steps before the tuning and warm-up" % (
+                                        a.settle_steps, a.relax_steps, a.collapse_steps))
+                          if a.scene == "column" else "lattice as generated"},
                "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
                "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
                             "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": traffic,

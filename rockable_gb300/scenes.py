@@ -173,14 +173,14 @@ def deposit(rng, radii, half_x, half_y, z0, gap=1e-5):
 
 
 def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2700.0, kn=1e6, kt=1e6,
-                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), pack=1.0):
+                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), pack=1.0, walls=False):
     """Granular column collapse: n hull grains (axes U[0.5, 1.5] cm, i.e.
     semi-axes U[0.25, 0.75] cm), loosely packed by ballistic deposition in a
-    0.5 x 0.5 m column above a rigid floor plate (the only driven body); the
-    column's side walls are released at t = 0, so they are not part of the
-    scene.  With pack < 1 the deposition uses bounding spheres shrunk by that
-    factor, so that the hulls interpenetrate slightly; relax() then pushes
-    them apart into a dense, contact-rich pile."""
+    0.5 x 0.5 m column above a rigid floor plate (body 0).  With walls, four
+    vertical plates (bodies 1-4, listed in "walls") confine the column, to be
+    removed (drop_bodies) when the collapse starts; without, the walls are
+    already released.  With pack < 1 the deposition uses bounding spheres
+    shrunk by that factor, so that the hulls interpenetrate slightly."""
     rng = np.random.default_rng(seed)
     shapes = [plate_shape("FLOOR", 1.5, 0.005)]
     shapes += [hull_shape(rng, "G%05d" % k) for k in range(nshapes)]
@@ -189,9 +189,47 @@ def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2
     pos = deposit(rng, pack * bound[shape_of], 0.5 * column[0], 0.5 * column[1], 0.005 + 1e-5)
     Q = random_quaternions(rng, n)
     bmax = float(bound[1:].max())
-    return _assemble(shapes, [np.zeros(3)], [np.array([1.0, 0, 0, 0])], pos, Q, shape_of, density, law, kn, kt, en2,
-                     mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax,
-                     interVerlet=100 * dt, name="column_collapse_%d" % n)
+    wall_pos, wall_Q, wall_shape = [np.zeros(3)], [np.array([1.0, 0, 0, 0])], [0]
+    if walls:
+        rw = 0.005
+        top = float(np.max(pos[:, 2] + bound[shape_of]))
+        half = max(0.5 * max(column[0], column[1]) + 0.05, 0.5 * top + 0.05)
+        shapes.append(plate_shape("WALL", half, rw))  # after the grain shapes: their indices do not move
+        ws = len(shapes) - 1
+        s2 = math.sqrt(0.5)
+        hx, hy, zc = 0.5 * column[0] + rw, 0.5 * column[1] + rw, 0.5 * top
+        wall_pos += [np.array([hx, 0, zc]), np.array([-hx, 0, zc]), np.array([0, hy, zc]), np.array([0, -hy, zc])]
+        wall_Q += [np.array([s2, 0, s2, 0]), np.array([s2, 0, s2, 0]), np.array([s2, s2, 0, 0]),
+                   np.array([s2, s2, 0, 0])]
+        wall_shape += [ws] * 4
+    out = _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, en2,
+                    mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax,
+                    interVerlet=100 * dt, name="column_collapse_%d" % n, wall_shape=wall_shape)
+    if walls:
+        out["walls"] = [1, 2, 3, 4]
+    return out
+
+
+def drop_bodies(scene, drop):
+    """The scene without the given bodies (e.g. released walls); the other
+    bodies keep their relative order and the entries that involve a dropped
+    body are removed (the others keep their key order)."""
+    n = len(scene["bodies"]["mass"])
+    keep = np.setdiff1d(np.arange(n), np.asarray(drop, np.int64))
+    new = -np.ones(n, np.int64)
+    new[keep] = np.arange(len(keep))
+    out = dict(scene)
+    out["bodies"] = {k: np.asarray(v)[keep] for k, v in scene["bodies"].items()}
+    out["n_driven"] = int(np.sum(keep < scene["n_driven"]))
+    out.pop("walls", None)
+    if scene.get("entries") is not None:
+        e = scene["entries"]
+        ok = (new[e["i"]] >= 0) & (new[e["j"]] >= 0)
+        ne = {k: np.asarray(v)[ok] for k, v in e.items()}
+        ne["i"] = new[ne["i"]].astype(np.int32)
+        ne["j"] = new[ne["j"]].astype(np.int32)
+        out["entries"] = ne
+    return out
 
 
 def sphero_cube_box(n_side=8, seed=SEED, dt=1e-6):
@@ -357,7 +395,7 @@ def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, 
               dVerlet, interVerlet, name, wall_shape=0):
     nd = len(wall_pos)
     n = nd + len(pos)
-    shape = np.concatenate([np.full(nd, wall_shape), shape_of]).astype(np.int32)
+    shape = np.concatenate([np.broadcast_to(np.asarray(wall_shape), (nd,)), shape_of]).astype(np.int32)
     P = np.concatenate([np.array(wall_pos), pos])
     Qa = np.concatenate([np.array(wall_Q), Q])
     group = np.concatenate([np.ones(nd), np.zeros(len(pos))]).astype(np.int32)
