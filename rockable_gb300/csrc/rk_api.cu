@@ -254,6 +254,10 @@ static int skin_train(Ctx& c) {
 }
 
 static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
+  {  // the flags are not read every step when the guard is pipelined
+    const int rf = read_flags(c);
+    if (rf) return rf;
+  }
   Skin& k = c.skin;
   Scene& s = c.s;
   const double N = (double)std::max<int64_t>(1, s.n - s.n_driven);
@@ -553,17 +557,48 @@ static int skin_partial(Ctx& c, int64_t nflag) {
   return 0;
 }
 
+// The guard's read-back is pipelined when the prediction it makes is exact
+// for the scene: no control moves a driven body between steps, and neither
+// interfaces nor the reference guard can request an update.  Then the host
+// reads the previous step's prediction of this state while the GPU already
+// runs this step, and waits for this step's own guard only when a refresh
+// is due.
+static bool guard_pipelined(const Ctx& c) {
+  const Scene& s = c.s;
+  return s.ncontrols == 0 && s.servo_kind == 0 && s.nif == 0 && s.dynamic_nl == 0;
+}
+
 int skin_after_step(Ctx& c) {
   Skin& k = c.skin;
   Scene& s = c.s;
-  CK(cudaMemsetAsync(k.d_guard, 0, 32, c.stream));
+  const int slot = k.gslot;
+  unsigned int* dg = k.d_guard + 8 * slot;
+  unsigned int* hg = k.h_guard + 8 * slot;
+  CK(cudaMemsetAsync(dg, 0, 32, c.stream));
   // bodies past half of their budget are refreshed together with the one
   // that reached it
   const float flag_at = (float)(0.25 * k.skin);
-  c.kernels += launch_skin_guard(s, k.ref_pos, k.ref_q, k.rsw, k.maxd, k.path, flag_at, k.flag, k.d_guard, c.stream);
-  CK(cudaMemcpyAsync(k.h_guard, k.d_guard, 32, cudaMemcpyDeviceToHost, c.stream));
+  c.kernels += launch_skin_guard(s, k.ref_pos, k.ref_q, k.rsw, k.maxd, k.path, flag_at, k.flag, dg, c.stream);
+  CK(cudaMemcpyAsync(hg, dg, 32, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaEventRecord(k.gev[slot], c.stream));
+  k.gslot ^= 1;
+  k.since++;
+  const bool pipe = guard_pipelined(c);
+  if (pipe && k.have_pred) {
+    // the previous step's guard predicted this state
+    const unsigned int* hp = k.h_guard + 8 * (slot ^ 1);
+    CK(cudaEventSynchronize(k.gev[slot ^ 1]));
+    const double pcrit = to_f(k.partial_since_global > 0 ? hp[7] : hp[6]);
+    const bool due = pcrit >= 0.5 * k.skin * (1.0 - 1e-6) || k.since >= k.interval;
+    if (!due) {
+      k.narrow_timed = false;  // this step's events may still be running
+      return 0;
+    }
+  }
+  // this step's guard: the exact values of this state
+  CK(cudaEventSynchronize(k.gev[slot]));
   int rc;
-  if ((rc = read_flags(c))) return rc;
+  if (!pipe && (rc = read_flags(c))) return rc;
   if (k.narrow_timed) {
     float nms = 0.f;
     if (cudaEventElapsedTime(&nms, k.nev[0], k.nev[1]) == cudaSuccess) {
@@ -574,17 +609,21 @@ int skin_after_step(Ctx& c) {
     }
     k.narrow_timed = false;
   }
-  k.since++;
-  const double dmax = to_f(k.h_guard[0]), vmax = to_f(k.h_guard[1]), gmax = to_f(k.h_guard[2]);
-  const int64_t nflag = (int64_t)k.h_guard[3];
+  k.have_pred = pipe;  // holds until a refresh moves the snapshots
+  const double dmax = to_f(hg[0]), vmax = to_f(hg[1]), gmax = to_f(hg[2]);
+  const int64_t nflag = (int64_t)hg[3];
   double dsum = 0.0;
-  std::memcpy(&dsum, k.h_guard + 4, sizeof dsum);
+  std::memcpy(&dsum, hg + 4, sizeof dsum);
   k.dsum = dsum;
   const double crit = k.partial_since_global > 0 ? gmax : dmax;
   const bool forced = crit >= 0.5 * k.skin;
-  const bool need = c.h_flags[FLAG_NEED_UPDATE] != 0ull;
-  if (need || k.since >= k.interval) return skin_rebuild(c, dmax, vmax, false);
+  const bool need = !pipe && c.h_flags[FLAG_NEED_UPDATE] != 0ull;
+  if (need || k.since >= k.interval) {
+    k.have_pred = false;
+    return skin_rebuild(c, dmax, vmax, false);
+  }
   if (forced) {
+    k.have_pred = false;
     if (k.cfg.partial_fraction > 0.0 && nflag > 0 && (double)nflag <= k.cfg.partial_fraction * (double)s.n)
       return skin_partial(c, nflag);
     return skin_rebuild(c, dmax, vmax, true);
@@ -673,7 +712,7 @@ void rk_destroy(rk_ctx* x) {
     if (k.w) cudaFree(k.w);
     if (k.h_guard) cudaFreeHost(k.h_guard);
     if (k.ea) cudaEventDestroy(k.ea);
-    for (cudaEvent_t e : {k.nev[0], k.nev[1], k.pa, k.pb})
+    for (cudaEvent_t e : {k.nev[0], k.nev[1], k.pa, k.pb, k.gev[0], k.gev[1]})
       if (e) cudaEventDestroy(e);
     if (k.eb) cudaEventDestroy(k.eb);
   }
@@ -989,7 +1028,7 @@ static int skin_alloc(Ctx& c) {
   if (!k.ref_pos) {
     k.nalloc = s.n;
     if ((rc = dalloc(c, k.ref_pos, 3 * s.n)) || (rc = dalloc(c, k.ref_q, 4 * s.n)) || (rc = dalloc(c, k.rsw, s.n)) ||
-        (rc = dalloc(c, k.d_guard, 8)) || (rc = dalloc(c, k.d_hist, 64)) || (rc = dalloc(c, k.maxd, s.n)) ||
+        (rc = dalloc(c, k.d_guard, 16)) || (rc = dalloc(c, k.d_hist, 64)) || (rc = dalloc(c, k.maxd, s.n)) ||
         (rc = dalloc(c, k.path, s.n)) ||
         (rc = dalloc(c, k.flag, s.n)) || (rc = dalloc(c, k.master, np)) || (rc = dalloc(c, k.m, np)) ||
         (rc = dalloc(c, k.v, np)) || (rc = dalloc(c, k.grad, np)) || (rc = dalloc(c, k.loss, 1)) ||
@@ -999,7 +1038,7 @@ static int skin_alloc(Ctx& c) {
     char* wbuf = nullptr;
     CK(cudaMalloc(&wbuf, 2 * (size_t)np));
     k.w = wbuf;
-    CK(cudaMallocHost(&k.h_guard, 32));
+    CK(cudaMallocHost(&k.h_guard, 64));
     CK(cudaEventCreate(&k.ea));
     CK(cudaEventCreate(&k.eb));
   }
@@ -1121,8 +1160,10 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   for (double& r : k.rates) r = 0.0;
   s.dVerlet = k.skin;
   s.DVerlet = cfg->dverlet_ratio * k.skin;
-  for (cudaEvent_t* e : {&k.nev[0], &k.nev[1], &k.pa, &k.pb})
+  for (cudaEvent_t* e : {&k.nev[0], &k.nev[1], &k.pa, &k.pb, &k.gev[0], &k.gev[1]})
     if (!*e) CK(cudaEventCreate(e));
+  k.gslot = 0;
+  k.have_pred = false;
   k.narrow_acc = k.partial_ms = 0.0;
   k.narrow_cnt = k.partial_in_window = 0;
   k.on = true;
@@ -1269,6 +1310,7 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
   Scene& s = c.s;
   const bool need_flags = s.dynamic_nl != 0 || s.nif > 0;
   int64_t k0 = c.kernels, nl0 = c.nl_updates;
+  c.skin.have_pred = false;  // the state may have been changed since the last call (uploads)
   CK(cudaEventRecord(c.ev0, c.stream));
   for (int64_t it = 0; it < nsteps; it++) {
     c.t += s.dt;

@@ -71,6 +71,10 @@ struct Skin {
   int64_t narrow_cnt = 0, partial_in_window = 0;
   cudaEvent_t nev[2] = {nullptr, nullptr}, pa = nullptr, pb = nullptr;
   bool narrow_timed = false;
+  // double-buffered guard read-back (8 words per slot) and its events
+  cudaEvent_t gev[2] = {nullptr, nullptr};
+  int gslot = 0;
+  bool have_pred = false;  // the last guard read holds a prediction for the next state
   double dsum = 0.0;                // sum of delta over bodies at the last step
   // MLP
   float* master = nullptr;

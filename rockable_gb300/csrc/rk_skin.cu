@@ -89,11 +89,16 @@ __global__ void k_skin_reset(Scene s, const uint8_t* only, double* ref_pos, doub
 
 // Guard of every body after a step.  out (zeroed before): [0] max delta,
 // [1] max |v| of the free bodies, [2] max g (float bits, atomicMax),
-// [3] number of flagged bodies (g >= flag_at), [4..5] sum of delta (double).
+// [3] number of flagged bodies (g >= flag_at), [4..5] sum of delta (double),
+// [6] max delta and [7] max g predicted for the state after the NEXT step.
+// The prediction applies the next drift (the same formulas as k_drift, from
+// the velocities and accelerations this step leaves) to the free bodies;
+// driven bodies do not move between steps when no control drives them,
+// which is the only case the host uses the prediction for.
 __global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q, const float* rsw, float* maxd,
                              const float* path, float flag_at, uint8_t* flag, unsigned int* out) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  float dmax = 0.f, vmax = 0.f, gmax = 0.f;
+  float dmax = 0.f, vmax = 0.f, gmax = 0.f, pdmax = 0.f, pgmax = 0.f;
   double dsum = 0.0;
   unsigned nflag = 0;
   if (b < s.n) {
@@ -113,12 +118,38 @@ __global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q
     if (b >= s.n_driven) {
       double vx = s.vel[3 * b], vy = s.vel[3 * b + 1], vz = s.vel[3 * b + 2];
       vmax = (float)sqrt(vx * vx + vy * vy + vz * vz);
+      // next drift
+      const V3 v = v3(vx, vy, vz), acc = v3(s.acc[3 * b], s.acc[3 * b + 1], s.acc[3 * b + 2]);
+      const V3 w = v3(s.vrot[3 * b], s.vrot[3 * b + 1], s.vrot[3 * b + 2]);
+      const V3 al = v3(s.arot[3 * b], s.arot[3 * b + 1], s.arot[3 * b + 2]);
+      const V3 dxn = s.dt * v + s.dt2_2 * acc;
+      const V3 pn = v3(s.pos[3 * b] + dxn.x, s.pos[3 * b + 1] + dxn.y, s.pos[3 * b + 2] + dxn.z);
+      const Q4 q0 = q4(s.Q[4 * b], s.Q[4 * b + 1], s.Q[4 * b + 2], s.Q[4 * b + 3]);
+      Q4 qn = q0;
+      qaddscaled(qn, qdot(qn, w), s.dt);
+      qaddscaled(qn, qddot(qn, w, al), s.dt2_2);
+      qnormalize(qn);
+      const double qa[4] = {qn.s, qn.v.x, qn.v.y, qn.v.z};
+      const double ex = pn.x - ref_pos[3 * b], ey = pn.y - ref_pos[3 * b + 1], ez = pn.z - ref_pos[3 * b + 2];
+      const double dn1 = sqrt(ex * ex + ey * ey + ez * ez) + rot_bound(qa, ref_q + 4 * b) * (double)rsw[b];
+      pdmax = (float)(dn1 * (1.0 + 1e-6)) + 1e-12f;
+      // path increment of the next drift, as k_drift adds it
+      const double cx = qn.s - q0.s, cy = qn.v.x - q0.v.x, cz = qn.v.y - q0.v.y, cw = qn.v.z - q0.v.z;
+      const double ch = sqrt(cx * cx + cy * cy + cz * cz + cw * cw);
+      const double inc = sqrt(dxn.x * dxn.x + dxn.y * dxn.y + dxn.z * dxn.z) + 2.0 * ch * (1.0 + ch) * (double)rsw[b];
+      const float pth1 = path[b] + (float)(inc * (1.0 + 1e-5)) + 1e-12f;
+      pgmax = fminf(pth1, 2.f * fmaxf(md, pdmax));
+    } else {
+      pdmax = dmax;
+      pgmax = gmax;
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
     dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     gmax = fmaxf(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+    pdmax = fmaxf(pdmax, __shfl_xor_sync(0xffffffffu, pdmax, o));
+    pgmax = fmaxf(pgmax, __shfl_xor_sync(0xffffffffu, pgmax, o));
     dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
     nflag += __shfl_xor_sync(0xffffffffu, nflag, o);
   }
@@ -128,6 +159,8 @@ __global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q
     atomicMax(&out[2], __float_as_uint(gmax));
     if (nflag) atomicAdd(&out[3], nflag);
     atomicAdd(reinterpret_cast<double*>(out + 4), dsum);
+    atomicMax(&out[6], __float_as_uint(pdmax));
+    atomicMax(&out[7], __float_as_uint(pgmax));
   }
 }
 
