@@ -49,11 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--settle-steps", type=int, default=4000)
-    ap.add_argument("--relax-steps", type=int, default=3000,
-                    help="steps at 1 g (soft contacts, damped) after settling, walls still in place")
-    ap.add_argument("--collapse-steps", type=int, default=10000,
-                    help="untimed steps of the collapse after the walls are removed")
+    ap.add_argument("--collapse-steps", type=int, default=50000,
+                    help="untimed steps of the collapse before the timed forms (the middle of a 100k-step run)")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin,mixed_learned_skin_exact",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--batch-scenes", type=int, default=256,
@@ -255,27 +252,28 @@ def batched_workload(a, dev):
 
 def prepare_column(a, dev=0, report=None):
     """The column-collapse state every timed run starts from: the seeded
-    deposit is settled inside four side walls (soft contacts, gravity x 20,
-    numerical damping), relaxed at 1 g, the walls are removed (t = 0 of the
-    collapse) and the collapse develops for --collapse-steps steps at the
-    benchmark parameters (mixed form, not timed)."""
+    loose deposit (t = 0, the column released onto the floor) advanced by
+    --collapse-steps steps at the benchmark parameters (mixed form, not
+    timed), i.e. a slice from the middle of the workload's 100k-step run."""
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=a.n, walls=True)
-    g = scenes.settle(scene, steps=a.settle_steps, device=dev, report=report, relax_steps=a.relax_steps)
-    src = scenes.scene_from_gpu(scene, g)
-    g.close()
-    src = scenes.drop_bodies(src, scene["walls"])
-    if a.collapse_steps > 0:
-        e = GpuScene(device=dev, form=RK_FORM_MIXED)
-        e.upload_shapes(src["shape_tables"])
-        e.upload_bodies(src["bodies"], src["n_driven"])
-        scenes.set_scene_params(e, src)
-        e.upload_entries(src["entries"])
-        e.set_graphs(True)
-        e.step(a.collapse_steps)
-        src = scenes.scene_from_gpu(src, e)
-        e.close()
+    scene = scenes.column_collapse(n=a.n)
+    e = GpuScene(device=dev, form=RK_FORM_MIXED)
+    e.upload_shapes(scene["shape_tables"])
+    e.upload_bodies(scene["bodies"], scene["n_driven"])
+    scenes.set_scene_params(e, scene)
+    e.update_nl()
+    e.set_graphs(True)
+    done = 0
+    while done < a.collapse_steps:
+        k = min(10000, a.collapse_steps - done)
+        e.step(k)
+        done += k
+        if report is not None:
+            st = e.stats()
+            report.append((done, st["n_entries"], st["n_active"], st["e_trans"]))
+    src = scenes.scene_from_gpu(scene, e)
+    e.close()
     return src
 
 
@@ -294,8 +292,8 @@ def reference_input(a):
         have_gpu = False
     if not have_gpu:
         return scene, "deposited pile (no GPU to settle it)"
-    return prepare_column(a), ("the benchmark state: pile settled in walls by the same generator, walls "
-                               "released, %d collapse steps; prepared on the GPU, not timed" % a.collapse_steps)
+    return prepare_column(a), ("the benchmark state: the seeded loose column after %d collapse steps, "
+                               "prepared on the GPU, not timed" % a.collapse_steps)
 
 
 def run_reference(a, rank):
@@ -493,9 +491,8 @@ def main():
                           "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
                           "parallelism": "replicas" if ws > 1 else "single GPU",
                           "setup_before_warmup": "%d untimed block-size tuning steps; step graphs on" % TUNE_STEPS,
-                          "state": ("pile settled inside 4 walls (%d steps at 20 g + %d at 1 g, soft contacts), "
-                                    "walls removed, %d collapse steps before the tuning and warm-up" % (
-                                        a.settle_steps, a.relax_steps, a.collapse_steps))
+                          "state": ("loose column (ballistic deposit) released onto the floor, %d collapse steps "
+                                    "before the tuning and warm-up" % a.collapse_steps)
                           if a.scene == "column" else "lattice as generated"},
                "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
                "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
