@@ -1171,7 +1171,7 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   s.sk_rsw = k.rsw;
   s.near_geometric = cfg->exact_contacts ? 1 : 0;
   // start from a fresh list built with the initial skin
-  launch_glob_vertices(s, c.stream);
+  launch_glob_vertices(s, c.stream, true);
   if ((rc = rebuild_nl(c))) return rc;
   launch_skin_reset(s, nullptr, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
   CK(cudaEventRecord(k.ea, c.stream));
@@ -1272,7 +1272,7 @@ int rk_accelerations(rk_ctx* x) {
   if ((rc = ready(c))) return rc;
   Scene& s = c.s;
   CK(cudaMemsetAsync(s.flags + FLAG_NACTIVE, 0, sizeof(unsigned long long), c.stream));
-  launch_glob_vertices(s, c.stream);
+  launch_glob_vertices(s, c.stream, true);
   if (c.form == RK_FORM_MIXED) launch_narrow_force_mixed(s, c.stream);
   else launch_narrow_force(s, c.stream);
   launch_gather_heavy(s, c.stream);
@@ -1291,7 +1291,7 @@ int rk_update_nl(rk_ctx* x) {
   int rc;
   if ((rc = ready(c))) return rc;
   settle_lazy_forces(c);
-  launch_glob_vertices(c.s, c.stream);
+  launch_glob_vertices(c.s, c.stream, true);
   if ((rc = rebuild_nl(c))) return rc;
   c.nl_updates++;
   CK(cudaStreamSynchronize(c.stream));

@@ -143,7 +143,8 @@ enum { FLAG_NEED_UPDATE = 0, FLAG_NACTIVE = 1, FLAG_NBROKEN = 2, FLAG_GPOS = 3, 
 // step kernels (rk_step.cu)
 int launch_controls_pre(const Scene& s, cudaStream_t st);
 int launch_drift(const Scene& s, cudaStream_t st);
-int launch_glob_vertices(const Scene& s, cudaStream_t st);
+// all = false: only bodies with neighbour-list entries (the step's use)
+int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all = false);
 int launch_narrow_force(const Scene& s, cudaStream_t st);
 int launch_narrow_force_mixed(const Scene& s, cudaStream_t st);
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st);

@@ -930,6 +930,7 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   const int64_t N = s.n;
   if (N <= 0) return 0;
   RKCHK(cudaMemsetAsync(s.flags + FLAG_NONFINITE, 0, sizeof(unsigned long long), st));
+  c.kernels += launch_glob_vertices(s, st, true);  // the step computed only the listed bodies' vertices
   k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
   const int64_t nsph = c.nsph;
   RKCHK(cudaMemsetAsync(s.bnd, 0, (size_t)N * sizeof(float), st));

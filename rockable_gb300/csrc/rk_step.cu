@@ -139,10 +139,14 @@ __global__ void k_drift(Scene s) {
 }
 
 // global vertex k of body b: pos + Q (h v)
-__global__ void k_glob_vertices(Scene s) {
+// With only_listed, bodies without a neighbour-list entry are skipped: within
+// a step only the narrow phase reads these positions, and only for bodies in
+// the list; a list update recomputes every body first.
+__global__ void k_glob_vertices(Scene s, int only_listed) {
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= s.nvert) return;
   int b = s.gv_body[k];
+  if (only_listed && s.iofs[b + 1] == s.iofs[b] && s.jofs[b + 1] == s.jofs[b]) return;
   int local = (int)(k - s.gv_ofs[b]);
   int sh = s.shape[b];
   double h = s.hom[b];
@@ -777,10 +781,10 @@ int launch_drift(const Scene& s, cudaStream_t st) {
   k_drift<<<nblk(nf, t), t, 0, st>>>(s);
   return 1;
 }
-int launch_glob_vertices(const Scene& s, cudaStream_t st) {
+int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all) {
   if (s.nvert <= 0) return 0;
   const int t = tpb_or(s, 2, 256);
-  k_glob_vertices<<<nblk(s.nvert, t), t, 0, st>>>(s);
+  k_glob_vertices<<<nblk(s.nvert, t), t, 0, st>>>(s, all ? 0 : 1);
   return 1;
 }
 int launch_narrow_force(const Scene& s, cudaStream_t st) {
