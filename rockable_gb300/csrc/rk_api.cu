@@ -253,6 +253,22 @@ static int skin_train(Ctx& c) {
   return 0;
 }
 
+// Scene fields of the fused guard (null when the skin is off).  Bodies past
+// half of their budget are flagged, to be refreshed together with the one
+// that reached it.
+static void skin_bind(Ctx& c, bool on) {
+  Skin& k = c.skin;
+  Scene& s = c.s;
+  s.sk_path = on ? k.path : nullptr;
+  s.sk_rsw = on ? k.rsw : nullptr;
+  s.sk_ref_pos = on ? k.ref_pos : nullptr;
+  s.sk_ref_q = on ? k.ref_q : nullptr;
+  s.sk_maxd = on ? k.maxd : nullptr;
+  s.sk_flag = on ? k.flag : nullptr;
+  s.sk_out = on ? k.d_guard : nullptr;
+  s.sk_flag_at = on ? (float)(0.25 * k.skin) : 0.f;
+}
+
 static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   {  // the flags are not read every step when the guard is pipelined
     const int rf = read_flags(c);
@@ -371,6 +387,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   k.interval = best_k;
   s.dVerlet = k.skin;
   s.DVerlet = k.cfg.dverlet_ratio * k.skin;
+  s.sk_flag_at = (float)(0.25 * k.skin);
   settle_before_update(c);
   // the rebuild itself, timed
   float rms = 0.f, rbp = 0.f;
@@ -571,15 +588,10 @@ static bool guard_pipelined(const Ctx& c) {
 int skin_after_step(Ctx& c) {
   Skin& k = c.skin;
   Scene& s = c.s;
+  // the step's resultant kernel evaluated the guard into d_guard
   const int slot = k.gslot;
-  unsigned int* dg = k.d_guard + 8 * slot;
   unsigned int* hg = k.h_guard + 8 * slot;
-  CK(cudaMemsetAsync(dg, 0, 32, c.stream));
-  // bodies past half of their budget are refreshed together with the one
-  // that reached it
-  const float flag_at = (float)(0.25 * k.skin);
-  c.kernels += launch_skin_guard(s, k.ref_pos, k.ref_q, k.rsw, k.maxd, k.path, flag_at, k.flag, dg, c.stream);
-  CK(cudaMemcpyAsync(hg, dg, 32, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(hg, k.d_guard, 32, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaEventRecord(k.gev[slot], c.stream));
   k.gslot ^= 1;
   k.since++;
@@ -777,8 +789,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
   const int64_t n = b->n;
   // new bodies: the learned skin (per-body guard state) starts again with rk_set_skin
   c.skin.on = false;
-  c.s.sk_path = nullptr;
-  c.s.sk_rsw = nullptr;
+  skin_bind(c, false);
   c.s.near_geometric = 0;
   std::vector<int64_t> gv_ofs(n + 1, 0);
   std::vector<double> rad(n);
@@ -1110,8 +1121,7 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   Skin& k = c.skin;
   if (!cfg->enabled) {
     k.on = false;
-    c.s.sk_path = nullptr;
-    c.s.sk_rsw = nullptr;
+    skin_bind(c, false);
     c.s.near_geometric = 0;
     return RK_OK;
   }
@@ -1167,8 +1177,7 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   k.narrow_acc = k.partial_ms = 0.0;
   k.narrow_cnt = k.partial_in_window = 0;
   k.on = true;
-  s.sk_path = k.path;
-  s.sk_rsw = k.rsw;
+  skin_bind(c, true);
   s.near_geometric = cfg->exact_contacts ? 1 : 0;
   // start from a fresh list built with the initial skin
   launch_glob_vertices(s, c.stream, true);

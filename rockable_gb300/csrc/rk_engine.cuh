@@ -120,6 +120,13 @@ struct Scene {
   int tpb[4];         // threads per block of the narrow phase, resultants, global vertices, drift (0: default)
   float* sk_path;     // n: path-length bound of each free body since its last refresh (learned skin), or null
   const float* sk_rsw;  // n: swing radius (largest vertex distance from the centre), with sk_path
+  // learned-skin guard, evaluated at the end of the resultant kernel when sk_out is set
+  const double* sk_ref_pos;
+  const double* sk_ref_q;
+  float* sk_maxd;
+  uint8_t* sk_flag;
+  unsigned int* sk_out;  // 8 words, zeroed by the resultant kernel's launcher
+  float sk_flag_at;
   float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
   int64_t* sph_ofs;   // n+1
   int* sph_body;      // body of every sphere
@@ -161,8 +168,6 @@ int launch_skin_hist(const Scene& s, const double* rp, const double* rq, const f
                      unsigned int* hist, cudaStream_t st);
 int launch_skin_reset(const Scene& s, const uint8_t* only, double* rp, double* rq, float* maxd, float* path,
                       cudaStream_t st);
-int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, float* maxd,
-                      const float* path, float flag_at, uint8_t* flag, unsigned int* out, cudaStream_t st);
 int mlp_num_params();
 int mlp_max_batch();
 void launch_mlp_infer(const void* w, const float* x, float* y, cudaStream_t st);

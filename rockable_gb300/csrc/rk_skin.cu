@@ -18,6 +18,7 @@
 
 #include "../../include/rk_gpu.h"
 #include "rk_engine.cuh"
+#include "rk_guard.cuh"
 
 namespace rk {
 
@@ -34,20 +35,6 @@ namespace rk {
 // (|x(now) - x(T)| <= delta(now) + delta(T)).  So once a partial refresh has
 // happened, g_b = min(path_b, 2 maxd_b) < dVerlet / 2 for every body keeps
 // every missed sub-contact separated; before it, max delta_b suffices.
-// Upper bound of the rotation angle between two unit quaternions: with c
-// the shorter of the chords |q - q0| and |q + q0|, the angle is
-// 4 asin(c / 2) <= 2 c (1 + c).
-__device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
-  double m2 = 0.0, p2 = 0.0;
-  for (int d = 0; d < 4; d++) {
-    const double m = q[d] - q0[d], p = q[d] + q0[d];
-    m2 += m * m;
-    p2 += p * p;
-  }
-  const double c = sqrt(fmin(m2, p2));
-  return 2.0 * c * (1.0 + c);
-}
-
 // Histogram of delta_b over the bodies in quarter-octave bins of
 // log2(delta / unit), bins 0..63 covering 2^-14 .. 2^2 units (the skin's
 // displacement-rate percentile at a full rebuild).
@@ -87,91 +74,9 @@ __global__ void k_skin_reset(Scene s, const uint8_t* only, double* ref_pos, doub
   path[b] = 0.f;
 }
 
-// Guard of every body after a step.  out (zeroed before): [0] max delta,
-// [1] max |v| of the free bodies, [2] max g (float bits, atomicMax),
-// [3] number of flagged bodies (g >= flag_at), [4..5] sum of delta (double),
-// [6] max delta and [7] max g predicted for the state after the NEXT step.
-// The prediction applies the next drift (the same formulas as k_drift, from
-// the velocities and accelerations this step leaves) to the free bodies;
-// driven bodies do not move between steps when no control drives them,
-// which is the only case the host uses the prediction for.
-__global__ void k_skin_guard(Scene s, const double* ref_pos, const double* ref_q, const float* rsw, float* maxd,
-                             const float* path, float flag_at, uint8_t* flag, unsigned int* out) {
-  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  float dmax = 0.f, vmax = 0.f, gmax = 0.f, pdmax = 0.f, pgmax = 0.f;
-  double dsum = 0.0;
-  unsigned nflag = 0;
-  if (b < s.n) {
-    double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
-           dz = s.pos[3 * b + 2] - ref_pos[3 * b + 2];
-    double delta = sqrt(dx * dx + dy * dy + dz * dz) + rot_bound(s.Q + 4 * b, ref_q + 4 * b) * (double)rsw[b];
-    dmax = (float)(delta * (1.0 + 1e-6)) + 1e-12f;
-    dsum = delta;
-    const float md = fmaxf(maxd[b], dmax);
-    maxd[b] = md;
-    // driven bodies are moved by their controls, not by the drift: no path
-    const float pth = b >= s.n_driven ? path[b] : INFINITY;
-    gmax = fminf(pth, 2.f * md);
-    const bool f = gmax >= flag_at;
-    flag[b] = f ? 1 : 0;
-    nflag = f ? 1u : 0u;
-    if (b >= s.n_driven) {
-      double vx = s.vel[3 * b], vy = s.vel[3 * b + 1], vz = s.vel[3 * b + 2];
-      vmax = (float)sqrt(vx * vx + vy * vy + vz * vz);
-      // next drift
-      const V3 v = v3(vx, vy, vz), acc = v3(s.acc[3 * b], s.acc[3 * b + 1], s.acc[3 * b + 2]);
-      const V3 w = v3(s.vrot[3 * b], s.vrot[3 * b + 1], s.vrot[3 * b + 2]);
-      const V3 al = v3(s.arot[3 * b], s.arot[3 * b + 1], s.arot[3 * b + 2]);
-      const V3 dxn = s.dt * v + s.dt2_2 * acc;
-      const V3 pn = v3(s.pos[3 * b] + dxn.x, s.pos[3 * b + 1] + dxn.y, s.pos[3 * b + 2] + dxn.z);
-      const Q4 q0 = q4(s.Q[4 * b], s.Q[4 * b + 1], s.Q[4 * b + 2], s.Q[4 * b + 3]);
-      Q4 qn = q0;
-      qaddscaled(qn, qdot(qn, w), s.dt);
-      qaddscaled(qn, qddot(qn, w, al), s.dt2_2);
-      qnormalize(qn);
-      const double qa[4] = {qn.s, qn.v.x, qn.v.y, qn.v.z};
-      const double ex = pn.x - ref_pos[3 * b], ey = pn.y - ref_pos[3 * b + 1], ez = pn.z - ref_pos[3 * b + 2];
-      const double dn1 = sqrt(ex * ex + ey * ey + ez * ez) + rot_bound(qa, ref_q + 4 * b) * (double)rsw[b];
-      pdmax = (float)(dn1 * (1.0 + 1e-6)) + 1e-12f;
-      // path increment of the next drift, as k_drift adds it
-      const double cx = qn.s - q0.s, cy = qn.v.x - q0.v.x, cz = qn.v.y - q0.v.y, cw = qn.v.z - q0.v.z;
-      const double ch = sqrt(cx * cx + cy * cy + cz * cz + cw * cw);
-      const double inc = sqrt(dxn.x * dxn.x + dxn.y * dxn.y + dxn.z * dxn.z) + 2.0 * ch * (1.0 + ch) * (double)rsw[b];
-      const float pth1 = path[b] + (float)(inc * (1.0 + 1e-5)) + 1e-12f;
-      pgmax = fminf(pth1, 2.f * fmaxf(md, pdmax));
-    } else {
-      pdmax = dmax;
-      pgmax = gmax;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-    gmax = fmaxf(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
-    pdmax = fmaxf(pdmax, __shfl_xor_sync(0xffffffffu, pdmax, o));
-    pgmax = fmaxf(pgmax, __shfl_xor_sync(0xffffffffu, pgmax, o));
-    dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
-    nflag += __shfl_xor_sync(0xffffffffu, nflag, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&out[0], __float_as_uint(dmax));
-    atomicMax(&out[1], __float_as_uint(vmax));
-    atomicMax(&out[2], __float_as_uint(gmax));
-    if (nflag) atomicAdd(&out[3], nflag);
-    atomicAdd(reinterpret_cast<double*>(out + 4), dsum);
-    atomicMax(&out[6], __float_as_uint(pdmax));
-    atomicMax(&out[7], __float_as_uint(pgmax));
-  }
-}
-
 int launch_skin_reset(const Scene& s, const uint8_t* only, double* rp, double* rq, float* maxd, float* path,
                       cudaStream_t st) {
   k_skin_reset<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, only, rp, rq, maxd, path);
-  return 1;
-}
-int launch_skin_guard(const Scene& s, const double* rp, const double* rq, const float* rsw, float* maxd,
-                      const float* path, float flag_at, uint8_t* flag, unsigned int* out, cudaStream_t st) {
-  k_skin_guard<<<(unsigned)((s.n + 255) / 256), 256, 0, st>>>(s, rp, rq, rsw, maxd, path, flag_at, flag, out);
   return 1;
 }
 

@@ -18,6 +18,7 @@
 
 #include "../../include/rk_gpu.h"
 #include "rk_engine.cuh"
+#include "rk_guard.cuh"
 
 namespace rk {
 
@@ -519,9 +520,7 @@ __global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s, const int
   }
 }
 
-__global__ void k_gather_accel(Scene s, int apply_kick) {
-  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (b >= s.n) return;
+__device__ __forceinline__ void gather_body(const Scene& s, int64_t b, int apply_kick) {
   const bool driven = b < s.n_driven;
   V3 F, M;
   if (s.is_heavy[b] == 2) {
@@ -660,6 +659,13 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   st3(s.moment, b, M);
 }
 
+__global__ void k_gather_accel(Scene s, int apply_kick) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b < s.n) gather_body(s, b, apply_kick);
+  // the learned skin's guard on the state this step leaves (all lanes)
+  if (s.sk_out && apply_kick) skin_guard_body(s, b);
+}
+
 // ----------------------------------------------------------------- K4 ----
 __global__ void k_bond_break(Scene s) {
   int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -795,6 +801,7 @@ int launch_narrow_force(const Scene& s, cudaStream_t st) {
 }
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
   if (s.n <= 0) return 0;
+  if (s.sk_out && apply_kick) cudaMemsetAsync(s.sk_out, 0, 8 * sizeof(unsigned int), st);
   const int t = tpb_or(s, 1, 128);
   k_gather_accel<<<nblk(s.n, t), t, 0, st>>>(s, apply_kick);
   return 1;
