@@ -353,15 +353,17 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   k.pred_rate = u;
   // skin and interval minimising the predicted cost per step.  Entries grow
   // faster than the skin (more sub-element pairs come within reach): the
-  // non-active entries are scaled by (skin ratio)^1.6, the power measured on
-  // the hull-grain piles.  The step time is measured over the last window,
+  // non-active entries are scaled by (skin ratio)^alpha, alpha learnt from
+  // the rebuilds that changed the skin (1.6, the power measured on hull-grain
+  // piles, to start).  The step time is measured over the last window,
   // with the narrow phase (timed by events, proportional to the list) apart;
   // the last full rebuild is timed in two parts, the broad phase (70 %
   // fixed) and the candidates-to-index part (proportional to the list); the
   // partial refreshes of the window are counted and timed.  The interval is
   // the number of steps the predicted displacement rate takes to use half
   // the skin (with a margin), which is also when the guard would force it.
-  const double margin = 1.3, alpha = 1.6;
+  const double margin = 1.3, alpha = k.alpha;
+  const double skin_before = k.skin;
   const double C = (double)std::max<int64_t>(1, ne0), A = std::min(active, C);
   // partial refreshes of the window: their rate grows as the skin shrinks
   // (the fast bodies use it up sooner); their time is part of the window's
@@ -409,6 +411,12 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   if (forced) k.forced++;
   else k.scheduled++;
   const double churn_obs = std::fabs((double)s.ne - (double)ne0) / std::max(1.0, (double)ne0);
+  // growth exponent of the non-active entries with the skin, from this
+  // rebuild when the skin changed (exponential average, starts at 1.6)
+  if (std::fabs(std::log(k.skin / skin_before)) > 0.05 && (double)ne0 > 1.05 * A && (double)s.ne > 1.05 * A) {
+    const double obs = std::log(((double)s.ne - A) / ((double)ne0 - A)) / std::log(k.skin / skin_before);
+    k.alpha = 0.7 * k.alpha + 0.3 * std::max(0.3, std::min(3.0, obs));
+  }
   k.pred_churn = churn_obs;
   // training sample: the previous window's features -> this window's outcome
   if (k.have_prev) {
@@ -577,9 +585,9 @@ static int skin_partial(Ctx& c, int64_t nflag) {
 // The guard's read-back is pipelined when the prediction it makes is exact
 // for the scene: no control moves a driven body between steps, and neither
 // interfaces nor the reference guard can request an update.  Then the host
-// reads the previous step's prediction of this state while the GPU already
-// runs this step, and waits for this step's own guard only when a refresh
-// is due.
+// reads the previous step's bound of this state while the GPU already runs
+// this step, and waits for this step's own (exact) guard values only when
+// the bound comes within 2 % of the trigger.
 static bool guard_pipelined(const Ctx& c) {
   const Scene& s = c.s;
   return s.ncontrols == 0 && s.servo_kind == 0 && s.nif == 0 && s.dynamic_nl == 0;
@@ -601,7 +609,7 @@ int skin_after_step(Ctx& c) {
     const unsigned int* hp = k.h_guard + 8 * (slot ^ 1);
     CK(cudaEventSynchronize(k.gev[slot ^ 1]));
     const double pcrit = to_f(k.partial_since_global > 0 ? hp[7] : hp[6]);
-    const bool due = pcrit >= 0.5 * k.skin * (1.0 - 1e-6) || k.since >= k.interval;
+    const bool due = pcrit >= 0.5 * k.skin * 0.98 || k.since >= k.interval;
     if (!due) {
       k.narrow_timed = false;  // this step's events may still be running
       return 0;
@@ -1165,6 +1173,7 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   k.rebuilds = k.forced = k.scheduled = 0;
   k.partial = k.partial_bodies = k.partial_since_global = 0;
   k.rebuild_bp_ms = k.rebuild_var_ms = 0.0;
+  k.alpha = 1.6;
   k.dsum = 0.0;
   k.step_ms = k.rebuild_ms = 0.0;
   for (double& r : k.rates) r = 0.0;

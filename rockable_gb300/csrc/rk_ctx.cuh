@@ -96,6 +96,7 @@ struct Skin {
   double step_ms = 0.0, rebuild_ms = 0.0;  // measured costs (exponential averages)
   unsigned int* d_hist = nullptr;   // 64 bins (k_skin_hist)
   double rebuild_bp_ms = 0.0, rebuild_var_ms = 0.0;  // last full rebuild: broad phase, the rest
+  double alpha = 1.6;  // entries ~ skin^alpha (non-active part), learnt
   cudaEvent_t ea = nullptr, eb = nullptr;
   double window_ms = 0.0;
 };

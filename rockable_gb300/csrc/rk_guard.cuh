@@ -9,14 +9,17 @@ namespace rk {
 // Upper bound of the rotation angle between two unit quaternions: with c
 // the shorter of the chords |q - q0| and |q + q0|, the angle is
 // 4 asin(c / 2) <= 2 c (1 + c).
-__device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
+__device__ __forceinline__ double quat_chord(const double* q, const double* q0) {
   double m2 = 0.0, p2 = 0.0;
   for (int d = 0; d < 4; d++) {
     const double m = q[d] - q0[d], p = q[d] + q0[d];
     m2 += m * m;
     p2 += p * p;
   }
-  const double c = sqrt(fmin(m2, p2));
+  return sqrt(fmin(m2, p2));
+}
+__device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
+  const double c = quat_chord(q, q0);
   return 2.0 * c * (1.0 + c);
 }
 
@@ -25,11 +28,11 @@ __device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
 // (warp reduction).  sk_out (zeroed before the step): [0] max delta,
 // [1] max |v| of the free bodies, [2] max g (float bits, atomicMax),
 // [3] number of flagged bodies (g >= flag_at), [4..5] sum of delta (double),
-// [6] max delta and [7] max g predicted for the state after the NEXT step.
-// The prediction applies the next drift (the same formulas as k_drift, from
-// the velocities and accelerations this step leaves) to the free bodies;
-// driven bodies do not move between steps when no control drives them,
-// which is the only case the host uses the prediction for.
+// [6] max delta and [7] max g bounded for the state after the NEXT step:
+// the next drift's motion is bounded from the velocities and accelerations
+// this step leaves (free bodies); driven bodies do not move between steps
+// when no control drives them, which is the only case the host uses the
+// bound for.
 __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   const double* ref_pos = s.sk_ref_pos;
   const double* ref_q = s.sk_ref_q;
@@ -45,7 +48,8 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   if (b < s.n) {
     double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
            dz = s.pos[3 * b + 2] - ref_pos[3 * b + 2];
-    double delta = sqrt(dx * dx + dy * dy + dz * dz) + rot_bound(s.Q + 4 * b, ref_q + 4 * b) * (double)rsw[b];
+    const double chord = quat_chord(s.Q + 4 * b, ref_q + 4 * b);
+    double delta = sqrt(dx * dx + dy * dy + dz * dz) + 2.0 * chord * (1.0 + chord) * (double)rsw[b];
     dmax = (float)(delta * (1.0 + 1e-6)) + 1e-12f;
     dsum = delta;
     const float md = fmaxf(maxd[b], dmax);
@@ -59,27 +63,19 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
     if (b >= s.n_driven) {
       double vx = s.vel[3 * b], vy = s.vel[3 * b + 1], vz = s.vel[3 * b + 2];
       vmax = (float)sqrt(vx * vx + vy * vy + vz * vz);
-      // next drift
-      const V3 v = v3(vx, vy, vz), acc = v3(s.acc[3 * b], s.acc[3 * b + 1], s.acc[3 * b + 2]);
-      const V3 w = v3(s.vrot[3 * b], s.vrot[3 * b + 1], s.vrot[3 * b + 2]);
-      const V3 al = v3(s.arot[3 * b], s.arot[3 * b + 1], s.arot[3 * b + 2]);
-      const V3 dxn = s.dt * v + s.dt2_2 * acc;
-      const V3 pn = v3(s.pos[3 * b] + dxn.x, s.pos[3 * b + 1] + dxn.y, s.pos[3 * b + 2] + dxn.z);
-      const Q4 q0 = q4(s.Q[4 * b], s.Q[4 * b + 1], s.Q[4 * b + 2], s.Q[4 * b + 3]);
-      Q4 qn = q0;
-      qaddscaled(qn, qdot(qn, w), s.dt);
-      qaddscaled(qn, qddot(qn, w, al), s.dt2_2);
-      qnormalize(qn);
-      const double qa[4] = {qn.s, qn.v.x, qn.v.y, qn.v.z};
-      const double ex = pn.x - ref_pos[3 * b], ey = pn.y - ref_pos[3 * b + 1], ez = pn.z - ref_pos[3 * b + 2];
-      const double dn1 = sqrt(ex * ex + ey * ey + ez * ez) + rot_bound(qa, ref_q + 4 * b) * (double)rsw[b];
-      pdmax = (float)(dn1 * (1.0 + 1e-6)) + 1e-12f;
-      // path increment of the next drift, as k_drift adds it
-      const double cx = qn.s - q0.s, cy = qn.v.x - q0.v.x, cz = qn.v.y - q0.v.y, cw = qn.v.z - q0.v.z;
-      const double ch = sqrt(cx * cx + cy * cy + cz * cz + cw * cw);
-      const double inc = sqrt(dxn.x * dxn.x + dxn.y * dxn.y + dxn.z * dxn.z) + 2.0 * ch * (1.0 + ch) * (double)rsw[b];
-      const float pth1 = path[b] + (float)(inc * (1.0 + 1e-5)) + 1e-12f;
-      pgmax = fminf(pth1, 2.f * fmaxf(md, pdmax));
+      // bound of the next drift: |dt v + dt^2/2 a| and a rotation of at most
+      // |w| dt + |alpha| dt^2/2 (the normalised quaternion update, 1 % margin
+      // for its second-order terms); a step of angle t moves the chord c by at
+      // most t/2, so 2c(1 + c) grows by at most t (1 + 2c + t/2).  Only decides
+      // when the exact values must be read, so a bound is enough.
+      const double ax = s.acc[3 * b], ay = s.acc[3 * b + 1], az = s.acc[3 * b + 2];
+      const double wx = s.vrot[3 * b], wy = s.vrot[3 * b + 1], wz = s.vrot[3 * b + 2];
+      const double lx = s.arot[3 * b], ly = s.arot[3 * b + 1], lz = s.arot[3 * b + 2];
+      const float dxb = (float)(s.dt * sqrt(vx * vx + vy * vy + vz * vz) + s.dt2_2 * sqrt(ax * ax + ay * ay + az * az));
+      const float thb = (float)(s.dt * sqrt(wx * wx + wy * wy + wz * wz) + s.dt2_2 * sqrt(lx * lx + ly * ly + lz * lz));
+      const float inc = 1.01f * (dxb + thb * rsw[b] * (1.f + 2.f * (float)chord + thb)) + 1e-12f;
+      pdmax = dmax + inc;
+      pgmax = fminf(path[b] + inc, 2.f * fmaxf(md, pdmax));
     } else {
       pdmax = dmax;
       pgmax = gmax;
