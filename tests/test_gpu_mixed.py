@@ -90,3 +90,76 @@ def test_mixed_one_step_settled_column(gpu_lib):
     print("after 200 steps:", s64, sm)
     assert abs(s64["n_active"] - sm["n_active"]) <= 0.01 * s64["n_active"] + 5
     assert abs(s64["e_trans"] - sm["e_trans"]) <= 0.05 * s64["e_trans"] + 1e-12
+
+
+def _sticked_variant(golden_dir):
+    case = "518_poly"
+    conf = variant_conf(
+        str(golden_dir / case / CONF[case]), str(golden_dir / case / "v_stick_mixed.conf"),
+        subs=[(r"^forceLaw Default", "forceLaw StickedLinks"), (r"^muContact 0 0 0$", "muContact 0 0 0.3"),
+              (r"^gravity 0 0 0$", "gravity 0 0 -500"), (r"^dt .*$", "dt 2e-07")],
+        append="knInnerBond 0 0 100\nktInnerBond 0 0 80\nkrInnerBond 0 0 1e-4\nen2InnerBond 0 0 0.1\n"
+               "fn0InnerBond 0 0 0.05\nft0InnerBond 0 0 0.05\nmom0InnerBond 0 0 1.0\npowInnerBond 0 0 2\n")
+    open(conf, "a").write("stickVerticesInClusters 0.001\n")
+    return conf
+
+
+def test_mixed_rupture_set_matches_plain(golden_dir, oracle_lib, gpu_lib):
+    """Bonded scene (stickVerticesInClusters, StickedLinks law, strengths
+    lowered so that bonds break): the set of broken interfaces of the mixed
+    form equals the FP64 form's after every 50 steps."""
+    from helpers import set_params_from_oracle
+    from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
+    o = oracle_lib.Oracle(_sticked_variant(golden_dir))
+    for name, v in [("fn0InnerBond", 2e-5), ("ft0InnerBond", 1e-6)]:
+        o.set_param(name, 0, 0, v)
+    g64 = gpu_from_oracle(o, form=RK_FORM_FP64)
+    gm = gpu_from_oracle(o, form=RK_FORM_MIXED)
+    for g in (g64, gm):
+        set_params_from_oracle(g, o)
+        g.update_nl()
+    seen = 0
+    for k in range(6):
+        g64.step(50)
+        gm.step(50)
+        _, _, b64 = g64.interfaces()
+        _, _, bm = gm.interfaces()
+        assert np.array_equal(b64, bm), (k, np.flatnonzero(b64 != bm)[:10])
+        seen = int(b64.sum())
+    assert seen > 0
+
+
+def test_long_run_statistics_match_plain(gpu_lib):
+    """A 3000-step column collapse in the mixed form and with the learned
+    skin: the time averages of the kinetic energy and of the coordination
+    number stay within 5 % of the FP64 form's (the trajectories themselves
+    diverge, as in any granular flow)."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
+    scene = scenes.column_collapse(n=3000, nshapes=64)
+    gs = scenes.settle(scene, steps=1200)
+    src = scenes.scene_from_gpu(scene, gs)
+    gs.close()
+    series = {}
+    for name in ["plain", "mixed", "skin"]:
+        g = GpuScene(form=RK_FORM_FP64 if name == "plain" else RK_FORM_MIXED)
+        g.upload_shapes(src["shape_tables"])
+        g.upload_bodies(src["bodies"], src["n_driven"])
+        scenes.set_scene_params(g, src)
+        g.upload_entries(src["entries"])
+        if name == "skin":
+            g.set_skin(use_mlp=True, skin_min=0.05 * scene["dVerlet"], skin_max=4.0 * scene["dVerlet"],
+                       interval_min=2, interval_max=1000, seed=5)
+        ke, z = [], []
+        for _ in range(12):
+            g.step(250)
+            st = g.stats()
+            ke.append(st["e_trans"] + st["e_rot"])
+            z.append(st["coordination"])
+        series[name] = (np.mean(ke), np.mean(z))
+        g.close()
+    print("long-run means (kinetic energy, coordination):", series)
+    for name in ["mixed", "skin"]:
+        for q in range(2):
+            ref = series["plain"][q]
+            assert abs(series[name][q] - ref) <= 0.05 * abs(ref), (name, q, series)
