@@ -632,9 +632,6 @@ int skin_after_step(Ctx& c) {
   k.have_pred = pipe;  // holds until a refresh moves the snapshots
   const double dmax = to_f(hg[0]), vmax = to_f(hg[1]), gmax = to_f(hg[2]);
   const int64_t nflag = (int64_t)hg[3];
-  double dsum = 0.0;
-  std::memcpy(&dsum, hg + 4, sizeof dsum);
-  k.dsum = dsum;
   const double crit = k.partial_since_global > 0 ? gmax : dmax;
   const bool forced = crit >= 0.5 * k.skin;
   const bool need = !pipe && c.h_flags[FLAG_NEED_UPDATE] != 0ull;
@@ -1174,7 +1171,6 @@ int rk_set_skin(rk_ctx* x, const rk_skin_config* cfg) {
   k.partial = k.partial_bodies = k.partial_since_global = 0;
   k.rebuild_bp_ms = k.rebuild_var_ms = 0.0;
   k.alpha = 1.6;
-  k.dsum = 0.0;
   k.step_ms = k.rebuild_ms = 0.0;
   for (double& r : k.rates) r = 0.0;
   s.dVerlet = k.skin;

@@ -75,7 +75,6 @@ struct Skin {
   cudaEvent_t gev[2] = {nullptr, nullptr};
   int gslot = 0;
   bool have_pred = false;  // the last guard read holds a prediction for the next state
-  double dsum = 0.0;                // sum of delta over bodies at the last step
   // MLP
   float* master = nullptr;
   void* w = nullptr;

@@ -24,10 +24,10 @@ __device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
 }
 
 // Guard of body b after a step, evaluated by the thread that finished the
-// body's update (the resultant kernel); every lane of the warp must call it
-// (warp reduction).  sk_out (zeroed before the step): [0] max delta,
+// body's update (the resultant kernel); every thread of the block must call
+// it (block reduction, blocks of at most 512 threads).  sk_out (zeroed before the step): [0] max delta,
 // [1] max |v| of the free bodies, [2] max g (float bits, atomicMax),
-// [3] number of flagged bodies (g >= flag_at), [4..5] sum of delta (double),
+// [3] number of flagged bodies (g >= flag_at), [4..5] unused,
 // [6] max delta and [7] max g bounded for the state after the NEXT step:
 // the next drift's motion is bounded from the velocities and accelerations
 // this step leaves (free bodies); driven bodies do not move between steps
@@ -43,7 +43,6 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   uint8_t* flag = s.sk_flag;
   unsigned int* out = s.sk_out;
   float dmax = 0.f, vmax = 0.f, gmax = 0.f, pdmax = 0.f, pgmax = 0.f;
-  double dsum = 0.0;
   unsigned nflag = 0;
   if (b < s.n) {
     double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
@@ -51,7 +50,6 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
     const double chord = quat_chord(s.Q + 4 * b, ref_q + 4 * b);
     double delta = sqrt(dx * dx + dy * dy + dz * dz) + 2.0 * chord * (1.0 + chord) * (double)rsw[b];
     dmax = (float)(delta * (1.0 + 1e-6)) + 1e-12f;
-    dsum = delta;
     const float md = fmaxf(maxd[b], dmax);
     maxd[b] = md;
     // driven bodies are moved by their controls, not by the drift: no path
@@ -81,21 +79,41 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
       pgmax = gmax;
     }
   }
+  // warp, then block reduction through shared memory: one atomic per block
+  // and quantity (the block size is at most 512 threads)
   for (int o = 16; o > 0; o >>= 1) {
     dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     gmax = fmaxf(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
     pdmax = fmaxf(pdmax, __shfl_xor_sync(0xffffffffu, pdmax, o));
     pgmax = fmaxf(pgmax, __shfl_xor_sync(0xffffffffu, pgmax, o));
-    dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
     nflag += __shfl_xor_sync(0xffffffffu, nflag, o);
   }
-  if ((threadIdx.x & 31) == 0) {
+  __shared__ float red[16][5];
+  __shared__ unsigned redn[16];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    red[warp][0] = dmax;
+    red[warp][1] = vmax;
+    red[warp][2] = gmax;
+    red[warp][3] = pdmax;
+    red[warp][4] = pgmax;
+    redn[warp] = nflag;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; w++) {
+      dmax = fmaxf(dmax, red[w][0]);
+      vmax = fmaxf(vmax, red[w][1]);
+      gmax = fmaxf(gmax, red[w][2]);
+      pdmax = fmaxf(pdmax, red[w][3]);
+      pgmax = fmaxf(pgmax, red[w][4]);
+      nflag += redn[w];
+    }
     atomicMax(&out[0], __float_as_uint(dmax));
     atomicMax(&out[1], __float_as_uint(vmax));
     atomicMax(&out[2], __float_as_uint(gmax));
     if (nflag) atomicAdd(&out[3], nflag);
-    atomicAdd(reinterpret_cast<double*>(out + 4), dsum);
     atomicMax(&out[6], __float_as_uint(pdmax));
     atomicMax(&out[7], __float_as_uint(pgmax));
   }
