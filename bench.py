@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
 TUNE_STEPS = 8  # untimed block-size tuning steps before the warm-up (rk_set_autotune, 2 rounds)
 NCU_NARROW_MIXED_BYTES_PER_ENTRY = 22.877e6 / 183166  # ncu, 50k-grain column, mixed form (124.9 B)
+NCU_GATHER_BYTES_PER_BODY = None  # ncu DRAM bytes per body of k_gather_accel, once captured
 
 
 def parse():
@@ -434,15 +435,26 @@ def main():
     ms, launches, wall, rep, ck, value = (head["ms"], head["launches"], head["wall"], head["rep"], head["clocks"],
                                           head["value"])
     prof, nprof = head["prof"], head["nprof"]
-    nphase = prof["narrow_force"]
-    t_narrow = nphase[0] / max(nphase[1], 1)  # ms per launch
+    # roofline of the headline form's dominant kernel: the narrow phase (140
+    # algorithmic bytes per entry: 12 B key + history read and written) or the
+    # resultant / integration kernel (352 B per body: 200 B of state read, 152 B
+    # written), whichever takes more device time per step
     C = head["entries"]
     hbm, src_peak = peaks()
-    achieved = 140.0 * C / (t_narrow / 1000.0) / 1e9 if t_narrow > 0 else None
-    # DRAM bytes per entry of k_narrow_force_mixed, from one ncu capture of the
-    # 50k-grain column (dram__bytes_read.sum + dram__bytes_write.sum per launch /
-    # entries); the same kernel serves the mixed and learned-skin forms
-    traffic = NCU_NARROW_MIXED_BYTES_PER_ENTRY * C
+    per_step = {k: prof[k][0] / max(nprof, 1) for k in ("narrow_force", "gather_accel")}
+    dominant = max(per_step, key=per_step.get)
+    if dominant == "narrow_force":
+        unit_bytes, units, unit_name = 140.0, C, "entries"
+        t_launch = prof["narrow_force"][0] / max(prof["narrow_force"][1], 1)  # ms per launch
+        traffic = NCU_NARROW_MIXED_BYTES_PER_ENTRY * C
+        tnote = "ncu DRAM bytes per entry of k_narrow_force_mixed (column, mixed form) x this form's entries"
+    else:
+        unit_bytes, units, unit_name = 352.0, N, "bodies"
+        t_launch = per_step["gather_accel"]  # ms per step (k_gather_accel, plus k_gather_heavy when used)
+        traffic = NCU_GATHER_BYTES_PER_BODY * N if NCU_GATHER_BYTES_PER_BODY else None
+        tnote = ("ncu DRAM bytes per body of k_gather_accel (column, learned-skin form) x bodies"
+                 if NCU_GATHER_BYTES_PER_BODY else "not captured for this kernel")
+    achieved = unit_bytes * units / (t_launch / 1000.0) / 1e9 if t_launch > 0 else None
     st = {"n_entries": C, "n_active": head["active"]}
     # ---- e2e through the C ABI with host-owned state (headline form)
     e2e = None
@@ -495,13 +507,14 @@ def main():
                                     "before the tuning and warm-up" % a.collapse_steps)
                           if a.scene == "column" else "lattice as generated"},
                "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
-               "roofline": {"bound": "hbm", "kernel": "narrow_force", "achieved": achieved, "peak": hbm,
+               "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm,
                             "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                            "traffic_note": "bytes per launch: ncu DRAM bytes per entry of this kernel (column, "
-                                            "mixed form) x this form's entries",
-                            "limiter": "FP64 pipe (ncu: 73% busy in the narrow phase, 81% in the global vertices)",
-                            "peak_source": src_peak, "bytes_per_entry": 140, "entries": int(C),
-                            "ms_per_launch": t_narrow},
+                            "traffic_note": tnote,
+                            "limiter": "FP64 pipe (ncu: 73% busy in the narrow phase and the resultants, "
+                                       "81% in the global vertices)",
+                            "peak_source": src_peak, "algorithmic_bytes_per_unit": unit_bytes,
+                            "units": int(units), "unit_name": unit_name, "ms_per_launch": t_launch,
+                            "phase_ms_per_step": per_step},
                "setup": {"settle_s": t_settle, "settle_log": settle_log},
                "phases_ms_per_step": {k: v[0] / nprof for k, v in prof.items()},
                "phases_launches": {k: v[1] for k, v in prof.items()},

@@ -45,11 +45,18 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   float dmax = 0.f, vmax = 0.f, gmax = 0.f, pdmax = 0.f, pgmax = 0.f;
   unsigned nflag = 0;
   if (b < s.n) {
-    double dx = s.pos[3 * b] - ref_pos[3 * b], dy = s.pos[3 * b + 1] - ref_pos[3 * b + 1],
-           dz = s.pos[3 * b + 2] - ref_pos[3 * b + 2];
-    const double chord = quat_chord(s.Q + 4 * b, ref_q + 4 * b);
-    double delta = sqrt(dx * dx + dy * dy + dz * dz) + 2.0 * chord * (1.0 + chord) * (double)rsw[b];
-    dmax = (float)(delta * (1.0 + 1e-6)) + 1e-12f;
+    // differences in FP64, the rest in float rounded up (relative 1e-5 covers
+    // the float rounding of the norms, 1e-12 m the conversions)
+    const float dx = (float)(s.pos[3 * b] - ref_pos[3 * b]), dy = (float)(s.pos[3 * b + 1] - ref_pos[3 * b + 1]),
+                dz = (float)(s.pos[3 * b + 2] - ref_pos[3 * b + 2]);
+    float m2 = 0.f, p2 = 0.f;
+    for (int d = 0; d < 4; d++) {
+      const float m = (float)(s.Q[4 * b + d] - ref_q[4 * b + d]), p = (float)(s.Q[4 * b + d] + ref_q[4 * b + d]);
+      m2 += m * m;
+      p2 += p * p;
+    }
+    const float chord = sqrtf(fminf(m2, p2)) * (1.f + 1e-5f);
+    dmax = (sqrtf(dx * dx + dy * dy + dz * dz) + 2.f * chord * (1.f + chord) * rsw[b]) * (1.f + 1e-5f) + 1e-12f;
     const float md = fmaxf(maxd[b], dmax);
     maxd[b] = md;
     // driven bodies are moved by their controls, not by the drift: no path
@@ -59,19 +66,20 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
     flag[b] = f ? 1 : 0;
     nflag = f ? 1u : 0u;
     if (b >= s.n_driven) {
-      double vx = s.vel[3 * b], vy = s.vel[3 * b + 1], vz = s.vel[3 * b + 2];
-      vmax = (float)sqrt(vx * vx + vy * vy + vz * vz);
+      const float vx = (float)s.vel[3 * b], vy = (float)s.vel[3 * b + 1], vz = (float)s.vel[3 * b + 2];
+      vmax = sqrtf(vx * vx + vy * vy + vz * vz);
       // bound of the next drift: |dt v + dt^2/2 a| and a rotation of at most
       // |w| dt + |alpha| dt^2/2 (the normalised quaternion update, 1 % margin
       // for its second-order terms); a step of angle t moves the chord c by at
       // most t/2, so 2c(1 + c) grows by at most t (1 + 2c + t/2).  Only decides
       // when the exact values must be read, so a bound is enough.
-      const double ax = s.acc[3 * b], ay = s.acc[3 * b + 1], az = s.acc[3 * b + 2];
-      const double wx = s.vrot[3 * b], wy = s.vrot[3 * b + 1], wz = s.vrot[3 * b + 2];
-      const double lx = s.arot[3 * b], ly = s.arot[3 * b + 1], lz = s.arot[3 * b + 2];
-      const float dxb = (float)(s.dt * sqrt(vx * vx + vy * vy + vz * vz) + s.dt2_2 * sqrt(ax * ax + ay * ay + az * az));
-      const float thb = (float)(s.dt * sqrt(wx * wx + wy * wy + wz * wz) + s.dt2_2 * sqrt(lx * lx + ly * ly + lz * lz));
-      const float inc = 1.01f * (dxb + thb * rsw[b] * (1.f + 2.f * (float)chord + thb)) + 1e-12f;
+      const float ax = (float)s.acc[3 * b], ay = (float)s.acc[3 * b + 1], az = (float)s.acc[3 * b + 2];
+      const float wx = (float)s.vrot[3 * b], wy = (float)s.vrot[3 * b + 1], wz = (float)s.vrot[3 * b + 2];
+      const float lx = (float)s.arot[3 * b], ly = (float)s.arot[3 * b + 1], lz = (float)s.arot[3 * b + 2];
+      const float dt = (float)s.dt, dt2 = (float)s.dt2_2;
+      const float dxb = dt * vmax + dt2 * sqrtf(ax * ax + ay * ay + az * az);
+      const float thb = dt * sqrtf(wx * wx + wy * wy + wz * wz) + dt2 * sqrtf(lx * lx + ly * ly + lz * lz);
+      const float inc = 1.01f * (dxb + thb * rsw[b] * (1.f + 2.f * chord + thb)) + 1e-12f;
       pdmax = dmax + inc;
       pgmax = fminf(path[b] + inc, 2.f * fmaxf(md, pdmax));
     } else {

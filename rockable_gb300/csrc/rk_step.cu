@@ -128,10 +128,12 @@ __global__ void k_drift(Scene s) {
     // learned-skin path bound: |dx| plus the rotation angle of the step
     // (at most 2c(1 + c) for the chord c = |q - q0| of unit quaternions)
     // times the swing radius, rounded up
-    const double cx = q.s - q0.s, cy = q.v.x - q0.v.x, cz = q.v.y - q0.v.y, cw = q.v.z - q0.v.z;
-    const double c = sqrt(cx * cx + cy * cy + cz * cz + cw * cw);
-    const double inc = sqrt(dx.x * dx.x + dx.y * dx.y + dx.z * dx.z) + 2.0 * c * (1.0 + c) * (double)s.sk_rsw[i];
-    s.sk_path[i] += (float)(inc * (1.0 + 1e-5)) + 1e-12f;
+    const float cx = (float)(q.s - q0.s), cy = (float)(q.v.x - q0.v.x), cz = (float)(q.v.y - q0.v.y),
+                cw = (float)(q.v.z - q0.v.z);
+    const float c = sqrtf(cx * cx + cy * cy + cz * cz + cw * cw);
+    const float ex = (float)dx.x, ey = (float)dx.y, ez = (float)dx.z;
+    const float inc = sqrtf(ex * ex + ey * ey + ez * ez) + 2.f * c * (1.f + c) * s.sk_rsw[i];
+    s.sk_path[i] += inc * (1.f + 1e-5f) + 1e-12f;
   }
   st3(s.pos, i, p);
   st3(s.vel, i, v);
