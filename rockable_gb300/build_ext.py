@@ -25,6 +25,7 @@ UNITS = {
     "rk_nl.cu": ["--fmad=false"],
     "rk_api.cu": ["--fmad=false"],
     "rk_mixed.cu": [],
+    "rk_fast.cu": [],
     "rk_skin.cu": [],
     "rk_noalloc.cu": [],
 }

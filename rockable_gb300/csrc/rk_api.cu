@@ -660,6 +660,7 @@ int rk_create(rk_ctx** out, const rk_config* cfg) {
   Ctx& c = x->c;
   c.device = cfg ? cfg->device : 0;
   c.form = cfg ? cfg->form : RK_FORM_FP64;
+  c.s.fast_body = c.form == RK_FORM_MIXED ? 1 : 0;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || c.device < 0 || c.device >= ndev) {
     delete x;
@@ -1267,6 +1268,7 @@ int rk_set_form(rk_ctx* x, int form) {
   if (!x) return RK_ERR_ARG;
   if (form != RK_FORM_FP64 && form != RK_FORM_MIXED) return fail(x->c, RK_ERR_UNSUPPORTED, "unknown form");
   x->c.form = form;
+  x->c.s.fast_body = form == RK_FORM_MIXED ? 1 : 0;
   return RK_OK;
 }
 

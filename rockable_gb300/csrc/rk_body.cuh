@@ -1,0 +1,260 @@
+// rk_body.cuh -- per-body kernels of the step (drift, world vertices of the
+// listed bodies, resultants + Newton-Euler + second half-kick with the fused
+// learned-skin guard), included twice: by rk_step.cu, compiled without
+// contraction into fused multiply-adds (kernels in rk::exact, the FP64 form
+// that reproduces the reference arithmetic bit for bit), and by rk_fast.cu,
+// compiled with it (kernels in rk::fused, the mixed form, where the last-bit
+// differences are within its tolerance).  Define RK_BODY_NS before including.
+#ifndef RK_BODY_HELPERS
+#define RK_BODY_HELPERS
+#include "rk_engine.cuh"
+#include "rk_guard.cuh"
+
+namespace rk {
+
+__device__ __forceinline__ V3 ld3(const double* a, int64_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
+__device__ __forceinline__ void st3(double* a, int64_t k, V3 v) {
+  a[3 * k] = v.x;
+  a[3 * k + 1] = v.y;
+  a[3 * k + 2] = v.z;
+}
+__device__ __forceinline__ Q4 ldq(const double* a, int64_t k) {
+  return q4(a[4 * k], a[4 * k + 1], a[4 * k + 2], a[4 * k + 3]);
+}
+__device__ __forceinline__ void stq(double* a, int64_t k, Q4 q) {
+  a[4 * k] = q.s;
+  a[4 * k + 1] = q.v.x;
+  a[4 * k + 2] = q.v.y;
+  a[4 * k + 3] = q.v.z;
+}
+
+__device__ __forceinline__ V3 euler_domega(V3 I, V3 w, V3 M) {
+  return v3((M.x - (I.z - I.y) * w.y * w.z) / I.x, (M.y - (I.x - I.z) * w.z * w.x) / I.y,
+            (M.z - (I.y - I.x) * w.x * w.y) / I.z);
+}
+
+// imposed force / moment components of a driven body (Rockable.cpp:2904-2928)
+__device__ __forceinline__ void init_resultant(const Scene& s, int64_t b, V3& F, V3& M) {
+  F = v3(0, 0, 0);
+  M = v3(0, 0, 0);
+  if (b >= s.n_driven) return;
+  for (int k = 0; k < s.ncontrols; k++) {
+    const Control c = s.controls[k];
+    if (c.body != b) continue;
+    switch (c.type) {
+      case RK_X_FOR: F.x = c.value; break;
+      case RK_Y_FOR: F.y = c.value; break;
+      case RK_Z_FOR: F.z = c.value; break;
+      case RK_XROT_MOM: M.x = c.value; break;
+      case RK_YROT_MOM: M.y = c.value; break;
+      case RK_ZROT_MOM: M.z = c.value; break;
+      case RK_XYZROT_MOM: M = v3(c.vec[0], c.vec[1], c.vec[2]); break;
+      default: break;
+    }
+  }
+}
+
+__device__ __forceinline__ void gather_body(const Scene& s, int64_t b, int apply_kick) {
+  const bool driven = b < s.n_driven;
+  V3 F, M;
+  if (s.is_heavy[b] == 2) {
+    // a driven body whose resultant feeds no state (no force / moment
+    // control): summed on demand by k_gather_heavy when downloaded
+    st3(s.acc, b, v3(0, 0, 0));
+    st3(s.arot, b, v3(0, 0, 0));
+    return;
+  }
+  if (s.is_heavy[b]) {  // summed by k_gather_heavy, in the same order
+    F = ld3(s.force, b);
+    M = ld3(s.moment, b);
+  } else {
+    init_resultant(s, b, F, M);
+    // Resultants in the serial order of the active entries (key order): the
+    // j-side entries before b's own block, b's block, the remaining j-side.
+    // Four positions of that sequence are loaded together, then added in
+    // order (same sums, a quarter of the dependent load chains).
+    const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
+    const int64_t j0 = s.jofs[b], j1 = s.jofs[b + 1], js = s.jsplit[b];
+    const int64_t nA = js - j0, nAB = nA + (i1 - i0), L = nAB + (j1 - js);
+    for (int64_t p0 = 0; p0 < L; p0 += 4) {
+      int64_t e[4];
+      bool jside[4], on[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int64_t p = p0 + u;
+        on[u] = p < L;
+        jside[u] = p < nA || p >= nAB;
+        e[u] = !on[u] ? 0 : (p < nA ? (int64_t)s.jlist[j0 + p] : (p < nAB ? i0 + (p - nA) : (int64_t)s.jlist[js + (p - nAB)]));
+      }
+      bool a[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) a[u] = on[u] && s.act[e[u]];
+      V3 f[4], m[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (a[u]) {
+          f[u] = ld3(s.cf, e[u]);
+          m[u] = jside[u] ? ld3(s.cmj, e[u]) : ld3(s.cmi, e[u]);
+        } else {
+          f[u] = v3(0, 0, 0);
+          m[u] = v3(0, 0, 0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (!a[u]) continue;
+        F = jside[u] ? F - f[u] : F + f[u];
+        M = M + m[u];
+      }
+    }
+  }
+  const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
+  const V3 vel = ld3(s.vel, b), vrot = ld3(s.vrot, b);
+  const double mass = s.mass[b];
+  const V3 inertia = ld3(s.inertia, b);
+  const Q4 q = ldq(s.Q, b);
+  if (driven) {
+    V3 acc = v3(0, 0, 0), arot = v3(0, 0, 0);
+    if (s.num_damp > 0.0) {  // Rockable.cpp:3814-3835
+      for (int k = 0; k < s.ncontrols; k++) {
+        const Control c = s.controls[k];
+        if (c.body != b) continue;
+        if (c.type == RK_X_FOR) F.x *= (F.x * vel.x > 0.0) ? fm : fp;
+        else if (c.type == RK_Y_FOR) F.y *= (F.y * vel.y > 0.0) ? fm : fp;
+        else if (c.type == RK_Z_FOR) F.z *= (F.z * vel.z > 0.0) ? fm : fp;
+      }
+    }
+    for (int k = 0; k < s.ncontrols; k++) {  // Rockable.cpp:3448-3507
+      const Control c = s.controls[k];
+      if (c.body != b) continue;
+      switch (c.type) {
+        case RK_X_FOR: acc.x = F.x / mass; break;
+        case RK_Y_FOR: acc.y = F.y / mass; break;
+        case RK_Z_FOR: acc.z = F.z / mass; break;
+        case RK_XROT_MOM: case RK_YROT_MOM: case RK_ZROT_MOM: case RK_XYZROT_MOM: {
+          Q4 qi = qconj(q);
+          V3 w;
+          if (c.type == RK_XROT_MOM) w = v3(vrot.x, 0.0, 0.0);
+          else if (c.type == RK_YROT_MOM) w = v3(0.0, vrot.y, 0.0);
+          else if (c.type == RK_ZROT_MOM) w = v3(0.0, 0.0, vrot.z);
+          else w = vrot;
+          V3 om = qrot(qi, w);
+          V3 Mb = qrot(qi, M);
+          V3 dw = qrot(q, euler_domega(inertia, om, Mb));
+          if (c.type == RK_XROT_MOM) arot.x = dw.x;
+          else if (c.type == RK_YROT_MOM) arot.y = dw.y;
+          else if (c.type == RK_ZROT_MOM) arot.z = dw.z;
+          else arot = dw;
+        } break;
+        default: break;
+      }
+    }
+    V3 v = vel, wr = vrot;
+    if (apply_kick) {  // Rockable.cpp:2084-2117
+      for (int k = 0; k < s.ncontrols; k++) {
+        const Control c = s.controls[k];
+        if (c.body != b) continue;
+        switch (c.type) {
+          case RK_X_FOR: v.x += s.dt_2 * acc.x; break;
+          case RK_Y_FOR: v.y += s.dt_2 * acc.y; break;
+          case RK_Z_FOR: v.z += s.dt_2 * acc.z; break;
+          case RK_XROT_MOM: wr.x += s.dt_2 * arot.x; break;
+          case RK_YROT_MOM: wr.y += s.dt_2 * arot.y; break;
+          case RK_ZROT_MOM: wr.z += s.dt_2 * arot.z; break;
+          case RK_XYZROT_MOM: wr = wr + s.dt_2 * arot; break;
+          default: break;
+        }
+      }
+    }
+    st3(s.acc, b, acc);
+    st3(s.arot, b, arot);
+    st3(s.vel, b, v);
+    st3(s.vrot, b, wr);
+  } else {
+    if (s.num_damp > 0.0) {  // Rockable.cpp:3837-3866
+      double factor = (dot(F, vel) > 0.0) ? fm : fp;
+      F = F * factor;
+      factor = (dot(M, vrot) > 0.0) ? fm : fp;
+      M = M * factor;
+    }
+    V3 acc = vdiv(F, mass) + v3(s.gravity[0], s.gravity[1], s.gravity[2]);
+    Q4 qi = qconj(q);
+    V3 om = qrot(qi, vrot);
+    V3 Mb = qrot(qi, M);
+    V3 arot = qrot(q, euler_domega(inertia, om, Mb));
+    st3(s.acc, b, acc);
+    st3(s.arot, b, arot);
+    if (apply_kick) {
+      st3(s.vel, b, vel + s.dt_2 * acc);
+      st3(s.vrot, b, vrot + s.dt_2 * arot);
+    }
+  }
+  st3(s.force, b, F);
+  st3(s.moment, b, M);
+}
+
+}  // namespace rk
+#endif  // RK_BODY_HELPERS
+
+namespace rk {
+namespace RK_BODY_NS {
+
+// ----------------------------------------------------------------- K1 ----
+__global__ void k_drift(Scene s) {
+  int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.n) return;
+  V3 p = ld3(s.pos, i), v = ld3(s.vel, i), a = ld3(s.acc, i);
+  V3 w = ld3(s.vrot, i), al = ld3(s.arot, i);
+  Q4 q = ldq(s.Q, i);
+  const Q4 q0 = q;
+  const V3 dx = s.dt * v + s.dt2_2 * a;
+  p = p + dx;
+  v = v + s.dt_2 * a;
+  qaddscaled(q, qdot(q, w), s.dt);
+  qaddscaled(q, qddot(q, w, al), s.dt2_2);
+  qnormalize(q);
+  w = w + s.dt_2 * al;
+  if (s.sk_path) {
+    // learned-skin path bound: |dx| plus the rotation angle of the step
+    // (at most 2c(1 + c) for the chord c = |q - q0| of unit quaternions)
+    // times the swing radius, rounded up
+    const float cx = (float)(q.s - q0.s), cy = (float)(q.v.x - q0.v.x), cz = (float)(q.v.y - q0.v.y),
+                cw = (float)(q.v.z - q0.v.z);
+    const float c = sqrtf(cx * cx + cy * cy + cz * cz + cw * cw);
+    const float ex = (float)dx.x, ey = (float)dx.y, ez = (float)dx.z;
+    const float inc = sqrtf(ex * ex + ey * ey + ez * ez) + 2.f * c * (1.f + c) * s.sk_rsw[i];
+    s.sk_path[i] += inc * (1.f + 1e-5f) + 1e-12f;
+  }
+  st3(s.pos, i, p);
+  st3(s.vel, i, v);
+  stq(s.Q, i, q);
+  st3(s.vrot, i, w);
+}
+
+// global vertex k of body b: pos + Q (h v)
+// With only_listed, bodies without a neighbour-list entry are skipped: within
+// a step only the narrow phase reads these positions, and only for bodies in
+// the list; a list update recomputes every body first.
+__global__ void k_glob_vertices(Scene s, int only_listed) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= s.nvert) return;
+  int b = s.gv_body[k];
+  if (only_listed && s.iofs[b + 1] == s.iofs[b] && s.jofs[b + 1] == s.jofs[b]) return;
+  int local = (int)(k - s.gv_ofs[b]);
+  int sh = s.shape[b];
+  double h = s.hom[b];
+  const double* sv = s.svert + 3 * (int64_t)(s.vert_ofs[sh] + local);
+  V3 u = h * v3(sv[0], sv[1], sv[2]);
+  V3 g = ld3(s.pos, b) + qrot(ldq(s.Q, b), u);
+  st3(s.gv, k, g);
+}
+
+__global__ void k_gather_accel(Scene s, int apply_kick) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b < s.n) gather_body(s, b, apply_kick);
+  // the learned skin's guard on the state this step leaves (all lanes)
+  if (s.sk_out && apply_kick) skin_guard_body(s, b);
+}
+
+}  // namespace RK_BODY_NS
+}  // namespace rk

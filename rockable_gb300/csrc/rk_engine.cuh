@@ -117,6 +117,7 @@ struct Scene {
   float* bnd;         // n: largest distance of a vertex from the body centre (world, rounded up)
   int* scene_of;      // n: scene index (bodies of different scenes never interact)
   int near_geometric;  // 1: distance-only NEAR tests in the rebuild (learned skin), 0: Rockable's predicates
+  int fast_body;       // 1: per-body kernels built with fused multiply-adds (mixed form)
   int tpb[4];         // threads per block of the narrow phase, resultants, global vertices, drift (0: default)
   float* sk_path;     // n: path-length bound of each free body since its last refresh (learned skin), or null
   const float* sk_rsw;  // n: swing radius (largest vertex distance from the centre), with sk_path
@@ -161,6 +162,11 @@ int launch_breakage(const Scene& s, cudaStream_t st);
 int launch_guard(const Scene& s, cudaStream_t st);
 int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);
 int max_tpb(int which, int form_mixed);
+// per-body kernels compiled with fused multiply-adds (rk_fast.cu, mixed form)
+int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
+int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st);
+int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
+cudaError_t fused_attributes(int which, cudaFuncAttributes* a);
 cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a);
 
 // learned skin (rk_skin.cu)
