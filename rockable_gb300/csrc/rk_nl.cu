@@ -101,21 +101,45 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
     const double dx = g[3 * v] - s.pos[3 * b], dy = g[3 * v + 1] - s.pos[3 * b + 1], dz = g[3 * v + 2] - s.pos[3 * b + 2];
     const float d = __double2float_ru(sqrt(dx * dx + dy * dy + dz * dz));
     atomicMax(reinterpret_cast<unsigned int*>(s.bnd) + b, __float_as_uint(d));  // non-negative floats order as their bits
-  } else if (local < nv + ne) {  // edge: midpoint, half length
-    const int e = local - nv;
-    V3 a = g3(g, s.edges[2 * (e0 + e)]), c = g3(g, s.edges[2 * (e0 + e) + 1]);
-    V3 m = 0.5 * (a + c);
-    double h = 0.5 * sqrt(norm2(c - a));
-    s.sph[k] = make_float4((float)m.x, (float)m.y, (float)m.z, __double2float_ru(h));
-  } else {  // face: centroid of its vertices, largest vertex distance
-    const int f = local - nv - ne;
-    const int v0 = s.face_vofs[f0 + f], cnt = s.face_vofs[f0 + f + 1] - v0;
-    V3 c = v3(0, 0, 0);
-    for (int q = 0; q < cnt; q++) c = c + g3(g, s.face_verts[v0 + q]);
-    c = (1.0 / cnt) * c;
-    double rf2 = 0.0;
-    for (int q = 0; q < cnt; q++) rf2 = fmax(rf2, norm2(g3(g, s.face_verts[v0 + q]) - c));
-    s.sph[k] = make_float4((float)c.x, (float)c.y, (float)c.z, __double2float_ru(sqrt(rf2)));
+  } else {
+    // Edge (midpoint, half length) or face (centroid, largest vertex
+    // distance), in float on FP64 offsets from the element's first vertex;
+    // the float centre is off the exact one by rounding, so the radius is the
+    // largest distance from that float centre, scaled up by 1e-5 and padded
+    // by 1e-6 of the coordinate magnitude: the sphere still holds the element.
+    const bool edge = local < nv + ne;
+    const int* vl;
+    int cnt;
+    if (edge) {
+      vl = s.edges + 2 * (e0 + (local - nv));
+      cnt = 2;
+    } else {
+      const int f = local - nv - ne;
+      const int v0 = s.face_vofs[f0 + f];
+      vl = s.face_verts + v0;
+      cnt = s.face_vofs[f0 + f + 1] - v0;
+    }
+    const V3 o = g3(g, vl[0]);
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int q = 1; q < cnt; q++) {
+      const V3 d = g3(g, vl[q]) - o;
+      cx += (float)d.x;
+      cy += (float)d.y;
+      cz += (float)d.z;
+    }
+    const float inv = 1.f / (float)cnt;
+    cx *= inv;
+    cy *= inv;
+    cz *= inv;
+    float r2 = cx * cx + cy * cy + cz * cz;  // vertex 0
+    for (int q = 1; q < cnt; q++) {
+      const V3 d = g3(g, vl[q]) - o;
+      const float ex = (float)d.x - cx, ey = (float)d.y - cy, ez = (float)d.z - cz;
+      r2 = fmaxf(r2, ex * ex + ey * ey + ez * ez);
+    }
+    const float px = (float)(o.x + (double)cx), py = (float)(o.y + (double)cy), pz = (float)(o.z + (double)cz);
+    const float mag = fmaxf(fmaxf(fabsf(px), fabsf(py)), fabsf(pz));
+    s.sph[k] = make_float4(px, py, pz, sqrtf(r2) * (1.f + 1e-5f) + 1e-6f * mag + 1e-9f);
   }
 }
 
@@ -631,17 +655,47 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
       Obb op = load_obb(s.bobb + 15 * p);
       enlarge(op, P.dmax);
       const double r = P.Rb + P.dmax;
+      // Float pre-test along the partner box's own axes (the first three
+      // axes of the separating-axis test): separated there by more than the
+      // rounding margin -> the FP64 test is false as well; the vertex inside
+      // the box shrunk by the margin -> the FP64 test is true as well; only
+      // the cases in between run the FP64 test, so the mask is unchanged.
+      const float fcx = (float)op.c.x, fcy = (float)op.c.y, fcz = (float)op.c.z;
+      const float fe[3][3] = {{(float)op.e0.x, (float)op.e0.y, (float)op.e0.z},
+                              {(float)op.e1.x, (float)op.e1.y, (float)op.e1.z},
+                              {(float)op.e2.x, (float)op.e2.y, (float)op.e2.z}};
+      const float fext[3] = {(float)op.ext.x, (float)op.ext.y, (float)op.ext.z};
+      const float fr = (float)r;
+      const float4* sbv = s.sph + s.sph_ofs[b];
+      const float mag = fmaxf(fmaxf(fabsf(fcx), fabsf(fcy)), fabsf(fcz)) + fext[0] + fext[1] + fext[2] + fr;
       bool hit0 = false, hit1 = false;
       for (int half = 0; half < 2; half++) {
         const int v = lane + 32 * half;
         if (v < nvb) {
-          Obb sub;
-          sub.c = g3(P.gb, v);
-          sub.e0 = v3(1, 0, 0);
-          sub.e1 = v3(0, 1, 0);
-          sub.e2 = v3(0, 0, 1);
-          sub.ext = v3(r, r, r);
-          const bool hit = obb_intersect(op, sub);
+          const float4 pv = sbv[v];
+          const float dx = pv.x - fcx, dy = pv.y - fcy, dz = pv.z - fcz;
+          bool out = false, in = true;
+          for (int i = 0; i < 3; i++) {
+            const float t = fabsf(dx * fe[i][0] + dy * fe[i][1] + dz * fe[i][2]);
+            const float lim = fext[i] + fr * (fabsf(fe[i][0]) + fabsf(fe[i][1]) + fabsf(fe[i][2]));
+            const float m = 1e-6f * (mag + t) + 1e-9f;
+            out = out || t > lim + m;
+            in = in && t < fext[i] - m;
+          }
+          bool hit;
+          if (out) {
+            hit = false;
+          } else if (in) {
+            hit = true;
+          } else {
+            Obb sub;
+            sub.c = g3(P.gb, v);
+            sub.e0 = v3(1, 0, 0);
+            sub.e1 = v3(0, 1, 0);
+            sub.e2 = v3(0, 0, 1);
+            sub.ext = v3(r, r, r);
+            hit = obb_intersect(op, sub);
+          }
           if (half == 0) hit0 = hit;
           else hit1 = hit;
         }
