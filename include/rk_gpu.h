@@ -216,10 +216,10 @@ int rk_set_scenes(rk_ctx* ctx, const int32_t* scene_of);
 int rk_set_graphs(rk_ctx* ctx, int on);
 /* Number of step-graph captures and replays since the context was created. */
 int rk_get_graph_stats(const rk_ctx* ctx, int64_t* captures, int64_t* replays);
-/* Block-size autotuner: the next 4 * rounds steps run the narrow phase, the
- * resultants, the global vertices and the drift with block sizes 64, 128,
- * 256 and 512 in turn, timed with events; each kernel then keeps its fastest
- * size.  These kernels give the same results at any block size, so the
+/* Block-size autotuner: the next 5 * rounds steps run the narrow phase, the
+ * resultants, the global vertices and the drift with block sizes 32, 64,
+ * 128, 256 and 512 in turn, timed with events; each kernel then keeps its
+ * fastest size.  These kernels give the same results at any block size, so the
  * tuning steps are ordinary steps.  No reference counterpart. */
 int rk_set_autotune(rk_ctx* ctx, int rounds);
 /* Current block sizes of those four kernels, in that order. */

@@ -469,16 +469,17 @@ static int step_launches(Ctx& c) {
 
 // Online block-size tuning: during the first steps after rk_set_autotune,
 // step k launches the four tuned kernels (narrow phase, resultants, global
-// vertices, drift) with candidate block size k mod 4, timed with events;
+// vertices, drift) with candidate block size k mod 5, timed with events;
 // then each kernel keeps its fastest size.  Every thread of these kernels
 // works on its own entry, body or vertex (ordered sums included), so the
 // block size changes no result and the tuning steps are ordinary steps.
-static const int kTuneCand[4] = {64, 128, 256, 512};
+static const int kTuneCand[5] = {32, 64, 128, 256, 512};
+constexpr int kNumCand = 5;
 
 static int tune_step(Ctx& c) {
   Scene& s = c.s;
   const int64_t done = c.tune_total - c.tune_left;
-  const int ci = (int)(done % 4);
+  const int ci = (int)(done % kNumCand);
   for (int k = 0; k < 4; k++) s.tpb[k] = std::min(kTuneCand[ci], max_tpb(k, c.form == RK_FORM_MIXED));
   cudaStream_t st = c.stream;
   int n = launch_controls_pre(s, st);
@@ -504,8 +505,8 @@ static int tune_step(Ctx& c) {
   for (int k = 0; k < 4; k++) c.tune_ms[k][ci] += ms[k];
   if (--c.tune_left == 0) {
     for (int k = 0; k < 4; k++) {
-      int best = 1;
-      for (int q = 0; q < 4; q++)
+      int best = 2;
+      for (int q = 0; q < kNumCand; q++)
         if (c.tune_ms[k][q] < c.tune_ms[k][best]) best = q;
       s.tpb[k] = std::min(kTuneCand[best], max_tpb(k, c.form == RK_FORM_MIXED));
     }
@@ -1240,7 +1241,7 @@ int rk_set_autotune(rk_ctx* x, int rounds) {
     if (!c.tev[k]) CK(cudaEventCreate(&c.tev[k]));
   for (auto& row : c.tune_ms)
     for (double& v : row) v = 0.0;
-  c.tune_total = c.tune_left = 4 * (int64_t)rounds;
+  c.tune_total = c.tune_left = kNumCand * (int64_t)rounds;
   return RK_OK;
 }
 

@@ -145,7 +145,7 @@ struct Ctx {
   std::vector<uint8_t> needres_host;
   // block-size autotuner of the step kernels (results do not depend on it)
   int64_t tune_left = 0, tune_total = 0;
-  double tune_ms[4][4] = {};
+  double tune_ms[4][5] = {};  // [kernel][candidate block size]
   cudaEvent_t tev[8] = {};
   // CUDA graph of one step's launches (re-captured when the scene changes)
   int use_graphs = 0;
