@@ -73,6 +73,7 @@ struct Scene {
   int* gv_body;      // nvert
   double* gv;        // 3*nvert
   double* bobb;      // 15 per body (placed OBB, not enlarged)
+  float* bobbf;      // float copy of bobb
   float* baabb;      // 6 per body: outward-rounded AABB of the OBB enlarged by DVerlet/2
   // dynamic guard
   double *dpos, *dq;  // 3n, 4n

@@ -66,6 +66,8 @@ __global__ void k_body_obb(Scene s) {
   out[6] = o.e1.x; out[7] = o.e1.y; out[8] = o.e1.z;
   out[9] = o.e2.x; out[10] = o.e2.y; out[11] = o.e2.z;
   out[12] = o.ext.x; out[13] = o.ext.y; out[14] = o.ext.z;
+  float* of = s.bobbf + 15 * b;  // float copy for the pair test's pre-classification
+  for (int q = 0; q < 15; q++) of[q] = (float)out[q];
   const double d = 0.5 * s.DVerlet;
   const double ex = o.ext.x + d, ey = o.ext.y + d, ez = o.ext.z + d;
   const double hw[3] = {ex * fabs(o.e0.x) + ey * fabs(o.e1.x) + ez * fabs(o.e2.x),
@@ -192,6 +194,45 @@ __device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
   return lo < s.if_ofs[i + 1] && s.if_j[lo] == j && !s.if_broken[lo];
 }
 
+// The FP64 separating-axis test of two placed boxes enlarged by DVerlet/2
+// (Rockable.cpp:1627-1654), decided in float where the answer is clear: a
+// separation along one of the six face axes by more than the rounding
+// margin makes the FP64 test false as well, and one box's centre inside the
+// other (shrunk by the margin) makes it true as well; only the cases in
+// between run the FP64 test, so the result is the FP64 test's.
+__device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, int64_t j) {
+  const float* A = s.bobbf + 15 * i;
+  const float* B = s.bobbf + 15 * j;
+  const float d = 0.5f * (float)s.DVerlet;
+  const float ea[3] = {A[12] + d, A[13] + d, A[14] + d}, eb[3] = {B[12] + d, B[13] + d, B[14] + d};
+  const float tx = B[0] - A[0], ty = B[1] - A[1], tz = B[2] - A[2];
+  float R[3][3];
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++)
+      R[a][b] = A[3 + 3 * a] * B[3 + 3 * b] + A[4 + 3 * a] * B[4 + 3 * b] + A[5 + 3 * a] * B[5 + 3 * b];
+  const float mag = fmaxf(fmaxf(fabsf(A[0]), fabsf(A[1])), fabsf(A[2])) + fmaxf(fmaxf(fabsf(B[0]), fabsf(B[1])), fabsf(B[2])) +
+                    ea[0] + ea[1] + ea[2] + eb[0] + eb[1] + eb[2];
+  const float m = 1e-6f * mag + 1e-9f;
+  bool in_a = true, in_b = true;
+  for (int a = 0; a < 3; a++) {  // face axes of A
+    const float t = fabsf(tx * A[3 + 3 * a] + ty * A[4 + 3 * a] + tz * A[5 + 3 * a]);
+    const float r = ea[a] + eb[0] * fabsf(R[a][0]) + eb[1] * fabsf(R[a][1]) + eb[2] * fabsf(R[a][2]);
+    if (t > r + m) return false;
+    in_a = in_a && t < ea[a] - m;
+  }
+  for (int b = 0; b < 3; b++) {  // face axes of B
+    const float t = fabsf(tx * B[3 + 3 * b] + ty * B[4 + 3 * b] + tz * B[5 + 3 * b]);
+    const float r = eb[b] + ea[0] * fabsf(R[0][b]) + ea[1] * fabsf(R[1][b]) + ea[2] * fabsf(R[2][b]);
+    if (t > r + m) return false;
+    in_b = in_b && t < eb[b] - m;
+  }
+  if (in_a || in_b) return true;
+  Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
+  enlarge(oi, 0.5 * s.DVerlet);
+  enlarge(oj, 0.5 * s.DVerlet);
+  return obb_intersect(oi, oj);
+}
+
 // All-pairs broad phase: float AABB filter (tiled through shared memory),
 // then eligibility and the FP64 SAT of the enlarged OBBs.
 constexpr int kPairTile = 128;
@@ -220,10 +261,7 @@ __global__ void k_pairs(Scene s, const uint8_t* only, uint64_t* pairs, int64_t c
       if (only && !only[i] && !only[j]) continue;
       if (s.scene_of && s.scene_of[i] != s.scene_of[j]) continue;
       if (has_iface(s, (int)i, (int)j)) continue;
-      Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
-      enlarge(oi, 0.5 * s.DVerlet);
-      enlarge(oj, 0.5 * s.DVerlet);
-      if (!obb_intersect(oi, oj)) continue;
+      if (!obb_pair_intersect(s, i, j)) continue;
       unsigned long long k = atomicAdd(counter, 1ull);
       if ((int64_t)k < cap) pairs[k] = ((uint64_t)i << 21) | (uint64_t)j;
     }
@@ -246,10 +284,7 @@ __device__ __forceinline__ bool pair_predicate(const Scene& s, int64_t i, int64_
   const float* b = s.baabb + 6 * j;
   if (a[0] > b[3] || b[0] > a[3] || a[1] > b[4] || b[1] > a[4] || a[2] > b[5] || b[2] > a[5]) return false;
   if (has_iface(s, (int)i, (int)j)) return false;
-  Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
-  enlarge(oi, 0.5 * s.DVerlet);
-  enlarge(oj, 0.5 * s.DVerlet);
-  return obb_intersect(oi, oj);
+  return obb_pair_intersect(s, i, j);
 }
 
 __device__ __forceinline__ float extent_of(const float* bb) {
