@@ -525,6 +525,27 @@ __device__ __forceinline__ float pt_seg_d2(G3 p, G3 a, G3 b) {
   return gdot(d, d);
 }
 
+// squared distance of a point to the line through a and b
+__device__ __forceinline__ float pt_line_d2(G3 p, G3 a, G3 b) {
+  const G3 ab = gsub(b, a), ap = gsub(p, a);
+  const float l2 = gdot(ab, ab);
+  const float t = l2 > 0.f ? gdot(ap, ab) / l2 : 0.f;
+  const G3 d = gmad(ap, -t, ab);
+  return gdot(d, d);
+}
+
+// true when the lines through two segments are farther apart than sqrt(lim2)
+// (the line distance bounds the segment distance from below); never for
+// nearly parallel lines, where that distance is ill-conditioned
+__device__ __forceinline__ bool lines_far(G3 p1, G3 q1, G3 p2, G3 q2, float lim2) {
+  const G3 d1 = gsub(q1, p1), d2 = gsub(q2, p2), r = gsub(p1, p2);
+  const G3 n = gcross(d1, d2);
+  const float nn = gdot(n, n);
+  if (!(nn > 1e-6f * gdot(d1, d1) * gdot(d2, d2))) return false;
+  const float rn = gdot(r, n);
+  return rn * rn > lim2 * nn;
+}
+
 // squared distance of two segments: the closest-point parameters minimise
 // |p1 + s d1 - p2 - t d2| over [0,1]^2 (interior stationary point, else the
 // best clamped edge of the square)
@@ -809,7 +830,12 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
           ok = !far(sb[v], se, se.w) &&
                pt_seg_d2(gpt(sb[v]), gpt(sp[s.edges[2 * eo]]), gpt(sp[s.edges[2 * eo + 1]])) <= glim2;
         } else {
-          ok = !far(sb[v], se, ve_ext * se.w) && near_ve(s, P, v, e);
+          // exact rejection first: Rockable's vertex-edge test accepts a
+          // projection slightly off the edge, never a line distance above it
+          const int eo = s.edge_ofs[P.sp] + e;
+          ok = !far(sb[v], se, ve_ext * se.w) &&
+               pt_line_d2(gpt(sb[v]), gpt(sp[s.edges[2 * eo]]), gpt(sp[s.edges[2 * eo + 1]])) <= glim2 &&
+               near_ve(s, P, v, e);
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 1u, (uint32_t)v, (uint32_t)e), lane, out, cap, counter);
@@ -824,7 +850,8 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         f = L.pf[c % npf];
         const float4 sf = sp[nvp + nep + f];
         if (GEOM) ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2;
-        else ok = !far(sb[v], sf, sf.w) && near_vf(s, P, v, f);
+        else  // exact rejection first: NEAR needs the polygon within reach
+          ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2 && near_vf(s, P, v, f);
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 2u, (uint32_t)v, (uint32_t)f), lane, out, cap, counter);
     }
@@ -838,12 +865,21 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         e2 = L.pe[c % npe];
         const float4 s1 = sb[nvb + e1], s2 = sp[nvp + e2];
         if (GEOM) {
+          // nearly parallel edges (ill-conditioned closest points) within
+          // sphere reach are kept: an extra entry is harmless, a missing one not
+          const int ob = s.edge_ofs[P.sb] + e1, op = s.edge_ofs[P.sp] + e2;
+          const G3 a0 = gpt(sb[s.edges[2 * ob]]), a1 = gpt(sb[s.edges[2 * ob + 1]]);
+          const G3 b0 = gpt(sp[s.edges[2 * op]]), b1 = gpt(sp[s.edges[2 * op + 1]]);
+          const G3 d1 = gsub(a1, a0), d2 = gsub(b1, b0), nx = gcross(d1, d2);
+          const bool parallel = !(gdot(nx, nx) > 1e-6f * gdot(d1, d1) * gdot(d2, d2));
+          ok = !far(s1, s2, s1.w + s2.w) && (parallel || seg_seg_d2(a0, a1, b0, b1) <= glim2);
+        } else {
+          // exact rejection first: NEAR needs the edges' lines within reach
           const int ob = s.edge_ofs[P.sb] + e1, op = s.edge_ofs[P.sp] + e2;
           ok = !far(s1, s2, s1.w + s2.w) &&
-               seg_seg_d2(gpt(sb[s.edges[2 * ob]]), gpt(sb[s.edges[2 * ob + 1]]), gpt(sp[s.edges[2 * op]]),
-                          gpt(sp[s.edges[2 * op + 1]])) <= glim2;
-        } else {
-          ok = !far(s1, s2, s1.w + s2.w) && near_ee(s, P, e1, e2);
+               !lines_far(gpt(sb[s.edges[2 * ob]]), gpt(sb[s.edges[2 * ob + 1]]), gpt(sp[s.edges[2 * op]]),
+                          gpt(sp[s.edges[2 * op + 1]]), glim2) &&
+               near_ee(s, P, e1, e2);
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 3u, (uint32_t)e1, (uint32_t)e2), lane, out, cap, counter);
