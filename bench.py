@@ -459,22 +459,21 @@ def main():
     # ---- e2e through the C ABI with host-owned state (headline form)
     e2e = None
     if not a.no_e2e:
-        hb = {k: pinned((N, 4 if k == "Q" else 3)) for k in ["pos", "vel", "acc", "Q", "vrot", "arot"]}
-        cur = g.bodies()
-        for k in hb:
-            hb[k][...] = cur[k]
+        hb = pinned((19 * N,))  # packed pos | vel | acc | Q | vrot | arot
+        g.download_kinematics_packed(hb)
         k_e2e = max(5, min(a.steps, 50))
         g.synchronize()
         t0 = time.perf_counter()
         for _ in range(k_e2e):
-            g.upload_kinematics(hb["pos"], hb["vel"], hb["acc"], hb["Q"], hb["vrot"], hb["arot"])
+            g.upload_kinematics_packed(hb)
             g.step(1)
-            g.bodies(out=hb)
+            g.download_kinematics_packed(hb)
         el = time.perf_counter() - t0
         e2e = {"value": ws * nfree * k_e2e / el, "unit": "particle-steps/s",
                "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8),
-               "steps": k_e2e, "note": "every step: kinematics (pos, vel, acc, Q, vrot, arot) H2D from pinned host, "
-                                       "rk_step(1), the same fields D2H into the pinned buffers"}
+               "steps": k_e2e, "note": "every step: the kinematics (pos, vel, acc, Q, vrot, arot) of every body "
+                                       "H2D from one pinned packed buffer, rk_step(1), the same fields D2H back "
+                                       "(rk_upload/download_kinematics_packed)"}
     batched = None
     if rank == 0 and a.batch_scenes > 0:
         batched = batched_workload(a, dev)

@@ -248,6 +248,15 @@ int rk_download_interfaces(rk_ctx* ctx, int32_t* i, int32_t* j, uint8_t* broken)
  * after a host-side plugin modified them. */
 int rk_upload_kinematics(rk_ctx* ctx, const double* pos, const double* vel, const double* acc, const double* Q,
                          const double* vrot, const double* arot);
+/* The same kinematics in one packed host buffer of 19 n doubles, in this
+ * order: pos (3n), vel (3n), acc (3n), Q (4n), vrot (3n), arot (3n).  One
+ * copy and one scatter (upload, asynchronous: keep the buffer alive until the
+ * next synchronising call) or one gather and one copy (download, returns when
+ * the buffer is filled).  With a pinned buffer this is the cheapest way to
+ * hand the bodies' state to and from the host every step.  No reference
+ * counterpart (Rockable keeps the state in host memory). */
+int rk_upload_kinematics_packed(rk_ctx* ctx, const double* buf);
+int rk_download_kinematics_packed(rk_ctx* ctx, double* buf);
 int rk_get_stats(rk_ctx* ctx, rk_stats* out);
 /* Device time (ms) of the last rk_step call, measured with CUDA events on the
  * context's stream, and the number of kernels it launched. */

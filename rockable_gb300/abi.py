@@ -125,6 +125,8 @@ SIGNATURES = {
     "rk_set_profiling": (C.c_int, [P, C.c_int]),
     "rk_get_profile": (C.c_int, [P, P, P]),
     "rk_sort_keys": (C.c_int, [P, I64, C.c_int, C.c_int, P]),
+    "rk_upload_kinematics_packed": (C.c_int, [P, P]),
+    "rk_download_kinematics_packed": (C.c_int, [P, P]),
     "rk_sort_keys_noalloc": (C.c_int, [P, I64, C.c_int, C.c_int, P]),
     "rk_set_skin": (C.c_int, [P, C.POINTER(RkSkinConfig)]),
     "rk_get_skin_stats": (C.c_int, [P, C.POINTER(RkSkinStats)]),
@@ -305,6 +307,19 @@ class GpuScene:
         """Host arrays must stay alive until the next synchronising call."""
         self._chk(self.L.rk_upload_kinematics(self.h, _p(pos), _p(vel), _p(acc), _p(Q), _p(vrot), _p(arot)),
                   "rk_upload_kinematics")
+
+    def upload_kinematics_packed(self, buf):
+        """buf: C-contiguous float64 array of 19 n values (pos, vel, acc, Q,
+        vrot, arot); must stay alive until the next synchronising call."""
+        if buf.dtype != np.float64 or not buf.flags["C_CONTIGUOUS"] or buf.size != 19 * self.n:
+            raise ValueError("packed kinematics: a C-contiguous float64 array of 19 x %d values" % self.n)
+        self._chk(self.L.rk_upload_kinematics_packed(self.h, _p(buf)), "rk_upload_kinematics_packed")
+
+    def download_kinematics_packed(self, buf):
+        if buf.dtype != np.float64 or not buf.flags["C_CONTIGUOUS"] or buf.size != 19 * self.n:
+            raise ValueError("packed kinematics: a C-contiguous float64 array of 19 x %d values" % self.n)
+        self._chk(self.L.rk_download_kinematics_packed(self.h, _p(buf)), "rk_download_kinematics_packed")
+        return buf
 
     def set_profiling(self, on=True):
         self._chk(self.L.rk_set_profiling(self.h, 1 if on else 0), "rk_set_profiling")

@@ -253,6 +253,16 @@ static int skin_train(Ctx& c) {
   return 0;
 }
 
+// Device staging buffer of the packed kinematics transfers (19 doubles per body).
+static int ensure_kin_stage(Ctx& c) {
+  if (c.kin_stage_n < c.s.n) {
+    int rc;
+    if ((rc = dalloc(c, c.kin_stage, 19 * c.s.n))) return rc;
+    c.kin_stage_n = c.s.n;
+  }
+  return 0;
+}
+
 // Scene fields of the fused guard (null when the skin is off).  Bodies past
 // half of their budget are flagged, to be refreshed together with the one
 // that reached it.
@@ -722,6 +732,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(w.tmp); dfree(w.counter); dfree(w.gkeys); dfree(w.gtmp); dfree(w.gover); dfree(w.gis_over);
   if (w.gstat) cudaFree(w.gstat);
   if (w.split) cudaEventDestroy(w.split);
+  dfree(c.kin_stage);
   dfree(c.d_ke);
   {
     Skin& k = c.skin;
@@ -1564,6 +1575,31 @@ int rk_upload_kinematics(rk_ctx* x, const double* pos, const double* vel, const 
   if (Q) CK(cudaMemcpyAsync(s.Q, Q, 4 * (size_t)s.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
   if (vrot) CK(cudaMemcpyAsync(s.vrot, vrot, n3, cudaMemcpyHostToDevice, c.stream));
   if (arot) CK(cudaMemcpyAsync(s.arot, arot, n3, cudaMemcpyHostToDevice, c.stream));
+  return RK_OK;
+}
+
+int rk_upload_kinematics_packed(rk_ctx* x, const double* buf) {
+  if (!x || !buf) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies first");
+  int rc;
+  if ((rc = ensure_kin_stage(c))) return rc;
+  CK(cudaMemcpyAsync(c.kin_stage, buf, 19 * (size_t)c.s.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  c.kernels += launch_kin_pack(c.s, c.kin_stage, 0, c.stream);
+  return RK_OK;
+}
+
+int rk_download_kinematics_packed(rk_ctx* x, double* buf) {
+  if (!x || !buf) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies first");
+  int rc;
+  if ((rc = ensure_kin_stage(c))) return rc;
+  c.kernels += launch_kin_pack(c.s, c.kin_stage, 1, c.stream);
+  CK(cudaMemcpyAsync(buf, c.kin_stage, 19 * (size_t)c.s.n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
   return RK_OK;
 }
 

@@ -142,6 +142,8 @@ struct Ctx {
   bool forces_stale = false;
   bool more_steps_follow = false;  // inside rk_step, before its last step
   int64_t nsph = 0;                // sub-element spheres of all bodies
+  double* kin_stage = nullptr;     // packed kinematics transfers (19 doubles per body)
+  int64_t kin_stage_n = 0;
   std::vector<uint8_t> needres_host;
   // block-size autotuner of the step kernels (results do not depend on it)
   int64_t tune_left = 0, tune_total = 0;

@@ -162,6 +162,7 @@ int launch_gather_heavy_lazy(const Scene& s, cudaStream_t st);
 int launch_breakage(const Scene& s, cudaStream_t st);
 int launch_guard(const Scene& s, cudaStream_t st);
 int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);
+int launch_kin_pack(const Scene& s, double* stage, int dir, cudaStream_t st);
 int max_tpb(int which, int form_mixed);
 // per-body kernels compiled with fused multiply-adds (rk_fast.cu, mixed form)
 int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);

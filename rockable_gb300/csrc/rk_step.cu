@@ -612,6 +612,35 @@ int launch_guard(const Scene& s, cudaStream_t st) {
   k_guard_finalize<<<1, 32, 0, st>>>(s);
   return 2;
 }
+// Packed kinematics: stage = pos (3n) | vel (3n) | acc (3n) | Q (4n) |
+// vrot (3n) | arot (3n); dir 0 scatters it into the body arrays, 1 gathers.
+__global__ void k_kin_pack(Scene s, double* stage, int dir) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t n = s.n;
+  if (k >= 19 * n) return;
+  double* dst;
+  int64_t off;
+  if (k < 9 * n) {
+    const int64_t a = k / (3 * n);
+    off = k - a * 3 * n;
+    dst = a == 0 ? s.pos : (a == 1 ? s.vel : s.acc);
+  } else if (k < 13 * n) {
+    off = k - 9 * n;
+    dst = s.Q;
+  } else {
+    const int64_t a = (k - 13 * n) / (3 * n);
+    off = k - 13 * n - a * 3 * n;
+    dst = a == 0 ? s.vrot : s.arot;
+  }
+  if (dir == 0) dst[off] = stage[k];
+  else stage[k] = dst[off];
+}
+int launch_kin_pack(const Scene& s, double* stage, int dir, cudaStream_t st) {
+  if (s.n <= 0) return 0;
+  k_kin_pack<<<nblk(19 * s.n, 256), 256, 0, st>>>(s, stage, dir);
+  return 1;
+}
+
 int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st) {
   if (s.n <= 0) return 0;
   k_kinetic<<<nblk(s.n, 256), 256, 0, st>>>(s, d_out2);

@@ -92,3 +92,28 @@ def test_autotuned_block_sizes_change_no_result(gpu_lib):
             assert bitwise_equal(ba[k], bb[k]), (form, k)
         a.close()
         b.close()
+
+
+def test_packed_kinematics_round_trip(gpu_lib):
+    """rk_download/upload_kinematics_packed move exactly the six kinematic
+    arrays, in the documented order."""
+    from rockable_gb300 import scenes
+    scene = scenes.column_collapse(n=700, nshapes=16)
+    g = _engine(scene)
+    g.step(20)
+    n = g.n
+    buf = np.zeros(19 * n)
+    g.download_kinematics_packed(buf)
+    b = g.bodies()
+    parts = np.split(buf, np.cumsum([3 * n, 3 * n, 3 * n, 4 * n, 3 * n]))
+    for k, part in zip(["pos", "vel", "acc", "Q", "vrot", "arot"], parts):
+        assert bitwise_equal(part, b[k].ravel()), k
+    rng = np.random.default_rng(3)
+    new = rng.normal(size=19 * n)
+    g.upload_kinematics_packed(new)
+    g.synchronize()
+    b2 = g.bodies()
+    parts = np.split(new, np.cumsum([3 * n, 3 * n, 3 * n, 4 * n, 3 * n]))
+    for k, part in zip(["pos", "vel", "acc", "Q", "vrot", "arot"], parts):
+        assert bitwise_equal(part, b2[k].ravel()), k
+    g.close()
