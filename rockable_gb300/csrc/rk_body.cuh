@@ -54,16 +54,8 @@ __device__ __forceinline__ void init_resultant(const Scene& s, int64_t b, V3& F,
   }
 }
 
-__device__ __forceinline__ void gather_body(const Scene& s, int64_t b, int apply_kick) {
-  const bool driven = b < s.n_driven;
-  V3 F, M;
-  if (s.is_heavy[b] == 2) {
-    // a driven body whose resultant feeds no state (no force / moment
-    // control): summed on demand by k_gather_heavy when downloaded
-    st3(s.acc, b, v3(0, 0, 0));
-    st3(s.arot, b, v3(0, 0, 0));
-    return;
-  }
+// Resultant force and moment of body b (is_heavy 0 or 1) in the serial order.
+__device__ __forceinline__ void body_resultant(const Scene& s, int64_t b, V3& F, V3& M) {
   if (s.is_heavy[b]) {  // summed by k_gather_heavy, in the same order
     F = ld3(s.force, b);
     M = ld3(s.moment, b);
@@ -108,6 +100,19 @@ __device__ __forceinline__ void gather_body(const Scene& s, int64_t b, int apply
       }
     }
   }
+}
+
+__device__ __forceinline__ void gather_body(const Scene& s, int64_t b, int apply_kick) {
+  const bool driven = b < s.n_driven;
+  if (s.is_heavy[b] == 2) {
+    // a driven body whose resultant feeds no state (no force / moment
+    // control): summed on demand by k_gather_heavy when downloaded
+    st3(s.acc, b, v3(0, 0, 0));
+    st3(s.arot, b, v3(0, 0, 0));
+    return;
+  }
+  V3 F, M;
+  body_resultant(s, b, F, M);
   const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
   const V3 vel = ld3(s.vel, b), vrot = ld3(s.vrot, b);
   const double mass = s.mass[b];
@@ -232,14 +237,14 @@ __global__ void k_drift(Scene s) {
 }
 
 // global vertex k of body b: pos + Q (h v)
-// With only_listed, bodies without a neighbour-list entry are skipped: within
-// a step only the narrow phase reads these positions, and only for bodies in
-// the list; a list update recomputes every body first.
+// With only_listed, the vertices of s.lv (the bodies with neighbour-list
+// entries): within a step only the narrow phase reads these positions, and
+// only for bodies in the list; a list update recomputes every body first.
 __global__ void k_glob_vertices(Scene s, int only_listed) {
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= s.nvert) return;
+  if (k >= (only_listed ? s.nlv : s.nvert)) return;
+  if (only_listed) k = s.lv[k];
   int b = s.gv_body[k];
-  if (only_listed && s.iofs[b + 1] == s.iofs[b] && s.jofs[b + 1] == s.jofs[b]) return;
   int local = (int)(k - s.gv_ofs[b]);
   int sh = s.shape[b];
   double h = s.hom[b];

@@ -71,6 +71,8 @@ struct Scene {
   int64_t nvert;     // total global vertices
   int64_t* gv_ofs;   // n+1
   int* gv_body;      // nvert
+  int* lv;           // nvert: vertices of the bodies that have neighbour-list entries (nlv of them)
+  int64_t nlv;
   double* gv;        // 3*nvert
   double* bobb;      // 15 per body (placed OBB, not enlarged)
   float* bobbf;      // float copy of bobb
@@ -168,6 +170,7 @@ int max_tpb(int which, int form_mixed);
 int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st);
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
+int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);
 cudaError_t fused_attributes(int which, cudaFuncAttributes* a);
 cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a);
 

@@ -1,15 +1,224 @@
-// rk_fast.cu -- the per-body kernels of rk_body.cuh compiled with fused
-// multiply-adds allowed, for the mixed form (see rk_body.cuh).
+// rk_fast.cu -- per-body kernels of the mixed form.
+//
+// The generic per-body kernels of rk_body.cuh are compiled here a second time
+// with fused multiply-adds allowed (namespace rk::fused); the mixed form uses
+// them for the world vertices and for driven bodies.  Free bodies take the
+// kernels of namespace rk::mx, written for GB300's FP64 rate (about 1/77 of
+// its FP32 rate, and a hardware FP64 <-> FP32 conversion costs as much as an
+// FP64 add): the state (positions, velocities, quaternions, angular
+// velocities) stays FP64 and is advanced by FP64 additions of increments
+// computed in FP32 -- dt v + dt^2/2 a, dt/2 a, the quaternion derivative terms
+// and its normalisation -- and the Newton-Euler update runs in FP32 from the
+// FP64 resultants (the force plus m g summed in FP64 first, so that a body at
+// rest keeps a small acceleration to float precision).  Conversions use the
+// integer-pipe routines of rk_bits.cuh.  An increment's relative error is
+// 2^-24 (6e-8): a position moves by dt v ~ 1e-6 m per step, so its error is
+// ~1e-13 m against contact overlaps of 1e-8 m and more.
 #include "../../include/rk_gpu.h"
+#include "rk_bits.cuh"
 #include "rk_engine.cuh"
 #include "rk_guard.cuh"
 #define RK_BODY_NS fused
 #include "rk_body.cuh"
 
 namespace rk {
+namespace mx {
+
+struct f3v {
+  float x, y, z;
+};
+struct q4f {
+  float s, x, y, z;
+};
+__device__ __forceinline__ f3v mk3(float x, float y, float z) {
+  f3v r;
+  r.x = x; r.y = y; r.z = z;
+  return r;
+}
+__device__ __forceinline__ q4f mk4(float s, float x, float y, float z) {
+  q4f r;
+  r.s = s; r.x = x; r.y = y; r.z = z;
+  return r;
+}
+__device__ __forceinline__ f3v operator+(f3v a, f3v b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3v operator*(float k, f3v a) { return mk3(k * a.x, k * a.y, k * a.z); }
+__device__ __forceinline__ f3v crossf(f3v a, f3v b) {
+  return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float dotf(f3v a, f3v b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3v cvt3(V3 a) { return mk3(d2f(a.x), d2f(a.y), d2f(a.z)); }
+__device__ __forceinline__ q4f cvt4(Q4 q) { return mk4(d2f(q.s), d2f(q.v.x), d2f(q.v.y), d2f(q.v.z)); }
+__device__ __forceinline__ f3v ld3f(const double* a, int64_t k) { return mk3(d2f(a[3 * k]), d2f(a[3 * k + 1]), d2f(a[3 * k + 2])); }
+// FP64 a + FP32 increment d (one FP64 add per component)
+__device__ __forceinline__ V3 addinc(V3 a, f3v d) { return v3(a.x + f2d(d.x), a.y + f2d(d.y), a.z + f2d(d.z)); }
+__device__ __forceinline__ void st3f(double* a, int64_t k, f3v v) {
+  a[3 * k] = f2d(v.x);
+  a[3 * k + 1] = f2d(v.y);
+  a[3 * k + 2] = f2d(v.z);
+}
+
+// u rotated by the unit quaternion q: t = 2 v x u; u + s t + v x t
+__device__ __forceinline__ f3v qrotf(q4f q, f3v u) {
+  const f3v v = mk3(q.x, q.y, q.z);
+  const f3v t = 2.f * crossf(v, u);
+  return u + q.s * t + crossf(v, t);
+}
+// dQ/dt = 1/2 (0, w) (x) Q and d2Q/dt2 = 1/2 (0, a) (x) Q - 1/4 |w|^2 Q
+__device__ __forceinline__ q4f qdotf(q4f q, f3v w) {
+  const f3v v = mk3(q.x, q.y, q.z);
+  const f3v r = 0.5f * (q.s * w + crossf(w, v));
+  return mk4(-0.5f * dotf(w, v), r.x, r.y, r.z);
+}
+__device__ __forceinline__ q4f qddotf(q4f q, f3v w, f3v a) {
+  const f3v v = mk3(q.x, q.y, q.z);
+  const float w2 = 0.25f * dotf(w, w);
+  const f3v r = 0.5f * (q.s * a + crossf(a, v));
+  return mk4(-0.5f * dotf(a, v) - w2 * q.s, r.x - w2 * v.x, r.y - w2 * v.y, r.z - w2 * v.z);
+}
+// Euler's equations in the principal frame
+__device__ __forceinline__ f3v euler_f(f3v I, f3v w, f3v M) {
+  return mk3((M.x - (I.z - I.y) * w.y * w.z) / I.x, (M.y - (I.x - I.z) * w.z * w.x) / I.y,
+             (M.z - (I.y - I.x) * w.x * w.y) / I.z);
+}
+
+// First half of the velocity-Verlet step for the free bodies (the FP64 form:
+// Rockable.cpp:2056-2083 through rk_body.cuh's k_drift).
+__global__ void k_drift(Scene s) {
+  const int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.n) return;
+  const float dt = d2f(s.dt), dt_2 = d2f(s.dt_2), dt2_2 = d2f(s.dt2_2);
+  const V3 p = ld3(s.pos, i), v = ld3(s.vel, i), w = ld3(s.vrot, i);
+  const Q4 q = ldq(s.Q, i);
+  const f3v vf = cvt3(v), af = ld3f(s.acc, i), wf = cvt3(w), lf = ld3f(s.arot, i);
+  const q4f qf = cvt4(q);
+  const f3v dx = dt * vf + dt2_2 * af;
+  // quaternion: the same two terms as the FP64 form (the second from the
+  // quaternion after the first), then the normalisation folded into the
+  // increment: with eps = |q + dq|^2 - 1 (|q|^2 - 1 from the FP64 state),
+  // (q + dq) / sqrt(1 + eps) = q + [dq + c (q + dq)], c = -eps/2 + 3 eps^2/8
+  const q4f d1 = qdotf(qf, wf);
+  const q4f q1 = mk4(qf.s + dt * d1.s, qf.x + dt * d1.x, qf.y + dt * d1.y, qf.z + dt * d1.z);
+  const q4f d2 = qddotf(q1, wf, lf);
+  const q4f dq = mk4(dt * d1.s + dt2_2 * d2.s, dt * d1.x + dt2_2 * d2.x, dt * d1.y + dt2_2 * d2.y,
+                     dt * d1.z + dt2_2 * d2.z);
+  double e0 = fma(q.s, q.s, -1.0);
+  e0 = fma(q.v.x, q.v.x, e0);
+  e0 = fma(q.v.y, q.v.y, e0);
+  e0 = fma(q.v.z, q.v.z, e0);
+  const float eps = d2f(e0) + 2.f * (qf.s * dq.s + qf.x * dq.x + qf.y * dq.y + qf.z * dq.z) +
+                    (dq.s * dq.s + dq.x * dq.x + dq.y * dq.y + dq.z * dq.z);
+  const float c = eps * (-0.5f + 0.375f * eps);
+  const q4f inc = mk4(dq.s + c * (qf.s + dq.s), dq.x + c * (qf.x + dq.x), dq.y + c * (qf.y + dq.y),
+                      dq.z + c * (qf.z + dq.z));
+  if (s.sk_path) {
+    // learned-skin path bound (as in rk_body.cuh's k_drift): |dx| plus the
+    // rotation bound 2c(1 + c) of the chord c = |q_new - q| times the swing
+    // radius, rounded up
+    const float ch = sqrtf(inc.s * inc.s + inc.x * inc.x + inc.y * inc.y + inc.z * inc.z);
+    const float d = sqrtf(dotf(dx, dx)) + 2.f * ch * (1.f + ch) * s.sk_rsw[i];
+    s.sk_path[i] += d * (1.f + 1e-5f) + 1e-12f;
+  }
+  st3(s.pos, i, addinc(p, dx));
+  st3(s.vel, i, addinc(v, dt_2 * af));
+  st3(s.vrot, i, addinc(w, dt_2 * lf));
+  stq(s.Q, i, q4(q.s + f2d(inc.s), q.v.x + f2d(inc.x), q.v.y + f2d(inc.y), q.v.z + f2d(inc.z)));
+}
+
+// Resultants, Newton-Euler and the second half-kick (Rockable.cpp:3837-3866,
+// 2084-2117 in the FP64 form); driven bodies take the generic FP64 path.
+__global__ void k_gather_accel(Scene s, int apply_kick) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float kin[12] = {};
+  bool have = false;
+  if (b < s.n) {
+    if (b < s.n_driven) {
+      gather_body(s, b, apply_kick);
+    } else {
+      V3 F, M;
+      body_resultant(s, b, F, M);
+      const V3 vel = ld3(s.vel, b), vrot = ld3(s.vrot, b);
+      if (s.num_damp > 0.0) {  // the sign tests stay FP64: near zero they decide a factor 1 +- damp
+        const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
+        F = F * ((dot(F, vel) > 0.0) ? fm : fp);
+        M = M * ((dot(M, vrot) > 0.0) ? fm : fp);
+      }
+      const double mass = s.mass[b];
+      const f3v Fg = cvt3(v3(fma(mass, s.gravity[0], F.x), fma(mass, s.gravity[1], F.y), fma(mass, s.gravity[2], F.z)));
+      const float im = 1.f / d2f(mass);
+      const f3v acc = im * Fg;
+      const q4f qf = cvt4(ldq(s.Q, b));
+      const q4f qi = mk4(qf.s, -qf.x, -qf.y, -qf.z);
+      const f3v wf = cvt3(vrot);
+      const f3v om = qrotf(qi, wf), Mb = qrotf(qi, cvt3(M));
+      const f3v arot = qrotf(qf, euler_f(ld3f(s.inertia, b), om, Mb));
+      st3f(s.acc, b, acc);
+      st3f(s.arot, b, arot);
+      f3v vf = cvt3(vel), wk = wf;
+      if (apply_kick) {
+        const float h = d2f(s.dt_2);
+        st3(s.vel, b, addinc(vel, h * acc));
+        st3(s.vrot, b, addinc(vrot, h * arot));
+        vf = vf + h * acc;
+        wk = wk + h * arot;
+      }
+      st3(s.force, b, F);
+      st3(s.moment, b, M);
+      const float k[12] = {vf.x, vf.y, vf.z, acc.x, acc.y, acc.z, wk.x, wk.y, wk.z, arot.x, arot.y, arot.z};
+#pragma unroll
+      for (int d = 0; d < 12; d++) kin[d] = k[d];
+      have = true;
+    }
+  }
+  // the learned skin's guard on the state this step leaves (all lanes)
+  if (s.sk_out && apply_kick) skin_guard_body_t<CvtBits>(s, b, have, kin);
+}
+
+// Resultant of a body with many entries (one block per body): threads sum
+// strided parts, then a tree reduction.  The order differs from the serial
+// order the FP64 form keeps (rk_step.cu's k_gather_heavy); the mixed form
+// does not promise bit parity.
+constexpr int kHeavyThreads = 256;
+__global__ void __launch_bounds__(kHeavyThreads) k_gather_heavy(Scene s, const int* list) {
+  __shared__ double red[kHeavyThreads / 32][6];
+  const int b = list[blockIdx.x];
+  const int t = threadIdx.x;
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1], j0 = s.jofs[b], j1 = s.jofs[b + 1];
+  for (int64_t e = i0 + t; e < i1; e += kHeavyThreads) {
+    if (!s.act[e]) continue;
+    const V3 f = ld3(s.cf, e), m = ld3(s.cmi, e);
+    a[0] += f.x; a[1] += f.y; a[2] += f.z;
+    a[3] += m.x; a[4] += m.y; a[5] += m.z;
+  }
+  for (int64_t p = j0 + t; p < j1; p += kHeavyThreads) {
+    const int64_t e = s.jlist[p];
+    if (!s.act[e]) continue;
+    const V3 f = ld3(s.cf, e), m = ld3(s.cmj, e);
+    a[0] -= f.x; a[1] -= f.y; a[2] -= f.z;
+    a[3] += m.x; a[4] += m.y; a[5] += m.z;
+  }
+#pragma unroll
+  for (int d = 0; d < 6; d++)
+    for (int o = 16; o > 0; o >>= 1) a[d] += __shfl_down_sync(0xffffffffu, a[d], o);
+  if ((t & 31) == 0)
+    for (int d = 0; d < 6; d++) red[t >> 5][d] = a[d];
+  __syncthreads();
+  if (t == 0) {
+    V3 F, M;
+    init_resultant(s, b, F, M);
+    for (int w = 0; w < kHeavyThreads / 32; w++) {
+      F = F + v3(red[w][0], red[w][1], red[w][2]);
+      M = M + v3(red[w][3], red[w][4], red[w][5]);
+    }
+    st3(s.force, b, F);
+    st3(s.moment, b, M);
+  }
+}
+
+}  // namespace mx
 
 int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st) {
-  fused::k_drift<<<blocks, threads, 0, st>>>(s);
+  mx::k_drift<<<blocks, threads, 0, st>>>(s);
   return 1;
 }
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st) {
@@ -17,13 +226,17 @@ int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_lis
   return 1;
 }
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st) {
-  fused::k_gather_accel<<<blocks, threads, 0, st>>>(s, apply_kick);
+  mx::k_gather_accel<<<blocks, threads, 0, st>>>(s, apply_kick);
+  return 1;
+}
+int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st) {
+  mx::k_gather_heavy<<<count, mx::kHeavyThreads, 0, st>>>(s, list);
   return 1;
 }
 cudaError_t fused_attributes(int which, cudaFuncAttributes* a) {
-  if (which == 1) return cudaFuncGetAttributes(a, fused::k_gather_accel);
+  if (which == 1) return cudaFuncGetAttributes(a, mx::k_gather_accel);
   if (which == 2) return cudaFuncGetAttributes(a, fused::k_glob_vertices);
-  return cudaFuncGetAttributes(a, fused::k_drift);
+  return cudaFuncGetAttributes(a, mx::k_drift);
 }
 
 }  // namespace rk

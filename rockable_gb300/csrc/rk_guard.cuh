@@ -2,6 +2,7 @@
 // (see rk_skin.cu for the bounds), shared by the resultant kernel, which
 // runs it at the end of every step of the skin mode.
 #pragma once
+#include "rk_bits.cuh"
 #include "rk_engine.cuh"
 
 namespace rk {
@@ -23,6 +24,15 @@ __device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
   return 2.0 * c * (1.0 + c);
 }
 
+// FP64 -> float conversion of the guard: the hardware one (FP64 form) or
+// the integer-pipe one (mixed form); the margins below cover either.
+struct CvtHw {
+  __device__ static float f(double x) { return (float)x; }
+};
+struct CvtBits {
+  __device__ static float f(double x) { return d2f(x); }
+};
+
 // Guard of body b after a step, evaluated by the thread that finished the
 // body's update (the resultant kernel); every thread of the block must call
 // it (block reduction, blocks of at most 512 threads).  sk_out (zeroed before the step): [0] max delta,
@@ -33,7 +43,11 @@ __device__ __forceinline__ double rot_bound(const double* q, const double* q0) {
 // this step leaves (free bodies); driven bodies do not move between steps
 // when no control drives them, which is the only case the host uses the
 // bound for.
-__device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
+// With have_kin, kin holds the body's velocity, acceleration, angular
+// velocity and angular acceleration after the step as floats (12 values,
+// the caller's registers); otherwise they are read back and converted.
+template <class C>
+__device__ __forceinline__ void skin_guard_body_t(const Scene& s, int64_t b, bool have_kin, const float* kin) {
   const double* ref_pos = s.sk_ref_pos;
   const double* ref_q = s.sk_ref_q;
   const float* rsw = s.sk_rsw;
@@ -47,11 +61,11 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   if (b < s.n) {
     // differences in FP64, the rest in float rounded up (relative 1e-5 covers
     // the float rounding of the norms, 1e-12 m the conversions)
-    const float dx = (float)(s.pos[3 * b] - ref_pos[3 * b]), dy = (float)(s.pos[3 * b + 1] - ref_pos[3 * b + 1]),
-                dz = (float)(s.pos[3 * b + 2] - ref_pos[3 * b + 2]);
+    const float dx = C::f(s.pos[3 * b] - ref_pos[3 * b]), dy = C::f(s.pos[3 * b + 1] - ref_pos[3 * b + 1]),
+                dz = C::f(s.pos[3 * b + 2] - ref_pos[3 * b + 2]);
     float m2 = 0.f, p2 = 0.f;
     for (int d = 0; d < 4; d++) {
-      const float m = (float)(s.Q[4 * b + d] - ref_q[4 * b + d]), p = (float)(s.Q[4 * b + d] + ref_q[4 * b + d]);
+      const float m = C::f(s.Q[4 * b + d] - ref_q[4 * b + d]), p = C::f(s.Q[4 * b + d] + ref_q[4 * b + d]);
       m2 += m * m;
       p2 += p * p;
     }
@@ -66,16 +80,28 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
     flag[b] = f ? 1 : 0;
     nflag = f ? 1u : 0u;
     if (b >= s.n_driven) {
-      const float vx = (float)s.vel[3 * b], vy = (float)s.vel[3 * b + 1], vz = (float)s.vel[3 * b + 2];
+      float k[12];
+      if (have_kin) {
+#pragma unroll
+        for (int d = 0; d < 12; d++) k[d] = kin[d];
+      } else {
+        for (int d = 0; d < 3; d++) {
+          k[d] = C::f(s.vel[3 * b + d]);
+          k[3 + d] = C::f(s.acc[3 * b + d]);
+          k[6 + d] = C::f(s.vrot[3 * b + d]);
+          k[9 + d] = C::f(s.arot[3 * b + d]);
+        }
+      }
+      const float vx = k[0], vy = k[1], vz = k[2];
       vmax = sqrtf(vx * vx + vy * vy + vz * vz);
       // bound of the next drift: |dt v + dt^2/2 a| and a rotation of at most
       // |w| dt + |alpha| dt^2/2 (the normalised quaternion update, 1 % margin
       // for its second-order terms); a step of angle t moves the chord c by at
       // most t/2, so 2c(1 + c) grows by at most t (1 + 2c + t/2).  Only decides
       // when the exact values must be read, so a bound is enough.
-      const float ax = (float)s.acc[3 * b], ay = (float)s.acc[3 * b + 1], az = (float)s.acc[3 * b + 2];
-      const float wx = (float)s.vrot[3 * b], wy = (float)s.vrot[3 * b + 1], wz = (float)s.vrot[3 * b + 2];
-      const float lx = (float)s.arot[3 * b], ly = (float)s.arot[3 * b + 1], lz = (float)s.arot[3 * b + 2];
+      const float ax = k[3], ay = k[4], az = k[5];
+      const float wx = k[6], wy = k[7], wz = k[8];
+      const float lx = k[9], ly = k[10], lz = k[11];
       const float dt = (float)s.dt, dt2 = (float)s.dt2_2;
       const float dxb = dt * vmax + dt2 * sqrtf(ax * ax + ay * ay + az * az);
       const float thb = dt * sqrtf(wx * wx + wy * wy + wz * wz) + dt2 * sqrtf(lx * lx + ly * ly + lz * lz);
@@ -127,5 +153,9 @@ __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   }
 }
 
+__device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
+  const float none[12] = {};
+  skin_guard_body_t<CvtHw>(s, b, false, none);
+}
 
 }  // namespace rk

@@ -15,6 +15,7 @@
 // particle size, which FP32 cannot resolve; all the other quantities are well
 // conditioned.  Compiled with fused multiply-adds allowed.
 #include "../../include/rk_gpu.h"
+#include "rk_bits.cuh"
 #include "rk_engine.cuh"
 
 namespace rk {
@@ -27,7 +28,7 @@ __device__ __forceinline__ F3 f3(float x, float y, float z) {
   r.x = x; r.y = y; r.z = z;
   return r;
 }
-__device__ __forceinline__ F3 tof(V3 a) { return f3((float)a.x, (float)a.y, (float)a.z); }
+__device__ __forceinline__ F3 tof(V3 a) { return f3(d2f(a.x), d2f(a.y), d2f(a.z)); }
 __device__ __forceinline__ F3 operator+(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ F3 operator-(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ F3 operator-(F3 a) { return f3(-a.x, -a.y, -a.z); }
@@ -39,16 +40,16 @@ __device__ __forceinline__ F3 crossf(F3 a, F3 b) {
 
 __device__ __forceinline__ V3 ld3m(const double* a, int64_t k) { return v3(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
 __device__ __forceinline__ void st3m(double* a, int64_t k, F3 v) {
-  a[3 * k] = (double)v.x;
-  a[3 * k + 1] = (double)v.y;
-  a[3 * k + 2] = (double)v.z;
+  a[3 * k] = f2d(v.x);
+  a[3 * k + 1] = f2d(v.y);
+  a[3 * k + 2] = f2d(v.z);
 }
 __device__ __forceinline__ V3 gvm(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
 
 // |d| in FP64 from an FP32 reciprocal-sqrt seed and two Newton steps
 __device__ __forceinline__ double len64(V3 d, double& inv) {
   double s = d.x * d.x + d.y * d.y + d.z * d.z;
-  double y = (double)rsqrtf((float)s);
+  double y = f2d(rsqrtf(d2f(s)));
   y = y * (1.5 - 0.5 * s * y * y);
   y = y * (1.5 - 0.5 * s * y * y);
   inv = y;
@@ -81,7 +82,7 @@ __global__ void k_narrow_force_mixed(Scene s) {
       double L = len64(d, inv);
       dn = L - (Ri + Rj);
       n = tof(d * inv);
-      ci = tof(a - xi) - (float)(Ri + 0.5 * dn) * n;
+      ci = tof(a - xi) - d2f(Ri + 0.5 * dn) * n;
     } else if (type == 1) {
       const int sj = s.shape[j];
       const int eo = s.edge_ofs[sj] + jsub;
@@ -93,12 +94,12 @@ __global__ void k_narrow_force_mixed(Scene s) {
       if (r <= 0.f || r >= 1.f) {
         ok = false;
       } else {
-        V3 d = w - (double)r * E;
+        V3 d = w - f2d(r) * E;
         double inv;
         double L = len64(d, inv);
         dn = L - (Ri + Rj);
         n = tof(d * inv);
-        ci = tof(a - xi) - (float)(Ri + 0.5 * dn) * n;
+        ci = tof(a - xi) - d2f(Ri + 0.5 * dn) * n;
       }
     } else if (type == 2) {
       const int sj = s.shape[j];
@@ -134,7 +135,7 @@ __global__ void k_narrow_force_mixed(Scene s) {
       if (odd) {
         dn = dist - (Ri + Rj);
         n = nf;
-        ci = tof(a - xi) - (float)(Ri + 0.5 * dn) * n;
+        ci = tof(a - xi) - d2f(Ri + 0.5 * dn) * n;
       } else {
         ok = false;
       }
@@ -155,131 +156,129 @@ __global__ void k_narrow_force_mixed(Scene s) {
         if (ss <= 0.f || ss >= 1.f || tt <= 0.f || tt >= 1.f) {
           ok = false;
         } else {
-          V3 dd = (w + (double)ss * Ei) - (double)tt * Ej;
+          V3 dd = (w + f2d(ss) * Ei) - f2d(tt) * Ej;
           double inv;
           double L = len64(dd, inv);
           dn = L - (Ri + Rj);
           n = tof(dd * inv);
-          ci = tof((pi1 - xi) + (double)ss * Ei) - (float)(Ri + 0.5 * dn) * n;
+          ci = tof((pi1 - xi) + f2d(ss) * Ei) - d2f(Ri + 0.5 * dn) * n;
         }
       } else {
         ok = false;
       }
     }
-    const F3 dx = tof(xj - xi);
-    const F3 wi = tof(ld3m(s.vrot, i)), wj = tof(ld3m(s.vrot, j));
-    F3 cj = ci - dx;
-    F3 cvel;
-    double fn;
-    F3 ft, mom;
-    if (ok) {
-      const F3 dv = tof(ld3m(s.vel, j) - ld3m(s.vel, i));
-      cvel = (dv - crossf(cj, wj)) + crossf(ci, wi);
-      fn = s.fn[e];
-      ft = tof(ld3m(s.ft, e));
-      mom = tof(ld3m(s.mom, e));
-      if (s.record_geom || bond >= 0) {
-        st3m(s.gn, e, n);
-        st3m(s.gpos, e, tof(xi) + ci);
-        st3m(s.gvel, e, cvel);
-      }
-    } else {
-      dn = 0.0;
-      fn = 0.0;
-      ft = f3(0, 0, 0);
-      mom = f3(0, 0, 0);
-      if (bond >= 0) {
+    // a separated entry (no bond) keeps only its dn: the relative velocity,
+    // the history and the law are skipped unless its geometry is recorded;
+    // a lost sub-contact restarts its history from zero
+    if (!ok) dn = 0.0;
+    active = (dn < 0.0 || bond >= 0);
+    double fn = 0.0;
+    F3 ft = f3(0, 0, 0), mom = f3(0, 0, 0);
+    if (active || (ok && s.record_geom)) {
+      const F3 dx = tof(xj - xi);
+      const F3 wi = tof(ld3m(s.vrot, i)), wj = tof(ld3m(s.vrot, j));
+      F3 cj = ci - dx;
+      F3 cvel;
+      if (ok) {
+        const F3 dv = tof(ld3m(s.vel, j) - ld3m(s.vel, i));
+        cvel = (dv - crossf(cj, wj)) + crossf(ci, wi);
+        fn = s.fn[e];
+        ft = tof(ld3m(s.ft, e));
+        mom = tof(ld3m(s.mom, e));
+        if (s.record_geom || bond >= 0) {
+          st3m(s.gn, e, n);
+          st3m(s.gpos, e, tof(xi) + ci);
+          st3m(s.gvel, e, cvel);
+        }
+      } else {  // a bond whose sub-contact is lost: its last recorded geometry
         n = tof(ld3m(s.gn, e));
         ci = tof(ld3m(s.gpos, e) - xi);
         cj = ci - dx;
         cvel = tof(ld3m(s.gvel, e));
-      } else {
-        cvel = f3(0, 0, 0);
       }
-    }
-    active = (dn < 0.0 || bond >= 0);
-    if (active) {
-      const double* P = s.table[s.group[i] * s.ngroup + s.group[j]].p;
-      const float dt = (float)s.dt;
-      const float damp = (float)s.damp[e];
-      const F3 dw = wj - wi;
-      if (s.law == RK_LAW_STICKEDLINKS && bond >= 0) {
-        float kn, kt, kr, fn0, ft0, mom0, power;
-        double dn0 = s.if_dn0[bond];
-        if (s.params_in_interfaces == 1) {
-          const double* q = s.if_par + 8 * (int64_t)bond;
-          kn = (float)q[0]; kt = (float)q[1]; kr = (float)q[2]; fn0 = (float)q[3]; ft0 = (float)q[4];
-          mom0 = (float)q[5]; power = (float)q[6];
-        } else if (s.cluster[i] == s.cluster[j]) {
-          kn = (float)P[RK_P_KN_IN]; kt = (float)P[RK_P_KT_IN]; kr = (float)P[RK_P_KR_IN]; fn0 = (float)P[RK_P_FN0_IN];
-          ft0 = (float)P[RK_P_FT0_IN]; mom0 = (float)P[RK_P_MOM0_IN]; power = (float)P[RK_P_POW_IN];
-          dn0 = 0.0;
-        } else {
-          kn = (float)P[RK_P_KN_OUT]; kt = (float)P[RK_P_KT_OUT]; kr = (float)P[RK_P_KR_OUT];
-          fn0 = (float)P[RK_P_FN0_OUT]; ft0 = (float)P[RK_P_FT0_OUT]; mom0 = (float)P[RK_P_MOM0_OUT];
-          power = (float)P[RK_P_POW_OUT];
-        }
-        float vn = dotf(cvel, n);
-        fn = -(double)kn * (dn - dn0) + (double)(damp * vn);
-        F3 vt = cvel - vn * n;
-        ft = ft + (kt * dt) * vt;
-        ft = ft + damp * vt;
-        mom = mom + (kr * dt) * dw;
-        float yield = powf(sqrtf(dotf(ft, ft)) / ft0, power) + powf(sqrtf(dotf(mom, mom)) / mom0, power) -
-                      (float)fn / fn0 - 1.0f;
-        if (yield > 0.f) s.if_break[bond] = 1;
-      } else if (dn > 0.0) {
-        fn = 0.0;
-        ft = f3(0, 0, 0);
-        mom = f3(0, 0, 0);
-      } else if (s.law == RK_LAW_AVALANCHE) {
-        const float kn = (float)P[RK_P_KN], en2 = (float)P[RK_P_EN2], kt = (float)P[RK_P_KT];
-        const float mu = (float)P[RK_P_MU], kr = (float)P[RK_P_KR], mur = (float)P[RK_P_MUR];
-        double prev_dn = ok ? dn_old : 0.0;
-        if (prev_dn > 0.0) prev_dn = 0.0;
-        double ddn = dn - prev_dn;
-        if (ddn > 0.0) fn = -(double)(kn * en2) * dn;
-        else if (ddn < 0.0) fn = fn - (double)kn * ddn;
-        if (fn < 0.0) fn = 0.0;
-        F3 vt = cvel - dotf(cvel, n) * n;
-        ft = ft + (kt * dt) * vt;
-        float thr = fabsf(mu * (float)fn);
-        float ft2 = dotf(ft, ft);
-        if (ft2 > 0.f && ft2 > thr * thr) ft = (thr * rsqrtf(ft2)) * ft;
-        mom = mom + (kr * dt) * dw;
-        F3 br;
-        F3 w0;
-        if (i < s.n_driven) { br = cj; w0 = wj; }
-        else { br = ci; w0 = wi; }
-        float r = dotf(br, w0) / dotf(w0, w0);
-        br = br - r * w0;
-        float thm = fabsf(mur * sqrtf(dotf(br, br)) * (float)fn);
-        float m2 = dotf(mom, mom);
-        if (m2 > 0.f && m2 > thm * thm) mom = (thm * rsqrtf(m2)) * mom;
-      } else {  // Default law, and the contact branch of StickedLinks
-        const float kn = (float)P[RK_P_KN], kt = (float)P[RK_P_KT], mu = (float)P[RK_P_MU];
-        const float kr = (float)P[RK_P_KR], mur = (float)P[RK_P_MUR];
-        const bool sticked = s.law == RK_LAW_STICKEDLINKS;
-        float vn = dotf(cvel, n);
-        double fne = -(double)kn * dn;
-        fn = fne + (double)(damp * vn);
-        if (fn < 0.0) fn = 0.0;
-        F3 vt = cvel - vn * n;
-        ft = ft + (kt * dt) * vt;
-        float thr = fabsf(mu * (float)(sticked ? fn : fne));
-        float ft2 = dotf(ft, ft);
-        if (ft2 > 0.f && ft2 >= thr * thr) ft = (thr * rsqrtf(ft2)) * ft;
-        if (sticked || kr > 0.f) {
+      if (active) {
+        const double* P = s.table[s.group[i] * s.ngroup + s.group[j]].p;
+        const float dt = d2f(s.dt);
+        const float damp = d2f(s.damp[e]);
+        const F3 dw = wj - wi;
+        if (s.law == RK_LAW_STICKEDLINKS && bond >= 0) {
+          float kn, kt, kr, fn0, ft0, mom0, power;
+          double dn0 = s.if_dn0[bond];
+          if (s.params_in_interfaces == 1) {
+            const double* q = s.if_par + 8 * (int64_t)bond;
+            kn = d2f(q[0]); kt = d2f(q[1]); kr = d2f(q[2]); fn0 = d2f(q[3]); ft0 = d2f(q[4]);
+            mom0 = d2f(q[5]); power = d2f(q[6]);
+          } else if (s.cluster[i] == s.cluster[j]) {
+            kn = d2f(P[RK_P_KN_IN]); kt = d2f(P[RK_P_KT_IN]); kr = d2f(P[RK_P_KR_IN]); fn0 = d2f(P[RK_P_FN0_IN]);
+            ft0 = d2f(P[RK_P_FT0_IN]); mom0 = d2f(P[RK_P_MOM0_IN]); power = d2f(P[RK_P_POW_IN]);
+            dn0 = 0.0;
+          } else {
+            kn = d2f(P[RK_P_KN_OUT]); kt = d2f(P[RK_P_KT_OUT]); kr = d2f(P[RK_P_KR_OUT]);
+            fn0 = d2f(P[RK_P_FN0_OUT]); ft0 = d2f(P[RK_P_FT0_OUT]); mom0 = d2f(P[RK_P_MOM0_OUT]);
+            power = d2f(P[RK_P_POW_OUT]);
+          }
+          float vn = dotf(cvel, n);
+          fn = -f2d(kn) * (dn - dn0) + f2d(damp * vn);
+          F3 vt = cvel - vn * n;
+          ft = ft + (kt * dt) * vt;
+          ft = ft + damp * vt;
           mom = mom + (kr * dt) * dw;
-          float thm = fabsf(mur * (float)fn);
+          float yield = powf(sqrtf(dotf(ft, ft)) / ft0, power) + powf(sqrtf(dotf(mom, mom)) / mom0, power) -
+                        d2f(fn) / fn0 - 1.0f;
+          if (yield > 0.f) s.if_break[bond] = 1;
+        } else if (dn > 0.0) {
+          fn = 0.0;
+          ft = f3(0, 0, 0);
+          mom = f3(0, 0, 0);
+        } else if (s.law == RK_LAW_AVALANCHE) {
+          const float kn = d2f(P[RK_P_KN]), en2 = d2f(P[RK_P_EN2]), kt = d2f(P[RK_P_KT]);
+          const float mu = d2f(P[RK_P_MU]), kr = d2f(P[RK_P_KR]), mur = d2f(P[RK_P_MUR]);
+          double prev_dn = ok ? dn_old : 0.0;
+          if (prev_dn > 0.0) prev_dn = 0.0;
+          double ddn = dn - prev_dn;
+          if (ddn > 0.0) fn = -f2d(kn * en2) * dn;
+          else if (ddn < 0.0) fn = fn - f2d(kn) * ddn;
+          if (fn < 0.0) fn = 0.0;
+          F3 vt = cvel - dotf(cvel, n) * n;
+          ft = ft + (kt * dt) * vt;
+          float thr = fabsf(mu * d2f(fn));
+          float ft2 = dotf(ft, ft);
+          if (ft2 > 0.f && ft2 > thr * thr) ft = (thr * rsqrtf(ft2)) * ft;
+          mom = mom + (kr * dt) * dw;
+          F3 br;
+          F3 w0;
+          if (i < s.n_driven) { br = cj; w0 = wj; }
+          else { br = ci; w0 = wi; }
+          float r = dotf(br, w0) / dotf(w0, w0);
+          br = br - r * w0;
+          float thm = fabsf(mur * sqrtf(dotf(br, br)) * d2f(fn));
           float m2 = dotf(mom, mom);
-          if (m2 > 0.f && m2 >= thm * thm) mom = (thm * rsqrtf(m2)) * mom;
+          if (m2 > 0.f && m2 > thm * thm) mom = (thm * rsqrtf(m2)) * mom;
+        } else {  // Default law, and the contact branch of StickedLinks
+          const float kn = d2f(P[RK_P_KN]), kt = d2f(P[RK_P_KT]), mu = d2f(P[RK_P_MU]);
+          const float kr = d2f(P[RK_P_KR]), mur = d2f(P[RK_P_MUR]);
+          const bool sticked = s.law == RK_LAW_STICKEDLINKS;
+          float vn = dotf(cvel, n);
+          double fne = -f2d(kn) * dn;
+          fn = fne + f2d(damp * vn);
+          if (fn < 0.0) fn = 0.0;
+          F3 vt = cvel - vn * n;
+          ft = ft + (kt * dt) * vt;
+          float thr = fabsf(mu * d2f(sticked ? fn : fne));
+          float ft2 = dotf(ft, ft);
+          if (ft2 > 0.f && ft2 >= thr * thr) ft = (thr * rsqrtf(ft2)) * ft;
+          if (sticked || kr > 0.f) {
+            mom = mom + (kr * dt) * dw;
+            float thm = fabsf(mur * d2f(fn));
+            float m2 = dotf(mom, mom);
+            if (m2 > 0.f && m2 >= thm * thm) mom = (thm * rsqrtf(m2)) * mom;
+          }
         }
+        F3 f = d2f(fn) * n + ft;
+        st3m(s.cf, e, f);
+        st3m(s.cmi, e, crossf(ci, f) + mom);
+        st3m(s.cmj, e, crossf(cj, -f) - mom);
       }
-      F3 f = (float)fn * n + ft;
-      st3m(s.cf, e, f);
-      st3m(s.cmi, e, crossf(ci, f) + mom);
-      st3m(s.cmj, e, crossf(cj, -f) - mom);
     }
     s.dn[e] = dn;
     if (active || !ok) {

@@ -146,11 +146,18 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
 }
 
 // bodies whose resultant is summed by a block (see k_gather_heavy): in the
-// step when the resultant is used, on demand otherwise
+// step when the resultant is used, on demand otherwise; and the vertices of
+// the bodies with entries (the only ones the step's narrow phase reads), in
+// per-body runs whose order between bodies does not matter
 __global__ void k_heavy(Scene s, unsigned long long* count) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
   int64_t c = (s.iofs[b + 1] - s.iofs[b]) + (s.jofs[b + 1] - s.jofs[b]);
+  if (c > 0) {
+    const int64_t v0 = s.gv_ofs[b], nv = s.gv_ofs[b + 1] - v0;
+    const int64_t at = (int64_t)atomicAdd(&count[3], (unsigned long long)nv);
+    for (int64_t l = 0; l < nv; l++) s.lv[at + l] = (int)(v0 + l);
+  }
   {  // split of the j-side list around b's own block (entry indices ascend in it)
     const int64_t i0 = s.iofs[b];
     int64_t lo = s.jofs[b], hi = s.jofs[b + 1];
@@ -1308,14 +1315,16 @@ int heavy_list(Ctx& c) {
     const int rc = entry_order(c);
     if (rc) return rc;
   }
-  RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 16, c.stream));
+  // counter slots 1, 2: heavy bodies, deferred heavy bodies; 4: listed vertices
+  RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 32, c.stream));
   k_heavy<<<nblk(s.n, 256), 256, 0, c.stream>>>(s, c.w.counter + 1);
   c.kernels++;
-  unsigned long long nh[2] = {0, 0};
-  RKCHK(cudaMemcpyAsync(nh, c.w.counter + 1, 16, cudaMemcpyDeviceToHost, c.stream));
+  unsigned long long nh[4] = {0, 0, 0, 0};
+  RKCHK(cudaMemcpyAsync(nh, c.w.counter + 1, 32, cudaMemcpyDeviceToHost, c.stream));
   RKCHK(cudaStreamSynchronize(c.stream));
   s.nheavy = (int)nh[0];
   s.nheavy_lazy = (int)nh[1];
+  s.nlv = (int64_t)nh[3];
   return 0;
 }
 

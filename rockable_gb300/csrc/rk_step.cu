@@ -557,10 +557,11 @@ int launch_drift(const Scene& s, cudaStream_t st) {
   return 1;
 }
 int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all) {
-  if (s.nvert <= 0) return 0;
+  const int64_t nv = all ? s.nvert : s.nlv;
+  if (nv <= 0) return 0;
   const int t = tpb_or(s, 2, 256);
-  if (s.fast_body) return launch_fused_glob(s, nblk(s.nvert, t), t, all ? 0 : 1, st);
-  exact::k_glob_vertices<<<nblk(s.nvert, t), t, 0, st>>>(s, all ? 0 : 1);
+  if (s.fast_body) return launch_fused_glob(s, nblk(nv, t), t, all ? 0 : 1, st);
+  exact::k_glob_vertices<<<nblk(nv, t), t, 0, st>>>(s, all ? 0 : 1);
   return 1;
 }
 int launch_narrow_force(const Scene& s, cudaStream_t st) {
@@ -591,11 +592,13 @@ int max_tpb(int which, int form_mixed) {
 }
 int launch_gather_heavy(const Scene& s, cudaStream_t st) {
   if (s.nheavy <= 0) return 0;
+  if (s.fast_body) return launch_fused_heavy(s, s.heavy, (int)s.nheavy, st);
   k_gather_heavy<<<s.nheavy, kHeavyChunk, 0, st>>>(s, s.heavy);
   return 1;
 }
 int launch_gather_heavy_lazy(const Scene& s, cudaStream_t st) {
   if (s.nheavy_lazy <= 0) return 0;
+  if (s.fast_body) return launch_fused_heavy(s, s.heavy_lazy, (int)s.nheavy_lazy, st);
   k_gather_heavy<<<s.nheavy_lazy, kHeavyChunk, 0, st>>>(s, s.heavy_lazy);
   return 1;
 }

@@ -163,3 +163,42 @@ def test_long_run_statistics_match_plain(gpu_lib):
         for q in range(2):
             ref = series["plain"][q]
             assert abs(series[name][q] - ref) <= 0.05 * abs(ref), (name, q, series)
+
+
+def test_mixed_free_flight_tracks_fp64():
+    """No contacts: 200 grains far apart, spinning fast about random axes
+    (torque-free precession through Euler's equations) and falling under
+    gravity for 5000 steps.  The mixed form advances the FP64 state by FP32
+    increments; it stays within a few float roundings of the FP64 form per
+    step, and its quaternions stay unit to FP64 precision."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
+    scene = scenes.drop_bodies(scenes.column_collapse(n=200, nshapes=16), [0])
+    b = dict(scene["bodies"])
+    rng = np.random.default_rng(21)
+    n = len(b["mass"])
+    b["pos"] = np.asarray(b["pos"]) * 20.0
+    b["vel"] = rng.normal(size=(n, 3))
+    b["vrot"] = rng.normal(size=(n, 3)) * 40.0
+    scene = dict(scene, bodies=b, entries=None)
+    out = {}
+    for form in (RK_FORM_FP64, RK_FORM_MIXED):
+        g = GpuScene(form=form)
+        g.upload_shapes(scene["shape_tables"])
+        g.upload_bodies(b, scene["n_driven"])
+        scenes.set_scene_params(g, scene)
+        g.update_nl()
+        g.step(5000)
+        out[form] = g.bodies()
+        g.close()
+    a, m = out[RK_FORM_FP64], out[RK_FORM_MIXED]
+    assert len(a["pos"]) == n
+    dq = np.abs(a["Q"] - m["Q"]).max()
+    dpos = np.abs(a["pos"] - m["pos"]).max()
+    dw = (np.linalg.norm(a["vrot"] - m["vrot"], axis=1) / np.linalg.norm(a["vrot"], axis=1)).max()
+    dv = np.abs(a["vel"] - m["vel"]).max()
+    unit = np.abs(np.linalg.norm(m["Q"], axis=1) - 1.0).max()
+    print("free flight: |dQ| %.3g |dpos| %.3g m |dw|/|w| %.3g |dv| %.3g m/s, ||Q|-1| %.3g" % (dq, dpos, dw, dv, unit))
+    assert np.abs(a["vrot"]).max() > 20.0  # spinning throughout
+    assert dq <= 1e-6 and dpos <= 1e-9 and dw <= 1e-5 and dv <= 1e-9, (dq, dpos, dw, dv)
+    assert unit <= 1e-12
