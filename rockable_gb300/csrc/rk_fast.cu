@@ -94,7 +94,8 @@ __global__ void k_drift(Scene s) {
   const f3v dx = dt * vf + dt2_2 * af;
   // quaternion: the same two terms as the FP64 form (the second from the
   // quaternion after the first), then the normalisation folded into the
-  // increment: with eps = |q + dq|^2 - 1 (|q|^2 - 1 from the FP64 state),
+  // increment: with eps = |q + dq|^2 - 1 = (|q|^2 - 1) + 2 q.dq + |dq|^2
+  // (the first two summed in FP64, so that |q| stays 1 to FP64 precision),
   // (q + dq) / sqrt(1 + eps) = q + [dq + c (q + dq)], c = -eps/2 + 3 eps^2/8
   const q4f d1 = qdotf(qf, wf);
   const q4f q1 = mk4(qf.s + dt * d1.s, qf.x + dt * d1.x, qf.y + dt * d1.y, qf.z + dt * d1.z);
@@ -105,8 +106,11 @@ __global__ void k_drift(Scene s) {
   e0 = fma(q.v.x, q.v.x, e0);
   e0 = fma(q.v.y, q.v.y, e0);
   e0 = fma(q.v.z, q.v.z, e0);
-  const float eps = d2f(e0) + 2.f * (qf.s * dq.s + qf.x * dq.x + qf.y * dq.y + qf.z * dq.z) +
-                    (dq.s * dq.s + dq.x * dq.x + dq.y * dq.y + dq.z * dq.z);
+  e0 = fma(q.s, f2d(2.f * dq.s), e0);
+  e0 = fma(q.v.x, f2d(2.f * dq.x), e0);
+  e0 = fma(q.v.y, f2d(2.f * dq.y), e0);
+  e0 = fma(q.v.z, f2d(2.f * dq.z), e0);
+  const float eps = d2f(e0) + (dq.s * dq.s + dq.x * dq.x + dq.y * dq.y + dq.z * dq.z);
   const float c = eps * (-0.5f + 0.375f * eps);
   const q4f inc = mk4(dq.s + c * (qf.s + dq.s), dq.x + c * (qf.x + dq.x), dq.y + c * (qf.y + dq.y),
                       dq.z + c * (qf.z + dq.z));

@@ -169,8 +169,10 @@ def test_mixed_free_flight_tracks_fp64():
     """No contacts: 200 grains far apart, spinning fast about random axes
     (torque-free precession through Euler's equations) and falling under
     gravity for 5000 steps.  The mixed form advances the FP64 state by FP32
-    increments; it stays within a few float roundings of the FP64 form per
-    step, and its quaternions stay unit to FP64 precision."""
+    increments whose relative error is at most 2^-24; a constant increment
+    (free fall) repeats its rounding every step, so the state deviates from
+    the FP64 form's by up to ~1e-7 of its accumulated change, and no more.
+    The quaternions stay unit to FP64 precision."""
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
     scene = scenes.drop_bodies(scenes.column_collapse(n=200, nshapes=16), [0])
@@ -193,12 +195,19 @@ def test_mixed_free_flight_tracks_fp64():
         g.close()
     a, m = out[RK_FORM_FP64], out[RK_FORM_MIXED]
     assert len(a["pos"]) == n
+    rel = 4 * 2.0 ** -24
+    moved = np.abs(a["pos"] - b["pos"])
+    dv_acc = np.abs(a["vel"] - b["vel"])
+    dpos = np.abs(a["pos"] - m["pos"])
+    dv = np.abs(a["vel"] - m["vel"])
     dq = np.abs(a["Q"] - m["Q"]).max()
-    dpos = np.abs(a["pos"] - m["pos"]).max()
     dw = (np.linalg.norm(a["vrot"] - m["vrot"], axis=1) / np.linalg.norm(a["vrot"], axis=1)).max()
-    dv = np.abs(a["vel"] - m["vel"]).max()
     unit = np.abs(np.linalg.norm(m["Q"], axis=1) - 1.0).max()
-    print("free flight: |dQ| %.3g |dpos| %.3g m |dw|/|w| %.3g |dv| %.3g m/s, ||Q|-1| %.3g" % (dq, dpos, dw, dv, unit))
+    print("free flight: |dQ| %.3g |dpos| %.3g m (moved %.3g) |dw|/|w| %.3g |dv| %.3g m/s (change %.3g), ||Q|-1| %.3g"
+          % (dq, dpos.max(), moved.max(), dw, dv.max(), dv_acc.max(), unit))
     assert np.abs(a["vrot"]).max() > 20.0  # spinning throughout
-    assert dq <= 1e-6 and dpos <= 1e-9 and dw <= 1e-5 and dv <= 1e-9, (dq, dpos, dw, dv)
-    assert unit <= 1e-12
+    assert np.all(dpos <= rel * moved + 1e-12), float(np.max(dpos - rel * moved))
+    assert np.all(dv <= rel * dv_acc + 1e-12), float(np.max(dv - rel * dv_acc))
+    # rotations of at most ~0.6 rad: the same relative bound on the quaternions
+    assert dq <= 1e-7 and dw <= 1e-5, (dq, dw)
+    assert unit <= 1e-14
