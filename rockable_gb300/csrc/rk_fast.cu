@@ -8,7 +8,7 @@
 // FP64 add): the state (positions, velocities, quaternions, angular
 // velocities) stays FP64 and is advanced by FP64 additions of increments
 // computed in FP32 -- dt v + dt^2/2 a, dt/2 a, the quaternion derivative terms
-// and its normalisation -- and the Newton-Euler update runs in FP32 from the
+// (normalised in FP64) -- and the Newton-Euler update runs in FP32 from the
 // FP64 resultants (the force plus m g summed in FP64 first, so that a body at
 // rest keeps a small acceleration to float precision).  Conversions use the
 // integer-pipe routines of rk_bits.cuh.  An increment's relative error is
@@ -93,39 +93,34 @@ __global__ void k_drift(Scene s) {
   const q4f qf = cvt4(q);
   const f3v dx = dt * vf + dt2_2 * af;
   // quaternion: the same two terms as the FP64 form (the second from the
-  // quaternion after the first), then the normalisation folded into the
-  // increment: with eps = |q + dq|^2 - 1 = (|q|^2 - 1) + 2 q.dq + |dq|^2
-  // (the first two summed in FP64, so that |q| stays 1 to FP64 precision),
-  // (q + dq) / sqrt(1 + eps) = q + [dq + c (q + dq)], c = -eps/2 + 3 eps^2/8
+  // quaternion after the first) as an FP32 increment dq; qd = q + dq in FP64,
+  // then the normalisation as an FP64 scale: with eps = |qd|^2 - 1 (FP64),
+  // qd / sqrt(1 + eps) = qd + c qd, c = -eps/2 + 3 eps^2/8 (|eps| ~ |dq|^2)
   const q4f d1 = qdotf(qf, wf);
   const q4f q1 = mk4(qf.s + dt * d1.s, qf.x + dt * d1.x, qf.y + dt * d1.y, qf.z + dt * d1.z);
   const q4f d2 = qddotf(q1, wf, lf);
   const q4f dq = mk4(dt * d1.s + dt2_2 * d2.s, dt * d1.x + dt2_2 * d2.x, dt * d1.y + dt2_2 * d2.y,
                      dt * d1.z + dt2_2 * d2.z);
-  double e0 = fma(q.s, q.s, -1.0);
-  e0 = fma(q.v.x, q.v.x, e0);
-  e0 = fma(q.v.y, q.v.y, e0);
-  e0 = fma(q.v.z, q.v.z, e0);
-  e0 = fma(q.s, f2d(2.f * dq.s), e0);
-  e0 = fma(q.v.x, f2d(2.f * dq.x), e0);
-  e0 = fma(q.v.y, f2d(2.f * dq.y), e0);
-  e0 = fma(q.v.z, f2d(2.f * dq.z), e0);
-  const float eps = d2f(e0) + (dq.s * dq.s + dq.x * dq.x + dq.y * dq.y + dq.z * dq.z);
-  const float c = eps * (-0.5f + 0.375f * eps);
-  const q4f inc = mk4(dq.s + c * (qf.s + dq.s), dq.x + c * (qf.x + dq.x), dq.y + c * (qf.y + dq.y),
-                      dq.z + c * (qf.z + dq.z));
+  const Q4 qd = q4(q.s + f2d(dq.s), q.v.x + f2d(dq.x), q.v.y + f2d(dq.y), q.v.z + f2d(dq.z));
+  double e = fma(qd.s, qd.s, -1.0);
+  e = fma(qd.v.x, qd.v.x, e);
+  e = fma(qd.v.y, qd.v.y, e);
+  e = fma(qd.v.z, qd.v.z, e);
+  const float ef = d2f(e);
+  const float cf = ef * (-0.5f + 0.375f * ef);
+  const double c = f2d(cf);
   if (s.sk_path) {
     // learned-skin path bound (as in rk_body.cuh's k_drift): |dx| plus the
-    // rotation bound 2c(1 + c) of the chord c = |q_new - q| times the swing
-    // radius, rounded up
-    const float ch = sqrtf(inc.s * inc.s + inc.x * inc.x + inc.y * inc.y + inc.z * inc.z);
+    // rotation bound 2ch(1 + ch) of the chord ch = |q_new - q| <= |dq| + |c| |qd|
+    // times the swing radius, rounded up
+    const float ch = sqrtf(dq.s * dq.s + dq.x * dq.x + dq.y * dq.y + dq.z * dq.z) + fabsf(cf) * 1.001f;
     const float d = sqrtf(dotf(dx, dx)) + 2.f * ch * (1.f + ch) * s.sk_rsw[i];
     s.sk_path[i] += d * (1.f + 1e-5f) + 1e-12f;
   }
   st3(s.pos, i, addinc(p, dx));
   st3(s.vel, i, addinc(v, dt_2 * af));
   st3(s.vrot, i, addinc(w, dt_2 * lf));
-  stq(s.Q, i, q4(q.s + f2d(inc.s), q.v.x + f2d(inc.x), q.v.y + f2d(inc.y), q.v.z + f2d(inc.z)));
+  stq(s.Q, i, q4(fma(c, qd.s, qd.s), fma(c, qd.v.x, qd.v.x), fma(c, qd.v.y, qd.v.y), fma(c, qd.v.z, qd.v.z)));
 }
 
 // Resultants, Newton-Euler and the second half-kick (Rockable.cpp:3837-3866,
