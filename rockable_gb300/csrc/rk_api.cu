@@ -462,13 +462,14 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
 // rebuild swaps the entry buffers, a parameter call changes scalars), then
 // replayed.  Same kernels, same arguments, same order as the launch-by-launch
 // path, so the results are identical.
-static int step_launches(Ctx& c) {
+static int step_launches(Ctx& c, bool time_narrow = true) {
   Scene& s = c.s;
   int n = 0;
   n += launch_controls_pre(s, c.stream);
   n += launch_drift(s, c.stream);
   n += launch_glob_vertices(s, c.stream);
-  const bool timed = c.skin.on && c.skin.nev[0];  // the skin's cost model wants the narrow-phase time
+  // the skin's cost model wants the narrow-phase time
+  const bool timed = time_narrow && c.skin.on && c.skin.nev[0];
   if (timed) cudaEventRecord(c.skin.nev[0], c.stream);
   n += c.form == RK_FORM_MIXED ? launch_narrow_force_mixed(s, c.stream) : launch_narrow_force(s, c.stream);
   if (timed) cudaEventRecord(c.skin.nev[1], c.stream);
@@ -524,6 +525,32 @@ static int tune_step(Ctx& c) {
   return RK_OK;
 }
 
+// Instantiates captured graph g into *ex (updating it in place when the
+// topology allows); g is destroyed.
+static int graph_install(Ctx& c, cudaGraph_t g, cudaGraphExec_t* ex, const char* what) {
+  bool updated = false;
+  if (*ex) {
+    cudaGraphExecUpdateResultInfo info;
+    updated = cudaGraphExecUpdate(*ex, g, &info) == cudaSuccess;
+    if (!updated) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(*ex);
+      *ex = nullptr;
+    }
+  }
+  if (!updated) {
+    const cudaError_t e = cudaGraphInstantiate(ex, g, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      *ex = nullptr;
+      c.err = std::string(what) + " instantiation: " + cudaGetErrorString(e);
+      return RK_ERR_CUDA;
+    }
+  }
+  cudaGraphDestroy(g);
+  return RK_OK;
+}
+
 static int step_graph(Ctx& c) {
   Scene& s = c.s;
   const bool stale = !c.gexec || c.gform != c.form || std::memcmp(&c.gscene, &s, sizeof(Scene)) != 0;
@@ -538,26 +565,8 @@ static int step_graph(Ctx& c) {
       c.err = std::string("step graph capture: ") + cudaGetErrorString(e);
       return RK_ERR_CUDA;
     }
-    bool updated = false;
-    if (c.gexec) {
-      cudaGraphExecUpdateResultInfo info;
-      updated = cudaGraphExecUpdate(c.gexec, g, &info) == cudaSuccess;
-      if (!updated) {
-        cudaGetLastError();
-        cudaGraphExecDestroy(c.gexec);
-        c.gexec = nullptr;
-      }
-    }
-    if (!updated) {
-      e = cudaGraphInstantiate(&c.gexec, g, 0);
-      if (e != cudaSuccess) {
-        cudaGraphDestroy(g);
-        c.gexec = nullptr;
-        c.err = std::string("step graph instantiation: ") + cudaGetErrorString(e);
-        return RK_ERR_CUDA;
-      }
-    }
-    cudaGraphDestroy(g);
+    const int rc = graph_install(c, g, &c.gexec, "step graph");
+    if (rc) return rc;
     std::memcpy(&c.gscene, &s, sizeof(Scene));  // byte copy: the comparison above is bytewise
     c.gform = c.form;
     c.glaunched = n;
@@ -568,6 +577,114 @@ static int step_graph(Ctx& c) {
   c.graph_replays++;
   c.kernels += c.glaunched;
   return RK_OK;
+}
+
+// Steps per batch of the device-decided skin mode (skin_batch): long enough
+// to take the host round trip out of almost every step, short enough that the
+// steps skipped after a trigger (each a handful of launches that return at
+// once) stay cheap.
+constexpr int kSkinBatch = 16;
+
+// The graph of kSkinBatch steps, each opened by k_skin_begin and closed by
+// k_skin_end (rk_skin.cu); the narrow phase of the first step is timed for the
+// skin's cost model.  Captured with s.sk_ctl set, like the launches it holds.
+static int batch_graph(Ctx& c) {
+  Scene& s = c.s;
+  const bool stale = !c.bexec || c.bform != c.form || std::memcmp(&c.bscene, &s, sizeof(Scene)) != 0;
+  if (stale) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    int n = 0;
+    for (int q = 0; q < kSkinBatch; q++) {
+      n += launch_skin_begin(s, c.stream);
+      n += step_launches(c, q == 0);
+      n += launch_skin_end(s, c.stream);
+    }
+    const cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      c.err = std::string("skin batch graph capture: ") + cudaGetErrorString(e);
+      return RK_ERR_CUDA;
+    }
+    const int rc = graph_install(c, g, &c.bexec, "skin batch graph");
+    if (rc) return rc;
+    std::memcpy(&c.bscene, &s, sizeof(Scene));
+    c.bform = c.form;
+    c.blaunched = n;
+    c.graph_captures++;
+  }
+  CK(cudaGraphLaunch(c.bexec, c.stream));
+  c.graph_replays++;
+  c.kernels += c.blaunched;
+  return RK_OK;
+}
+
+static int skin_partial(Ctx& c, int64_t nflag);
+
+// Up to `left` steps of the skin mode as one batch: the device checks the
+// exact guard after every step and halts the batch when a refresh is due, so
+// the host syncs once per batch; it then takes the same decision as
+// skin_after_step from the halting step's guard words.  *done = steps run.
+static int skin_batch(Ctx& c, int64_t left, int64_t* done) {
+  Skin& k = c.skin;
+  Scene& s = c.s;
+  const int64_t want = std::min<int64_t>(kSkinBatch, left);
+  unsigned int* in = k.h_ctl;
+  unsigned int* out = k.h_ctl + 16;
+  float trig = (float)(0.5 * k.skin);
+  if ((double)trig < 0.5 * k.skin) trig = std::nextafter(trig, INFINITY);
+  in[0] = 0u;
+  in[1] = 0u;
+  in[2] = (unsigned)std::min<int64_t>(k.since, 0x7fffffff);
+  in[3] = (unsigned)want;
+  in[4] = (unsigned)std::min<int64_t>(std::max<int64_t>(k.interval, 1), 0x7fffffff);
+  std::memcpy(&in[5], &trig, 4);
+  in[6] = k.partial_since_global > 0 ? 1u : 0u;
+  in[7] = 0u;
+  CK(cudaMemcpyAsync(k.d_ctl, in, 8 * sizeof(unsigned int), cudaMemcpyHostToDevice, c.stream));
+  s.sk_ctl = k.d_ctl;
+  int rc = batch_graph(c);
+  s.sk_ctl = nullptr;
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, k.d_ctl, 16 * sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaEventRecord(k.bev, c.stream));
+  CK(cudaEventSynchronize(k.bev));
+  const int64_t ex = out[1];
+  if (ex < 1 || ex > want) {
+    c.err = "skin batch: step count out of range";
+    return RK_ERR_STATE;
+  }
+  for (int64_t q = 0; q < ex; q++) {
+    c.t += s.dt;
+    c.interVerletC += s.dt;
+  }
+  c.steps += ex;
+  *done = ex;
+  c.more_steps_follow = ex < left;
+  c.forces_stale = s.nheavy_lazy > 0;
+  k.since = out[2];
+  if (k.nev[0]) {  // the first step of the batch ran its narrow phase between these events
+    float nms = 0.f;
+    if (cudaEventElapsedTime(&nms, k.nev[0], k.nev[1]) == cudaSuccess) {
+      k.narrow_acc += nms;
+      k.narrow_cnt++;
+    } else {
+      cudaGetLastError();
+    }
+  }
+  k.narrow_timed = false;
+  k.have_pred = false;
+  const unsigned int* hg = out + 8;
+  const double dmax = to_f(hg[0]), vmax = to_f(hg[1]), gmax = to_f(hg[2]);
+  const int64_t nflag = (int64_t)hg[3];
+  const double crit = k.partial_since_global > 0 ? gmax : dmax;
+  if (k.since >= k.interval) return skin_rebuild(c, dmax, vmax, false);
+  if (crit >= 0.5 * k.skin) {
+    if (k.cfg.partial_fraction > 0.0 && nflag > 0 && (double)nflag <= k.cfg.partial_fraction * (double)s.n)
+      return skin_partial(c, nflag);
+    return skin_rebuild(c, dmax, vmax, true);
+  }
+  return 0;
 }
 
 // Partial refresh of the flagged bodies (see rk_skin.cu): the neighbour
@@ -710,6 +827,7 @@ void rk_destroy(rk_ctx* x) {
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.gexec) cudaGraphExecDestroy(c.gexec);
+  if (c.bexec) cudaGraphExecDestroy(c.bexec);
   for (int k = 0; k < 8; k++)
     if (c.tev[k]) cudaEventDestroy(c.tev[k]);
   Scene& s = c.s;
@@ -741,6 +859,9 @@ void rk_destroy(rk_ctx* x) {
     dfree(k.grad); dfree(k.loss); dfree(k.X); dfree(k.T); dfree(k.io);
     if (k.w) cudaFree(k.w);
     if (k.h_guard) cudaFreeHost(k.h_guard);
+    if (k.d_ctl) cudaFree(k.d_ctl);
+    if (k.h_ctl) cudaFreeHost(k.h_ctl);
+    if (k.bev) cudaEventDestroy(k.bev);
     if (k.ea) cudaEventDestroy(k.ea);
     for (cudaEvent_t e : {k.nev[0], k.nev[1], k.pa, k.pb, k.gev[0], k.gev[1]})
       if (e) cudaEventDestroy(e);
@@ -1071,6 +1192,9 @@ static int skin_alloc(Ctx& c) {
     CK(cudaMalloc(&wbuf, 2 * (size_t)np));
     k.w = wbuf;
     CK(cudaMallocHost(&k.h_guard, 64));
+    CK(cudaMalloc(&k.d_ctl, 32 * sizeof(unsigned int)));
+    CK(cudaMallocHost(&k.h_ctl, 32 * sizeof(unsigned int)));
+    CK(cudaEventCreateWithFlags(&k.bev, cudaEventDisableTiming));
     CK(cudaEventCreate(&k.ea));
     CK(cudaEventCreate(&k.eb));
   }
@@ -1344,11 +1468,18 @@ int rk_step(rk_ctx* x, int64_t nsteps, rk_step_report* rep) {
   c.skin.have_pred = false;  // the state may have been changed since the last call (uploads)
   CK(cudaEventRecord(c.ev0, c.stream));
   for (int64_t it = 0; it < nsteps; it++) {
+    const bool tuning = c.tune_left > 0 && !c.profiling;
+    const bool graphed = c.use_graphs && !c.profiling && !tuning;
+    if (graphed && c.skin.on && c.skin.d_ctl && guard_pipelined(c)) {
+      // the skin's decisions taken on the device, a batch of steps per round trip
+      int64_t ex = 0;
+      if ((rc = skin_batch(c, nsteps - it, &ex))) return rc;
+      it += ex - 1;
+      continue;
+    }
     c.t += s.dt;
     c.interVerletC += s.dt;
     c.more_steps_follow = it + 1 < nsteps;
-    const bool tuning = c.tune_left > 0 && !c.profiling;
-    const bool graphed = c.use_graphs && !c.profiling && !tuning;
     if (graphed) {
       if ((rc = step_graph(c))) return rc;
     } else {

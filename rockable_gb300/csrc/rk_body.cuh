@@ -206,6 +206,7 @@ namespace RK_BODY_NS {
 
 // ----------------------------------------------------------------- K1 ----
 __global__ void k_drift(Scene s) {
+  if (step_halted(s)) return;
   int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= s.n) return;
   V3 p = ld3(s.pos, i), v = ld3(s.vel, i), a = ld3(s.acc, i);
@@ -241,6 +242,7 @@ __global__ void k_drift(Scene s) {
 // entries): within a step only the narrow phase reads these positions, and
 // only for bodies in the list; a list update recomputes every body first.
 __global__ void k_glob_vertices(Scene s, int only_listed) {
+  if (step_halted(s)) return;
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= (only_listed ? s.nlv : s.nvert)) return;
   if (only_listed) k = s.lv[k];
@@ -255,6 +257,7 @@ __global__ void k_glob_vertices(Scene s, int only_listed) {
 }
 
 __global__ void k_gather_accel(Scene s, int apply_kick) {
+  if (step_halted(s)) return;
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b < s.n) gather_body(s, b, apply_kick);
   // the learned skin's guard on the state this step leaves (all lanes)

@@ -64,6 +64,11 @@ struct Skin {
   uint8_t* flag = nullptr;          // n: bodies due for a partial refresh
   unsigned int* d_guard = nullptr;  // guard reductions (see k_skin_guard)
   unsigned int* h_guard = nullptr;  // pinned
+  // batched steps: control block (see k_skin_end) on the device, and its
+  // pinned host copies (words 0-15 written before a batch, 16-31 read after)
+  unsigned int* d_ctl = nullptr;
+  unsigned int* h_ctl = nullptr;
+  cudaEvent_t bev = nullptr;
   int64_t partial = 0, partial_bodies = 0, partial_since_global = 0, since_global = 0;
   // measured in the current window: narrow-phase time per step (events
   // around its launch, in the step graph too) and partial-refresh cost
@@ -156,6 +161,11 @@ struct Ctx {
   int gform = -1;
   int glaunched = 0;    // kernels per replay
   int64_t graph_captures = 0, graph_replays = 0;
+  // the graph of a batch of skin steps (same rules as the step graph)
+  cudaGraphExec_t bexec = nullptr;
+  Scene bscene{};
+  int bform = -1;
+  int blaunched = 0;
 };
 
 // Neighbour-list update; with `only` (device flags per body), only the pairs

@@ -129,8 +129,11 @@ struct Scene {
   const double* sk_ref_q;
   float* sk_maxd;
   uint8_t* sk_flag;
-  unsigned int* sk_out;  // 8 words, zeroed by the resultant kernel's launcher
+  unsigned int* sk_out;  // 8 words, zeroed by the resultant kernel's launcher (by k_skin_begin in a batch)
   float sk_flag_at;
+  // batched skin steps (rk_skin.cu, k_skin_end): when set, every step kernel
+  // returns at once while sk_ctl[0] (halt) is set
+  unsigned int* sk_ctl;
   float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
   int64_t* sph_ofs;   // n+1
   int* sph_body;      // body of every sphere
@@ -167,10 +170,15 @@ int launch_kinetic_energy(const Scene& s, double* d_out2, cudaStream_t st);
 int launch_kin_pack(const Scene& s, double* stage, int dir, cudaStream_t st);
 int max_tpb(int which, int form_mixed);
 // per-body kernels compiled with fused multiply-adds (rk_fast.cu, mixed form)
+// a batched skin step after the guard asked for a refresh: the kernel does nothing
+__device__ __forceinline__ bool step_halted(const Scene& s) { return s.sk_ctl != nullptr && s.sk_ctl[0] != 0u; }
+
 int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st);
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);
+int launch_skin_begin(const Scene& s, cudaStream_t st);
+int launch_skin_end(const Scene& s, cudaStream_t st);
 cudaError_t fused_attributes(int which, cudaFuncAttributes* a);
 cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a);
 

@@ -84,6 +84,7 @@ __device__ __forceinline__ f3v euler_f(f3v I, f3v w, f3v M) {
 // First half of the velocity-Verlet step for the free bodies (the FP64 form:
 // Rockable.cpp:2056-2083 through rk_body.cuh's k_drift).
 __global__ void k_drift(Scene s) {
+  if (step_halted(s)) return;
   const int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= s.n) return;
   const float dt = d2f(s.dt), dt_2 = d2f(s.dt_2), dt2_2 = d2f(s.dt2_2);
@@ -126,6 +127,7 @@ __global__ void k_drift(Scene s) {
 // Resultants, Newton-Euler and the second half-kick (Rockable.cpp:3837-3866,
 // 2084-2117 in the FP64 form); driven bodies take the generic FP64 path.
 __global__ void k_gather_accel(Scene s, int apply_kick) {
+  if (step_halted(s)) return;
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   float kin[12] = {};
   bool have = false;
@@ -178,6 +180,7 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
 // does not promise bit parity.
 constexpr int kHeavyThreads = 256;
 __global__ void __launch_bounds__(kHeavyThreads) k_gather_heavy(Scene s, const int* list) {
+  if (step_halted(s)) return;
   __shared__ double red[kHeavyThreads / 32][6];
   const int b = list[blockIdx.x];
   const int t = threadIdx.x;

@@ -57,6 +57,7 @@ __device__ __forceinline__ double len64(V3 d, double& inv) {
 }
 
 __global__ void k_narrow_force_mixed(Scene s) {
+  if (step_halted(s)) return;
   // threads follow the entries grouped by sub-contact type (fewer divergent
   // branches per warp); every entry is computed on its own
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

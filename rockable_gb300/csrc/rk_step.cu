@@ -26,6 +26,7 @@ namespace rk {
 
 // ----------------------------------------------------------------- K0 ----
 __global__ void k_controls_pre(Scene s) {
+  if (step_halted(s)) return;
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (s.servo_kind == 1) {  // tritriIsostaticCompression
     const int* w = s.servo_walls;
@@ -214,6 +215,7 @@ __device__ __forceinline__ void law_sticked(const Scene& s, const LawIn& L, doub
 __device__ __forceinline__ V3 gvx(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
 
 __global__ void k_narrow_force(Scene s) {
+  if (step_halted(s)) return;
   // threads follow the entries grouped by sub-contact type (fewer divergent
   // branches per warp); every entry is computed on its own
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -376,6 +378,7 @@ __global__ void k_narrow_force(Scene s) {
 // memory latency.
 constexpr int kHeavyChunk = 256;
 __global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s, const int* list) {
+  if (step_halted(s)) return;
   __shared__ double sf[kHeavyChunk][3], sm[kHeavyChunk][3];
   __shared__ int sgn[kHeavyChunk];
   __shared__ int64_t split;
@@ -434,6 +437,7 @@ __global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s, const int
 
 // ----------------------------------------------------------------- K4 ----
 __global__ void k_bond_break(Scene s) {
+  if (step_halted(s)) return;
   int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= s.ne) return;
   int bond = s.bond[e];
@@ -453,6 +457,7 @@ __global__ void k_bond_break(Scene s) {
 }
 
 __global__ void k_iface_break(Scene s) {
+  if (step_halted(s)) return;
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= s.nif) return;
   if (!s.if_break[k]) return;
@@ -572,7 +577,8 @@ int launch_narrow_force(const Scene& s, cudaStream_t st) {
 }
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
   if (s.n <= 0) return 0;
-  if (s.sk_out && apply_kick) cudaMemsetAsync(s.sk_out, 0, 8 * sizeof(unsigned int), st);
+  // (a batched skin step zeroes it in k_skin_begin)
+  if (s.sk_out && apply_kick && !s.sk_ctl) cudaMemsetAsync(s.sk_out, 0, 8 * sizeof(unsigned int), st);
   const int t = tpb_or(s, 1, 128);
   if (s.fast_body) return launch_fused_gather(s, nblk(s.n, t), t, apply_kick, st);
   exact::k_gather_accel<<<nblk(s.n, t), t, 0, st>>>(s, apply_kick);

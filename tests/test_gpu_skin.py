@@ -147,3 +147,41 @@ def test_every_touching_subcontact_is_in_the_skin_list(partial_fraction, gpu_lib
     print("skin stats (partial_fraction=%g):" % partial_fraction, sk)
     if partial_fraction > 0:
         assert sk["partial"] >= 1
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_batched_skin_steps_match_the_per_step_path(form, gpu_lib):
+    """With step graphs the skin mode runs batches of steps whose refresh
+    decisions are taken on the device (k_skin_end); without them the host
+    decides after every step.  With the skin size and the interval pinned the
+    decisions depend on the state alone, so both paths must give the same
+    refreshes and bit-identical bodies, over calls whose lengths do not
+    divide the batch."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
+    scene = scenes.column_collapse(n=2000, nshapes=64)
+    gs = scenes.settle(scene, steps=1500)
+    src = scenes.scene_from_gpu(scene, gs)
+    gs.close()
+    skin = 0.1 * scene["dVerlet"]
+    out = []
+    for graphs in (False, True):
+        g = GpuScene(form=RK_FORM_FP64 if form == "fp64" else RK_FORM_MIXED)
+        g.upload_shapes(src["shape_tables"])
+        g.upload_bodies(src["bodies"], src["n_driven"])
+        scenes.set_scene_params(g, src)
+        g.upload_entries(src["entries"])
+        g.set_skin(use_mlp=False, skin_min=skin, skin_max=skin, interval_min=45, interval_max=45)
+        g.set_graphs(graphs)
+        for n in (7, 100, 33, 160):
+            g.step(n)
+        out.append((g.bodies(), g.skin_stats(), g.graph_stats()))
+        g.close()
+    (b0, s0, _), (b1, s1, gst) = out
+    print(form, "per-step:", s0, "batched:", s1, "graphs:", gst)
+    assert s0["rebuilds"] >= 3 and s0["partial"] + s0["forced"] >= 1
+    for k in ("rebuilds", "forced", "scheduled", "partial", "partial_bodies"):
+        assert s0[k] == s1[k], (k, s0[k], s1[k])
+    for k in ("pos", "vel", "Q", "vrot", "acc", "arot"):
+        assert np.array_equal(b0[k], b1[k]), k
+    assert gst["replays"] > 0
