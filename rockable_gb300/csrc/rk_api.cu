@@ -579,23 +579,25 @@ static int step_graph(Ctx& c) {
   return RK_OK;
 }
 
-// Steps per batch of the device-decided skin mode (skin_batch): long enough
-// to take the host round trip out of almost every step, short enough that the
+// Largest batch of the device-decided skin mode (skin_batch): long enough to
+// take the host round trip out of almost every step, short enough that the
 // steps skipped after a trigger (each a handful of launches that return at
-// once) stay cheap.
+// once) stay cheap.  A call for fewer steps runs the largest power-of-two
+// batch that fits, so that no step is skipped for want of work.
 constexpr int kSkinBatch = 16;
 
-// The graph of kSkinBatch steps, each opened by k_skin_begin and closed by
-// k_skin_end (rk_skin.cu); the narrow phase of the first step is timed for the
-// skin's cost model.  Captured with s.sk_ctl set, like the launches it holds.
-static int batch_graph(Ctx& c) {
+// The graph of a batch of 2^lg steps, each opened by k_skin_begin and closed
+// by k_skin_end (rk_skin.cu); the narrow phase of the first step is timed for
+// the skin's cost model.  Captured with s.sk_ctl set, like the launches it holds.
+static int batch_graph(Ctx& c, int lg) {
   Scene& s = c.s;
-  const bool stale = !c.bexec || c.bform != c.form || std::memcmp(&c.bscene, &s, sizeof(Scene)) != 0;
+  const bool stale =
+      !c.bexec[lg] || c.bform[lg] != c.form || std::memcmp(&c.bscene[lg], &s, sizeof(Scene)) != 0;
   if (stale) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
     int n = 0;
-    for (int q = 0; q < kSkinBatch; q++) {
+    for (int q = 0; q < (1 << lg); q++) {
       n += launch_skin_begin(s, c.stream);
       n += step_launches(c, q == 0);
       n += launch_skin_end(s, c.stream);
@@ -606,16 +608,16 @@ static int batch_graph(Ctx& c) {
       c.err = std::string("skin batch graph capture: ") + cudaGetErrorString(e);
       return RK_ERR_CUDA;
     }
-    const int rc = graph_install(c, g, &c.bexec, "skin batch graph");
+    const int rc = graph_install(c, g, &c.bexec[lg], "skin batch graph");
     if (rc) return rc;
-    std::memcpy(&c.bscene, &s, sizeof(Scene));
-    c.bform = c.form;
-    c.blaunched = n;
+    std::memcpy(&c.bscene[lg], &s, sizeof(Scene));
+    c.bform[lg] = c.form;
+    c.blaunched[lg] = n;
     c.graph_captures++;
   }
-  CK(cudaGraphLaunch(c.bexec, c.stream));
+  CK(cudaGraphLaunch(c.bexec[lg], c.stream));
   c.graph_replays++;
-  c.kernels += c.blaunched;
+  c.kernels += c.blaunched[lg];
   return RK_OK;
 }
 
@@ -628,7 +630,9 @@ static int skin_partial(Ctx& c, int64_t nflag);
 static int skin_batch(Ctx& c, int64_t left, int64_t* done) {
   Skin& k = c.skin;
   Scene& s = c.s;
-  const int64_t want = std::min<int64_t>(kSkinBatch, left);
+  int lg = 0;
+  while (lg < 4 && (int64_t)2 << lg <= left) lg++;
+  const int64_t want = (int64_t)1 << lg;
   unsigned int* in = k.h_ctl;
   unsigned int* out = k.h_ctl + 16;
   float trig = (float)(0.5 * k.skin);
@@ -643,7 +647,7 @@ static int skin_batch(Ctx& c, int64_t left, int64_t* done) {
   in[7] = 0u;
   CK(cudaMemcpyAsync(k.d_ctl, in, 8 * sizeof(unsigned int), cudaMemcpyHostToDevice, c.stream));
   s.sk_ctl = k.d_ctl;
-  int rc = batch_graph(c);
+  int rc = batch_graph(c, lg);
   s.sk_ctl = nullptr;
   if (rc) return rc;
   CK(cudaMemcpyAsync(out, k.d_ctl, 16 * sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
@@ -827,7 +831,8 @@ void rk_destroy(rk_ctx* x) {
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.gexec) cudaGraphExecDestroy(c.gexec);
-  if (c.bexec) cudaGraphExecDestroy(c.bexec);
+  for (cudaGraphExec_t e : c.bexec)
+    if (e) cudaGraphExecDestroy(e);
   for (int k = 0; k < 8; k++)
     if (c.tev[k]) cudaEventDestroy(c.tev[k]);
   Scene& s = c.s;

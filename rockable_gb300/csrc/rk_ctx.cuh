@@ -161,11 +161,11 @@ struct Ctx {
   int gform = -1;
   int glaunched = 0;    // kernels per replay
   int64_t graph_captures = 0, graph_replays = 0;
-  // the graph of a batch of skin steps (same rules as the step graph)
-  cudaGraphExec_t bexec = nullptr;
-  Scene bscene{};
-  int bform = -1;
-  int blaunched = 0;
+  // the graphs of batches of 1, 2, 4, 8, 16 skin steps (same rules as the step graph)
+  cudaGraphExec_t bexec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  Scene bscene[5]{};
+  int bform[5] = {-1, -1, -1, -1, -1};
+  int blaunched[5] = {0, 0, 0, 0, 0};
 };
 
 // Neighbour-list update; with `only` (device flags per body), only the pairs
