@@ -586,9 +586,10 @@ static int step_graph(Ctx& c) {
 // batch that fits, so that no step is skipped for want of work.
 constexpr int kSkinBatch = 16;
 
-// The graph of a batch of 2^lg steps, each opened by k_skin_begin and closed
-// by k_skin_end (rk_skin.cu); the narrow phase of the first step is timed for
-// the skin's cost model.  Captured with s.sk_ctl set, like the launches it holds.
+// The graph of a batch of 2^lg steps, opened by k_skin_begin; each step's
+// resultant kernel closes it (skin_batch_step_end); the narrow phase of the
+// first step is timed for the skin's cost model.  Captured with s.sk_ctl set,
+// like the launches it holds.
 static int batch_graph(Ctx& c, int lg) {
   Scene& s = c.s;
   const bool stale =
@@ -597,11 +598,8 @@ static int batch_graph(Ctx& c, int lg) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
     int n = 0;
-    for (int q = 0; q < (1 << lg); q++) {
-      n += launch_skin_begin(s, c.stream);
-      n += step_launches(c, q == 0);
-      n += launch_skin_end(s, c.stream);
-    }
+    n += launch_skin_begin(s, c.stream);
+    for (int q = 0; q < (1 << lg); q++) n += step_launches(c, q == 0);
     const cudaError_t e = cudaStreamEndCapture(c.stream, &g);
     if (e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
@@ -1411,8 +1409,18 @@ int rk_get_graph_stats(const rk_ctx* x, int64_t* captures, int64_t* replays) {
 int rk_set_form(rk_ctx* x, int form) {
   if (!x) return RK_ERR_ARG;
   if (form != RK_FORM_FP64 && form != RK_FORM_MIXED) return fail(x->c, RK_ERR_UNSUPPORTED, "unknown form");
-  x->c.form = form;
-  x->c.s.fast_body = form == RK_FORM_MIXED ? 1 : 0;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  const int fb = form == RK_FORM_MIXED ? 1 : 0;
+  c.form = form;
+  if (c.s.fast_body != fb) {
+    c.s.fast_body = fb;
+    // the resultant kernels split the heavy bodies differently (is_heavy 3)
+    if (c.s.ne > 0) {
+      const int rc = heavy_list(c);
+      if (rc) return rc;
+    }
+  }
   return RK_OK;
 }
 

@@ -262,6 +262,7 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   if (b < s.n) gather_body(s, b, apply_kick);
   // the learned skin's guard on the state this step leaves (all lanes)
   if (s.sk_out && apply_kick) skin_guard_body(s, b);
+  if (s.sk_ctl) skin_batch_step_end(s);
 }
 
 }  // namespace RK_BODY_NS

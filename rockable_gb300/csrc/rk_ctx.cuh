@@ -64,7 +64,7 @@ struct Skin {
   uint8_t* flag = nullptr;          // n: bodies due for a partial refresh
   unsigned int* d_guard = nullptr;  // guard reductions (see k_skin_guard)
   unsigned int* h_guard = nullptr;  // pinned
-  // batched steps: control block (see k_skin_end) on the device, and its
+  // batched steps: control block (see rk_skin.cu) on the device, and its
   // pinned host copies (words 0-15 written before a batch, 16-31 read after)
   unsigned int* d_ctl = nullptr;
   unsigned int* h_ctl = nullptr;

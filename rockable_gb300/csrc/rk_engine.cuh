@@ -27,6 +27,7 @@ constexpr int kMaxSub = 1024;       // sub-element index limit of the sort key
 constexpr int kMaxBody = 1 << 21;   // body index limit of the sort key
 constexpr int kMaskWords = 2;       // vertex cull mask words per half-pair (<= 64 vertices)
 constexpr int kHeavy = 64;          // entries above which a body's resultant is summed by a block
+constexpr int kHeavyWarp = 1024;    // mixed form: up to this many, by its warp inside the resultant kernel
 
 __host__ __device__ __forceinline__ uint64_t entry_key(uint32_t i, uint32_t j, uint32_t t, uint32_t isub,
                                                        uint32_t jsub) {
@@ -115,7 +116,7 @@ struct Scene {
   int nheavy;
   int* heavy_lazy;    // heavy driven bodies whose resultant feeds no state (summed on demand)
   int nheavy_lazy;
-  uint8_t* is_heavy;  // n: 1 summed by k_gather_heavy in the step, 2 deferred
+  uint8_t* is_heavy;  // n: 1 summed by k_gather_heavy in the step, 2 deferred, 3 summed by its warp (mixed form)
   uint8_t* needres;   // n: 1 when the body's resultant is used by the step (free or force-controlled)
   float* bnd;         // n: largest distance of a vertex from the body centre (world, rounded up)
   int* scene_of;      // n: scene index (bodies of different scenes never interact)
@@ -131,7 +132,7 @@ struct Scene {
   uint8_t* sk_flag;
   unsigned int* sk_out;  // 8 words, zeroed by the resultant kernel's launcher (by k_skin_begin in a batch)
   float sk_flag_at;
-  // batched skin steps (rk_skin.cu, k_skin_end): when set, every step kernel
+  // batched skin steps (rk_skin.cu, skin_batch_step_end): when set, every step kernel
   // returns at once while sk_ctl[0] (halt) is set
   unsigned int* sk_ctl;
   float4* sph;        // per body: vertex, edge and face bounding spheres (world frame, float)
@@ -178,7 +179,6 @@ int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_lis
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);
 int launch_skin_begin(const Scene& s, cudaStream_t st);
-int launch_skin_end(const Scene& s, cudaStream_t st);
 cudaError_t fused_attributes(int which, cudaFuncAttributes* a);
 cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a);
 

@@ -131,6 +131,44 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   float kin[12] = {};
   bool have = false;
+  {
+    // bodies of this warp with is_heavy 3 (more than kHeavy entries): the
+    // warp sums each one's entries (lanes take strided entries, then a
+    // shuffle reduction) and the body's lane stores the resultant, which
+    // body_resultant reads back below
+    const bool hv = b < s.n && s.is_heavy[b] == 3;
+    unsigned hm = __ballot_sync(0xffffffffu, hv);
+    const int lane = threadIdx.x & 31;
+    while (hm) {
+      const int src = __ffs(hm) - 1;
+      hm &= hm - 1;
+      const int64_t hb = __shfl_sync(0xffffffffu, b, src);
+      double a[6] = {0, 0, 0, 0, 0, 0};
+      const int64_t i0 = s.iofs[hb], i1 = s.iofs[hb + 1], j0 = s.jofs[hb], j1 = s.jofs[hb + 1];
+      for (int64_t e = i0 + lane; e < i1; e += 32) {
+        if (!s.act[e]) continue;
+        const V3 f = ld3(s.cf, e), m = ld3(s.cmi, e);
+        a[0] += f.x; a[1] += f.y; a[2] += f.z;
+        a[3] += m.x; a[4] += m.y; a[5] += m.z;
+      }
+      for (int64_t p = j0 + lane; p < j1; p += 32) {
+        const int64_t e = s.jlist[p];
+        if (!s.act[e]) continue;
+        const V3 f = ld3(s.cf, e), m = ld3(s.cmj, e);
+        a[0] -= f.x; a[1] -= f.y; a[2] -= f.z;
+        a[3] += m.x; a[4] += m.y; a[5] += m.z;
+      }
+#pragma unroll
+      for (int d = 0; d < 6; d++)
+        for (int o = 16; o > 0; o >>= 1) a[d] += __shfl_xor_sync(0xffffffffu, a[d], o);
+      if (lane == src) {
+        V3 F, M;
+        init_resultant(s, hb, F, M);
+        st3(s.force, hb, F + v3(a[0], a[1], a[2]));
+        st3(s.moment, hb, M + v3(a[3], a[4], a[5]));
+      }
+    }
+  }
   if (b < s.n) {
     if (b < s.n_driven) {
       gather_body(s, b, apply_kick);
@@ -172,6 +210,7 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   }
   // the learned skin's guard on the state this step leaves (all lanes)
   if (s.sk_out && apply_kick) skin_guard_body_t<CvtBits>(s, b, have, kin);
+  if (s.sk_ctl) skin_batch_step_end(s);
 }
 
 // Resultant of a body with many entries (one block per body): threads sum

@@ -153,6 +153,41 @@ __device__ __forceinline__ void skin_guard_body_t(const Scene& s, int64_t b, boo
   }
 }
 
+// End of a batched skin step (control block sk_ctl, see rk_skin.cu): every
+// block of the resultant kernel calls it after its guard atomics (all its
+// threads); the last block to arrive reads the step's guard words, counts the
+// step and halts the batch when the host has to act -- a refresh is due or
+// the batch's step budget is spent -- and otherwise zeroes the counters for
+// the next step (the guard words and the active-contact count).
+__device__ __forceinline__ void skin_batch_step_end(const Scene& s) {
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&s.sk_ctl[7], 1u) == gridDim.x - 1 ? 1 : 0;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  volatile unsigned int* ctl = s.sk_ctl;
+  volatile unsigned int* out = s.sk_out;
+  const unsigned ex = ctl[1] + 1u, since = ctl[2] + 1u;
+  ctl[1] = ex;
+  ctl[2] = since;
+  ctl[7] = 0u;
+  unsigned int g[8];
+  for (int d = 0; d < 8; d++) {
+    g[d] = out[d];
+    ctl[8 + d] = g[d];
+  }
+  const float crit = __uint_as_float(ctl[6] ? g[2] : g[0]);
+  if (crit >= __uint_as_float(ctl[5]) || since >= ctl[4] || ex >= ctl[3]) {
+    ctl[0] = 1u;
+  } else {
+    for (int d = 0; d < 8; d++) out[d] = 0u;
+    s.flags[FLAG_NACTIVE] = 0ull;
+  }
+}
+
 __device__ __forceinline__ void skin_guard_body(const Scene& s, int64_t b) {
   const float none[12] = {};
   skin_guard_body_t<CvtHw>(s, b, false, none);

@@ -170,7 +170,9 @@ __global__ void k_heavy(Scene s, unsigned long long* count) {
   }
   bool h = c > kHeavy;
   uint8_t kind = 0;
-  if (h && s.needres[b]) {
+  if (h && s.needres[b] && s.fast_body && c <= kHeavyWarp) {
+    kind = 3;  // the mixed form's resultant kernel sums it with the body's warp
+  } else if (h && s.needres[b]) {
     kind = 1;
     s.heavy[atomicAdd(&count[0], 1ull)] = (int)b;
   } else if (h) {

@@ -82,16 +82,18 @@ int launch_skin_reset(const Scene& s, const uint8_t* only, double* rp, double* r
 
 // ------------------------------------------------------ batched steps ----
 // A batch of steps runs as one graph without a host round trip per step:
-// each step opens with k_skin_begin and closes with k_skin_end, which reads
-// the exact guard the resultant kernel just reduced and halts the rest of the
-// batch when the host has to act (a refresh is due, or the batch's step
-// budget is spent); a halted step's kernels return at once.  Control block
-// sk_ctl (words, set by the host before the batch):
+// k_skin_begin opens the batch, and the last block of each step's resultant
+// kernel reads the exact guard the kernel just reduced (skin_batch_step_end,
+// rk_guard.cuh) and halts the rest of the batch when the host has to act (a
+// refresh is due, or the batch's step budget is spent); a halted step's
+// kernels return at once.  Control block sk_ctl (words, set by the host
+// before the batch):
 //   [0] halt  [1] steps executed  [2] steps since the last refresh
 //   [3] step budget  [4] refresh interval (steps)  [5] trigger (float bits,
 //   the smallest float >= skin/2)  [6] 1: the trigger compares the path bound
-//   g, 0: the displacement bound delta  [8..15] guard words of the last
-//   executed step (the layout of sk_out).
+//   g, 0: the displacement bound delta  [7] arrival ticket of the resultant
+//   kernel's blocks  [8..15] guard words of the last executed step (the
+//   layout of sk_out).
 __global__ void k_skin_begin(Scene s) {
   if (step_halted(s)) return;
   const int t = threadIdx.x;
@@ -99,23 +101,8 @@ __global__ void k_skin_begin(Scene s) {
   if (t < 8) s.sk_out[t] = 0u;
 }
 
-__global__ void k_skin_end(Scene s) {
-  if (threadIdx.x != 0 || step_halted(s)) return;
-  unsigned int* ctl = s.sk_ctl;
-  const unsigned ex = ctl[1] + 1u, since = ctl[2] + 1u;
-  ctl[1] = ex;
-  ctl[2] = since;
-  for (int d = 0; d < 8; d++) ctl[8 + d] = s.sk_out[d];
-  const float crit = __uint_as_float(ctl[6] ? s.sk_out[2] : s.sk_out[0]);
-  if (crit >= __uint_as_float(ctl[5]) || since >= ctl[4] || ex >= ctl[3]) ctl[0] = 1u;
-}
-
 int launch_skin_begin(const Scene& s, cudaStream_t st) {
   k_skin_begin<<<1, 32, 0, st>>>(s);
-  return 1;
-}
-int launch_skin_end(const Scene& s, cudaStream_t st) {
-  k_skin_end<<<1, 32, 0, st>>>(s);
   return 1;
 }
 
