@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
 TUNE_STEPS = 10  # untimed block-size tuning steps before the warm-up (rk_set_autotune, 2 rounds of 5 sizes)
 NCU_NARROW_MIXED_BYTES_PER_ENTRY = 22.877e6 / 183166  # ncu, 50k-grain column, mixed form (124.9 B)
-NCU_GATHER_BYTES_PER_BODY = 11.5386e6 / 50001  # ncu, 50k-grain column, exact learned skin (230.8 B)
+NCU_GATHER_BYTES_PER_BODY = 11.54432e6 / 50001  # ncu --set full, 50k-grain column, exact learned skin (230.9 B)
 
 
 def parse():
