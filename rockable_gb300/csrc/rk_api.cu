@@ -94,7 +94,8 @@ int ensure_entry_capacity(Ctx& c, int which, int64_t n) {
     int64_t cap = std::max<int64_t>(n + n / 2, 1024);
     Scene& s = c.s;
     if ((rc = dalloc(c, s.act, cap)) || (rc = dalloc(c, s.cf, 3 * cap)) || (rc = dalloc(c, s.cmi, 3 * cap)) ||
-        (rc = dalloc(c, s.cmj, 3 * cap)) || (rc = dalloc(c, s.jlist, cap)) || (rc = dalloc(c, s.nperm, cap)))
+        (rc = dalloc(c, s.cmj, 3 * cap)) || (rc = dalloc(c, s.jlist, cap)) || (rc = dalloc(c, s.nperm, cap)) ||
+        (rc = dalloc(c, s.egv, cap)))
       return rc;
     c.contrib_cap = cap;
   }
@@ -837,10 +838,10 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.vert_ofs); dfree(s.edge_ofs); dfree(s.edges); dfree(s.face_ofs); dfree(s.face_vofs); dfree(s.face_verts);
   dfree(s.svert); dfree(s.sradius); dfree(s.sobb);
   dfree(s.pos); dfree(s.vel); dfree(s.acc); dfree(s.Q); dfree(s.vrot); dfree(s.arot); dfree(s.force); dfree(s.moment);
-  dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.shape); dfree(s.group); dfree(s.cluster);
+  dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.inv_mi); dfree(s.shape); dfree(s.group); dfree(s.cluster);
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
-  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm);
+  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
   dfree(s.needres); dfree(s.scene_of);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
@@ -935,11 +936,14 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
   c.s.near_geometric = 0;
   std::vector<int64_t> gv_ofs(n + 1, 0);
   std::vector<double> rad(n);
+  std::vector<float> inv_mi(4 * n);  // the mixed form's 1/m, 1/Ix, 1/Iy, 1/Iz
   for (int64_t i = 0; i < n; i++) {
     int sh = b->shape[i];
     if (sh < 0 || sh >= c.s.nshapes) return fail(c, RK_ERR_ARG, "body shape index out of range");
     gv_ofs[i + 1] = gv_ofs[i] + c.shape_nv[sh];
     rad[i] = b->homothety[i] * c.shape_radius[sh];  // Particle::MinkowskiRadius (Particle.cpp:71)
+    inv_mi[4 * i] = (float)(1.0 / b->mass[i]);
+    for (int d = 0; d < 3; d++) inv_mi[4 * i + 1 + d] = (float)(1.0 / b->inertia[3 * i + d]);
   }
   const int64_t nv = gv_ofs[n];
   std::vector<int64_t> sph_ofs(n + 1, 0);
@@ -962,7 +966,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.force, (const double*)nullptr, 3 * n)) ||
       (rc = dupload(c, s.moment, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.hom, b->homothety, n)) ||
       (rc = dupload(c, s.mass, b->mass, n)) || (rc = dupload(c, s.inertia, b->inertia, 3 * n)) ||
-      (rc = dupload(c, s.rad, rad.data(), n)) || (rc = dupload(c, s.shape, b->shape, n)) ||
+      (rc = dupload(c, s.rad, rad.data(), n)) || (rc = dupload(c, s.inv_mi, inv_mi.data(), 4 * n)) || (rc = dupload(c, s.shape, b->shape, n)) ||
       (rc = dupload(c, s.group, b->group, n)) || (rc = dupload(c, s.cluster, b->cluster, n)) ||
       (rc = dupload(c, s.gv_ofs, gv_ofs.data(), n + 1)) || (rc = dupload(c, s.gv_body, gv_body.data(), nv)) ||
       (rc = dalloc(c, s.lv, std::max<int64_t>(nv, 1))) ||

@@ -68,6 +68,7 @@ struct Scene {
   int64_t n_driven;
   double *pos, *vel, *acc, *Q, *vrot, *arot, *force, *moment;
   double *hom, *mass, *inertia, *rad;
+  float* inv_mi;  // 4 per body: 1/m and the inverse principal moments, rounded to float (mixed form)
   int *shape, *group, *cluster;
   int64_t nvert;     // total global vertices
   int64_t* gv_ofs;   // n+1
@@ -112,6 +113,11 @@ struct Scene {
   int64_t* jsplit;  // n: first j-side slot of body b whose entry follows b's own block
   int* jlist;     // ne
   int* nperm;     // ne: entries grouped by sub-contact type (the narrow phase's thread order)
+  // ne: global vertex indices of each entry's sub-elements (k_entry_gv, after every list change):
+  // vertex-vertex (a, b), vertex-edge (a, p1, p2), vertex-triangle (a, A, B, C; w = -1 for
+  // faces of more than 3 vertices), edge-edge (pi1, pi2, pj1, pj2)
+  int4* egv;
+  int egv_ok;     // egv holds the current list (global vertex indices fit in an int)
   int* heavy;     // bodies whose entry count exceeds kHeavy (summed by a block each)
   int nheavy;
   int* heavy_lazy;    // heavy driven bodies whose resultant feeds no state (summed on demand)

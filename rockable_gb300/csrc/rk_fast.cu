@@ -75,10 +75,10 @@ __device__ __forceinline__ q4f qddotf(q4f q, f3v w, f3v a) {
   const f3v r = 0.5f * (q.s * a + crossf(a, v));
   return mk4(-0.5f * dotf(a, v) - w2 * q.s, r.x - w2 * v.x, r.y - w2 * v.y, r.z - w2 * v.z);
 }
-// Euler's equations in the principal frame
-__device__ __forceinline__ f3v euler_f(f3v I, f3v w, f3v M) {
-  return mk3((M.x - (I.z - I.y) * w.y * w.z) / I.x, (M.y - (I.x - I.z) * w.z * w.x) / I.y,
-             (M.z - (I.y - I.x) * w.x * w.y) / I.z);
+// Euler's equations in the principal frame (iI: the inverse moments)
+__device__ __forceinline__ f3v euler_f(f3v I, f3v iI, f3v w, f3v M) {
+  return mk3((M.x - (I.z - I.y) * w.y * w.z) * iI.x, (M.y - (I.x - I.z) * w.z * w.x) * iI.y,
+             (M.z - (I.y - I.x) * w.x * w.y) * iI.z);
 }
 
 // First half of the velocity-Verlet step for the free bodies (the FP64 form:
@@ -183,13 +183,13 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
       }
       const double mass = s.mass[b];
       const f3v Fg = cvt3(v3(fma(mass, s.gravity[0], F.x), fma(mass, s.gravity[1], F.y), fma(mass, s.gravity[2], F.z)));
-      const float im = 1.f / d2f(mass);
-      const f3v acc = im * Fg;
+      const float4 imi = reinterpret_cast<const float4*>(s.inv_mi)[b];
+      const f3v acc = imi.x * Fg;
       const q4f qf = cvt4(ldq(s.Q, b));
       const q4f qi = mk4(qf.s, -qf.x, -qf.y, -qf.z);
       const f3v wf = cvt3(vrot);
       const f3v om = qrotf(qi, wf), Mb = qrotf(qi, cvt3(M));
-      const f3v arot = qrotf(qf, euler_f(ld3f(s.inertia, b), om, Mb));
+      const f3v arot = qrotf(qf, euler_f(ld3f(s.inertia, b), mk3(imi.y, imi.z, imi.w), om, Mb));
       st3f(s.acc, b, acc);
       st3f(s.arot, b, arot);
       f3v vf = cvt3(vel), wk = wf;

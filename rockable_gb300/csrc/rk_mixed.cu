@@ -45,6 +45,10 @@ __device__ __forceinline__ void st3m(double* a, int64_t k, F3 v) {
   a[3 * k + 2] = f2d(v.z);
 }
 __device__ __forceinline__ V3 gvm(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
+__device__ __forceinline__ V3 gvg(const double* g, int k) {
+  const int64_t q = 3 * (int64_t)k;
+  return v3(g[q], g[q + 1], g[q + 2]);
+}
 
 // |d| in FP64 from an FP32 reciprocal-sqrt seed and two Newton steps
 __device__ __forceinline__ double len64(V3 d, double& inv) {
@@ -69,15 +73,24 @@ __global__ void k_narrow_force_mixed(Scene s) {
     const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);
     const double dn_old = s.dn[e];
     const int bond = s.bond[e];
-    const double* gi = s.gv + 3 * s.gv_ofs[i];
-    const double* gj = s.gv + 3 * s.gv_ofs[j];
+    // the sub-elements' global vertices: from the per-entry index table when
+    // it holds the list (one load), else through the shape tables
+    const bool pre = s.egv_ok != 0;
+    const int4 G = pre ? s.egv[e] : make_int4(-1, -1, -1, -1);
     const double Ri = s.rad[i], Rj = s.rad[j];
     const V3 xi = ld3m(s.pos, i), xj = ld3m(s.pos, j);
     double dn = 0.0;
     F3 n = f3(0, 0, 0), ci = f3(0, 0, 0);  // normal, contact point relative to x_i
     bool ok = true;
     if (type == 0) {
-      V3 a = gvm(gi, isub), b = gvm(gj, jsub);
+      V3 a, b;
+      if (pre) {
+        a = gvg(s.gv, G.x);
+        b = gvg(s.gv, G.y);
+      } else {
+        a = gvm(s.gv + 3 * s.gv_ofs[i], isub);
+        b = gvm(s.gv + 3 * s.gv_ofs[j], jsub);
+      }
       V3 d = a - b;
       double inv;
       double L = len64(d, inv);
@@ -85,10 +98,18 @@ __global__ void k_narrow_force_mixed(Scene s) {
       n = tof(d * inv);
       ci = tof(a - xi) - d2f(Ri + 0.5 * dn) * n;
     } else if (type == 1) {
-      const int sj = s.shape[j];
-      const int eo = s.edge_ofs[sj] + jsub;
-      V3 p1 = gvm(gj, s.edges[2 * eo]), p2 = gvm(gj, s.edges[2 * eo + 1]);
-      V3 a = gvm(gi, isub);
+      V3 a, p1, p2;
+      if (pre) {
+        a = gvg(s.gv, G.x);
+        p1 = gvg(s.gv, G.y);
+        p2 = gvg(s.gv, G.z);
+      } else {
+        const double* gj = s.gv + 3 * s.gv_ofs[j];
+        const int eo = s.edge_ofs[s.shape[j]] + jsub;
+        p1 = gvm(gj, s.edges[2 * eo]);
+        p2 = gvm(gj, s.edges[2 * eo + 1]);
+        a = gvm(s.gv + 3 * s.gv_ofs[i], isub);
+      }
       V3 E = p2 - p1, w = a - p1;
       F3 Ef = tof(E), wf = tof(w);
       float r = dotf(wf, Ef) / dotf(Ef, Ef);
@@ -103,12 +124,28 @@ __global__ void k_narrow_force_mixed(Scene s) {
         ci = tof(a - xi) - d2f(Ri + 0.5 * dn) * n;
       }
     } else if (type == 2) {
-      const int sj = s.shape[j];
-      const int fo = s.face_ofs[sj] + jsub;
-      const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
-      const int* fv = s.face_verts + v0;
-      V3 A = gvm(gj, fv[0]), B = gvm(gj, fv[1]), C = gvm(gj, fv[nbv - 1]);
-      V3 a = gvm(gi, isub);
+      // a triangle's three vertices come from the table; other polygons
+      // walk the shape's face list
+      const bool tri = pre && G.w >= 0;
+      const double* gj = s.gv + 3 * (tri ? (int64_t)0 : s.gv_ofs[j]);
+      const int* fv = nullptr;
+      int nbv = 3;
+      V3 A, B, C, a;
+      if (tri) {
+        A = gvg(s.gv, G.y);
+        B = gvg(s.gv, G.z);
+        C = gvg(s.gv, G.w);
+        a = gvg(s.gv, G.x);
+      } else {
+        const int fo = s.face_ofs[s.shape[j]] + jsub;
+        const int v0 = s.face_vofs[fo];
+        nbv = s.face_vofs[fo + 1] - v0;
+        fv = s.face_verts + v0;
+        A = gvm(gj, fv[0]);
+        B = gvm(gj, fv[1]);
+        C = gvm(gj, fv[nbv - 1]);
+        a = pre ? gvg(s.gv, G.x) : gvm(s.gv + 3 * s.gv_ofs[i], isub);
+      }
       V3 w = a - A;
       V3 nn = cross(B - A, C - A);
       double inv;
@@ -118,19 +155,28 @@ __global__ void k_narrow_force_mixed(Scene s) {
       if (dist < 0.0) { nn = -nn; dist = -dist; }
       // crossing-number test in FP32, relative to the face vertex A
       F3 nf = tof(nn);
-      F3 v1 = tof(B - A);
-      v1 = rsqrtf(dotf(v1, v1)) * v1;
+      const F3 bA = tof(B - A);
+      F3 v1 = rsqrtf(dotf(bA, bA)) * bA;
       F3 v2 = crossf(nf, v1);
       F3 P = tof(w - dist * nn);
       float ori1 = dotf(P, v1), ori2 = dotf(P, v2);
       int odd = 0;
-      for (int iva = 0; iva < nbv; ++iva) {
-        int ivb = iva + 1;
-        if (ivb == nbv) ivb = 0;
-        F3 pa = tof(gvm(gj, fv[iva]) - A), pb = tof(gvm(gj, fv[ivb]) - A);
+      auto edge = [&](F3 pa, F3 pb) {
         float pa1 = dotf(pa, v1), pb1 = dotf(pb, v1), pa2 = dotf(pa, v2), pb2 = dotf(pb, v2);
         if ((pa2 < ori2 && pb2 >= ori2) || (pb2 < ori2 && pa2 >= ori2)) {
           if (pa1 + (ori2 - pa2) / (pb2 - pa2) * (pb1 - pa1) < ori1) odd = 1 - odd;
+        }
+      };
+      if (tri) {
+        const F3 z = f3(0, 0, 0), cA = tof(C - A);
+        edge(z, bA);
+        edge(bA, cA);
+        edge(cA, z);
+      } else {
+        for (int iva = 0; iva < nbv; ++iva) {
+          int ivb = iva + 1;
+          if (ivb == nbv) ivb = 0;
+          edge(tof(gvm(gj, fv[iva]) - A), tof(gvm(gj, fv[ivb]) - A));
         }
       }
       if (odd) {
@@ -141,10 +187,21 @@ __global__ void k_narrow_force_mixed(Scene s) {
         ok = false;
       }
     } else {
-      const int si = s.shape[i], sj = s.shape[j];
-      const int eoi = s.edge_ofs[si] + isub, eoj = s.edge_ofs[sj] + jsub;
-      V3 pi1 = gvm(gi, s.edges[2 * eoi]), pi2 = gvm(gi, s.edges[2 * eoi + 1]);
-      V3 pj1 = gvm(gj, s.edges[2 * eoj]), pj2 = gvm(gj, s.edges[2 * eoj + 1]);
+      V3 pi1, pi2, pj1, pj2;
+      if (pre) {
+        pi1 = gvg(s.gv, G.x);
+        pi2 = gvg(s.gv, G.y);
+        pj1 = gvg(s.gv, G.z);
+        pj2 = gvg(s.gv, G.w);
+      } else {
+        const double* gi = s.gv + 3 * s.gv_ofs[i];
+        const double* gj = s.gv + 3 * s.gv_ofs[j];
+        const int eoi = s.edge_ofs[s.shape[i]] + isub, eoj = s.edge_ofs[s.shape[j]] + jsub;
+        pi1 = gvm(gi, s.edges[2 * eoi]);
+        pi2 = gvm(gi, s.edges[2 * eoi + 1]);
+        pj1 = gvm(gj, s.edges[2 * eoj]);
+        pj2 = gvm(gj, s.edges[2 * eoj + 1]);
+      }
       V3 Ei = pi2 - pi1, Ej = pj2 - pj1, w = pi1 - pj1;
       F3 Eif = tof(Ei), Ejf = tof(Ej), wf = tof(w);
       float c = dotf(Eif, Eif), d = dotf(Ejf, Ejf), ee = dotf(Eif, Ejf);

@@ -1311,11 +1311,45 @@ static int entry_order(Ctx& c) {
   return 0;
 }
 
+// Global vertex indices of each entry's sub-elements (see Scene::egv): the
+// mixed narrow phase loads its vertices without the shape tables' chain of
+// dependent loads.
+__global__ void k_entry_gv(Scene s) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= s.ne) return;
+  const int i = s.ei[e], j = s.ej[e];
+  const uint32_t ts = s.etsub[e];
+  const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);
+  const int oi = (int)s.gv_ofs[i], oj = (int)s.gv_ofs[j];
+  int4 g = make_int4(-1, -1, -1, -1);
+  if (type == 0) {
+    g = make_int4(oi + isub, oj + jsub, -1, -1);
+  } else if (type == 1) {
+    const int eo = s.edge_ofs[s.shape[j]] + jsub;
+    g = make_int4(oi + isub, oj + s.edges[2 * eo], oj + s.edges[2 * eo + 1], -1);
+  } else if (type == 2) {
+    const int fo = s.face_ofs[s.shape[j]] + jsub;
+    const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
+    const int* fv = s.face_verts + v0;
+    g = nbv == 3 ? make_int4(oi + isub, oj + fv[0], oj + fv[1], oj + fv[2]) : make_int4(oi + isub, -1, -1, -1);
+  } else {
+    const int eoi = s.edge_ofs[s.shape[i]] + isub, eoj = s.edge_ofs[s.shape[j]] + jsub;
+    g = make_int4(oi + s.edges[2 * eoi], oi + s.edges[2 * eoi + 1], oj + s.edges[2 * eoj], oj + s.edges[2 * eoj + 1]);
+  }
+  s.egv[e] = g;
+}
+
 int heavy_list(Ctx& c) {
   Scene& s = c.s;
   {
     const int rc = entry_order(c);
     if (rc) return rc;
+  }
+  s.egv_ok = 0;
+  if (s.ne > 0 && s.nvert < (int64_t)0x7fffffff) {
+    k_entry_gv<<<nblk(s.ne, 256), 256, 0, c.stream>>>(s);
+    c.kernels++;
+    s.egv_ok = 1;
   }
   // counter slots 1, 2: heavy bodies, deferred heavy bodies; 4: listed vertices
   RKCHK(cudaMemsetAsync(c.w.counter + 1, 0, 32, c.stream));
