@@ -118,6 +118,9 @@ class Clocks:
 
 
 def dist_setup():
+    """One process per GPU under torchrun (RANK / LOCAL_RANK / WORLD_SIZE /
+    MASTER_* from the environment): NCCL with a GPU, gloo without one (the
+    CPU tests of the multi-rank path).  Returns (rank, world size, module)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, None
@@ -125,9 +128,29 @@ def dist_setup():
     import torch.distributed as dist
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    backend = "gloo"
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+        backend = "nccl"
+    dist.init_process_group(backend)
     return rank, ws, dist
+
+
+def rank_max(x, dist):
+    """The largest x over the ranks (the slowest replica's time sets the job's)."""
+    if not dist:
+        return float(x)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(ws, units_per_rank, steps, ms):
+    """Whole-job throughput: every rank's units over the slowest rank's time
+    (replicas: each rank runs the full workload on its own GPU)."""
+    return ws * units_per_rank * steps / (ms / 1000.0)
 
 
 def pinned(shape):
@@ -332,10 +355,12 @@ def run_reference(a, rank):
 
 def main():
     a = parse()
-    rank, ws, dist = dist_setup()
     if a.impl == "reference":
-        run_reference(a, rank)
+        # the reference's CPU path runs once, on rank 0; under torchrun the
+        # other ranks exit without work (no process group: nothing to join)
+        run_reference(a, int(os.environ.get("RANK", "0")))
         return
+    rank, ws, dist = dist_setup()
     from rockable_gb300 import build_ext
     if rank == 0:
         build_ext.build()
@@ -388,13 +413,9 @@ def main():
             nvtx.range_pop()
         ms, launches = e.last_step_timing()
         ck = clocks.stop()
-        if dist:
-            import torch
-            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = rank_max(ms, dist)
         return {"ms": ms, "launches": launches, "wall": wall, "rep": rep, "clocks": ck,
-                "value": ws * nfree * steps / (ms / 1000.0)}
+                "value": job_rate(ws, nfree, steps, ms)}
 
     def profile(e, n):
         e.set_profiling(True)
@@ -463,13 +484,15 @@ def main():
         g.download_kinematics_packed(hb)
         k_e2e = max(5, min(a.steps, 50))
         g.synchronize()
+        if dist:
+            dist.barrier()
         t0 = time.perf_counter()
         for _ in range(k_e2e):
             g.upload_kinematics_packed(hb)
             g.step(1)
             g.download_kinematics_packed(hb)
-        el = time.perf_counter() - t0
-        e2e = {"value": ws * nfree * k_e2e / el, "unit": "particle-steps/s",
+        el = rank_max(time.perf_counter() - t0, dist)
+        e2e = {"value": job_rate(ws, nfree, k_e2e, 1000.0 * el), "unit": "particle-steps/s",
                "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8),
                "steps": k_e2e, "note": "every step: the kinematics (pos, vel, acc, Q, vrot, arot) of every body "
                                        "H2D from one pinned packed buffer, rk_step(1), the same fields D2H back "
