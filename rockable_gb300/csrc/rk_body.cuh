@@ -3,8 +3,9 @@
 // learned-skin guard), included twice: by rk_step.cu, compiled without
 // contraction into fused multiply-adds (kernels in rk::exact, the FP64 form
 // that reproduces the reference arithmetic bit for bit), and by rk_fast.cu,
-// compiled with it (kernels in rk::fused, the mixed form, where the last-bit
-// differences are within its tolerance).  Define RK_BODY_NS before including.
+// compiled with it (rk::fused: only the world-vertex kernel, with
+// RK_BODY_GLOB_ONLY defined; the mixed form has its own drift and resultant
+// kernels there).  Define RK_BODY_NS before including.
 #ifndef RK_BODY_HELPERS
 #define RK_BODY_HELPERS
 #include "rk_engine.cuh"
@@ -204,6 +205,7 @@ __device__ __forceinline__ void gather_body(const Scene& s, int64_t b, int apply
 namespace rk {
 namespace RK_BODY_NS {
 
+#ifndef RK_BODY_GLOB_ONLY
 // ----------------------------------------------------------------- K1 ----
 __global__ void k_drift(Scene s) {
   if (step_halted(s)) return;
@@ -237,6 +239,8 @@ __global__ void k_drift(Scene s) {
   st3(s.vrot, i, w);
 }
 
+#endif  // RK_BODY_GLOB_ONLY
+
 // global vertex k of body b: pos + Q (h v)
 // With only_listed, the vertices of s.lv (the bodies with neighbour-list
 // entries): within a step only the narrow phase reads these positions, and
@@ -256,6 +260,7 @@ __global__ void k_glob_vertices(Scene s, int only_listed) {
   st3(s.gv, k, g);
 }
 
+#ifndef RK_BODY_GLOB_ONLY
 __global__ void k_gather_accel(Scene s, int apply_kick) {
   if (step_halted(s)) return;
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -264,6 +269,8 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   if (s.sk_out && apply_kick) skin_guard_body(s, b);
   if (s.sk_ctl) skin_batch_step_end(s);
 }
+
+#endif  // RK_BODY_GLOB_ONLY
 
 }  // namespace RK_BODY_NS
 }  // namespace rk

@@ -1,9 +1,9 @@
 // rk_fast.cu -- per-body kernels of the mixed form.
 //
-// The generic per-body kernels of rk_body.cuh are compiled here a second time
-// with fused multiply-adds allowed (namespace rk::fused); the mixed form uses
-// them for the world vertices and for driven bodies.  Free bodies take the
-// kernels of namespace rk::mx, written for GB300's FP64 rate (about 1/77 of
+// The world-vertex kernel of rk_body.cuh is compiled here a second time with
+// fused multiply-adds allowed (rk::fused::k_glob_vertices), and driven bodies
+// go through its FP64 helpers (gather_body).  Free bodies take the kernels of
+// namespace rk::mx, written for GB300's FP64 rate (about 1/77 of
 // its FP32 rate, and a hardware FP64 <-> FP32 conversion costs as much as an
 // FP64 add): the state (positions, velocities, quaternions, angular
 // velocities) stays FP64 and is advanced by FP64 additions of increments
@@ -19,6 +19,7 @@
 #include "rk_engine.cuh"
 #include "rk_guard.cuh"
 #define RK_BODY_NS fused
+#define RK_BODY_GLOB_ONLY
 #include "rk_body.cuh"
 
 namespace rk {
