@@ -193,6 +193,11 @@ bool Rockable::parse(std::istream& conf) {  // Rockable.cpp:643-1069
     } else if (tok == "AddOrRemoveInteractions") {
       std::string n; conf >> n;
       if (n == "bruteForce" || n == "OBBtree") optionNames["AddOrRemoveInteractions"] = n;
+      // the GPU list update tests every sub-element pair of a visited body pair
+      // (AddOrRemoveInteractions_bruteForce, Rockable.cpp:1309-1432); the tree
+      // variant (1440-1541) tests only the pairs whose leaf boxes overlap
+      if (n == "OBBtree")
+        std::cerr << "[rockable-gb300] AddOrRemoveInteractions OBBtree runs the bruteForce sub-element test\n";
     } else if (tok == "UpdateNL") {
       std::string n; conf >> n;
       if (n == "bruteForce" || n == "linkCells") optionNames["UpdateNL"] = n;
