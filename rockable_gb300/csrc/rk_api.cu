@@ -1466,6 +1466,15 @@ int rk_update_nl(rk_ctx* x) {
   launch_glob_vertices(c.s, c.stream, true);
   if ((rc = rebuild_nl(c))) return rc;
   c.nl_updates++;
+  if (c.skin.on) {
+    // the list now holds the current state (which the host may have moved):
+    // the skin's guard restarts from it, as after a full skin rebuild
+    Skin& k = c.skin;
+    c.kernels += launch_skin_reset(c.s, nullptr, k.ref_pos, k.ref_q, k.maxd, k.path, c.stream);
+    k.since = 0;
+    k.partial_since_global = 0;
+    k.have_pred = false;
+  }
   CK(cudaStreamSynchronize(c.stream));
   return RK_OK;
 }
