@@ -37,3 +37,34 @@ def test_drop_bodies_remaps_entries_in_key_order():
     old = {0: 0, **{k: k - 4 for k in range(5, 55)}}
     assert np.array_equal(de["i"], [old[x] for x in e["i"][keep]])
     assert np.array_equal(d["bodies"]["pos"][1:], sc["bodies"]["pos"][5:])
+
+
+def test_sphero_cube_box_runs_on_the_oracle():
+    """Workload config 0 (512 sphero-cubes on a lattice in a box of 6 plates,
+    Default law, brute-force neighbour list, 20k steps of 1e-6 s) written as
+    a Rockable conf and run by the oracle: the top layer falls freely by
+    g t^2 / 2, nothing leaves the box or sinks through the floor by more than
+    a contact overlap, and contacts form."""
+    import tempfile
+    from oracle import oracle
+    from rockable_gb300 import scenes
+    oracle.build()
+    sc = scenes.sphero_cube_box()
+    o = oracle.Oracle(scenes.write_conf(sc, tempfile.mkdtemp(prefix="rk_cubes_")))
+    assert o.n == 518 and o.n_driven == 6 and o.law == 0
+    o.update_nl()
+    p0 = o.bodies()["pos"][6:].copy()
+    steps = 20000
+    o.run(steps)
+    p = o.bodies()["pos"][6:]
+    assert np.all(np.isfinite(p))
+    t = steps * sc["dt"]
+    fall = 0.5 * 9.81 * t * t
+    top = np.argmax(p0[:, 2])
+    assert abs((p0[top, 2] - p[top, 2]) - fall) <= 0.05 * fall
+    L = float(np.max(sc["bodies"]["pos"][:6, 0]))  # the box's side (wall plates at 0 and L)
+    assert np.all(p[:, :2] > 0.0) and np.all(p[:, :2] < L)
+    # a cube resting on a face has its centre half a side plus the rounding (0.5 mm) above the
+    # floor; the contact overlap under its weight is far below a micrometre
+    assert p[:, 2].min() >= 0.5e-3 - 1e-6
+    assert o.stats()["n_active"] > 0
