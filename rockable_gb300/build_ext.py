@@ -80,7 +80,7 @@ def build_host(gpu_lib):
     cxx = shutil.which("g++") or "g++"
     host = os.path.join(LIBDIR, "librk_host.so")
     stamp = os.path.join(BUILD, "librk_host.so.stamp")
-    srcs = [os.path.join(hsrc, "rk_host.cpp")]
+    srcs = [os.path.join(hsrc, "rk_host.cpp"), os.path.join(hsrc, "rk_extractors.cpp")]
     deps = srcs + [os.path.join(hsrc, "rk_host.hpp"), os.path.join(HERE, "..", "include", "rk_gpu.h"), gpu_lib]
     if not os.path.exists(stamp) or any(os.path.getmtime(d) > os.path.getmtime(stamp) for d in deps):
         cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-o", host] + srcs + \

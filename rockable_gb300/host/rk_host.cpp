@@ -294,6 +294,19 @@ bool Rockable::parse(std::istream& conf) {  // Rockable.cpp:643-1069
       bf->read(conf);
       bodyForce.reset(bf);
       return fail("BodyForce plugins are evaluated on the host; the GPU step does not take them yet");
+    } else if (tok == "DataExtractor") {  // Rockable.cpp:1003-1022 (kept for compatibility)
+      std::string name; conf >> name;
+      register_builtin_extractors();
+      std::cerr << "[rockable-gb300] the DataExtractor named " << name
+                << " is defined in the input file; dataExtractors.txt is the place for it\n";
+      DataExtractor* de = Factory<DataExtractor>::instance().create(name);
+      if (!de) {
+        std::cerr << "[rockable-gb300] the DataExtractor named " << name << " is unknown\n";
+      } else {
+        de->plug(this);
+        de->read(conf);
+        dataExtractors.emplace_back(de);
+      }
     } else if (tok == "usePeriodicCell" || tok == "initSpringJoint" || tok == "useSoftParticles") {
       return fail("keyword " + tok + " is outside the GPU engine (periodic cells, spring joints, soft particles)");
     }
@@ -725,13 +738,37 @@ bool Rockable::run(long nsteps) {
 long Rockable::consoleRun(const std::string& outdir, long max_steps) {  // run.cpp + Rockable.cpp:2538-2746
   if (!uploaded_) { fail("load a conf first"); return -1; }
   if (!updateNL()) return -1;
-  for (auto& de : dataExtractors) de->init();
+  // the data extractors of ./dataExtractors.txt (Rockable.cpp:1152-1180,
+  // 1241-1250), documented in extractedDataDoc.txt, then initialised
+  if (!extractorsRead_) {
+    extractorsRead_ = true;
+    readDataExtractors("dataExtractors.txt");
+  }
+  if (!dataExtractors.empty()) {
+    std::ofstream doc("extractedDataDoc.txt");
+    for (auto& de : dataExtractors) de->generateHelp(doc);
+  }
+  bool geo_extractor = false;
+  for (auto& de : dataExtractors) {
+    de->init();
+    geo_extractor = geo_extractor || de->needsGeometry();
+  }
+  // the reference's step counter: (size_t)(t / dt) at the start, compared
+  // with nstep / nrec after the step's body, then incremented
+  auto due = [&](long s, bool geometry_only) {
+    for (auto& de : dataExtractors) {
+      if (geometry_only && !de->needsGeometry()) continue;
+      if ((!geometry_only && de->nstep > 0 && s % de->nstep == 0) || (de->nrec > 0 && s % de->nrec == 0)) return true;
+    }
+    return false;
+  };
   const double dt_2 = 0.5 * dt;
   if (!syncFromDevice(true) || !saveConf(outdir + "/conf" + std::to_string(iconf))) return -1;
   step_ = (long)(t / dt);
   long steps = 0;
   while (t <= tmax && (max_steps <= 0 || steps < max_steps)) {
-    // steps until the next conf output (same accumulation as the reference)
+    // steps until the next conf output or extractor call (same accumulation
+    // as the reference)
     long n = 0;
     double tt = t, cc = interConfC_;
     bool save = false;
@@ -742,17 +779,19 @@ long Rockable::consoleRun(const std::string& outdir, long max_steps) {  // run.c
       cc += dt;
       n++;
       if (cc >= interConf - dt_2) { save = true; break; }
-      if (!dataExtractors.empty()) break;
+      if (!dataExtractors.empty() && due(step_ + n - 1, false)) break;
     }
     if (n == 0) break;
+    const long s_last = step_ + n - 1;
+    const bool geo = save || (geo_extractor && due(s_last, true));
     if (n > 1) {
       rk_step_report rep{};
       if (!ck(rk_step(ctx_, n - 1, &rep), "rk_step")) return -1;
     }
-    if (!ck(rk_set_record_geometry(ctx_, save ? 1 : 0), "rk_set_record_geometry")) return -1;
+    if (!ck(rk_set_record_geometry(ctx_, geo ? 1 : 0), "rk_set_record_geometry")) return -1;
     rk_step_report rep{};
     if (!ck(rk_step(ctx_, 1, &rep), "rk_step")) return -1;
-    if (save) rk_set_record_geometry(ctx_, 0);
+    if (geo) rk_set_record_geometry(ctx_, 0);
     t = tt;
     interConfC_ = cc;
     steps += n;
@@ -762,12 +801,23 @@ long Rockable::consoleRun(const std::string& outdir, long max_steps) {  // run.c
       if (!syncFromDevice(true) || !saveConf(outdir + "/conf" + std::to_string(iconf))) return -1;
       interConfC_ = 0.0;
     }
-    if (!dataExtractors.empty()) {
-      if (!save && !syncFromDevice(false)) return -1;
+    if (!dataExtractors.empty() && due(s_last, false)) {
+      if (!save && !syncFromDevice(geo)) return -1;
       for (auto& de : dataExtractors) {
-        if (de->nstep > 0 && step_ % de->nstep == 0) de->exec();
-        if (de->nrec > 0 && step_ % de->nrec == 0) de->record();
+        if (de->nstep > 0 && s_last % de->nstep == 0) de->exec();
+        if (de->nrec > 0 && s_last % de->nrec == 0) de->record();
       }
+    }
+    if (computationStopAsked > 0) {
+      // the reference's loop makes one more step before it sees the request
+      // (Rockable.cpp:2586-2595)
+      rk_step_report r2{};
+      if (!ck(rk_step(ctx_, 1, &r2), "rk_step")) return -1;
+      t += dt;
+      interConfC_ += dt;
+      steps++;
+      step_++;
+      break;
     }
   }
   for (auto& de : dataExtractors) de->end();

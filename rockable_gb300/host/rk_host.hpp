@@ -10,10 +10,12 @@
 #pragma once
 #include <array>
 #include <cstdint>
+#include <fstream>
 #include <functional>
 #include <iosfwd>
 #include <map>
 #include <memory>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -48,11 +50,17 @@ class BodyForce {
 };
 
 // DataExtractor (src/DataExtractors/DataExtractor.hpp:46-73).  exec() and
-// record() see the host mirror of the state, downloaded at their cadence.
+// record() see the host mirror of the state, downloaded at their cadence
+// (consoleRun: exec when step % nstep == 0, record when step % nrec == 0, with
+// the reference's step counter, Rockable.cpp:2580, 2717-2738).
 class DataExtractor {
  public:
   Rockable* box{nullptr};
   int nstep{1}, nrec{1};
+  std::string filename;      // the data file, opened by read()
+  std::ofstream recordFile;
+  std::stringstream docString;
+  std::vector<std::string> columnDoc;
   virtual ~DataExtractor() = default;
   void plug(Rockable* b) { box = b; }
   virtual void read(std::istream& is) = 0;
@@ -60,7 +68,10 @@ class DataExtractor {
   virtual void exec() {}
   virtual void record() {}
   virtual void end() {}
-  virtual void generateHelp(std::ostream&) {}
+  // record() reads the contact points of the entries (downloaded only on demand)
+  virtual bool needsGeometry() const { return false; }
+  // the entry of extractedDataDoc.txt (DataExtractor.cpp: generateHelp)
+  virtual void generateHelp(std::ostream& os);
 };
 
 template <class T>
@@ -160,6 +171,16 @@ class Rockable {
 
   rk_ctx* ctx() { return ctx_; }
 
+  // for the data extractors (Particle::GlobVertex / MinkowskiRadius,
+  // Particle.cpp:55-71): vertex v of body b in world coordinates
+  void globVertex(size_t b, size_t v, double out[3]) const;
+  double minkowskiRadius(size_t b) const;
+  // reads "name parameters" records from a dataExtractors.txt file
+  // (Rockable::readDataExtractors, Rockable.cpp:1152-1180); unknown names are
+  // reported and skipped; a missing file adds none
+  bool readDataExtractors(const std::string& path);
+  int computationStopAsked{0};  // set by an extractor: the run stops after one more step
+
  private:
   bool parse(std::istream& is);
   bool loadShapes(const std::string& path);
@@ -177,9 +198,11 @@ class Rockable {
   bool uploaded_{false};
   double interConfC_{0.0};
   long step_{0};
+  bool extractorsRead_{false};
 };
 
 void register_builtin_plugins();
+void register_builtin_extractors();  // rk_extractors.cpp
 
 }  // namespace rkhost
 
