@@ -1,7 +1,8 @@
-"""bench.py's multi-rank path on the CPU: two ranks over gloo (what
+"""bench.py on the CPU: the multi-rank path with two ranks over gloo (what
 torchrun --nproc-per-node 2 sets up, with the GPUs hidden), the max-over-ranks
-time and the whole-job rate; and the reference arm, which runs on rank 0
-only while the other ranks exit at once without joining a process group."""
+time and the whole-job rate; the reference arm, which runs on rank 0 only
+while the other ranks exit at once without joining a process group; and the
+reference arm's JSON line."""
 import json
 import os
 import socket
@@ -62,3 +63,27 @@ def test_reference_arm_runs_on_rank_zero_only():
                        timeout=180)
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_json_line():
+    """The reference arm's one JSON line on rank 0 (the oracle on the host
+    cores; without a GPU the column is not collapsed first and `sample` says
+    so): the keys of the bench contract, with its own cpu_baseline and an e2e
+    object that moves no bytes."""
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n", "1500", "--steps", "3",
+                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.strip().splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ["metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config"]:
+        assert k in d, k
+    assert d["impl"] == "reference" and d["steps"] == 3 and d["warmup"] == 3 and d["value"] > 0
+    assert d["higher_is_better"] is True and d["vs_baseline"] is None and "workload" in d["config"]
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    e = d["e2e"]
+    assert e["value"] == d["value"] and e["unit"] == d["unit"]
+    assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
