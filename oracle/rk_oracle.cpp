@@ -697,34 +697,37 @@ static double contact_damping(const Sim& S, size_t i, size_t j, size_t idEn2, si
 // --------------------------------------------------- neighbour list ----
 typedef bool (*NearFn)(const Body&, const Body&, size_t, size_t, double);
 
-// Rockable.cpp:1309-1432 (AddOrRemoveInteractions_bruteForce)
-static int add_or_remove(Sim& S, size_t i, size_t j, double dmax) {
-  int nbAdd = 0;
-  double Damp = contact_damping(S, i, j, S.idEn2, S.idKn);
+// Rockable.cpp:1309-1432 (AddOrRemoveInteractions_bruteForce), in two
+// phases so that the NEAR predicates of many body pairs can run in parallel
+// (like the reference's OpenMP loop over link cells, Rockable.cpp:1697):
+// eval_pair tests the pair's sub-element candidates against the geometry
+// only and records the NEAR keys and which vertex-owned candidates were
+// tested; apply_pair then inserts the new NEAR keys and erases the tested
+// ones that are no longer NEAR.  A key belongs to one body pair only, so
+// applying the pairs in visit order gives exactly the sets of the serial
+// loop.
+struct PairWork {
+  size_t i, j;
+  bool visit{false};        // the enlarged OBBs intersect
+  double damp{0.0};
+  std::vector<Key> near;    // NEAR keys, in key order
+  std::vector<char> cull_i, cull_j;  // vertex-owned candidates of i (j) tested
+};
+
+static void eval_pair(const Sim& S, PairWork& w, double dmax) {
+  const size_t i = w.i, j = w.j;
+  w.damp = contact_damping(S, i, j, S.idEn2, S.idKn);
   auto single = [&](size_t i_, size_t j_, size_t isub, int type, size_t nbj, NearFn fn) {
-    auto& set = S.inter[i_];
-    for (size_t jsub = 0; jsub < nbj; ++jsub) {
-      Key k{i_, j_, type, isub, jsub};
-      auto it = set.find(k);
-      bool isNew = (it == set.end());
-      bool isNear = fn(S.bodies[i_], S.bodies[j_], isub, jsub, dmax);
-      if (isNear && isNew) {
-        Contact c;
-        c.k = k;
-        c.damp = Damp;
-        set.emplace(k, c);
-        ++nbAdd;
-      } else if (!isNear && !isNew) {
-        set.erase(it);
-        --nbAdd;
-      }
-    }
+    for (size_t jsub = 0; jsub < nbj; ++jsub)
+      if (fn(S.bodies[i_], S.bodies[j_], isub, jsub, dmax)) w.near.push_back(Key{i_, j_, type, isub, jsub});
   };
-  Body& Pi = S.bodies[i];
-  Body& Pj = S.bodies[j];
+  const Body& Pi = S.bodies[i];
+  const Body& Pj = S.bodies[j];
   size_t nvi = Pi.shape->vertex.size(), nvj = Pj.shape->vertex.size();
   size_t nei = Pi.shape->edge.size(), nej = Pj.shape->edge.size();
   size_t nfi = Pi.shape->face.size(), nfj = Pj.shape->face.size();
+  w.cull_i.assign(nvi, 0);
+  w.cull_j.assign(nvj, 0);
   for (size_t isub = 0; isub < nvi; ++isub) {
     Obb sub;
     sub.center = Pi.glob_vertex(isub);
@@ -732,6 +735,7 @@ static int add_or_remove(Sim& S, size_t i, size_t j, double dmax) {
     Obb obbj = Pj.obb;
     obbj.enlarge(dmax);
     if (!obb_intersect(obbj, sub)) continue;
+    w.cull_i[isub] = 1;
     single(i, j, isub, VV, nvj, near_vv);
     single(i, j, isub, VE, nej, near_ve);
     single(i, j, isub, VF, nfj, near_vf);
@@ -743,11 +747,57 @@ static int add_or_remove(Sim& S, size_t i, size_t j, double dmax) {
     Obb obbi = Pi.obb;
     obbi.enlarge(dmax);
     if (!obb_intersect(obbi, sub)) continue;
+    w.cull_j[jsub] = 1;
     single(j, i, jsub, VE, nei, near_ve);
     single(j, i, jsub, VF, nfi, near_vf);
   }
   for (size_t isub = 0; isub < nei; ++isub) single(i, j, isub, EE, nej, near_ee);
-  return nbAdd;
+  std::sort(w.near.begin(), w.near.end());  // key order, for apply_pair's lookups
+}
+
+static void apply_pair(Sim& S, const PairWork& w) {
+  auto sweep = [&](size_t a, size_t b, const std::vector<char>& cull) {
+    auto& set = S.inter[a];
+    auto it = set.lower_bound(Key{a, b, 0, 0, 0});
+    while (it != set.end() && it->first.i == a && it->first.j == b) {
+      const Key& k = it->first;
+      bool tested = (k.type == EE && a == w.i) || (k.isub < cull.size() && cull[k.isub] &&
+                                                   (a == w.i ? (k.type == VV || k.type == VE || k.type == VF)
+                                                             : (k.type == VE || k.type == VF)));
+      bool isNear = tested && std::binary_search(w.near.begin(), w.near.end(), k);
+      if (tested && !isNear) it = set.erase(it);
+      else ++it;
+    }
+  };
+  sweep(w.i, w.j, w.cull_i);
+  sweep(w.j, w.i, w.cull_j);
+  for (const Key& k : w.near) {
+    auto& set = S.inter[k.i];
+    if (set.find(k) == set.end()) {
+      Contact c;
+      c.k = k;
+      c.damp = w.damp;
+      set.emplace(k, c);
+    }
+  }
+}
+
+// The visited pairs of one list update: OBB test and NEAR predicates in
+// parallel, the list changes in visit order.
+static void process_pairs(Sim& S, std::vector<PairWork>& work) {
+  const long np = (long)work.size();
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long p = 0; p < np; ++p) {
+    PairWork& w = work[p];
+    Obb obbi = S.bodies[w.i].obb;
+    obbi.enlarge(0.5 * S.DVerlet);
+    Obb obbj = S.bodies[w.j].obb;
+    obbj.enlarge(0.5 * S.DVerlet);
+    w.visit = obb_intersect(obbi, obbj);
+    if (w.visit) eval_pair(S, w, S.dVerlet);
+  }
+  for (long p = 0; p < np; ++p)
+    if (work[p].visit) apply_pair(S, work[p]);
 }
 
 static bool has_iface(const Sim& S, size_t i, size_t j) {
@@ -757,19 +807,21 @@ static bool has_iface(const Sim& S, size_t i, size_t j) {
 // Rockable.cpp:1614-1662 (UpdateNL_bruteForce)
 static void update_nl_bruteforce(Sim& S) {
   size_t N = S.bodies.size();
-  for (size_t i = 0; i < N; ++i) S.bodies[i].update_obb();
+#pragma omp parallel for
+  for (long i = 0; i < (long)N; ++i) S.bodies[i].update_obb();
+  std::vector<PairWork> work;
   for (size_t i = 0; i < N; ++i) {
-    Obb obbi = S.bodies[i].obb;
-    obbi.enlarge(0.5 * S.DVerlet);
     size_t jnext = i + 1;
     if (jnext < S.nDriven) jnext = S.nDriven;
     for (size_t j = jnext; j < N; j++) {
       if (has_iface(S, i, j)) continue;
-      Obb obbj = S.bodies[j].obb;
-      obbj.enlarge(0.5 * S.DVerlet);
-      if (obb_intersect(obbi, obbj)) add_or_remove(S, i, j, S.dVerlet);
+      PairWork w;
+      w.i = i;
+      w.j = j;
+      work.push_back(std::move(w));
     }
   }
+  process_pairs(S, work);
 }
 
 // Rockable.cpp:1667-1809 (UpdateNL_linkCells).  The cell grid follows the
@@ -805,7 +857,8 @@ static void compute_aabb(Sim& S, size_t first, std::vector<V3>& bmin, std::vecto
 }
 static void update_nl_linkcells(Sim& S) {
   size_t N = S.bodies.size();
-  for (size_t i = 0; i < N; ++i) S.bodies[i].update_obb();
+#pragma omp parallel for
+  for (long i = 0; i < (long)N; ++i) S.bodies[i].update_obb();
   std::vector<V3> bmin, bmax;
   V3 smin, smax;
   compute_aabb(S, S.boxForLinkCellsOpt == 1 ? S.nDriven : 0, bmin, bmax, smin, smax);
@@ -833,15 +886,15 @@ static void update_nl_linkcells(Sim& S) {
     }
     cells[((size_t)c[0] * n[1] + c[1]) * n[2] + c[2]].push_back(i);
   }
+  std::vector<PairWork> work;
   auto visit = [&](size_t i, size_t j) {
     if (j < S.nDriven && i < S.nDriven) return;
     if (j <= i) return;
     if (has_iface(S, i, j)) return;
-    Obb obbi = S.bodies[i].obb;
-    obbi.enlarge(0.5 * S.DVerlet);
-    Obb obbj = S.bodies[j].obb;
-    obbj.enlarge(0.5 * S.DVerlet);
-    if (obb_intersect(obbi, obbj)) add_or_remove(S, i, j, S.dVerlet);
+    PairWork w;
+    w.i = i;
+    w.j = j;
+    work.push_back(std::move(w));
   };
   for (int ix = 0; ix < n[0]; ix++)
     for (int iy = 0; iy < n[1]; iy++)
@@ -860,6 +913,7 @@ static void update_nl_linkcells(Sim& S) {
   for (auto& Cv : cells)
     for (size_t a : oversized)
       for (size_t b : Cv) visit(a, b);
+  process_pairs(S, work);
 }
 
 static void update_nl(Sim& S) {

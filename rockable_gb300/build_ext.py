@@ -95,7 +95,28 @@ def build_host(gpu_lib):
         if r.returncode != 0:
             raise RuntimeError("runner build failed:\n%s\n%s" % (r.stdout, r.stderr))
         open(stamp, "w").write(host + "\n")
+    build_packer()
     return host
+
+
+def build_packer():
+    """rk_pack, the CPU packer of the benchmark and test scenes: a standalone
+    executable (no CUDA, no library of this package), so that a CPU-only
+    process can build the same initial states as a GPU one."""
+    src = os.path.join(HERE, "host", "rk_pack.cpp")
+    exe = os.path.join(LIBDIR, "rk_pack")
+    stamp = os.path.join(BUILD, "rk_pack.stamp")
+    if os.path.exists(exe) and os.path.exists(stamp) and os.path.getmtime(stamp) >= os.path.getmtime(src):
+        return exe
+    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(BUILD, exist_ok=True)
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-o", exe, src]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("packer build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    open(stamp, "w").write(exe + "\n")
+    return exe
 
 
 if __name__ == "__main__":

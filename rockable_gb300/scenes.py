@@ -131,6 +131,69 @@ def random_quaternions(rng, n):
     return q / np.linalg.norm(q, axis=1)[:, None]
 
 
+def resting_quaternions(rng, n, tilt_deg=25.0):
+    """Orientations of grains lying flat, as in a settled pile: the shape's
+    third principal axis (largest moment of inertia: the grain's shortest
+    dimension) near the vertical, tilted by a uniform angle up to tilt_deg
+    about a random horizontal axis, turned by a uniform angle about the
+    vertical and flipped upside down half of the time."""
+    turn = rng.uniform(0.0, 2.0 * np.pi, n)
+    flip = rng.random(n) < 0.5
+    tilt = np.radians(tilt_deg) * rng.random(n)
+    az = rng.uniform(0.0, 2.0 * np.pi, n)
+    qz = np.stack([np.cos(0.5 * turn), np.zeros(n), np.zeros(n), np.sin(0.5 * turn)], 1)
+    qf = np.where(flip[:, None], np.array([0.0, 1.0, 0.0, 0.0]), np.array([1.0, 0.0, 0.0, 0.0]))
+    qt = np.stack([np.cos(0.5 * tilt), np.sin(0.5 * tilt) * np.cos(az), np.sin(0.5 * tilt) * np.sin(az),
+                   np.zeros(n)], 1)
+    q = _qmul(qt, _qmul(qz, qf))
+    return q / np.linalg.norm(q, axis=1)[:, None]
+
+
+def _quat_from_to(a, b):
+    """Unit quaternion (w, x, y, z) of the shortest rotation taking unit
+    vector a to unit vector b."""
+    c = float(np.dot(a, b))
+    if c < -1.0 + 1e-12:  # opposite: half turn about any axis normal to a
+        ax = np.cross(a, [1.0, 0.0, 0.0])
+        if np.linalg.norm(ax) < 1e-6:
+            ax = np.cross(a, [0.0, 1.0, 0.0])
+        ax /= np.linalg.norm(ax)
+        return np.array([0.0, ax[0], ax[1], ax[2]])
+    v = np.cross(a, b)
+    q = np.array([1.0 + c, v[0], v[1], v[2]])
+    return q / np.linalg.norm(q)
+
+
+def stable_face_quaternions(rng, shapes, shape_of):
+    """Orientations of grains resting on a face: for each grain, the hull
+    facet nearest its centre of mass along its outward normal (for a convex
+    body that facet always holds it in equilibrium on a flat support: the
+    centre of mass projects inside it) is turned face down, then the grain is
+    turned by a uniform angle about the vertical."""
+    down = np.array([0.0, 0.0, -1.0])
+    face_q = {}
+    for s in np.unique(shape_of):
+        v = np.asarray(shapes[s]["vertices"])
+        best, qb = None, None
+        for f in shapes[s]["faces"]:
+            a, b, c = v[f[0]], v[f[1]], v[f[-1]]
+            nrm = np.cross(b - a, c - a)
+            ln = np.linalg.norm(nrm)
+            if ln == 0.0:
+                continue
+            nrm /= ln
+            h = float(np.dot(a, nrm))  # distance of the facet plane from the centre of mass
+            if h > 0.0 and (best is None or h < best):
+                best, qb = h, _quat_from_to(nrm, down)
+        face_q[int(s)] = qb if qb is not None else np.array([1.0, 0.0, 0.0, 0.0])
+    n = len(shape_of)
+    turn = rng.uniform(0.0, 2.0 * np.pi, n)
+    qz = np.stack([np.cos(0.5 * turn), np.zeros(n), np.zeros(n), np.sin(0.5 * turn)], 1)
+    qf = np.array([face_q[int(s)] for s in shape_of])
+    q = _qmul(qz, qf)
+    return q / np.linalg.norm(q, axis=1)[:, None]
+
+
 # ------------------------------------------------------------------ scenes --
 def deposit(rng, radii, half_x, half_y, z0, gap=1e-5):
     """Loose random packing by ballistic deposition: each grain, in the given
@@ -172,41 +235,146 @@ def deposit(rng, radii, half_x, half_y, z0, gap=1e-5):
     return pos
 
 
+PACK_MAGIC = 0x524b5041434b3032  # "RKPACK02"
+
+
+def _cache_dir():
+    import tempfile
+    d = os.environ.get("RK_SCENE_CACHE", os.path.join(tempfile.gettempdir(), "rockable_gb300_scenes"))
+    os.makedirs(d, exist_ok=True)
+    return d
+
+
+def pack(shapes, shape_of, Q, volume, lo, hi, scale=None, tol=1e-9, seed=SEED, max_iters=200, cache=True):
+    """Loose random packing by sequential ballistic deposition with the exact
+    grain geometry (the CPU packer host/rk_pack.cpp): the grains, with the
+    given shapes (indices into `shapes`), uniform scale factors and
+    orientations, one at a time from a seeded random point of the footprint
+    [lo, hi] (x, y, side walls there), fall onto the floor lo z or the grains
+    already there and slide without friction (translating only) until three
+    supports hold them, within `tol`; they never overlap.  Returns
+    (positions (n, 3), stats).  The result is cached by the hash of its input
+    (RK_SCENE_CACHE or the temp directory), so that the processes of one
+    benchmark run pack once."""
+    import hashlib
+    import subprocess
+    import tempfile
+    n = len(shape_of)
+    nv = np.array([len(s["vertices"]) for s in shapes], np.int32)
+    rad = np.array([s["radius"] for s in shapes], np.float64)
+    verts = np.concatenate([np.asarray(s["vertices"], np.float64).ravel() for s in shapes])
+    scale = np.ones(n) if scale is None else np.asarray(scale, np.float64)
+    prm = np.array(list(lo) + list(hi) + [tol, float(seed)], np.float64)
+    parts = [np.array([PACK_MAGIC, len(shapes)], np.int64).tobytes(), nv.tobytes(), rad.tobytes(), verts.tobytes(),
+             np.array([n], np.int64).tobytes(), np.asarray(shape_of, np.int32).tobytes(), scale.tobytes(),
+             np.ascontiguousarray(Q, np.float64).tobytes(), np.asarray(volume, np.float64).tobytes(), prm.tobytes(),
+             np.array([max_iters], np.int64).tobytes()]
+    blob = b"".join(parts)
+    from . import build_ext
+    exe = build_ext.build_packer()
+    key = hashlib.sha1(blob + open(os.path.join(build_ext.HERE, "host", "rk_pack.cpp"), "rb").read()).hexdigest()
+    out_path = os.path.join(_cache_dir(), "pack_%s.bin" % key)
+    if cache and os.path.exists(out_path) and os.path.getsize(out_path) == 8 * (3 * n + 8):
+        raw = np.fromfile(out_path, np.float64)
+    else:
+        with tempfile.TemporaryDirectory(prefix="rk_pack_") as d:
+            inp = os.path.join(d, "in.bin")
+            tmp = os.path.join(d, "out.bin")
+            with open(inp, "wb") as f:
+                f.write(blob)
+            r = subprocess.run([exe, inp, tmp], capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("rk_pack failed (%d): %s" % (r.returncode, r.stderr))
+            raw = np.fromfile(tmp, np.float64)
+            if cache:
+                os.replace(tmp, out_path)
+    s = raw[3 * n:]
+    return raw[:3 * n].reshape(n, 3), {"touching_pairs": int(s[0]), "on_floor": int(s[1]), "top": float(s[2]),
+                                       "solid_fraction": float(s[3]), "moves": int(s[4]), "at_rest": int(s[5]),
+                                       "max_overlap": float(s[6])}
+
+
 def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2700.0, kn=1e6, kt=1e6,
-                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), pack=1.0, walls=False):
-    """Granular column collapse: n hull grains (axes U[0.5, 1.5] cm, i.e.
-    semi-axes U[0.25, 0.75] cm), loosely packed by ballistic deposition in a
-    0.5 x 0.5 m column above a rigid floor plate (body 0).  With walls, four
-    vertical plates (bodies 1-4, listed in "walls") confine the column, to be
-    removed (drop_bodies) when the collapse starts; without, the walls are
-    already released.  With pack < 1 the deposition uses bounding spheres
-    shrunk by that factor, so that the hulls interpenetrate slightly."""
+                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), walls=False, semi=(0.005, 0.015)):
+    """Granular column collapse: n hull grains (semi-axes U[0.5, 1.5] cm,
+    rounding 5 % of the smallest), each resting on a face, in a loose random
+    packing (sequential deposition with frictionless sliding, pack()) that
+    fills a 0.5 x 0.5 m column on a rigid floor plate (body 0) to about
+    1.2 m.  With walls, four vertical plates (bodies 1-4, listed in "walls")
+    confine the column as it was packed, to be removed (drop_bodies) when the
+    collapse starts; without, the walls are already released (t = 0 of the
+    collapse)."""
     rng = np.random.default_rng(seed)
     shapes = [plate_shape("FLOOR", 1.5, 0.005)]
-    shapes += [hull_shape(rng, "G%05d" % k) for k in range(nshapes)]
-    bound = np.array([s["bound"] for s in shapes])
+    shapes += [hull_shape(rng, "G%05d" % k, semi_lo=semi[0], semi_hi=semi[1]) for k in range(nshapes)]
     shape_of = rng.integers(1, nshapes + 1, n)
-    pos = deposit(rng, pack * bound[shape_of], 0.5 * column[0], 0.5 * column[1], 0.005 + 1e-5)
-    Q = random_quaternions(rng, n)
-    bmax = float(bound[1:].max())
+    Q = stable_face_quaternions(rng, shapes, shape_of)
+    vol = np.array([shapes[k]["volume"] for k in shape_of])
+    hx, hy = 0.5 * column[0], 0.5 * column[1]
+    pos, st = pack(shapes, shape_of, Q, vol, (-hx, -hy, 0.005), (hx, hy, column[2]), seed=seed)
+    bmax = max(float(shapes[k]["bound"]) for k in np.unique(shape_of))
     wall_pos, wall_Q, wall_shape = [np.zeros(3)], [np.array([1.0, 0, 0, 0])], [0]
     if walls:
         rw = 0.005
-        top = float(np.max(pos[:, 2] + bound[shape_of]))
-        half = max(0.5 * max(column[0], column[1]) + 0.05, 0.5 * top + 0.05)
+        top = st["top"]
+        half = max(max(hx, hy) + 0.05, 0.5 * top + 0.05)
         shapes.append(plate_shape("WALL", half, rw))  # after the grain shapes: their indices do not move
         ws = len(shapes) - 1
         s2 = math.sqrt(0.5)
-        hx, hy, zc = 0.5 * column[0] + rw, 0.5 * column[1] + rw, 0.5 * top
-        wall_pos += [np.array([hx, 0, zc]), np.array([-hx, 0, zc]), np.array([0, hy, zc]), np.array([0, -hy, zc])]
+        zc = 0.5 * top
+        wall_pos += [np.array([hx + rw, 0, zc]), np.array([-hx - rw, 0, zc]), np.array([0, hy + rw, zc]),
+                     np.array([0, -hy - rw, zc])]
         wall_Q += [np.array([s2, 0, s2, 0]), np.array([s2, 0, s2, 0]), np.array([s2, s2, 0, 0]),
                    np.array([s2, s2, 0, 0])]
         wall_shape += [ws] * 4
     out = _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, en2,
                     mu, dt, gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax,
                     interVerlet=100 * dt, name="column_collapse_%d" % n, wall_shape=wall_shape)
+    out["pack"] = st
     if walls:
         out["walls"] = [1, 2, 3, 4]
+    return out
+
+
+def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=2700.0, kn=1e6, kt=1e6, en2=0.25,
+                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=1e5, size=(0.005, 0.015)):
+    """Dense isotropic compression: n hull grains (8-20 vertices, diameters
+    uniform in `size`, ratio 1:3, by homothety of a library of shapes of
+    about 1 cm), packed loosely (pack()) in a cubic box, then enclosed by six
+    rigid walls (bodies 0-5: Xmin, Xmax, Ymin, Ymax, Zmin, Zmax) driven by
+    Rockable's tritriIsostaticCompression servo at `pressure` (DrivingSystem.
+    cpp:242-268: the min walls are held, the max walls pushed with pressure x
+    their face area); no gravity."""
+    rng = np.random.default_rng(seed)
+    lib = [hull_shape(rng, "G%05d" % k, semi_lo=0.004, semi_hi=0.006) for k in range(nshapes)]
+    shape_of = rng.integers(0, nshapes, n)
+    lib_d = np.array([2.0 * s["bound"] for s in lib])
+    h = rng.uniform(size[0], size[1], n) / lib_d[shape_of]
+    Q = stable_face_quaternions(rng, lib, shape_of)
+    vol = np.array([lib[k]["volume"] for k in shape_of]) * h ** 3
+    L = float((vol.sum() / 0.36) ** (1.0 / 3.0))  # a cube at a loose solid fraction
+    pos, st = pack(lib, shape_of, Q, vol, (-0.5 * L, -0.5 * L, 0.0), (0.5 * L, 0.5 * L, 4.0 * L), scale=h,
+                   seed=seed)
+    top = st["top"]
+    rw = 0.005
+    half = 0.5 * max(L, top) + 0.02
+    shapes = [plate_shape("WALL", half, rw)] + lib
+    s2 = math.sqrt(0.5)
+    zc = 0.5 * top
+    wall_pos = [np.array([-0.5 * L - rw, 0, zc]), np.array([0.5 * L + rw, 0, zc]),
+                np.array([0, -0.5 * L - rw, zc]), np.array([0, 0.5 * L + rw, zc]),
+                np.array([0, 0, -rw]), np.array([0, 0, top + rw])]
+    wall_Q = [np.array([s2, 0, s2, 0])] * 2 + [np.array([s2, s2, 0, 0])] * 2 + [np.array([1.0, 0, 0, 0])] * 2
+    bmax = float(np.max(lib_d[shape_of] * h)) * 0.5
+    out = _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of + 1, density, law, kn, kt, en2, mu, dt,
+                    gravity=(0.0, 0.0, 0.0), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax, interVerlet=100 * dt,
+                    name="iso_compression_%d" % n, wall_shape=0, homothety=h, wall_density=wall_density)
+    out["pack"] = st
+    # tritriIsostaticCompression: x/y/z velocity controls on the min walls,
+    # force controls on the max walls, the servo setting the forces
+    out["controls"] = {"type": [0, 6, 1, 7, 2, 8], "body": [0, 1, 2, 3, 4, 5], "value": [0.0] * 6,
+                       "vec": [[0.0, 0.0, 0.0]] * 6}
+    out["servo"] = {"kind": 1, "icontr": 0, "walls": [0, 1, 2, 3, 4, 5], "pressure": pressure}
     return out
 
 
@@ -392,23 +560,30 @@ def slope_batch(nscenes=256, seed=SEED, nmin=200, nmax=5000, nshapes=256, densit
 
 
 def _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of, density, law, kn, kt, en2, mu, dt, gravity, DVerlet,
-              dVerlet, interVerlet, name, wall_shape=0):
+              dVerlet, interVerlet, name, wall_shape=0, homothety=None, wall_density=None):
+    """Driven bodies (walls, group 1) first, then the grains (group 0).  Mass
+    and inertia follow Rockable::loadConf (Rockable.cpp:918-920): mass =
+    h^3 V density(group), inertia = h^2 (I/m) mass, h the homothety."""
     nd = len(wall_pos)
     n = nd + len(pos)
     shape = np.concatenate([np.broadcast_to(np.asarray(wall_shape), (nd,)), shape_of]).astype(np.int32)
     P = np.concatenate([np.array(wall_pos), pos])
     Qa = np.concatenate([np.array(wall_Q), Q])
     group = np.concatenate([np.ones(nd), np.zeros(len(pos))]).astype(np.int32)
+    hom = np.ones(n)
+    if homothety is not None:
+        hom[nd:] = homothety
+    wall_density = density if wall_density is None else wall_density
     vol = np.array([shapes[s]["volume"] for s in shape])
-    mass = vol * density
-    im = np.array([shapes[s]["I/m"] for s in shape])
+    mass = hom ** 3 * vol * np.where(group == 1, wall_density, density)
+    im = np.array([shapes[s]["I/m"] for s in shape]) * (hom ** 2)[:, None]
     tab = law_table(kn=kn, kt=kt, en2=en2, mu=mu)
     return {"name": name, "shapes": shapes, "shape_tables": flatten_shapes(shapes), "n_driven": nd,
             "bodies": {"pos": P, "vel": np.zeros((n, 3)), "acc": np.zeros((n, 3)), "Q": Qa,
-                       "vrot": np.zeros((n, 3)), "arot": np.zeros((n, 3)), "homothety": np.ones(n), "mass": mass,
+                       "vrot": np.zeros((n, 3)), "arot": np.zeros((n, 3)), "homothety": hom, "mass": mass,
                        "inertia": im * mass[:, None], "shape": shape, "group": group,
                        "cluster": np.zeros(n, np.int32)},
-            "density": {0: density, 1: density}, "law": law, "ngroup": 2, "table": tab, "dt": dt,
+            "density": {0: density, 1: wall_density}, "law": law, "ngroup": 2, "table": tab, "dt": dt,
             "gravity": gravity, "DVerlet": DVerlet, "dVerlet": dVerlet, "interVerlet": interVerlet,
             "params": {"kn": kn, "kt": kt, "en2": en2, "mu": mu}}
 
@@ -455,10 +630,15 @@ def settle(scene, steps=4000, dt=1e-5, kn=1e4, gboost=20.0, damping=0.5, device=
 
 
 def set_scene_params(g, scene, t=0.0, numerical_damping=0.0):
+    """Law, table, time step and Verlet parameters of the scene, and its
+    controls and servo when it has them."""
     from .abi import RK_LAW
     g.set_params(t=t, dt=scene["dt"], gravity=scene["gravity"], DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
                  interVerlet=scene["interVerlet"], interVerletC=0.0, law=RK_LAW[scene["law"]],
                  ngroup=scene["ngroup"], table=scene["table"], numerical_damping=numerical_damping)
+    c = scene.get("controls")
+    if c is not None:
+        g.set_controls(c["type"], c["body"], c["value"], c["vec"], scene.get("servo"))
 
 
 def scene_from_gpu(scene, g):
@@ -526,7 +706,8 @@ def write_conf(scene, directory, conf_name="input.conf", shape_name="shapes.shp"
             lines += ["knContact %d %d %r" % (g1, g2, p["kn"]), "en2Contact %d %d %r" % (g1, g2, p["en2"]),
                       "ktContact %d %d %r" % (g1, g2, p["kt"]), "muContact %d %d %r" % (g1, g2, p["mu"]),
                       "krContact %d %d 0" % (g1, g2), "murContact %d %d 0" % (g1, g2)]
-    bound = max(s["bound"] for s in scene["shapes"][scene["n_driven"] and 1:])
+    nd = scene["n_driven"]
+    bound = float(np.max(np.array([scene["shapes"][k]["bound"] for k in b["shape"][nd:]]) * b["homothety"][nd:]))
     cs = 2.0 * bound + scene["DVerlet"]
     lines += ["cellMinSizes %r %r %r" % (cs, cs, cs), "nDriven %d" % scene["n_driven"],
               "shapeFile %s" % shape_name, "precision 16", "Particles %d" % len(b["mass"])]
@@ -550,4 +731,9 @@ def write_conf(scene, directory, conf_name="input.conf", shape_name="shapes.shp"
     lines += ["Interfaces 0", ""]
     with open(os.path.join(directory, conf_name), "w") as f:
         f.write("\n".join(lines))
+    sv = scene.get("servo")
+    if sv is not None:  # DrivingSystem::read format (DrivingSystem.cpp:188-199)
+        with open(os.path.join(directory, "drivingSystem.txt"), "w") as f:
+            f.write("Servo tritriIsostaticCompression %s %r\n" % (" ".join(str(int(w)) for w in sv["walls"]),
+                                                                   float(sv["pressure"])))
     return os.path.join(directory, conf_name)

@@ -10,11 +10,54 @@ def test_walls_do_not_change_the_grains():
     assert b["n_driven"] == 5 and b["walls"] == [1, 2, 3, 4]
     for k in ["pos", "Q", "shape", "mass"]:
         assert np.array_equal(a["bodies"][k][1:], b["bodies"][k][5:]), k
-    # walls flush with the column, outside every grain's bounding sphere
-    bound = np.array([s["bound"] for s in b["shapes"]])
-    g = b["bodies"]["pos"][5:]
-    r = bound[b["bodies"]["shape"][5:]]
-    assert np.all(np.abs(g[:, 0]) + r <= 0.25 + 1e-12) and np.all(np.abs(g[:, 1]) + r <= 0.25 + 1e-12)
+    # walls flush with the column: every grain (rotated vertices plus the
+    # rounding radius) inside it
+    lo, hi = _extents(b)
+    assert np.all(lo[5:, :2] >= -0.25 - 1e-12) and np.all(hi[5:, :2] <= 0.25 + 1e-12)
+    assert np.all(lo[5:, 2] >= 0.005 - 1e-12)  # on or above the floor plate's top face
+
+
+def _extents(sc):
+    """World-frame bounds (vertices plus rounding radius) of every body."""
+    b = sc["bodies"]
+    lo = np.zeros((len(b["mass"]), 3))
+    hi = np.zeros_like(lo)
+    for k, (s, q, x, h) in enumerate(zip(b["shape"], b["Q"], b["pos"], b["homothety"])):
+        w, a, c, d = q
+        R = np.array([[1 - 2 * (c * c + d * d), 2 * (a * c - w * d), 2 * (a * d + w * c)],
+                      [2 * (a * c + w * d), 1 - 2 * (a * a + d * d), 2 * (c * d - w * a)],
+                      [2 * (a * d - w * c), 2 * (c * d + w * a), 1 - 2 * (a * a + c * c)]])
+        v = h * np.asarray(sc["shapes"][s]["vertices"]) @ R.T + x
+        r = h * sc["shapes"][s]["radius"]
+        lo[k], hi[k] = v.min(0) - r, v.max(0) + r
+    return lo, hi
+
+
+def test_packing_is_dense_at_rest_without_overlap_and_seeded():
+    """The column's loose random packing (host/rk_pack.cpp): every grain at
+    rest, several touching neighbours per grain, no overlap anywhere -- checked
+    independently by the oracle's neighbour list after one step (every
+    sub-contact's dn at or above minus the packer's tolerance) -- and the same
+    positions from a second, uncached run."""
+    import tempfile
+    from oracle import oracle
+    from rockable_gb300 import scenes
+    sc = scenes.column_collapse(n=1500, nshapes=64, column=(0.2, 0.2, 1.5))
+    st = sc["pack"]
+    assert st["at_rest"] == 1500 and st["max_overlap"] <= 0.0
+    assert 2 * st["touching_pairs"] / 1500 >= 3.0  # coordination of the pile
+    assert st["solid_fraction"] > 0.2
+    oracle.build()
+    o = oracle.Oracle(scenes.write_conf(sc, tempfile.mkdtemp(prefix="rk_pack_")))
+    o.update_nl()
+    o.run(1)
+    e = o.entries()
+    assert len(e["dn"]) > 10 * 1500 and e["dn"].min() >= -2e-9
+    b = sc["bodies"]
+    pos, st2 = scenes.pack(sc["shapes"], b["shape"][1:], b["Q"][1:], b["mass"][1:] / 2700.0, (-0.1, -0.1, 0.005),
+                           (0.1, 0.1, 1.5), cache=False)
+    assert np.array_equal(pos, b["pos"][1:])
+    assert all(st2[k] == st[k] for k in ["touching_pairs", "on_floor", "moves", "at_rest"])
 
 
 def test_drop_bodies_remaps_entries_in_key_order():
