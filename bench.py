@@ -1,31 +1,46 @@
 """Benchmark: particle-steps/s of the DEM step on one GB300.
 
 Workload (default): the granular column collapse -- 50,000 convex hull grains
-(Avalanche law, linked-cell neighbour list) falling onto a rigid floor --
-generated with a fixed seed by rockable_gb300.scenes.  One "step" is one pass
-of the velocity-Verlet step loop (drift, narrow phase + force law, ordered
-resultants, accelerations, half-kick, plus the NL rebuild every interVerlet).
+(semi-axes U[0.5, 1.5] cm, Avalanche law, linked-cell neighbour list) in a
+loose random packing that fills a 0.5 x 0.5 m column about 1.2 m high on a
+rigid floor, released at t = 0.  The packing is built on the CPU by the
+seeded packer (rockable_gb300/host/rk_pack.cpp, through scenes.column_collapse),
+so the GPU forms and the CPU reference path start from the same state.
 
-Legs of one run:
-  value      : device-timed throughput of K steps, state resident in HBM
-               (CUDA events on the engine's stream);
-  e2e        : the same metric through the C ABI with host-owned state: every
-               step uploads the bodies' kinematics from pinned host memory and
-               downloads the stepped state;
-  roofline   : the narrow-phase kernel's algorithmic bytes (140 B per
-               neighbour-list entry) over its event-timed duration, against
-               the measured HBM copy bandwidth;
-  cpu_baseline: the oracle (CPU restatement of the reference path, OpenMP) on
-               a bounded sample of the same scene, on this host's cores.
-`--impl reference` times the CPU path alone, on this workload.
+One bench step is one segment of `--segment` DEM steps (100: the fixed
+schedule's interVerlet), each DEM step one pass of the velocity-Verlet step
+loop (drift, narrow phase + force law, ordered resultants, accelerations,
+half-kick), so every timed bench step of a fixed-schedule form holds exactly
+one neighbour-list rebuild; the learned-skin forms rebuild when they decide
+to, inside the same DEM steps.  `value` counts free bodies x DEM steps.
+
+Legs of one run (rank 0 prints one JSON line):
+  value       : device-timed throughput of the headline form over K bench
+                steps, state resident in HBM (CUDA events on the engine's
+                stream); every form is in `forms`;
+  e2e         : the same metric through the C ABI with host-owned state:
+                every bench step uploads the bodies' kinematics from pinned
+                host memory, runs rk_step(segment) and downloads the result;
+  roofline    : the headline form's dominant kernel (narrow phase or
+                resultants), algorithmic bytes over its event-timed launch
+                duration against the measured HBM copy bandwidth, with the
+                ncu DRAM traffic and FP64 rate from profiles/;
+  cpu_baseline: the oracle (CPU restatement of the reference path, OpenMP on
+                the host's cores) on a bounded sample of the same segment;
+  iso         : the 200k-grain isotropic compression (six servo walls at
+                100 kPa), plain FP64 and the headline form, with its own CPU
+                sample (the >= 50x target);
+  batched     : many independent slope scenes in one context.
+`--impl reference` times the CPU path alone on the column workload and never
+loads the GPU library.
 """
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -34,38 +49,46 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
-TUNE_STEPS = 10  # untimed block-size tuning steps before the warm-up (rk_set_autotune, 2 rounds of 5 sizes)
-NCU_NARROW_MIXED_BYTES_PER_ENTRY = 22.877e6 / 183166  # ncu, 50k-grain column, mixed form (124.9 B)
-NCU_GATHER_BYTES_PER_BODY = 11.54432e6 / 50001  # ncu --set full, 50k-grain column, exact learned skin (230.9 B)
+TUNE_STEPS = 10  # untimed block-size tuning steps (rk_set_autotune, 2 rounds of 5 sizes)
+PROFILE = os.path.join(ROOT, "profiles", "step_kernels_column_50k.md")
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20, help="timed bench steps (segments)")
+    ap.add_argument("--warmup", type=int, default=5, help="untimed bench steps before them")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--scene", default="column", choices=["column", "cubes"])
-    ap.add_argument("--n", type=int, default=50000)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--segment", type=int, default=100, help="DEM steps per bench step")
+    ap.add_argument("--n", type=int, default=50000, help="grains of the column")
+    ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact",
+                    help="comma list of the forms to time (the last one is the headline)")
+    ap.add_argument("--iso-n", type=int, default=200000, help="grains of the compression box (0: skip)")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of each CPU sample")
+    ap.add_argument("--ref-seconds", type=float, default=150.0, help="budget of the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--collapse-steps", type=int, default=50000,
-                    help="untimed steps of the collapse before the timed forms (the middle of a 100k-step run)")
-    ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin,mixed_learned_skin_exact",
-                    help="comma list of the forms to time (the last one is the headline)")
-    ap.add_argument("--batch-scenes", type=int, default=256,
-                    help="scenes of the batched slope workload (0: skip it)")
+    ap.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched slope workload (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-settle", type=int, default=3000)
     return ap.parse_args()
 
 
-def make_scene(a):
-    from rockable_gb300 import scenes
-    if a.scene == "cubes":
-        return scenes.sphero_cube_box()
-    return scenes.column_collapse(n=a.n)
+# ------------------------------------------------------------------ host --
+def cpu_info():
+    """Model and logical cores of this host (lscpu when present)."""
+    model = platform.processor() or platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                v = line.split(":", 1)[1].strip()
+                if v and not v.isdigit():
+                    model = v
+                    break
+    except Exception:
+        pass
+    return {"model": model, "logical_cores": os.cpu_count(), "machine": platform.machine()}
 
 
 def peaks():
@@ -75,6 +98,44 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def profile_constants():
+    """Per-unit figures of the headline kernels from the committed ncu
+    summary: lines `bench: <key> = <value>` (DRAM bytes and FP64 operations
+    per entry / per body, with the capture they come from)."""
+    out = {}
+    try:
+        for line in open(PROFILE):
+            if line.startswith("bench:") and "=" in line:
+                k, v = line[len("bench:"):].split("=", 1)
+                out[k.strip()] = float(v.split()[0])
+    except Exception:
+        pass
+    return out
+
+
+def fp64_peak():
+    """Measured FP64 peak of this GPU: a cuBLAS DGEMM burst (4096^3, best of
+    5), the FP64 counterpart of the driver's bf16 GEMM peak."""
+    try:
+        import torch
+        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b
+        return 2.0 * 4096 ** 3 / (best / 1e3) / 1e12
+    except Exception:
+        return None
 
 
 class Clocks:
@@ -162,41 +223,218 @@ def pinned(shape):
         return np.zeros(shape)
 
 
-def cpu_baseline(scene, budget_s):
-    """Oracle (CPU restatement, OpenMP) on a bounded sample of the workload."""
+# ------------------------------------------------------------- CPU path --
+def cpu_segments(scene, segment, count, budget_s, warm=0):
+    """The oracle (OpenMP over the host's cores) on `count` bench steps of
+    the scene from its initial state: each a full neighbour-list rebuild, timed,
+    and a sample of s DEM steps, timed; the segment's time is the rebuild plus
+    segment / s times the sample (linear extrapolation of the steps; s is
+    chosen from a first measurement so that all of it fits the budget).
+    `warm` untimed bench steps (one DEM step each) come first.  Returns the
+    segment times (s), s, the rebuild and step times, and the oracle."""
     from oracle import oracle
     from rockable_gb300 import scenes
     oracle.build()
     d = tempfile.mkdtemp(prefix="rk_cpu_")
     conf = scenes.write_conf(scene, d)
-    o = oracle.Oracle(conf)
+    drv = os.path.join(d, "drivingSystem.txt")
+    o = oracle.Oracle(conf, driving=drv if os.path.exists(drv) else None)
+    t0 = time.perf_counter()
     o.update_nl()
-    nfree = o.n - o.n_driven
-    o.run(1)  # warm-up: first-touch of the entry arrays
-    # chunks of steps until the budget is spent (the first steps' time is no
-    # guide to the rest: contacts and list updates come later)
+    t_rb = time.perf_counter() - t0
     t0 = time.perf_counter()
-    o.run(2)
-    t1 = (time.perf_counter() - t0) / 2.0
-    chunk = max(1, min(200, int(0.1 * budget_s / max(t1, 1e-6))))
-    steps = 0
-    t0 = time.perf_counter()
-    while steps < 2000 and (steps == 0 or time.perf_counter() - t0 < budget_s):
-        o.run(chunk)
-        steps += chunk
-    el = time.perf_counter() - t0
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": nfree * steps / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": "%d steps of the %d-body scene (after load and the initial NL update), %.1f s" % (
-                steps, o.n, el)}
+    o.run(1)
+    t_st = time.perf_counter() - t0
+    per = budget_s / max(1, count)
+    s = int(max(1, min(segment, (per - t_rb) / max(t_st, 1e-9))))
+    o.run(warm)  # the untimed bench steps: one DEM step each (they only warm the caches)
+    segs, rbs, sts = [], [], []
+    for k in range(count):
+        t0 = time.perf_counter()
+        o.update_nl()
+        rb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o.run(s)
+        st = (time.perf_counter() - t0) / s
+        segs.append(rb + segment * st)
+        rbs.append(rb)
+        sts.append(st)
+    return segs, s, float(np.mean(rbs)), float(np.mean(sts)), o
 
 
-def _nvtx():
-    try:
-        import torch
-        return torch.cuda.nvtx
-    except Exception:
-        return None
+def cpu_threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def cpu_baseline(scene, segment, budget_s, label):
+    """Bounded CPU sample of one bench step of the workload (reported only)."""
+    nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
+    segs, s, rb, st, o = cpu_segments(scene, segment, 1, budget_s)
+    v = nfree * segment / float(np.mean(segs))
+    return {"value": v, "unit": "particle-steps/s", "cores": cpu_threads(), "kind": "port", "cpu": cpu_info(),
+            "sample": ("%s at t = 0: one neighbour-list rebuild (%.2f s) and %d DEM steps (%.4f s each) of the "
+                       "%d-body scene; the %d-step segment's time is the rebuild plus %d x the step time "
+                       "(linear extrapolation)" % (label, rb, s, st, o.n, segment, segment))}
+
+
+def run_reference(a, rank):
+    """The reference's CPU path (the oracle: restatement of the reference
+    step loop, OpenMP over all host threads) on the column workload from its
+    initial state; W untimed bench steps, then exactly K timed ones, each a
+    sampled segment (cpu_segments).  Never loads the GPU library."""
+    if rank != 0:
+        return
+    from rockable_gb300 import scenes
+    scene = scenes.column_collapse(n=a.n)
+    nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
+    segs, s, rb, st, o = cpu_segments(scene, a.segment, a.steps, a.ref_seconds, warm=a.warmup)
+    T = float(np.sum(segs))
+    value = nfree * a.segment * a.steps / T
+    threads = cpu_threads()
+    sample = ("every bench step: one full neighbour-list rebuild (mean %.2f s) and %d DEM steps (mean %.4f s each) "
+              "of the %d-body column from t = 0, the %d-step segment's time being the rebuild plus %d x the step "
+              "time (linear extrapolation); %d untimed bench steps (one DEM step each) first" % (
+                  rb, s, st, o.n, a.segment, a.segment, a.warmup))
+    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": a.gpus, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": 1000.0 * T / max(1, a.steps), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+           "impl": "reference",
+           "config": {"workload": scene["name"], "law": scene["law"], "bodies": int(o.n), "free_bodies": int(nfree),
+                      "dem_steps_per_step": a.segment, "state": "the packed column at release (t = 0)",
+                      "cpu": cpu_info()},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------- GPU path --
+SKIN = {"plain_fp64": None, "mixed": None, "mixed_learned_skin": "ref", "mixed_learned_skin_exact": "exact",
+        "plain_fp64_learned_skin_exact": "exact"}
+
+
+def engine(scene, form, dev, skin=None):
+    """A context holding the scene at its initial state, ready to step."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
+    e = GpuScene(device=dev, form=RK_FORM_FP64 if form.startswith("plain") else RK_FORM_MIXED)
+    e.upload_shapes(scene["shape_tables"])
+    e.upload_bodies(scene["bodies"], scene["n_driven"])
+    if scene.get("scene_of") is not None:
+        e.set_scenes(scene["scene_of"])
+    scenes.set_scene_params(e, scene)
+    if skin:
+        d = scene["dVerlet"]
+        e.set_skin(use_mlp=True, skin_min=0.1 * d, skin_max=4.0 * d, dverlet_ratio=2.0, interval_min=2,
+                   interval_max=1000, seed=3, exact_contacts=(skin == "exact"))
+    else:
+        e.update_nl()
+    e.set_graphs(True)
+    return e
+
+
+def time_form(scene, label, a, dev, dist, ws, steps, warmup):
+    """One form: tuning steps and `warmup` untimed bench steps from the
+    scene's initial state, then exactly `steps` timed bench steps (one
+    rk_step call, CUDA events on the context stream, barrier and sync on both
+    sides), then one profiled segment.  Returns the context and the record."""
+    nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
+    e = engine(scene, label, dev, SKIN[label])
+    e.autotune(2)
+    e.step(TUNE_STEPS)
+    if warmup:
+        e.step(warmup * a.segment)
+    clocks = Clocks()
+    if dist:
+        dist.barrier()
+    e.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    rep = e.step(steps * a.segment)
+    wall = time.perf_counter() - t0
+    ms, launches = e.last_step_timing()
+    ck = clocks.stop()
+    ms = rank_max(ms, dist)
+    st = e.stats()
+    e.set_profiling(True)
+    e.step(a.segment)
+    prof = e.profile()
+    e.set_profiling(False)
+    rec = {"value": job_rate(ws, nfree, steps * a.segment, ms), "ms": ms, "ms_per_step": ms / steps,
+           "ms_per_dem_step": ms / (steps * a.segment), "wall_s": wall, "gpu_launches": int(launches),
+           "nl_rebuilds_in_timed": int(rep["nl_updates"]), "entries": int(st["n_entries"]),
+           "active": int(st["n_active"]), "active_per_free": st["n_active"] / max(1, nfree), "clocks": ck,
+           "skin": e.skin_stats() if SKIN[label] else None, "block_sizes": e.block_sizes(),
+           "phases_ms_per_dem_step": {q: w[0] / a.segment for q, w in prof.items()},
+           "phases_launches": {q: w[1] for q, w in prof.items()}, "profiled_steps": a.segment, "t_end": rep["t"]}
+    return e, rec
+
+
+def roofline(rec, scene, consts, fp64):
+    """The dominant kernel of a form (narrow phase or resultants, by device
+    time per DEM step): algorithmic bytes per launch (140 B per entry: 12 B key
+    + the history read and written; 352 B per body: 200 B of state read and
+    152 B written) over its event-timed launch duration, against the measured
+    HBM copy bandwidth; DRAM traffic and FP64 operations per unit from the
+    committed ncu summary."""
+    ph = rec["phases_ms_per_dem_step"]
+    la = rec["phases_launches"]
+    hbm, src = peaks()
+    nb = len(scene["bodies"]["mass"])
+    dom = "narrow_force" if ph["narrow_force"] >= ph["gather_accel"] else "gather_accel"
+    if dom == "narrow_force":
+        unit_bytes, units, unit_name, key = 140.0, rec["entries"], "entries", "narrow"
+    else:
+        unit_bytes, units, unit_name, key = 352.0, nb, "bodies", "gather"
+    # the phase's kernels per DEM step (one launch of k_narrow_force; the
+    # resultant kernel plus, when a body has many entries, its block sums),
+    # event-timed in the profiled segment
+    per_step_ms = ph[dom]
+    launches_per_step = la[dom] / max(1, rec["profiled_steps"])
+    achieved = unit_bytes * units / (per_step_ms / 1e3) / 1e9 if per_step_ms > 0 else None
+    per_launch_ms = per_step_ms / launches_per_step if launches_per_step else None
+    out = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+           "frac": (achieved / hbm) if achieved else None, "peak_source": src,
+           "algorithmic_bytes_per_unit": unit_bytes, "units": int(units), "unit_name": unit_name,
+           "ms_per_dem_step": per_step_ms, "launches_per_dem_step": launches_per_step,
+           "ms_per_launch": per_launch_ms, "phase_ms_per_dem_step": {k: ph[k] for k in ("narrow_force", "gather_accel")}}
+    tb = consts.get(key + "_dram_bytes_per_unit")
+    out["traffic"] = tb * units if tb is not None else None
+    out["traffic_note"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per %s of this kernel (%s) x this "
+                           "form's %s" % (unit_name[:-1], os.path.relpath(PROFILE, ROOT), unit_name)
+                           if tb is not None else "no ncu capture of this kernel on this workload")
+    fl = consts.get(key + "_fp64_ops_per_unit")
+    if fl is not None and per_step_ms > 0:
+        ach = fl * units / (per_step_ms / 1e3) / 1e12
+        out["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64, "frac": (ach / fp64) if fp64 else None,
+                       "peak_source": "measured: cuBLAS DGEMM 4096^3 burst on this GPU",
+                       "ops_per_unit": fl, "ops_source": "ncu dadd + dmul + 2 dfma thread instructions (%s)" %
+                       os.path.relpath(PROFILE, ROOT)}
+    return out
+
+
+def e2e_leg(g, scene, a, dist, ws, steps):
+    """The headline form through the C ABI with host-owned state: every bench
+    step uploads the kinematics (pos, vel, acc, Q, vrot, arot: 152 B per
+    body) from one pinned buffer, runs rk_step(segment) and downloads them
+    back (rk_upload/download_kinematics_packed)."""
+    N = len(scene["bodies"]["mass"])
+    nfree = N - scene["n_driven"]
+    hb = pinned((19 * N,))
+    g.download_kinematics_packed(hb)
+    g.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.upload_kinematics_packed(hb)
+        g.step(a.segment)
+        g.download_kinematics_packed(hb)
+    el = rank_max(time.perf_counter() - t0, dist)
+    return {"value": job_rate(ws, nfree, steps * a.segment, 1000.0 * el), "unit": "particle-steps/s",
+            "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8), "steps": steps,
+            "note": "every bench step: the kinematics (pos, vel, acc, Q, vrot, arot) of every body H2D from one "
+                    "pinned packed buffer, rk_step(%d), the same fields D2H back" % a.segment}
 
 
 def batched_workload(a, dev):
@@ -218,7 +456,7 @@ def batched_workload(a, dev):
     t_settle = time.perf_counter() - t0
     nfree = int(sum(bt["free_per_scene"]))
 
-    def engine(sc, entries=None):
+    def eng(sc, entries=None):
         e = GpuScene(device=dev)
         e.upload_shapes(sc["shape_tables"])
         e.upload_bodies(sc["bodies"], sc["n_driven"])
@@ -232,19 +470,14 @@ def batched_workload(a, dev):
         e.set_graphs(True)
         return e
 
-    e = engine(src, src["entries"])
+    e = eng(src, src["entries"])
     e.autotune(2)
     e.step(TUNE_STEPS)
     e.step(max(3, a.warmup))
     clocks = Clocks()
     e.synchronize()
     clocks.start()
-    nvtx = _nvtx()
-    if nvtx:
-        nvtx.range_push("timed_batch")
     rep = e.step(a.batch_steps)
-    if nvtx:
-        nvtx.range_pop()
     ms, launches = e.last_step_timing()
     ck = clocks.stop()
     st = e.stats()
@@ -257,7 +490,7 @@ def batched_workload(a, dev):
     solo = []
     for k in range(len(bt["free_per_scene"])):
         part = scenes.part_of(src, k)
-        p = engine(part)
+        p = eng(part)
         p.step(3)
         p.step(a.batch_steps)
         pms, _ = p.last_step_timing()
@@ -279,83 +512,32 @@ def batched_workload(a, dev):
             "setup_s": {"generate": t_gen, "settle": t_settle}}
 
 
-def prepare_column(a, dev=0, report=None):
-    """The column-collapse state every timed run starts from: the seeded
-    loose deposit (t = 0, the column released onto the floor) advanced by
-    --collapse-steps steps at the benchmark parameters (mixed form, not
-    timed), i.e. a slice from the middle of the workload's 100k-step run."""
+def iso_workload(a, dev, dist, ws, order):
+    """Config 4: the compression box, plain FP64 and the headline form, and
+    a CPU sample of the same segment (reported against the >= 50x target)."""
     from rockable_gb300 import scenes
-    from rockable_gb300.abi import GpuScene, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=a.n)
-    e = GpuScene(device=dev, form=RK_FORM_MIXED)
-    e.upload_shapes(scene["shape_tables"])
-    e.upload_bodies(scene["bodies"], scene["n_driven"])
-    scenes.set_scene_params(e, scene)
-    e.update_nl()
-    e.set_graphs(True)
-    done = 0
-    while done < a.collapse_steps:
-        k = min(10000, a.collapse_steps - done)
-        e.step(k)
-        done += k
-        if report is not None:
-            st = e.stats()
-            report.append((done, st["n_entries"], st["n_active"], st["e_trans"]))
-    src = scenes.scene_from_gpu(scene, e)
-    e.close()
-    return src
-
-
-def reference_input(a):
-    """The benchmark's input state for the CPU arm: the same seeded scene,
-    settled the same way when a GPU is present (input preparation only,
-    outside the timed region), else the freshly deposited pile."""
-    from rockable_gb300 import scenes
-    scene = make_scene(a)
-    if a.scene != "column":
-        return scene, "lattice as generated"
-    try:
-        import torch
-        have_gpu = torch.cuda.is_available()
-    except Exception:
-        have_gpu = False
-    if not have_gpu:
-        return scene, "deposited pile (no GPU to settle it)"
-    return prepare_column(a), ("the benchmark state: the seeded loose column after %d collapse steps, "
-                               "prepared on the GPU, not timed" % a.collapse_steps)
-
-
-def run_reference(a, rank):
-    """The reference's CPU path (the oracle: restatement of the reference
-    step loop, OpenMP over all host threads) on the same workload: W warm-up
-    steps, then exactly K timed steps."""
-    if rank != 0:
-        return
-    from oracle import oracle
-    from rockable_gb300 import scenes
-    src, how = reference_input(a)
-    oracle.build()
-    d = tempfile.mkdtemp(prefix="rk_ref_")
-    o = oracle.Oracle(scenes.write_conf(src, d))
-    o.update_nl()
-    nfree = o.n - o.n_driven
-    o.run(max(0, a.warmup))
     t0 = time.perf_counter()
-    o.run(a.steps)
-    el = time.perf_counter() - t0
-    value = nfree * a.steps / el
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    sample = "%d timed steps after %d warm-up steps of the %d-body scene (%s), %.1f s" % (
-        a.steps, a.warmup, o.n, how, el)
-    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": a.gpus, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": 1000.0 * el / max(1, a.steps), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-           "impl": "reference",
-           "config": {"workload": src["name"], "law": src["law"], "bodies": int(o.n), "free_bodies": int(nfree)},
-           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                            "sample": sample},
-           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(out), flush=True)
+    sc = scenes.iso_compression(n=a.iso_n)
+    t_gen = time.perf_counter() - t0
+    nfree = len(sc["bodies"]["mass"]) - sc["n_driven"]
+    steps = max(2, a.steps // 4)
+    forms = {}
+    for label in ["plain_fp64", order[-1]]:
+        e, rec = time_form(sc, label, a, dev, dist, ws, steps, 1)
+        e.close()
+        forms[label] = rec
+    head = forms[order[-1]]
+    out = {"workload": sc["name"], "bodies": len(sc["bodies"]["mass"]), "free_bodies": nfree,
+           "law": sc["law"], "servo": "tritriIsostaticCompression at %g Pa, no gravity" % sc["servo"]["pressure"],
+           "pack": sc["pack"], "dem_steps_per_step": a.segment, "steps": steps, "warmup": 1,
+           "forms": forms, "headline_form": order[-1],
+           "headline_vs_plain": head["value"] / forms["plain_fp64"]["value"], "setup_s": {"generate": t_gen}}
+    if not a.no_cpu:
+        cb = cpu_baseline(sc, a.segment, 2.0 * a.cpu_seconds, "the compression box")
+        out["cpu_baseline"] = cb
+        out["vs_cpu"] = {k: v["value"] / cb["value"] for k, v in forms.items()}
+        out["target_50x_at_200k"] = ("met" if min(out["vs_cpu"].values()) >= 50.0 else "not met")
+    return out
 
 
 def main():
@@ -372,182 +554,55 @@ def main():
     if dist:
         dist.barrier()
     from rockable_gb300 import scenes
-    from rockable_gb300.abi import GpuScene, RK_LAW
     dev = int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0
-    settle_log = []
-    t_settle = time.perf_counter()
-    if a.scene == "column":
-        src = prepare_column(a, dev, settle_log)  # the state S every form starts from
-        scene = src
-    else:
-        scene = make_scene(a)
-        src = None
-    t_settle = time.perf_counter() - t_settle
-    b = scene["bodies"]
-    N = len(b["mass"])
+    t0 = time.perf_counter()
+    scene = scenes.column_collapse(n=a.n)
+    t_gen = time.perf_counter() - t0
+    N = len(scene["bodies"]["mass"])
     nfree = N - scene["n_driven"]
-    from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
-
-    def engine(form):
-        e = GpuScene(device=dev, form=form)
-        e.upload_shapes(scene["shape_tables"])
-        e.upload_bodies(src["bodies"] if src else b, scene["n_driven"])
-        scenes.set_scene_params(e, scene)
-        if src:
-            e.upload_entries(src["entries"])
-        e.set_graphs(True)
-        return e
-
-    def timed(e, steps, label):
-        clocks = Clocks()
-        if dist:
-            dist.barrier()
-        e.synchronize()
-        clocks.start()
-        nvtx = None
-        try:
-            import torch
-            nvtx = torch.cuda.nvtx
-            nvtx.range_push("timed_" + label)
-        except Exception:
-            nvtx = None
-        t0 = time.perf_counter()
-        rep = e.step(steps)
-        wall = time.perf_counter() - t0
-        if nvtx:
-            nvtx.range_pop()
-        ms, launches = e.last_step_timing()
-        ck = clocks.stop()
-        ms = rank_max(ms, dist)
-        return {"ms": ms, "launches": launches, "wall": wall, "rep": rep, "clocks": ck,
-                "value": job_rate(ws, nfree, steps, ms)}
-
-    def profile(e, n):
-        e.set_profiling(True)
-        e.step(n)
-        p = e.profile()
-        e.set_profiling(False)
-        return p
-
-    forms = {}
-    dmin = scene["dVerlet"]
-    # skin: None (fixed interVerlet), "ref" (learned skin, Rockable's NEAR tests), "exact" (distance-only)
-    known = {"plain_fp64": (RK_FORM_FP64, None), "mixed": (RK_FORM_MIXED, None),
-             "mixed_learned_skin": (RK_FORM_MIXED, "ref"), "mixed_learned_skin_exact": (RK_FORM_MIXED, "exact")}
     order = [f.strip() for f in a.forms.split(",") if f.strip()]
+    forms = {}
+    g = None
     for label in order:
-        form, skin = known[label]
-        e = engine(form)
-        if skin:
-            e.set_skin(use_mlp=True, skin_min=0.1 * dmin, skin_max=4.0 * dmin, dverlet_ratio=2.0, interval_min=2,
-                       interval_max=1000, seed=3, exact_contacts=(skin == "exact"))
-        else:
-            e.update_nl()
-        e.autotune(2)
-        e.step(TUNE_STEPS)
-        e.step(a.warmup)
-        r = timed(e, a.steps, label)
-        st = e.stats()
-        nprof = max(1, min(a.steps, 120))
-        prof = profile(e, nprof)
-        r.update({"entries": st["n_entries"], "active": st["n_active"], "prof": prof, "nprof": nprof,
-                  "skin": e.skin_stats() if skin else None, "block_sizes": e.block_sizes()})
-        forms[label] = r
-        if label != order[-1]:
-            e.close()
-        else:
+        e, rec = time_form(scene, label, a, dev, dist, ws, a.steps, a.warmup)
+        forms[label] = rec
+        if label == order[-1]:
             g = e
+        else:
+            e.close()
     head = forms[order[-1]]
-    ms, launches, wall, rep, ck, value = (head["ms"], head["launches"], head["wall"], head["rep"], head["clocks"],
-                                          head["value"])
-    prof, nprof = head["prof"], head["nprof"]
-    # roofline of the headline form's dominant kernel: the narrow phase (140
-    # algorithmic bytes per entry: 12 B key + history read and written) or the
-    # resultant / integration kernel (352 B per body: 200 B of state read, 152 B
-    # written), whichever takes more device time per step
-    C = head["entries"]
-    hbm, src_peak = peaks()
-    per_step = {k: prof[k][0] / max(nprof, 1) for k in ("narrow_force", "gather_accel")}
-    dominant = max(per_step, key=per_step.get)
-    if dominant == "narrow_force":
-        unit_bytes, units, unit_name = 140.0, C, "entries"
-        t_launch = prof["narrow_force"][0] / max(prof["narrow_force"][1], 1)  # ms per launch
-        traffic = NCU_NARROW_MIXED_BYTES_PER_ENTRY * C
-        tnote = "ncu DRAM bytes per entry of k_narrow_force_mixed (column, mixed form) x this form's entries"
-    else:
-        unit_bytes, units, unit_name = 352.0, N, "bodies"
-        t_launch = per_step["gather_accel"]  # ms per step (k_gather_accel, plus k_gather_heavy when used)
-        traffic = NCU_GATHER_BYTES_PER_BODY * N if NCU_GATHER_BYTES_PER_BODY else None
-        tnote = ("ncu DRAM bytes per body of k_gather_accel (column, learned-skin form) x bodies"
-                 if NCU_GATHER_BYTES_PER_BODY else "not captured for this kernel")
-    achieved = unit_bytes * units / (t_launch / 1000.0) / 1e9 if t_launch > 0 else None
-    st = {"n_entries": C, "n_active": head["active"]}
-    # ---- e2e through the C ABI with host-owned state (headline form)
-    e2e = None
-    if not a.no_e2e:
-        hb = pinned((19 * N,))  # packed pos | vel | acc | Q | vrot | arot
-        g.download_kinematics_packed(hb)
-        k_e2e = max(5, min(a.steps, 50))
-        g.synchronize()
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(k_e2e):
-            g.upload_kinematics_packed(hb)
-            g.step(1)
-            g.download_kinematics_packed(hb)
-        el = rank_max(time.perf_counter() - t0, dist)
-        e2e = {"value": job_rate(ws, nfree, k_e2e, 1000.0 * el), "unit": "particle-steps/s",
-               "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8),
-               "steps": k_e2e, "note": "every step: the kinematics (pos, vel, acc, Q, vrot, arot) of every body "
-                                       "H2D from one pinned packed buffer, rk_step(1), the same fields D2H back "
-                                       "(rk_upload/download_kinematics_packed)"}
-    batched = None
-    if rank == 0 and a.batch_scenes > 0:
-        batched = batched_workload(a, dev)
-    cpu = None
-    if rank == 0 and not a.no_cpu:
-        cpu = cpu_baseline(src if src else scene, a.cpu_seconds)
+    consts = profile_constants()
+    fp64 = fp64_peak() if rank == 0 else None
+    roof = roofline(head, scene, consts, fp64)
+    e2e = None if a.no_e2e else e2e_leg(g, scene, a, dist, ws, max(2, min(a.steps, 10)))
+    g.close()
+    iso = iso_workload(a, dev, dist, ws, order) if (a.iso_n > 0 and rank == 0) else None
+    batched = batched_workload(a, dev) if (rank == 0 and a.batch_scenes > 0) else None
+    cpu = cpu_baseline(scene, a.segment, a.cpu_seconds, "the column") if (rank == 0 and not a.no_cpu) else None
     if rank == 0:
-        out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": a.steps,
-               "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64+f32 (mixed form; plain form is f64)",
-               "data": "synthetic (seeded generator, rockable_gb300.scenes)",
-               "form": ("mixed precision + learned skin with exact contact detection (headline); plain FP64, "
-                        "mixed, and the learned skin with Rockable's NEAR tests alongside"),
-               "forms": {k: {"value": v["value"], "ms_per_step": v["ms"] / a.steps, "entries": v["entries"],
-                             "active": v["active"], "nl_rebuilds_in_timed": v["rep"]["nl_updates"],
-                             "gpu_launches": v["launches"], "skin": v["skin"], "block_sizes": v["block_sizes"],
-                             "phases_ms_per_step": {q: w[0] / v["nprof"] for q, w in v["prof"].items()}}
-                         for k, v in forms.items()},
-               "headline_form": order[-1],
+        out = {"metric": METRIC, "value": head["value"], "unit": "particle-steps/s", "n_gpus": ws, "steps": a.steps,
+               "warmup": a.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64+f32 (mixed form; the plain form is f64)",
+               "data": "synthetic (seeded generator and CPU packer, rockable_gb300.scenes)",
+               "form": "mixed precision + learned skin with exact contact detection (headline); plain FP64 and "
+                       "mixed alongside",
+               "forms": forms, "headline_form": order[-1],
                "headline_vs_plain": (head["value"] / forms["plain_fp64"]["value"]) if "plain_fp64" in forms else None,
                "config": {"workload": scene["name"], "law": scene["law"], "bodies": N, "free_bodies": nfree,
-                          "entries": int(C), "active": int(st["n_active"]),
-                          "nl_rebuilds_in_timed": int(rep["nl_updates"]), "dt": scene["dt"],
+                          "dem_steps_per_step": a.segment, "entries": head["entries"], "active": head["active"],
+                          "active_per_free": head["active_per_free"],
+                          "nl_rebuilds_in_timed": head["nl_rebuilds_in_timed"], "dt": scene["dt"],
                           "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
-                          "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if C * 240 + N * 600 > 129e6 else
-                          "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
+                          "pack": scene["pack"],
+                          "state": ("the loose random packing released at t = 0 (no walls), then %d tuning and %d "
+                                    "warm-up DEM steps before the timed ones" % (TUNE_STEPS, a.warmup * a.segment)),
+                          "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if head["entries"] * 240 + N * 600 >
+                          129e6 else "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
                           "parallelism": "replicas" if ws > 1 else "single GPU",
-                          "setup_before_warmup": "%d untimed block-size tuning steps; step graphs on" % TUNE_STEPS,
-                          "state": ("loose column (ballistic deposit) released onto the floor, %d collapse steps "
-                                    "before the tuning and warm-up" % a.collapse_steps)
-                          if a.scene == "column" else "lattice as generated"},
-               "gpu_launches": int(launches), "wall_s": wall, "clocks": ck,
-               "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm,
-                            "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                            "traffic_note": tnote,
-                            "limiter": "FP64 pipe (ncu: 73% busy in the narrow phase and the resultants, "
-                                       "81% in the global vertices)",
-                            "peak_source": src_peak, "algorithmic_bytes_per_unit": unit_bytes,
-                            "units": int(units), "unit_name": unit_name, "ms_per_launch": t_launch,
-                            "phase_ms_per_step": per_step},
-               "setup": {"settle_s": t_settle, "settle_log": settle_log},
-               "phases_ms_per_step": {k: v[0] / nprof for k, v in prof.items()},
-               "phases_launches": {k: v[1] for k, v in prof.items()},
-               "e2e": e2e, "cpu_baseline": cpu, "batched": batched}
+                          "setup_s": {"generate": t_gen}},
+               "gpu_launches": head["gpu_launches"], "wall_s": head["wall_s"], "clocks": head["clocks"],
+               "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "iso": iso, "batched": batched}
         print(json.dumps(out), flush=True)
-    g.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()

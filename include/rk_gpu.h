@@ -318,6 +318,8 @@ typedef struct rk_skin_stats {
   double loss;            /* last training loss */
   int64_t partial;        /* partial refreshes */
   int64_t partial_bodies; /* bodies refreshed by them, summed */
+  int64_t train_steps;    /* optimiser steps of the network so far */
+  int64_t windows;        /* training windows in its replay buffer */
 } rk_skin_stats;
 int rk_set_skin(rk_ctx* ctx, const rk_skin_config* cfg);
 int rk_get_skin_stats(rk_ctx* ctx, rk_skin_stats* out);

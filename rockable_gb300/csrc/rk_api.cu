@@ -224,6 +224,12 @@ static void settle_before_update(Ctx& c) {
 }
 
 // ------------------------------------------------------------ learned skin ----
+// Windows in the replay buffer before the network trains and predicts.  Its
+// output layer starts at zero (it then predicts what the method without it
+// does), so it can act from the first windows and departs from that method
+// only as far as its training carries it.
+static const int kMinWindows = 2;
+
 static double to_f(unsigned int bits) {
   float f;
   std::memcpy(&f, &bits, 4);
@@ -233,7 +239,7 @@ static double to_f(unsigned int bits) {
 static int skin_train(Ctx& c) {
   Skin& k = c.skin;
   const int nb = (int)std::min<size_t>(k.rx.size(), (size_t)mlp_max_batch());
-  if (nb < 8) return 0;
+  if (nb < kMinWindows) return 0;
   std::vector<float> X(16 * nb), T(2 * nb);
   for (int i = 0; i < nb; i++) {
     for (int q = 0; q < 16; q++) X[16 * i + q] = k.rx[i][q];
@@ -348,7 +354,7 @@ static int skin_rebuild(Ctx& c, double dmax, double vmax, bool forced) {
   // and departs from it only as far as its training supports.
   const double churn_base = k.pred_churn;
   double u = rate, churn = churn_base;
-  if (k.cfg.use_mlp && k.rx.size() >= 8) {
+  if (k.cfg.use_mlp && k.rx.size() >= (size_t)kMinWindows) {
     float y[2];
     CK(cudaMemcpyAsync(k.io, f.data(), 64, cudaMemcpyHostToDevice, c.stream));
     launch_mlp_infer(k.w, k.io, k.io + 16, c.stream);
@@ -1353,6 +1359,8 @@ int rk_get_skin_stats(rk_ctx* x, rk_skin_stats* o) {
   o->loss = k.last_loss;
   o->partial = k.partial;
   o->partial_bodies = k.partial_bodies;
+  o->train_steps = (int64_t)k.adam_step;
+  o->windows = (int64_t)k.rx.size();
   return RK_OK;
 }
 
