@@ -325,8 +325,11 @@ def engine(scene, form, dev, skin=None):
     scenes.set_scene_params(e, scene)
     if skin:
         d = scene["dVerlet"]
+        # the interval stays within 3x the fixed schedule's, so that the
+        # network (which proposes it) sees a window every few hundred steps
         e.set_skin(use_mlp=True, skin_min=0.1 * d, skin_max=4.0 * d, dverlet_ratio=2.0, interval_min=2,
-                   interval_max=1000, seed=3, exact_contacts=(skin == "exact"))
+                   interval_max=3 * int(round(scene["interVerlet"] / scene["dt"])), seed=3,
+                   exact_contacts=(skin == "exact"))
     else:
         e.update_nl()
     e.set_graphs(True)

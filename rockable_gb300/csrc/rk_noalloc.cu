@@ -24,7 +24,14 @@
 //
 // The first call on each device does a one-time set-up: it looks up the
 // device address of the array (cudaGetSymbolAddress) with that device current.
-// Make that first call before any stream capture begins.
+// Make that first call before any stream capture begins.  The address is kept
+// for the life of the process: do not use the entry point on a device after
+// cudaDeviceReset (or anything else that tears down and recreates its primary
+// context), since the module, and with it the array, may then load elsewhere.
+//
+// Errors: the call returns RK_ERR_CUDA without sorting when a CUDA error is
+// already pending on the calling thread (it leaves that error in place for
+// its owner), and RK_ERR_CUDA when one of its own launches fails.
 #include <cstdint>
 #include <mutex>
 
@@ -71,6 +78,7 @@ extern "C" int rk_sort_keys_noalloc(uint64_t* keys, int64_t n, int lo_bit, int h
   if (n < 0 || (n > 0 && !keys) || lo_bit < 0 || hi_bit > 64 || lo_bit >= hi_bit) return RK_ERR_ARG;
   if (n > kNoAllocMaxKeys) return RK_ERR_CAPACITY;  // larger than the fixed scratch
   if (sort_temp_bytes(n) > kNoAllocTempBytes) return RK_ERR_CAPACITY;
+  if (cudaPeekAtLastError() != cudaSuccess) return RK_ERR_CUDA;  // an earlier error, not ours to clear
   unsigned char* base = nullptr;
   int rc = scratch_address(&base);  // first call on a device: the one-time lookup
   if (rc != RK_OK) return rc;
@@ -78,5 +86,5 @@ extern "C" int rk_sort_keys_noalloc(uint64_t* keys, int64_t n, int lo_bit, int h
   uint64_t* tmp = reinterpret_cast<uint64_t*>(base);
   void* temp = base + kNoAllocKeyBytes;
   radix_sort_u64(keys, tmp, n, lo_bit, hi_bit, temp, (cudaStream_t)stream);
-  return cudaGetLastError() == cudaSuccess ? RK_OK : RK_ERR_CUDA;
+  return cudaGetLastError() == cudaSuccess ? RK_OK : RK_ERR_CUDA;  // nothing was pending before: any error is ours
 }

@@ -104,7 +104,10 @@ constexpr int kSortThreads = 256;
 constexpr int kSortChunks = 16;
 constexpr int64_t kSortTile = (int64_t)kSortThreads * kSortChunks;
 
-__global__ void k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int sh, int64_t nblocks,
+// One pass of the LSD radix sort on the digit (key >> sh) & mask: 8 bits,
+// fewer in the last pass when hi_bit - lo_bit is not a multiple of 8 (the
+// bits at and above hi_bit must not take part in the order).
+__global__ void k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int sh, unsigned mask, int64_t nblocks,
                              int64_t* __restrict__ hist) {
   __shared__ unsigned h[256];
   h[threadIdx.x] = 0;
@@ -112,14 +115,14 @@ __global__ void k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int s
   const int64_t base = blockIdx.x * kSortTile;
   for (int c = 0; c < kSortChunks; c++) {
     int64_t idx = base + (int64_t)c * kSortThreads + threadIdx.x;
-    if (idx < n) atomicAdd(&h[(unsigned)((keys[idx] >> sh) & 255u)], 1u);
+    if (idx < n) atomicAdd(&h[(unsigned)((keys[idx] >> sh) & mask)], 1u);
   }
   __syncthreads();
   hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
 __global__ void k_radix_scatter(const uint64_t* __restrict__ keys, uint64_t* __restrict__ out, int64_t n, int sh,
-                                int64_t nblocks, const int64_t* __restrict__ ofs) {
+                                unsigned mask, int64_t nblocks, const int64_t* __restrict__ ofs) {
   __shared__ unsigned run[256];
   __shared__ unsigned wcnt[kSortThreads / 32][256];
   __shared__ int64_t base_ofs[256];
@@ -135,7 +138,7 @@ __global__ void k_radix_scatter(const uint64_t* __restrict__ keys, uint64_t* __r
     const int64_t idx = tile + (int64_t)c * kSortThreads + t;
     const bool valid = idx < n;
     const uint64_t key = valid ? keys[idx] : 0ull;
-    const unsigned d = valid ? (unsigned)((key >> sh) & 255u) : 256u;
+    const unsigned d = valid ? (unsigned)((key >> sh) & mask) : 256u;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const unsigned rank = __popc(peers & lt);
     if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
@@ -172,9 +175,10 @@ void radix_sort_u64(uint64_t* keys, uint64_t* tmp, int64_t n, int lo_bit, int hi
   uint64_t* dst = tmp;
   int passes = 0;
   for (int sh = lo_bit; sh < hi_bit; sh += 8) {
-    k_radix_hist<<<(unsigned)nb, kSortThreads, 0, st>>>(src, n, sh, nb, hist);
+    const unsigned mask = (1u << (hi_bit - sh < 8 ? hi_bit - sh : 8)) - 1u;
+    k_radix_hist<<<(unsigned)nb, kSortThreads, 0, st>>>(src, n, sh, mask, nb, hist);
     exclusive_scan_i64(hist, hist, 256 * nb, scan_tmp, st);
-    k_radix_scatter<<<(unsigned)nb, kSortThreads, 0, st>>>(src, dst, n, sh, nb, hist);
+    k_radix_scatter<<<(unsigned)nb, kSortThreads, 0, st>>>(src, dst, n, sh, mask, nb, hist);
     uint64_t* x = src;
     src = dst;
     dst = x;

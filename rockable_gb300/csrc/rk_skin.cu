@@ -250,11 +250,9 @@ void launch_mlp_infer(const void* w, const float* x, float* y, cudaStream_t st) 
 }
 void launch_mlp_grad(const void* w, const float* X, const float* T, int nb, float* grad, float* loss,
                      cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_grad_smem());
-    attr = true;
-  }
+  // the attribute belongs to the current device's context: set it before
+  // every launch (a few host instructions), so a context on any device has it
+  cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_grad_smem());
   k_mlp_grad<<<1, 256, mlp_grad_smem(), st>>>((const __half*)w, X, T, nb, grad, loss);
 }
 void launch_mlp_adam(float* master, void* w, float* m, float* v, const float* grad, float lr, int step,

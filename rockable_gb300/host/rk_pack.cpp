@@ -24,21 +24,20 @@
 // gap g from a support whose normal n closes at rate -u.n along the move u
 // can travel g / (-u.n) before they can touch.  No grain ever overlaps
 // another, the floor or a side wall.  The deposition is sequential and every
-// random draw comes from one seeded generator, so the packing is the same on
-// every run and host.
+// random draw comes from one seeded generator, so the same input gives the
+// same packing on every run and host (the shapes and orientations themselves
+// come from numpy and scipy, whose last bits can differ between hosts).
 //
 // Usage: rk_pack IN OUT.  IN is a little-endian binary file written by
 // rockable_gb300/scenes.py (layout in read_input); OUT receives the grains'
 // positions (3 doubles each) followed by 8 doubles of statistics.
-// Compiled with -ffp-contract=off and only + - * / sqrt in the arithmetic,
-// so the packing is the same on every host.
+// Compiled with -ffp-contract=off and only + - * / sqrt in the arithmetic.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <vector>
-
 
 namespace {
 
@@ -252,6 +251,15 @@ double gjk(const V* va, int na, const V* vb, int nb, V c, V* nrm) {
     bool dup = false;
     for (int k = 0; k < S.n; ++k) dup = dup || (S.ia[k] == ia && S.ib[k] == ib);
     if (dup || vv - dot(v, w) <= 1e-12 * vv) break;
+    if (S.n == 3) {
+      // a new point in the plane of the current triangle makes a flat
+      // tetrahedron whose inside test rounding can decide either way: the
+      // triangle's closest point is then final (a face-to-face contact)
+      V e1 = S.w[1] - S.w[0], e2 = S.w[2] - S.w[0], e3 = w - S.w[0];
+      double vol = dot(e1, cross(e2, e3));
+      double ref = std::sqrt(dot(e1, e1) * dot(e2, e2) * dot(e3, e3));
+      if (std::fabs(vol) <= 1e-10 * ref) break;
+    }
     S.w[S.n] = w;
     S.ia[S.n] = ia;
     S.ib[S.n] = ib;

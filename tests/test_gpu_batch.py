@@ -29,7 +29,7 @@ def _engine(scene, form=0, entries=None, graphs=False):
 @pytest.mark.parametrize("form", [0, 1])
 def test_graph_replay_is_bitwise_identical(form, gpu_lib):
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=3000, nshapes=64)
+    scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=800)
     src = scenes.scene_from_gpu(scene, gs)
     gs.close()
@@ -75,7 +75,7 @@ def test_batched_scenes_match_each_scene_alone(gpu_lib):
 
 def test_autotuned_block_sizes_change_no_result(gpu_lib):
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=3000, nshapes=64)
+    scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=800)
     src = scenes.scene_from_gpu(scene, gs)
     gs.close()
@@ -98,7 +98,7 @@ def test_packed_kinematics_round_trip(gpu_lib):
     """rk_download/upload_kinematics_packed move exactly the six kinematic
     arrays, in the documented order."""
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=700, nshapes=16)
+    scene = scenes.column_collapse(n=700, nshapes=16, semi=(0.0025, 0.0075))
     g = _engine(scene)
     g.step(20)
     n = g.n

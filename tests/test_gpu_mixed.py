@@ -69,7 +69,7 @@ def test_mixed_one_step_518_friction(golden_dir, oracle_lib, gpu_lib):
 def test_mixed_one_step_settled_column(gpu_lib):
     from rockable_gb300 import scenes
     from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=3000, nshapes=128)
+    scene = scenes.column_collapse(n=3000, nshapes=128, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=2000)
     gs.step(50)
     g64 = clone(gs, scene, RK_FORM_FP64)
@@ -136,7 +136,7 @@ def test_long_run_statistics_match_plain(gpu_lib):
     diverge, as in any granular flow)."""
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=3000, nshapes=64)
+    scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1200)
     src = scenes.scene_from_gpu(scene, gs)
     gs.close()
@@ -175,7 +175,7 @@ def test_mixed_free_flight_tracks_fp64():
     The quaternions stay unit to FP64 precision."""
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
-    scene = scenes.drop_bodies(scenes.column_collapse(n=200, nshapes=16), [0])
+    scene = scenes.drop_bodies(scenes.column_collapse(n=200, nshapes=16, semi=(0.0025, 0.0075)), [0])
     b = dict(scene["bodies"])
     rng = np.random.default_rng(21)
     n = len(b["mass"])

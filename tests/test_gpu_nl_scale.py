@@ -28,7 +28,7 @@ def _engine(scene, src_entries=None, broadphase=0):
 
 def test_grid_and_all_pairs_give_the_same_list(gpu_lib):
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=12000, nshapes=128)
+    scene = scenes.column_collapse(n=12000, nshapes=128, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1200)
     src = scenes.scene_from_gpu(scene, gs)
     ga = _engine(src, src["entries"], broadphase=1)
@@ -50,7 +50,7 @@ def test_grid_and_all_pairs_give_the_same_list(gpu_lib):
 
 def test_grid_list_matches_oracle_linkcells(gpu_lib, oracle_lib, tmp_path):
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=2500, nshapes=64)
+    scene = scenes.column_collapse(n=2500, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1200)
     src = scenes.scene_from_gpu(scene, gs)
     conf = scenes.write_conf(src, str(tmp_path))

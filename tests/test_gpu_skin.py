@@ -46,7 +46,7 @@ def _pairs(e):
 
 def test_guard_keeps_the_contacts_of_per_step_rebuilds(gpu_lib):
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=2000, nshapes=64)
+    scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1500)
     src = scenes.scene_from_gpu(scene, gs)
     gl = _engine(src)
@@ -77,7 +77,7 @@ def test_learned_skin_against_the_method_without_it(gpu_lib):
     """Same settled pile, 600 steps: fixed interval (plain), guard + last-window
     predictor, guard + trained network.  Prints rebuilds and device time."""
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=3000, nshapes=64)
+    scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1500)
     src = scenes.scene_from_gpu(scene, gs)
     res = {}
@@ -113,7 +113,7 @@ def test_every_touching_subcontact_is_in_the_skin_list(partial_fraction, gpu_lib
     contained in the skin engine's list."""
     import copy
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=2000, nshapes=64)
+    scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1500)
     src = scenes.scene_from_gpu(scene, gs)
     gs.close()
@@ -159,7 +159,7 @@ def test_batched_skin_steps_match_the_per_step_path(form, gpu_lib):
     divide the batch."""
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=2000, nshapes=64)
+    scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075))
     gs = scenes.settle(scene, steps=1500)
     src = scenes.scene_from_gpu(scene, gs)
     gs.close()

@@ -18,9 +18,11 @@ def _keys(n, seed, lo, hi):
     rng = np.random.default_rng(seed)
     a = rng.integers(0, 2 ** 63 - 1, n, dtype=np.int64).view(np.uint64)
     if hi - lo < 64:
-        # few distinct digits on the sorted bits, unique low bits: checks stability
+        # few distinct values in the sorted field (and random bits outside it,
+        # above hi_bit too, which must not take part in the order): checks
+        # stability and the masking of the last digit
         a = (a & ~np.uint64(((1 << (hi - lo)) - 1) << lo)) | (
-            (rng.integers(0, 97, n).astype(np.uint64)) << np.uint64(lo))
+            (rng.integers(0, min(97, 1 << (hi - lo)), n).astype(np.uint64)) << np.uint64(lo))
     return a.view(np.int64)
 
 
@@ -33,7 +35,7 @@ def _stable_ref(host, lo, hi):
 def test_noalloc_matches_allocating_sort_twice(gpu_lib):
     import torch
     lib = gpu_lib.load()
-    cases = [(300001, 0, 64, 11), (MAX_KEYS, 27, 51, 12), (4097, 0, 48, 13)]
+    cases = [(300001, 0, 64, 11), (MAX_KEYS, 27, 51, 12), (4097, 0, 48, 13), (70001, 3, 13, 14), (5000, 0, 4, 15)]
     for call in range(2):
         for n, lo, hi, seed in cases:
             host = _keys(n, seed + 100 * call, lo, hi)
@@ -57,3 +59,22 @@ def test_noalloc_rejects_oversize_and_bad_args(gpu_lib):
     assert lib.rk_sort_keys_noalloc(ctypes.c_void_p(t.data_ptr()), 10, 8, 8, None) == -1
     assert lib.rk_sort_keys_noalloc(None, 10, 0, 64, None) == -1
     assert lib.rk_sort_keys_noalloc(None, 0, 0, 64, None) == 0
+
+
+def test_noalloc_call_allocates_nothing(gpu_lib):
+    """The property the entry point exists for: once the first call on the
+    device has done its set-up, a call changes the device's free memory by
+    nothing (cudaMemGetInfo before and after)."""
+    import torch
+    lib = gpu_lib.load()
+    host = _keys(MAX_KEYS, 21, 0, 64)
+    t = torch.from_numpy(host).cuda()
+    torch.cuda.synchronize()
+    assert lib.rk_sort_keys_noalloc(ctypes.c_void_p(t.data_ptr()), MAX_KEYS, 0, 64, None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        assert lib.rk_sort_keys_noalloc(ctypes.c_void_p(t.data_ptr()), MAX_KEYS, 0, 64, None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
