@@ -256,8 +256,14 @@ __global__ void k_glob_vertices(Scene s, int only_listed) {
   double h = s.hom[b];
   const double* sv = s.svert + 3 * (int64_t)(s.vert_ofs[sh] + local);
   V3 u = h * v3(sv[0], sv[1], sv[2]);
-  V3 g = ld3(s.pos, b) + qrot(ldq(s.Q, b), u);
+  V3 r = qrot(ldq(s.Q, b), u);
+  V3 g = ld3(s.pos, b) + r;
   st3(s.gv, k, g);
+  if (s.gvr) {
+    s.gvr[3 * k] = (float)r.x;
+    s.gvr[3 * k + 1] = (float)r.y;
+    s.gvr[3 * k + 2] = (float)r.z;
+  }
 }
 
 #ifndef RK_BODY_GLOB_ONLY

@@ -23,6 +23,10 @@
 
 namespace rk {
 
+// Lanes that sum one body's resultant in the mixed form's resultant kernel.
+constexpr int kGatherLanes = 8;
+
+
 constexpr int kMaxSub = 1024;       // sub-element index limit of the sort key
 constexpr int kMaxBody = 1 << 21;   // body index limit of the sort key
 constexpr int kMaskWords = 2;       // vertex cull mask words per half-pair (<= 64 vertices)
@@ -76,6 +80,8 @@ struct Scene {
   int* lv;           // nvert: vertices of the bodies that have neighbour-list entries (nlv of them)
   int64_t nlv;
   double* gv;        // 3*nvert
+  float* gvr;        // 3*nvert: the same vertices relative to their body's centre, in FP32 (the
+                     // mixed form's test of clearly separated entries)
   double* bobb;      // 15 per body (placed OBB, not enlarged)
   float* bobbf;      // float copy of bobb
   float* baabb;      // 6 per body: outward-rounded AABB of the OBB enlarged by DVerlet/2

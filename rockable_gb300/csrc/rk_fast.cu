@@ -127,55 +127,57 @@ __global__ void k_drift(Scene s) {
 
 // Resultants, Newton-Euler and the second half-kick (Rockable.cpp:3837-3866,
 // 2084-2117 in the FP64 form); driven bodies take the generic FP64 path.
+// kGatherLanes lanes per body: each sums every kGatherLanes-th of the body's
+// active entries (its own block, then its j-side list), the lanes' sums are
+// reduced by shuffles in a fixed order, and the first lane does the
+// Newton-Euler update.  A body's serial sum would be a chain of ~50 dependent
+// loads on a dense list; the mixed form promises no serial order, and this
+// order is the same on every run.  Bodies summed by k_gather_heavy (one
+// block each) read that kernel's resultant.
 __global__ void k_gather_accel(Scene s, int apply_kick) {
   if (step_halted(s)) return;
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t b = t / kGatherLanes;
+  const int l = (int)(t % kGatherLanes);
   float kin[12] = {};
   bool have = false;
-  {
-    // bodies of this warp with is_heavy 3 (more than kHeavy entries): the
-    // warp sums each one's entries (lanes take strided entries, then a
-    // shuffle reduction) and the body's lane stores the resultant, which
-    // body_resultant reads back below
-    const bool hv = b < s.n && s.is_heavy[b] == 3;
-    unsigned hm = __ballot_sync(0xffffffffu, hv);
-    const int lane = threadIdx.x & 31;
-    while (hm) {
-      const int src = __ffs(hm) - 1;
-      hm &= hm - 1;
-      const int64_t hb = __shfl_sync(0xffffffffu, b, src);
-      double a[6] = {0, 0, 0, 0, 0, 0};
-      const int64_t i0 = s.iofs[hb], i1 = s.iofs[hb + 1], j0 = s.jofs[hb], j1 = s.jofs[hb + 1];
-      for (int64_t e = i0 + lane; e < i1; e += 32) {
-        if (!s.act[e]) continue;
-        const V3 f = ld3(s.cf, e), m = ld3(s.cmi, e);
-        a[0] += f.x; a[1] += f.y; a[2] += f.z;
-        a[3] += m.x; a[4] += m.y; a[5] += m.z;
-      }
-      for (int64_t p = j0 + lane; p < j1; p += 32) {
-        const int64_t e = s.jlist[p];
-        if (!s.act[e]) continue;
-        const V3 f = ld3(s.cf, e), m = ld3(s.cmj, e);
-        a[0] -= f.x; a[1] -= f.y; a[2] -= f.z;
-        a[3] += m.x; a[4] += m.y; a[5] += m.z;
-      }
-#pragma unroll
-      for (int d = 0; d < 6; d++)
-        for (int o = 16; o > 0; o >>= 1) a[d] += __shfl_xor_sync(0xffffffffu, a[d], o);
-      if (lane == src) {
-        V3 F, M;
-        init_resultant(s, hb, F, M);
-        st3(s.force, hb, F + v3(a[0], a[1], a[2]));
-        st3(s.moment, hb, M + v3(a[3], a[4], a[5]));
-      }
+  const bool inb = b < s.n;
+  const bool free_body = inb && b >= s.n_driven;
+  const int hv = inb ? (int)s.is_heavy[b] : 1;
+  const bool group_sum = free_body && (hv == 0 || hv == 3);
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  if (group_sum) {
+    const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1], j0 = s.jofs[b], j1 = s.jofs[b + 1];
+    for (int64_t e = i0 + l; e < i1; e += kGatherLanes) {
+      if (!s.act[e]) continue;
+      const V3 f = ld3(s.cf, e), m = ld3(s.cmi, e);
+      a[0] += f.x; a[1] += f.y; a[2] += f.z;
+      a[3] += m.x; a[4] += m.y; a[5] += m.z;
+    }
+    for (int64_t p = j0 + l; p < j1; p += kGatherLanes) {
+      const int64_t e = s.jlist[p];
+      if (!s.act[e]) continue;
+      const V3 f = ld3(s.cf, e), m = ld3(s.cmj, e);
+      a[0] -= f.x; a[1] -= f.y; a[2] -= f.z;
+      a[3] += m.x; a[4] += m.y; a[5] += m.z;
     }
   }
-  if (b < s.n) {
+#pragma unroll
+  for (int d = 0; d < 6; d++)
+    for (int o = kGatherLanes / 2; o > 0; o >>= 1) a[d] += __shfl_xor_sync(0xffffffffu, a[d], o);
+  if (inb && l == 0) {
     if (b < s.n_driven) {
       gather_body(s, b, apply_kick);
     } else {
       V3 F, M;
-      body_resultant(s, b, F, M);
+      if (group_sum) {
+        init_resultant(s, b, F, M);
+        F = F + v3(a[0], a[1], a[2]);
+        M = M + v3(a[3], a[4], a[5]);
+      } else {  // summed by k_gather_heavy
+        F = ld3(s.force, b);
+        M = ld3(s.moment, b);
+      }
       const V3 vel = ld3(s.vel, b), vrot = ld3(s.vrot, b);
       if (s.num_damp > 0.0) {  // the sign tests stay FP64: near zero they decide a factor 1 +- damp
         const double fm = 1.0 - s.num_damp, fp = 1.0 + s.num_damp;
@@ -209,8 +211,9 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
       have = true;
     }
   }
-  // the learned skin's guard on the state this step leaves (all lanes)
-  if (s.sk_out && apply_kick) skin_guard_body_t<CvtBits>(s, b, have, kin);
+  // the learned skin's guard on the state this step leaves (all lanes; one
+  // body per group)
+  if (s.sk_out && apply_kick) skin_guard_body_t<CvtBits>(s, (inb && l == 0) ? b : s.n, have, kin);
   if (s.sk_ctl) skin_batch_step_end(s);
 }
 

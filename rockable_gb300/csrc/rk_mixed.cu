@@ -10,7 +10,9 @@
 //   FP32  everything measured relative to a body centre or a face vertex:
 //         edge / segment parameters, the point-in-polygon test, the contact
 //         point, the relative velocity, the tangential force and rolling
-//         moment, and the force / moment contributions.
+//         moment, and the force / moment contributions; and a first test
+//         that proves most entries of a dense list apart (apart_f32), which
+//         then skip the FP64 path altogether.
 // An overlap dn is a small difference of lengths of the order of the
 // particle size, which FP32 cannot resolve; all the other quantities are well
 // conditioned.  Compiled with fused multiply-adds allowed.
@@ -60,6 +62,96 @@ __device__ __forceinline__ double len64(V3 d, double& inv) {
   return s * y;
 }
 
+__device__ __forceinline__ F3 ldgvr(const float* g, int64_t k) { return f3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
+__device__ __forceinline__ float amax(F3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
+
+// Whether an entry is clearly apart, from FP32 geometry alone: its
+// sub-elements' vertices relative to body j's centre (the FP32 offsets gvr,
+// plus the FP64 difference of the two centres rounded once), the same
+// projection parameters as the FP64 path, and the separation's length.  The
+// overlap estimate dnf errs by a few ulps of the coordinates (below 1e-7 of
+// their magnitude), so an estimate above a margin of 2e-6 m plus 2e-6 of the
+// coordinates' magnitude proves dn > 0: the FP64 length, the contact point
+// and everything after are skipped, and dnf is kept as the entry's dn (a
+// separated entry's dn only matters through its sign).  When the projection
+// falls outside the edge or face, or a vertex-face contact's face is not a
+// triangle, the FP64 path decides.
+__device__ __forceinline__ bool apart_f32(const Scene& s, int type, int i, int j, int isub, int jsub, bool pre,
+                                          int4 G, F3 dxij, float rsum, float* dnf) {
+  const float* g = s.gvr;
+  auto gi = [&](int local) { return (int64_t)s.gv_ofs[i] + local; };
+  auto gj = [&](int local) { return (int64_t)s.gv_ofs[j] + local; };
+  F3 d;
+  float mag;
+  if (type == 0) {
+    const F3 a = ldgvr(g, pre ? G.x : gi(isub)) + dxij, b = ldgvr(g, pre ? G.y : gj(jsub));
+    d = a - b;
+    mag = fmaxf(amax(a), amax(b));
+  } else if (type == 1) {
+    int64_t k1, k2;
+    if (pre) { k1 = G.y; k2 = G.z; }
+    else {
+      const int eo = s.edge_ofs[s.shape[j]] + jsub;
+      k1 = gj(s.edges[2 * eo]);
+      k2 = gj(s.edges[2 * eo + 1]);
+    }
+    const F3 a = ldgvr(g, pre ? G.x : gi(isub)) + dxij, p1 = ldgvr(g, k1), p2 = ldgvr(g, k2);
+    const F3 E = p2 - p1, w = a - p1;
+    const float r = dotf(w, E) / dotf(E, E);
+    if (r <= 0.f || r >= 1.f) return false;
+    d = w - r * E;
+    mag = fmaxf(amax(a), fmaxf(amax(p1), amax(p2)));
+  } else if (type == 2) {
+    if (!(pre && G.w >= 0)) return false;  // polygons other than triangles: the FP64 path
+    const F3 a = ldgvr(g, G.x) + dxij, A = ldgvr(g, G.y), B = ldgvr(g, G.z), C = ldgvr(g, G.w);
+    const F3 bA = B - A, cA = C - A, w = a - A;
+    F3 nn = crossf(bA, cA);
+    nn = rsqrtf(dotf(nn, nn)) * nn;
+    float dist = dotf(w, nn);
+    if (dist < 0.f) { nn = -nn; dist = -dist; }
+    // the crossing-number test (the FP64 path's, in the same FP32 frame)
+    const F3 v1 = rsqrtf(dotf(bA, bA)) * bA, v2 = crossf(nn, v1);
+    const F3 P = w - dist * nn;
+    const float ori1 = dotf(P, v1), ori2 = dotf(P, v2);
+    int odd = 0;
+    auto edge = [&](F3 pa, F3 pb) {
+      float pa1 = dotf(pa, v1), pb1 = dotf(pb, v1), pa2 = dotf(pa, v2), pb2 = dotf(pb, v2);
+      if ((pa2 < ori2 && pb2 >= ori2) || (pb2 < ori2 && pa2 >= ori2)) {
+        if (pa1 + (ori2 - pa2) / (pb2 - pa2) * (pb1 - pa1) < ori1) odd = 1 - odd;
+      }
+    };
+    const F3 z = f3(0, 0, 0);
+    edge(z, bA);
+    edge(bA, cA);
+    edge(cA, z);
+    if (!odd) return false;
+    mag = fmaxf(amax(a), fmaxf(amax(A), fmaxf(amax(B), amax(C))));
+    *dnf = dist - rsum;
+    return *dnf > 2e-6f + 2e-6f * mag;
+  } else {
+    int64_t a1, a2, b1, b2;
+    if (pre) { a1 = G.x; a2 = G.y; b1 = G.z; b2 = G.w; }
+    else {
+      const int eoi = s.edge_ofs[s.shape[i]] + isub, eoj = s.edge_ofs[s.shape[j]] + jsub;
+      a1 = gi(s.edges[2 * eoi]); a2 = gi(s.edges[2 * eoi + 1]);
+      b1 = gj(s.edges[2 * eoj]); b2 = gj(s.edges[2 * eoj + 1]);
+    }
+    const F3 pi1 = ldgvr(g, a1) + dxij, pi2 = ldgvr(g, a2) + dxij, pj1 = ldgvr(g, b1), pj2 = ldgvr(g, b2);
+    const F3 Ei = pi2 - pi1, Ej = pj2 - pj1, w = pi1 - pj1;
+    const float c = dotf(Ei, Ei), dd = dotf(Ej, Ej), ee = dotf(Ei, Ej);
+    float f = (c * dd) - (ee * ee);
+    if (fabsf(f) <= 1.0e-12f) return false;
+    f = 1.0f / f;
+    const float a = dotf(Ei, w), b = dotf(Ej, w);
+    const float ss = (ee * b - a * dd) * f, tt = (c * b - ee * a) * f;
+    if (ss <= 0.f || ss >= 1.f || tt <= 0.f || tt >= 1.f) return false;
+    d = (w + ss * Ei) - tt * Ej;
+    mag = fmaxf(fmaxf(amax(pi1), amax(pi2)), fmaxf(amax(pj1), amax(pj2)));
+  }
+  *dnf = sqrtf(dotf(d, d)) - rsum;
+  return *dnf > 2e-6f + 2e-6f * mag;
+}
+
 __global__ void k_narrow_force_mixed(Scene s) {
   if (step_halted(s)) return;
   // threads follow the entries grouped by sub-contact type (fewer divergent
@@ -82,7 +174,16 @@ __global__ void k_narrow_force_mixed(Scene s) {
     double dn = 0.0;
     F3 n = f3(0, 0, 0), ci = f3(0, 0, 0);  // normal, contact point relative to x_i
     bool ok = true;
-    if (type == 0) {
+    // clearly apart (and nothing else needed of it): FP32 alone decides
+    bool quick = false;
+    if (bond < 0 && !s.record_geom && s.gvr) {
+      float dnf = 0.f;
+      quick = apart_f32(s, type, i, j, isub, jsub, pre, G, tof(xi - xj), d2f(Ri + Rj), &dnf);
+      if (quick) dn = f2d(dnf);
+    }
+    if (quick) {
+      // dn > 0 proven: separated, history untouched
+    } else if (type == 0) {
       V3 a, b;
       if (pre) {
         a = gvg(s.gv, G.x);

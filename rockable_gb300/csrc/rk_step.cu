@@ -580,7 +580,7 @@ int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
   // (a batched skin step zeroes it in k_skin_begin)
   if (s.sk_out && apply_kick && !s.sk_ctl) cudaMemsetAsync(s.sk_out, 0, 8 * sizeof(unsigned int), st);
   const int t = tpb_or(s, 1, 128);
-  if (s.fast_body) return launch_fused_gather(s, nblk(s.n, t), t, apply_kick, st);
+  if (s.fast_body) return launch_fused_gather(s, nblk(s.n * kGatherLanes, t), t, apply_kick, st);
   exact::k_gather_accel<<<nblk(s.n, t), t, 0, st>>>(s, apply_kick);
   return 1;
 }

@@ -214,3 +214,120 @@ def test_mixed_free_flight_tracks_fp64():
     # rotations of at most ~0.6 rad: the same relative bound on the quaternions
     assert dq <= 1e-7 and dw <= 1e-5, (dq, dw)
     assert unit <= 1e-14
+
+
+def per_result_errors(g0, g64, gm, n_driven):
+    """Per-result relative errors of the mixed form against the FP64 form
+    after one step from the same state (g0: the bodies before it):
+      fn, ft   per active entry, |mixed - fp64| / max(|fp64|, 1e-6 x the
+               step's median |fn|) (the floor keeps a contact that has just
+               touched, with a force near zero, from dominating);
+      force,   per free body, |mixed - fp64| / the sum of the magnitudes of
+      moment   the body's active contact forces (its own force scale: a body
+               near equilibrium has a small net force);
+      pos, Q   per free body, |mixed - fp64| / the step's change |fp64 - before|
+               (with a floor of 1e-15).
+    Returns, per quantity, the largest error, the 99.9th percentile and the
+    fraction within 1e-4."""
+    e64, em = g64.entries(), gm.entries()
+    both = e64["active"] & em["active"]
+    med = float(np.median(np.abs(e64["fn"][both]))) if both.any() else 1.0
+    floor = 1e-6 * med
+    fn_err = np.abs(em["fn"][both] - e64["fn"][both]) / np.maximum(np.abs(e64["fn"][both]), floor)
+    ftm = np.linalg.norm(e64["ft"][both], axis=1)
+    ft_err = np.linalg.norm(em["ft"][both] - e64["ft"][both], axis=1) / np.maximum(ftm, floor)
+    b64, bm = g64.bodies(), gm.bodies()
+    nb = len(b64["pos"])
+    scale = np.zeros(nb)
+    mag = np.abs(e64["fn"][both]) + ftm
+    np.add.at(scale, e64["i"][both], mag)
+    np.add.at(scale, e64["j"][both], mag)
+    out = {}
+    free = slice(n_driven, nb)
+    have = scale[free] > 0
+    for k in ["force", "moment"]:
+        out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1)[have] / scale[free][have]
+    for k in ["pos", "Q"]:
+        step = np.linalg.norm(b64[k][free] - g0[k][free], axis=1)
+        out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1) / np.maximum(step, 1e-15)
+    out["fn"], out["ft"] = fn_err, ft_err
+    return {k: {"max": float(v.max()) if len(v) else 0.0, "p999": float(np.percentile(v, 99.9)) if len(v) else 0.0,
+                "within_1e-4": float(np.mean(v <= 1e-4)) if len(v) else 1.0, "n": int(len(v))}
+            for k, v in out.items()}
+
+
+def test_mixed_per_result_relative_errors_settled_column(gpu_lib):
+    """One step from a settled, contact-rich column in both forms: per-result
+    relative errors (per_result_errors).  The normal and tangential forces of
+    99.9 % of the active contacts, the body resultants (relative to the body's
+    own contact forces) and the step's motion agree within 1e-4."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
+    scene = scenes.column_collapse(n=3000, nshapes=128, semi=(0.0025, 0.0075))
+    gs = scenes.settle(scene, steps=2000)
+    gs.step(50)
+    g64 = clone(gs, scene, RK_FORM_FP64)
+    gm = clone(gs, scene, RK_FORM_MIXED)
+    g64.update_nl()
+    gm.update_nl()
+    before = g64.bodies()
+    g64.step(1)
+    gm.step(1)
+    r = per_result_errors(before, g64, gm, scene["n_driven"])
+    print("per-result relative errors:", r)
+    assert r["fn"]["n"] > 1000
+    for k in ["fn", "ft", "force", "moment", "pos", "Q"]:
+        assert r[k]["p999"] <= 1e-4, (k, r[k])
+
+
+def test_headline_contact_set_equals_fp64_rebuild_every_step(gpu_lib):
+    """The headline form (mixed precision, learned skin with exact contact
+    detection) on a settled, contact-rich column for 1000 steps: at every
+    10th step its active sub-contact set equals the one the FP64 form finds
+    at the same positions from a neighbour list rebuilt from scratch (a
+    fresh context: rk_update_nl, then the load-time force evaluation)."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
+    scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075), column=(0.15, 0.15, 1.5))
+    gs = scenes.settle(scene, steps=1500)
+    src = scenes.scene_from_gpu(scene, gs)
+    gs.close()
+    h = GpuScene(form=RK_FORM_MIXED)
+    h.upload_shapes(src["shape_tables"])
+    h.upload_bodies(src["bodies"], src["n_driven"])
+    scenes.set_scene_params(h, src)
+    d = src["dVerlet"]
+    h.set_skin(use_mlp=True, skin_min=0.1 * d, skin_max=4.0 * d, interval_min=2, interval_max=300, seed=7,
+               exact_contacts=True)
+
+    def active_keys(e):
+        a = e["active"]
+        return set(zip(e["i"][a].tolist(), e["j"][a].tolist(), e["type"][a].tolist(), e["isub"][a].tolist(),
+                       e["jsub"][a].tolist()))
+
+    checked, mismatched, active = 0, [], []
+    for step in range(1, 1001):
+        h.step(1)
+        if step % 10:
+            continue
+        st = h.bodies()
+        ha = active_keys(h.entries())
+        f = GpuScene(form=RK_FORM_FP64)
+        f.upload_shapes(src["shape_tables"])
+        b = dict(src["bodies"])
+        for k in ["pos", "vel", "acc", "Q", "vrot", "arot"]:
+            b[k] = st[k]
+        f.upload_bodies(b, src["n_driven"])
+        scenes.set_scene_params(f, src)
+        f.update_nl()
+        f.accelerations()
+        fa = active_keys(f.entries())
+        f.close()
+        checked += 1
+        active.append(len(fa))
+        if ha != fa:
+            mismatched.append((step, len(ha - fa), len(fa - ha)))
+    print("checked %d steps, active contacts %d..%d, mismatches %s, skin %s" % (
+        checked, min(active), max(active), mismatched[:10], h.skin_stats()))
+    assert checked == 100 and min(active) > 500
+    assert not mismatched

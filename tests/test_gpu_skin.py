@@ -74,31 +74,36 @@ def test_guard_keeps_the_contacts_of_per_step_rebuilds(gpu_lib):
 
 
 def test_learned_skin_against_the_method_without_it(gpu_lib):
-    """Same settled pile, 600 steps: fixed interval (plain), guard + last-window
-    predictor, guard + trained network.  Prints rebuilds and device time."""
+    """What the trained network gains over the method without it, on a run
+    long enough for more than 20 skin windows: a packed column released onto
+    its floor (its grains topple and settle: the displacement rate changes
+    from window to window), fixed interval (plain), guard + last-window
+    predictor (naive) and guard + the online-trained network (mlp), all from
+    the same state.  Both skin modes keep the contact set exact (the guard);
+    the network, which learns the window-to-window trend of the rate, must
+    need no more list refreshes than the last-window predictor, and less
+    device time than the fixed interval."""
     from rockable_gb300 import scenes
-    scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075))
-    gs = scenes.settle(scene, steps=1500)
-    src = scenes.scene_from_gpu(scene, gs)
+    scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075), column=(0.2, 0.2, 1.5))
     res = {}
     for name in ["plain", "naive", "mlp"]:
-        g = _engine(src)
-        g.upload_entries(src["entries"])
+        g = _engine(scene)
         if name != "plain":
             g.set_skin(use_mlp=(name == "mlp"), skin_min=0.05 * scene["dVerlet"], skin_max=4.0 * scene["dVerlet"],
-                       interval_min=2, interval_max=400, seed=11)
+                       interval_min=2, interval_max=150, seed=11)
         else:
             g.update_nl()
-        r = g.step(600)
+        r = g.step(6000)
         ms, _ = g.last_step_timing()
         sk = g.skin_stats() if name != "plain" else {}
         res[name] = {"ms": ms, "nl_updates": r["nl_updates"], "active": r["n_active"], "entries": r["n_entries"],
                      "skin": sk}
         g.close()
     print("learned skin comparison:", res)
-    for name in ["naive", "mlp"]:
-        assert res[name]["nl_updates"] >= 1
-        assert abs(res[name]["active"] - res["plain"]["active"]) <= 0.05 * res["plain"]["active"] + 5
+    mlp, naive = res["mlp"]["skin"], res["naive"]["skin"]
+    assert mlp["rebuilds"] >= 20 and mlp["train_steps"] > 0 and mlp["loss"] > 0.0
+    assert mlp["rebuilds"] + mlp["partial"] <= naive["rebuilds"] + naive["partial"]
+    assert res["mlp"]["ms"] < res["plain"]["ms"]
 
 
 def _keys(e):
