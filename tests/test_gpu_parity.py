@@ -221,3 +221,30 @@ def test_sticked_links_bonds_and_rupture_bitwise(golden_dir, oracle_lib, gpu_lib
     assert int(broken.sum()) == len(broken) - len(o.interfaces())
     assert int(broken.sum()) > 0
     assert_bodies_equal(o, g, "bonds")
+
+
+def test_stats_match_oracle(golden_dir, oracle_lib, gpu_lib):
+    """rk_get_stats (Rockable::getKineticEnergy, Rockable.cpp:3958-3970; the
+    coordination 2 A / N_free and the broken-bond count) against the oracle's
+    after a bonded run with ruptures: the counts exactly, the kinetic
+    energies to 1e-12 (the device reduction adds in another order)."""
+    import oracle_cases
+    from helpers import set_params_from_oracle
+    name = "sticked_rupture_518"
+    conf = oracle_cases.make_conf(name, str(golden_dir / "518_poly" / CONF["518_poly"]),
+                                  str(golden_dir / "518_poly" / "v_stats.conf"))
+    o = oracle_lib.Oracle(conf)
+    for p, v in oracle_cases.CASES[name]["after_load"]:
+        o.set_param(p, 0, 0, v)
+    g = gpu_from_oracle(o)
+    set_params_from_oracle(g, o)
+    o.update_nl()
+    g.update_nl()
+    o.run(200)
+    g.step(200)
+    so, sg = o.stats(), g.stats()
+    assert int(so["n_active"]) == sg["n_active"]
+    assert int(so["n_broken"]) == sg["n_broken"] and sg["n_broken"] > 0
+    assert so["coordination"] == pytest.approx(sg["coordination"], rel=1e-15)
+    for k in ["e_trans", "e_rot"]:
+        assert sg[k] == pytest.approx(so[k], rel=1e-12), k
