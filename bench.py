@@ -2,10 +2,17 @@
 
 Workload (default): the granular column collapse -- 50,000 convex hull grains
 (semi-axes U[0.5, 1.5] cm, Avalanche law, linked-cell neighbour list) in a
-loose random packing that fills a 0.5 x 0.5 m column about 1.2 m high on a
-rigid floor, released at t = 0.  The packing is built on the CPU by the
-seeded packer (rockable_gb300/host/rk_pack.cpp, through scenes.column_collapse),
-so the GPU forms and the CPU reference path start from the same state.
+random packing (bulk solid fraction ~0.52, coordination ~5) that fills a
+0.5 x 0.5 m column about 1.1 m high on a rigid floor.  The packing is built
+on the CPU by the seeded packer (rockable_gb300/host/rk_pack.cpp, through
+scenes.column_collapse); its grains touch but carry no load.  Before any
+timing the pile is loaded by gravity between four walls with the scene's own
+parameters in the FP64 form (`--load-steps` DEM steps, scenes.loaded), then
+the walls are removed: every form starts from that loaded column at release,
+contact history included.  The reference arm (`--impl reference`), which
+must not load the GPU library, times the same packing at t = 0 before
+loading; the `cpu_baseline` leg times the same CPU path on the loaded state,
+so the two CPU rates can be compared.
 
 One bench step is one segment of `--segment` DEM steps (100: the fixed
 schedule's interVerlet), each DEM step one pass of the velocity-Verlet step
@@ -61,6 +68,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--segment", type=int, default=100, help="DEM steps per bench step")
     ap.add_argument("--n", type=int, default=50000, help="grains of the column")
+    ap.add_argument("--load-steps", type=int, default=20000,
+                    help="DEM steps that load the column by gravity between walls before the release")
+    ap.add_argument("--iso-load-steps", type=int, default=10000,
+                    help="DEM steps of servo compression before the compression box is timed")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--iso-n", type=int, default=200000, help="grains of the compression box (0: skip)")
@@ -272,7 +283,7 @@ def cpu_baseline(scene, segment, budget_s, label):
     segs, s, rb, st, o = cpu_segments(scene, segment, 1, budget_s)
     v = nfree * segment / float(np.mean(segs))
     return {"value": v, "unit": "particle-steps/s", "cores": cpu_threads(), "kind": "port", "cpu": cpu_info(),
-            "sample": ("%s at t = 0: one neighbour-list rebuild (%.2f s) and %d DEM steps (%.4f s each) of the "
+            "sample": ("%s: one neighbour-list rebuild (%.2f s) and %d DEM steps (%.4f s each) of the "
                        "%d-body scene; the %d-step segment's time is the rebuild plus %d x the step time "
                        "(linear extrapolation)" % (label, rb, s, st, o.n, segment, segment))}
 
@@ -285,6 +296,8 @@ def run_reference(a, rank):
     if rank != 0:
         return
     from rockable_gb300 import scenes
+    # the GPU arm's packing before its gravity load (which runs on the GPU):
+    # the same grains, walls already removed
     scene = scenes.column_collapse(n=a.n)
     nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
     segs, s, rb, st, o = cpu_segments(scene, a.segment, a.steps, a.ref_seconds, warm=a.warmup)
@@ -300,7 +313,10 @@ def run_reference(a, rank):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
            "impl": "reference",
            "config": {"workload": scene["name"], "law": scene["law"], "bodies": int(o.n), "free_bodies": int(nfree),
-                      "dem_steps_per_step": a.segment, "state": "the packed column at release (t = 0)",
+                      "dem_steps_per_step": a.segment,
+                      "state": ("the packed column at t = 0, before the gravity load that the GPU arm runs on the "
+                                "GPU (this arm does not load the GPU library); the GPU arm's cpu_baseline times the "
+                                "same CPU path on the loaded state"),
                       "cpu": cpu_info()},
            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                             "sample": sample},
@@ -323,6 +339,8 @@ def engine(scene, form, dev, skin=None):
     if scene.get("scene_of") is not None:
         e.set_scenes(scene["scene_of"])
     scenes.set_scene_params(e, scene)
+    if scene.get("entries") is not None:  # a loaded state: its contacts and their history
+        e.upload_entries(scene["entries"])
     if skin:
         d = scene["dVerlet"]
         # the interval stays within 3x the fixed schedule's, so that the
@@ -330,7 +348,7 @@ def engine(scene, form, dev, skin=None):
         e.set_skin(use_mlp=True, skin_min=0.1 * d, skin_max=4.0 * d, dverlet_ratio=2.0, interval_min=2,
                    interval_max=3 * int(round(scene["interVerlet"] / scene["dt"])), seed=3,
                    exact_contacts=(skin == "exact"))
-    else:
+    elif scene.get("entries") is None:
         e.update_nl()
     e.set_graphs(True)
     return e
@@ -429,13 +447,15 @@ def e2e_leg(g, scene, a, dist, ws, steps):
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    rebuilds = 0
     for _ in range(steps):
         g.upload_kinematics_packed(hb)
-        g.step(a.segment)
+        rebuilds += int(g.step(a.segment)["nl_updates"])
         g.download_kinematics_packed(hb)
     el = rank_max(time.perf_counter() - t0, dist)
     return {"value": job_rate(ws, nfree, steps * a.segment, 1000.0 * el), "unit": "particle-steps/s",
             "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8), "steps": steps,
+            "nl_rebuilds": rebuilds,
             "note": "every bench step: the kinematics (pos, vel, acc, Q, vrot, arot) of every body H2D from one "
                     "pinned packed buffer, rk_step(%d), the same fields D2H back" % a.segment}
 
@@ -520,8 +540,11 @@ def iso_workload(a, dev, dist, ws, order):
     a CPU sample of the same segment (reported against the >= 50x target)."""
     from rockable_gb300 import scenes
     t0 = time.perf_counter()
-    sc = scenes.iso_compression(n=a.iso_n)
+    packed = scenes.iso_compression(n=a.iso_n)
     t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sc = scenes.loaded(packed, a.iso_load_steps, device=dev)
+    t_load = time.perf_counter() - t0
     nfree = len(sc["bodies"]["mass"]) - sc["n_driven"]
     steps = max(2, a.steps // 4)
     forms = {}
@@ -532,11 +555,14 @@ def iso_workload(a, dev, dist, ws, order):
     head = forms[order[-1]]
     out = {"workload": sc["name"], "bodies": len(sc["bodies"]["mass"]), "free_bodies": nfree,
            "law": sc["law"], "servo": "tritriIsostaticCompression at %g Pa, no gravity" % sc["servo"]["pressure"],
-           "pack": sc["pack"], "dem_steps_per_step": a.segment, "steps": steps, "warmup": 1,
+           "pack": sc["pack"], "load": sc["load"],
+           "state": "the packed box after %d DEM steps of servo compression (FP64 form)" % a.iso_load_steps,
+           "dem_steps_per_step": a.segment, "steps": steps, "warmup": 1,
            "forms": forms, "headline_form": order[-1],
-           "headline_vs_plain": head["value"] / forms["plain_fp64"]["value"], "setup_s": {"generate": t_gen}}
+           "headline_vs_plain": head["value"] / forms["plain_fp64"]["value"],
+           "setup_s": {"generate": t_gen, "load": t_load}}
     if not a.no_cpu:
-        cb = cpu_baseline(sc, a.segment, 2.0 * a.cpu_seconds, "the compression box")
+        cb = cpu_baseline(sc, a.segment, 2.0 * a.cpu_seconds, "the compressed box")
         out["cpu_baseline"] = cb
         out["vs_cpu"] = {k: v["value"] / cb["value"] for k, v in forms.items()}
         out["target_50x_at_200k"] = ("met" if min(out["vs_cpu"].values()) >= 50.0 else "not met")
@@ -559,8 +585,11 @@ def main():
     from rockable_gb300 import scenes
     dev = int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0
     t0 = time.perf_counter()
-    scene = scenes.column_collapse(n=a.n)
+    packed = scenes.column_collapse(n=a.n, walls=True)
     t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    scene = scenes.loaded(packed, a.load_steps, device=dev)
+    t_load = time.perf_counter() - t0
     N = len(scene["bodies"]["mass"])
     nfree = N - scene["n_driven"]
     order = [f.strip() for f in a.forms.split(",") if f.strip()]
@@ -577,11 +606,12 @@ def main():
     consts = profile_constants()
     fp64 = fp64_peak() if rank == 0 else None
     roof = roofline(head, scene, consts, fp64)
-    e2e = None if a.no_e2e else e2e_leg(g, scene, a, dist, ws, max(2, min(a.steps, 10)))
+    e2e = None if a.no_e2e else e2e_leg(g, scene, a, dist, ws, a.steps)
     g.close()
     iso = iso_workload(a, dev, dist, ws, order) if (a.iso_n > 0 and rank == 0) else None
     batched = batched_workload(a, dev) if (rank == 0 and a.batch_scenes > 0) else None
-    cpu = cpu_baseline(scene, a.segment, a.cpu_seconds, "the column") if (rank == 0 and not a.no_cpu) else None
+    cpu = cpu_baseline(scene, a.segment, a.cpu_seconds, "the loaded column at release") if (
+        rank == 0 and not a.no_cpu) else None
     if rank == 0:
         out = {"metric": METRIC, "value": head["value"], "unit": "particle-steps/s", "n_gpus": ws, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -596,13 +626,14 @@ def main():
                           "active_per_free": head["active_per_free"],
                           "nl_rebuilds_in_timed": head["nl_rebuilds_in_timed"], "dt": scene["dt"],
                           "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
-                          "pack": scene["pack"],
-                          "state": ("the loose random packing released at t = 0 (no walls), then %d tuning and %d "
-                                    "warm-up DEM steps before the timed ones" % (TUNE_STEPS, a.warmup * a.segment)),
+                          "pack": scene["pack"], "load": scene["load"],
+                          "state": ("the packed column loaded by gravity between four walls (%d DEM steps, FP64 "
+                                    "form), walls removed, then %d tuning and %d warm-up DEM steps of each form "
+                                    "before its timed ones" % (a.load_steps, TUNE_STEPS, a.warmup * a.segment)),
                           "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if head["entries"] * 240 + N * 600 >
                           129e6 else "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
                           "parallelism": "replicas" if ws > 1 else "single GPU",
-                          "setup_s": {"generate": t_gen}},
+                          "setup_s": {"generate": t_gen, "load": t_load}},
                "gpu_launches": head["gpu_launches"], "wall_s": head["wall_s"], "clocks": head["clocks"],
                "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "iso": iso, "batched": batched}
         print(json.dumps(out), flush=True)

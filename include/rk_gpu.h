@@ -54,6 +54,8 @@ enum {
 
 enum { RK_LAW_DEFAULT = 0, RK_LAW_AVALANCHE = 1, RK_LAW_STICKEDLINKS = 2 };
 enum { RK_FORM_FP64 = 0, RK_FORM_MIXED = 1 };
+/* BodyForce plugins (src/BodyForces/BodyForce_*.cpp). */
+enum { RK_BF_NONE = 0, RK_BF_ATTRACTING_POINT = 1, RK_BF_PREFERRED_DIRECTION = 2, RK_BF_VISCOUS_FLUID = 3 };
 
 /* Parameter slots of the per-group-pair table (DataTable ids of
  * Rockable.cpp:96-123).  table[(p * ngroup + g1) * ngroup + g2]. */
@@ -196,6 +198,27 @@ int rk_set_params(rk_ctx* ctx, const rk_params* p);
 int rk_upload_entries(rk_ctx* ctx, const rk_entries* e);
 int rk_upload_interfaces(rk_ctx* ctx, const rk_interfaces* f);
 int rk_set_controls(rk_ctx* ctx, const rk_control* c, int32_t n, const rk_servo* servo);
+/* The body force of every free body, added at the start of each force
+ * computation (replaces Rockable::bodyForce, Rockable.hpp:125, applied in
+ * Rockable.cpp:2887-2901; the plugin is selected by the conf keyword
+ * BodyForce, Rockable.cpp:1026-1040).  params are the plugin's conf values in
+ * the order its read() takes them:
+ *   RK_BF_NONE                 nparams 0 (no body force)
+ *   RK_BF_ATTRACTING_POINT     point x y z, acceleration (nparams 4;
+ *                              BodyForce_AttractingPoint.cpp:43-59)
+ *   RK_BF_PREFERRED_DIRECTION  axisBody x y z, axis x y z, momentMax
+ *                              (nparams 7; both axes are normalised here as
+ *                              read() does; BodyForce_PreferredDirection.cpp:
+ *                              43-80)
+ *   RK_BF_VISCOUS_FLUID        fluidDensity (nparams 1; BodyForce_ViscousFluid.
+ *                              cpp:42-58); body_volume[b] = V h^3 (the shape's
+ *                              volume times the homothety cubed, multiplied in
+ *                              that order) for every body, required
+ * body_volume is ignored by the other kinds.  Unknown kinds, a wrong nparams
+ * or a missing body_volume return RK_ERR_ARG.  Uploading bodies of another
+ * count afterwards drops a viscous-fluid body force (its volumes no longer
+ * match). */
+int rk_set_body_force(rk_ctx* ctx, int kind, const double* params, int32_t nparams, const double* body_volume);
 /* Select the arithmetic of the narrow phase and force laws for the next
  * steps: RK_FORM_FP64 (bit-identical to the reference CPU path) or
  * RK_FORM_MIXED (FP32 on body-relative coordinates, FP64 for positions, the

@@ -45,6 +45,7 @@ def lib():
             "orc_get_body_static": (None, [P] * 7), "orc_ngroup": (I, [P]), "orc_get_table": (None, [P, P]),
             "orc_ncontrols": (I, [P]), "orc_get_controls": (None, [P] * 7), "orc_get_flow": (None, [P, P]),
             "orc_set_variant": (None, [P]), "orc_set_param": (I, [P, C.c_char_p, I, I, D]),
+            "orc_get_body_force": (I, [P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -142,6 +143,13 @@ class Oracle:
         a = np.zeros(5)
         lib().orc_get_stats(self.h, _p(a))
         return dict(zip(["e_trans", "e_rot", "n_active", "coordination", "n_broken"], a))
+
+    def body_force(self):
+        """(kind, conf parameters, V h^3 per body) of the BodyForce plugin."""
+        p = np.zeros(8)
+        v = np.zeros(self.n)
+        k = lib().orc_get_body_force(self.h, _p(p), _p(v))
+        return k, p[:[0, 4, 7, 1][k]], v
 
     @property
     def law(self):

@@ -438,6 +438,17 @@ struct Sim {
   double interVerlet{0.01}, interConf{0.25};
   double DVerlet{0.0}, dVerlet{0.0};
   V3 gravity{0.0, -9.81, 0.0};
+  // BodyForce plugin (Rockable.cpp:1026-1040): 0 none, 1 AttractingPoint,
+  // 2 PreferredDirection, 3 ViscousFluid, with their read() members
+  // (BodyForce_AttractingPoint.cpp:43-45, BodyForce_PreferredDirection.cpp:
+  // 43-48, BodyForce_ViscousFluid.cpp:42)
+  int bf_kind{0};
+  V3 bf_point;
+  double bf_acceleration{0.0};
+  V3 bf_axisBody, bf_axis;
+  double bf_momentMax{0.0}, bf_Kr{0.0};
+  double bf_fluidDensity{0.0};
+  std::vector<double> bf_raw;  // the plugin's conf values as read
   int paramsInInterfaces{0};
   int dynamicUpdateNL{0};
   double dispUpdateNL{1.0}, angleUpdateNL{1.0};
@@ -1044,6 +1055,39 @@ static void law_sticked(Sim& S, Contact& I, std::vector<Iface*>& to_break) {
 }
 
 // --------------------------------------------------------- accelerations ----
+// The BodyForce plugins' getForceAndMoment (force and moment start at zero,
+// each plugin sets one of them)
+static void body_force(const Sim& S, const Body& P, V3& force, V3& moment) {
+  if (S.bf_kind == 1) {  // BodyForce_AttractingPoint.cpp:51-59
+    V3 direction = S.bf_point - P.pos;
+    double l2 = norm2(direction);
+    if (l2 > 0.0) {
+      direction *= 1.0 / sqrt(l2);
+      force = P.mass * S.bf_acceleration * direction;
+    }
+  } else if (S.bf_kind == 2) {  // BodyForce_PreferredDirection.cpp:58-80
+    V3 axisB = qrot(P.Q, S.bf_axisBody);
+    normalize(axisB);
+    V3 u = cross(S.bf_axis, axisB);
+    normalize(u);
+    double cosa = axisB * S.bf_axis;
+    double angle = acos(cosa);
+    double sgn = -1.0;
+    if (cosa < 0.0) {
+      sgn = 1.0;
+      angle = kPi - angle;
+    }
+    moment = S.bf_Kr * sgn * u * angle;
+  } else if (S.bf_kind == 3) {  // BodyForce_ViscousFluid.cpp:47-58
+    const double two_thirds = 2.0 / 3.0, half_cx_sphere = 0.5 * 0.47;
+    V3 velSqr(P.vel.x * P.vel.x, P.vel.y * P.vel.y, P.vel.z * P.vel.z);
+    double h = P.homothety;
+    double pVolume = P.shape->volume * h * h * h;
+    double pSurface = pow(pVolume, two_thirds);
+    force = half_cx_sphere * S.bf_fluidDensity * pSurface * velSqr;
+  }
+}
+
 // Rockable.cpp:2869-2929
 static void init_forces(Sim& S) {
   for (size_t i = 0; i < S.nDriven && i < S.bodies.size(); ++i) {
@@ -1053,6 +1097,12 @@ static void init_forces(Sim& S) {
   for (size_t i = S.nDriven; i < S.bodies.size(); ++i) {
     S.bodies[i].force.reset();
     S.bodies[i].moment.reset();
+    if (S.bf_kind != 0) {
+      V3 force_more, moment_more;
+      body_force(S, S.bodies[i], force_more, moment_more);
+      S.bodies[i].force += force_more;
+      S.bodies[i].moment += moment_more;
+    }
   }
   for (auto& c : S.controls) {
     Body& P = S.bodies[c.i];
@@ -1645,7 +1695,32 @@ static bool parse_conf(Sim& S, std::istream& conf) {
       std::string par, io; double lambda, m; int ts;
       conf >> par >> io >> lambda >> m >> ts;
       prepro_variable_params(S, par, io, lambda, m, ts);
-    } else if (tok == "BodyForce" || tok == "DataExtractor" || tok == "initSpringJoint" || tok == "Tempo" ||
+    } else if (tok == "BodyForce") {
+      std::string name; conf >> name;
+      if (name == "AttractingPoint") {
+        S.bf_kind = 1;
+        read_v3(conf, S.bf_point);
+        conf >> S.bf_acceleration;
+        S.bf_raw = {S.bf_point.x, S.bf_point.y, S.bf_point.z, S.bf_acceleration};
+      } else if (name == "PreferredDirection") {
+        S.bf_kind = 2;
+        read_v3(conf, S.bf_axisBody);
+        read_v3(conf, S.bf_axis);
+        conf >> S.bf_momentMax;
+        S.bf_raw = {S.bf_axisBody.x, S.bf_axisBody.y, S.bf_axisBody.z, S.bf_axis.x, S.bf_axis.y, S.bf_axis.z,
+                    S.bf_momentMax};
+        normalize(S.bf_axisBody);
+        normalize(S.bf_axis);
+        S.bf_Kr = 2.0 * S.bf_momentMax / kPi;
+      } else if (name == "ViscousFluid") {
+        S.bf_kind = 3;
+        conf >> S.bf_fluidDensity;
+        S.bf_raw = {S.bf_fluidDensity};
+      } else {
+        g_err = "BodyForce " + name + " is unknown";
+        return false;
+      }
+    } else if (tok == "DataExtractor" || tok == "initSpringJoint" || tok == "Tempo" ||
                tok == "usePeriodicCell" || tok == "useSoftParticles") {
       g_err = "keyword " + tok + " is out of the oracle's scope";
       return false;
@@ -1773,6 +1848,14 @@ static bool save_conf(Sim& S, const std::string& fname) {
   for (auto& kv : S.density)
     if (kv.second > 0.0) { head << "density " << kv.first << " "; put_g(head, kv.second); head << '\n'; }
   head << "gravity " << S.gravity.x << " " << S.gravity.y << " " << S.gravity.z << '\n';
+  if (S.bf_kind == 1)  // Rockable.cpp:470-473 with BodyForce_*.cpp write()
+    head << "BodyForce AttractingPoint " << S.bf_point.x << " " << S.bf_point.y << " " << S.bf_point.z << ' '
+         << S.bf_acceleration << '\n';
+  else if (S.bf_kind == 2)
+    head << "BodyForce PreferredDirection " << S.bf_axisBody.x << " " << S.bf_axisBody.y << " " << S.bf_axisBody.z
+         << ' ' << S.bf_axis.x << " " << S.bf_axis.y << " " << S.bf_axis.z << ' ' << S.bf_momentMax << '\n';
+  else if (S.bf_kind == 3)
+    head << "BodyForce ViscousFluid " << S.bf_fluidDensity << '\n';
   head << "ParamsInInterfaces " << S.paramsInInterfaces << '\n';
   head << "dynamicUpdateNL " << S.dynamicUpdateNL << '\n';
   if (S.dynamicUpdateNL != 0) {
@@ -2005,6 +2088,18 @@ void orc_get_scalars(const orc_sim* s, double* o) {
   o[6] = S.dVerlet; o[7] = S.iconf; o[8] = (double)S.nDriven; o[9] = S.numDamp; o[10] = S.totalBrokenArea;
   o[11] = (double)S.nbroken; o[12] = S.gravity.x; o[13] = S.gravity.y; o[14] = S.gravity.z;
 }
+int orc_get_body_force(const orc_sim* s, double* params, double* body_volume) {
+  const Sim& S = s->S;
+  for (size_t k = 0; k < S.bf_raw.size() && k < 8; ++k) params[k] = S.bf_raw[k];
+  if (body_volume)
+    for (size_t b = 0; b < S.bodies.size(); ++b) {
+      const Body& P = S.bodies[b];
+      double hh = P.homothety;
+      body_volume[b] = P.shape->volume * hh * hh * hh;
+    }
+  return S.bf_kind;
+}
+
 void orc_get_stats(const orc_sim* s, double* o) {  // Rockable.cpp:3958-3970
   const Sim& S = s->S;
   double Et = 0.0, Er = 0.0;

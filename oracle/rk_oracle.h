@@ -84,6 +84,10 @@ void orc_get_interfaces(const orc_sim* s, double* out);
 /* Scalars: t, dt, tmax, interVerlet, interConf, DVerlet, dVerlet, iconf,
  * nDriven, numericalDampingCoeff, totalBrokenArea, nbroken, gravity3 */
 void orc_get_scalars(const orc_sim* s, double* out);
+/* The BodyForce plugin: returns its kind (0 none, 1 AttractingPoint,
+ * 2 PreferredDirection, 3 ViscousFluid), its conf values as read into
+ * params[8], and when body_volume is not NULL, V h^3 of every body. */
+int orc_get_body_force(const orc_sim* s, double* params, double* body_volume);
 void orc_get_stats(const orc_sim* s, double* out); /* Etrans Erot nactive coordination nbroken */
 int orc_law_id(const orc_sim* s); /* 0 Default, 1 Avalanche, 2 StickedLinks */
 const char* orc_option(const orc_sim* s, const char* key);

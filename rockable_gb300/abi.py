@@ -16,6 +16,7 @@ LIBPATH = os.path.join(HERE, "_lib", "librk_gpu.so")
 RK_OK = 0
 RK_LAW = {"Default": 0, "Avalanche": 1, "StickedLinks": 2}
 RK_FORM_FP64, RK_FORM_MIXED = 0, 1
+RK_BF = {"none": 0, "AttractingPoint": 1, "PreferredDirection": 2, "ViscousFluid": 3}
 RK_NPARAM = 22
 ERRORS = {-1: "RK_ERR_ARG", -2: "RK_ERR_CUDA", -3: "RK_ERR_CAPACITY", -4: "RK_ERR_UNSUPPORTED",
           -5: "RK_ERR_TIMEOUT", -6: "RK_ERR_STATE", -7: "RK_ERR_NUMERIC"}
@@ -101,6 +102,7 @@ SIGNATURES = {
     "rk_upload_entries": (C.c_int, [P, C.POINTER(RkEntries)]),
     "rk_upload_interfaces": (C.c_int, [P, C.POINTER(RkInterfaces)]),
     "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
+    "rk_set_body_force": (C.c_int, [P, C.c_int, P, C.c_int32, P]),
     "rk_set_record_geometry": (C.c_int, [P, C.c_int]),
     "rk_set_form": (C.c_int, [P, C.c_int]),
     "rk_set_broadphase": (C.c_int, [P, C.c_int]),
@@ -251,6 +253,15 @@ class GpuScene:
                 sv.walls[d] = int(servo["walls"][d])
             sv.pressure = float(servo["pressure"])
         self._chk(self.L.rk_set_controls(self.h, arr, n, C.byref(sv)), "rk_set_controls")
+
+    def set_body_force(self, kind, params=(), body_volume=None):
+        """The BodyForce plugin `kind` (a name of RK_BF or its number) with
+        its conf parameters; body_volume (V h^3 per body) for ViscousFluid."""
+        k = RK_BF[kind] if isinstance(kind, str) else int(kind)
+        p = np.ascontiguousarray(params, np.float64)
+        v = None if body_volume is None else np.ascontiguousarray(body_volume, np.float64)
+        self._chk(self.L.rk_set_body_force(self.h, k, _p(p) if len(p) else None, len(p),
+                                           _p(v) if v is not None else None), "rk_set_body_force")
 
     def set_broadphase(self, mode):
         self._chk(self.L.rk_set_broadphase(self.h, int(mode)), "rk_set_broadphase")

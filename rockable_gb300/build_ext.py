@@ -45,7 +45,10 @@ def _compile(src, flags):
     deps.append(os.path.join(HERE, "..", "include", "rk_gpu.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps if os.path.exists(d)):
         return obj
-    cmd = [nvcc(), GENCODE, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-c", srcp, "-o", obj] + flags
+    # host code unfused too: the host-side arithmetic that feeds the FP64
+    # form (body force parameters) must round like the reference's
+    cmd = [nvcc(), GENCODE, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+           "-c", srcp, "-o", obj] + flags
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))

@@ -849,7 +849,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.table); dfree(s.controls);
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
-  dfree(s.needres); dfree(s.scene_of);
+  dfree(s.needres); dfree(s.scene_of); dfree(s.bf_surf);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
   dfree(s.if_break); dfree(s.if_ofs); dfree(s.flags);
   free_entrybuf(c.eb[0]);
@@ -1003,6 +1003,10 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
   for (int64_t i = 0; i < n; i++) dq[4 * i] = 1.0;
   CK(cudaMemcpyAsync(s.dq, dq.data(), dq.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
   CK(cudaStreamSynchronize(c.stream));
+  if (s.bf_kind == RK_BF_VISCOUS_FLUID && c.bf_n != n) {  // its per-body volumes no longer match
+    dfree(s.bf_surf);
+    s.bf_kind = RK_BF_NONE;
+  }
   s.n = n;
   s.n_driven = b->n_driven;
   s.nvert = nv;
@@ -1171,6 +1175,44 @@ int rk_set_controls(rk_ctx* x, const rk_control* cs, int32_t n, const rk_servo* 
   return RK_OK;
 }
 
+
+int rk_set_body_force(rk_ctx* x, int kind, const double* p, int32_t np, const double* body_volume) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies) return fail(c, RK_ERR_STATE, "upload the bodies before the body force");
+  static const int want[4] = {0, 4, 7, 1};
+  if (kind < RK_BF_NONE || kind > RK_BF_VISCOUS_FLUID) return fail(c, RK_ERR_ARG, "unknown body force kind");
+  if (np != want[kind] || (np > 0 && !p)) return fail(c, RK_ERR_ARG, "wrong number of body force parameters");
+  if (kind == RK_BF_VISCOUS_FLUID && !body_volume) return fail(c, RK_ERR_ARG, "the viscous fluid needs body volumes");
+  Scene& s = c.s;
+  double bf[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (kind == RK_BF_ATTRACTING_POINT) {
+    for (int k = 0; k < 4; k++) bf[k] = p[k];
+  } else if (kind == RK_BF_PREFERRED_DIRECTION) {  // read(): both axes normalised, Kr = 2 momentMax / pi
+    V3 a = v3(p[0], p[1], p[2]), b = v3(p[3], p[4], p[5]);
+    normalize(a);
+    normalize(b);
+    bf[0] = a.x; bf[1] = a.y; bf[2] = a.z;
+    bf[3] = b.x; bf[4] = b.y; bf[5] = b.z;
+    bf[6] = 2.0 * p[6] / M_PI;
+    bf[7] = M_PI;
+  } else if (kind == RK_BF_VISCOUS_FLUID) {  // the drag coefficient 0.47 of a sphere, halved
+    bf[0] = 0.5 * 0.47;
+    bf[1] = p[0];
+    std::vector<double> surf(s.n);
+    for (int64_t b = 0; b < s.n; b++) surf[b] = std::pow(body_volume[b], 2.0 / 3.0);
+    int rc;
+    dfree(s.bf_surf);
+    if ((rc = dupload(c, s.bf_surf, surf.data(), s.n))) return rc;
+    CK(cudaStreamSynchronize(c.stream));
+  }
+  if (kind != RK_BF_VISCOUS_FLUID) dfree(s.bf_surf);
+  for (int k = 0; k < 8; k++) s.bf[k] = bf[k];
+  s.bf_kind = kind;
+  c.bf_n = s.n;
+  return RK_OK;
+}
 
 static int ready(Ctx& c) {
   if (!c.have_shapes || !c.have_bodies || !c.have_params)

@@ -34,11 +34,54 @@ __device__ __forceinline__ V3 euler_domega(V3 I, V3 w, V3 M) {
             (M.z - (I.y - I.x) * w.x * w.y) / I.z);
 }
 
-// imposed force / moment components of a driven body (Rockable.cpp:2904-2928)
+// The body force plugin's force and moment on free body b, each starting at
+// zero (the plugins' getForceAndMoment).
+__device__ __forceinline__ void body_force(const Scene& s, int64_t b, V3& f, V3& m) {
+  f = v3(0, 0, 0);
+  m = v3(0, 0, 0);
+  const double* p = s.bf;
+  if (s.bf_kind == RK_BF_ATTRACTING_POINT) {  // BodyForce_AttractingPoint.cpp:51-59
+    V3 d = v3(p[0], p[1], p[2]) - ld3(s.pos, b);
+    const double l2 = norm2(d);
+    if (l2 > 0.0) {
+      d = d * (1.0 / sqrt(l2));
+      f = (s.mass[b] * p[3]) * d;
+    }
+  } else if (s.bf_kind == RK_BF_PREFERRED_DIRECTION) {  // BodyForce_PreferredDirection.cpp:58-80
+    V3 axisB = qrot(ldq(s.Q, b), v3(p[0], p[1], p[2]));
+    normalize(axisB);
+    const V3 axis = v3(p[3], p[4], p[5]);
+    V3 u = cross(axis, axisB);
+    normalize(u);
+    const double cosa = dot(axisB, axis);
+    double angle = acos(cosa);
+    double sgn = -1.0;
+    if (cosa < 0.0) {
+      sgn = 1.0;
+      angle = p[7] - angle;
+    }
+    m = ((p[6] * sgn) * u) * angle;
+  } else if (s.bf_kind == RK_BF_VISCOUS_FLUID) {  // BodyForce_ViscousFluid.cpp:47-58
+    const V3 v = ld3(s.vel, b);
+    f = ((p[0] * p[1]) * s.bf_surf[b]) * v3(v.x * v.x, v.y * v.y, v.z * v.z);
+  }
+}
+
+// Imposed force / moment components of a driven body (Rockable.cpp:2904-2928);
+// a free body starts from the body force (Rockable.cpp:2887-2901: zero plus
+// the plugin's force and moment).
 __device__ __forceinline__ void init_resultant(const Scene& s, int64_t b, V3& F, V3& M) {
   F = v3(0, 0, 0);
   M = v3(0, 0, 0);
-  if (b >= s.n_driven) return;
+  if (b >= s.n_driven) {
+    if (s.bf_kind != RK_BF_NONE) {
+      V3 f, m;
+      body_force(s, b, f, m);
+      F = F + f;
+      M = M + m;
+    }
+    return;
+  }
   for (int k = 0; k < s.ncontrols; k++) {
     const Control c = s.controls[k];
     if (c.body != b) continue;

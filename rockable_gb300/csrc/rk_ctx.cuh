@@ -150,6 +150,7 @@ struct Ctx {
   double* kin_stage = nullptr;     // packed kinematics transfers (19 doubles per body)
   int64_t kin_stage_n = 0;
   std::vector<uint8_t> needres_host;
+  int64_t bf_n = 0;  // body count the body force was set for
   // block-size autotuner of the step kernels (results do not depend on it)
   int64_t tune_left = 0, tune_total = 0;
   double tune_ms[4][5] = {};  // [kernel][candidate block size]

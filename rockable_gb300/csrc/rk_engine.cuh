@@ -96,8 +96,13 @@ struct Scene {
   double gravity[3];
   double DVerlet, dVerlet;
   double num_damp;
+  // body force on the free bodies (rk_set_body_force): its parameters and,
+  // for the viscous fluid, pow(h^3 V, 2/3) per body; the RK_BF_* kind below
+  double bf[8];
+  double* bf_surf;
   double disp_update, angle_update;
   int dynamic_nl;
+  int bf_kind;
   // ---- controls
   int ncontrols;
   Control* controls;

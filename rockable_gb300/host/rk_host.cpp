@@ -45,6 +45,107 @@ struct LawStickedLinks : LawDefault {
 };
 }  // namespace
 
+// ----------------------------------------------------------- body forces ----
+// The three BodyForce plugins: read() and write() like the reference's, the
+// force itself computed by the GPU step (rk_body.cuh body_force);
+// getForceAndMoment() gives the same values on the host state.
+namespace {
+void normalize3(double v[3]) {  // toofus vec3::normalize: times the inverse norm
+  double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  if (n > 0.0) {
+    double inv = 1.0 / n;
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+  }
+}
+void qrot3(const double* q, const double* u, double* r) {  // body to global frame: u + s t + v x t, t = 2 v x u
+  const double s = q[0], vx = q[1], vy = q[2], vz = q[3];
+  double t[3] = {2.0 * (vy * u[2] - vz * u[1]), 2.0 * (vz * u[0] - vx * u[2]), 2.0 * (vx * u[1] - vy * u[0])};
+  r[0] = u[0] + s * t[0] + (vy * t[2] - vz * t[1]);
+  r[1] = u[1] + s * t[1] + (vz * t[0] - vx * t[2]);
+  r[2] = u[2] + s * t[2] + (vx * t[1] - vy * t[0]);
+}
+
+struct AttractingPoint : BodyForce {  // BodyForce_AttractingPoint.cpp:43-59
+  double point[3]{0, 0, 0}, acceleration{0.0};
+  void read(std::istream& is) override { is >> point[0] >> point[1] >> point[2] >> acceleration; }
+  void write(std::ostream& os) override {
+    os << "AttractingPoint " << point[0] << " " << point[1] << " " << point[2] << ' ' << acceleration << '\n';
+  }
+  void getForceAndMoment(size_t b, double force[3], double moment[3]) override {
+    (void)moment;
+    const double* p = &box->P.pos[3 * b];
+    double d[3] = {point[0] - p[0], point[1] - p[1], point[2] - p[2]};
+    double l2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (l2 > 0.0) {
+      double inv = 1.0 / std::sqrt(l2);
+      double ma = box->P.mass[b] * acceleration;
+      for (int k = 0; k < 3; k++) force[k] = ma * (d[k] * inv);
+    }
+  }
+  int device_body_force(std::vector<double>& p) const override {
+    p = {point[0], point[1], point[2], acceleration};
+    return RK_BF_ATTRACTING_POINT;
+  }
+};
+
+struct PreferredDirection : BodyForce {  // BodyForce_PreferredDirection.cpp:43-80
+  double raw[7]{0, 0, 0, 0, 0, 0, 0};  // as read: axisBody, axis, momentMax
+  double axisBody[3]{0, 0, 0}, axis[3]{0, 0, 0}, momentMax{0.0}, Kr{0.0};
+  void read(std::istream& is) override {
+    for (double& v : raw) is >> v;
+    for (int k = 0; k < 3; k++) {
+      axisBody[k] = raw[k];
+      axis[k] = raw[3 + k];
+    }
+    momentMax = raw[6];
+    normalize3(axisBody);
+    normalize3(axis);
+    Kr = 2.0 * momentMax / M_PI;
+  }
+  void write(std::ostream& os) override {
+    os << "PreferredDirection " << axisBody[0] << " " << axisBody[1] << " " << axisBody[2] << ' ' << axis[0] << " "
+       << axis[1] << " " << axis[2] << ' ' << momentMax << '\n';
+  }
+  void getForceAndMoment(size_t b, double force[3], double moment[3]) override {
+    (void)force;
+    double a[3];
+    qrot3(&box->P.Q[4 * b], axisBody, a);
+    normalize3(a);
+    double u[3] = {axis[1] * a[2] - axis[2] * a[1], axis[2] * a[0] - axis[0] * a[2], axis[0] * a[1] - axis[1] * a[0]};
+    normalize3(u);
+    double cosa = a[0] * axis[0] + a[1] * axis[1] + a[2] * axis[2];
+    double angle = std::acos(cosa), sgn = -1.0;
+    if (cosa < 0.0) {
+      sgn = 1.0;
+      angle = M_PI - angle;
+    }
+    for (int k = 0; k < 3; k++) moment[k] = ((Kr * sgn) * u[k]) * angle;
+  }
+  int device_body_force(std::vector<double>& p) const override {
+    p.assign(raw, raw + 7);
+    return RK_BF_PREFERRED_DIRECTION;
+  }
+};
+
+struct ViscousFluid : BodyForce {  // BodyForce_ViscousFluid.cpp:42-58
+  double fluidDensity{0.0};
+  void read(std::istream& is) override { is >> fluidDensity; }
+  void write(std::ostream& os) override { os << "ViscousFluid " << fluidDensity << '\n'; }
+  void getForceAndMoment(size_t b, double force[3], double moment[3]) override {
+    (void)moment;
+    const double* v = &box->P.vel[3 * b];
+    double h = box->P.homothety[b];
+    double vol = box->Shapes[box->P.shape[b]].volume * h * h * h;
+    double c = (0.5 * 0.47) * fluidDensity * std::pow(vol, 2.0 / 3.0);
+    for (int k = 0; k < 3; k++) force[k] = c * (v[k] * v[k]);
+  }
+  int device_body_force(std::vector<double>& p) const override {
+    p = {fluidDensity};
+    return RK_BF_VISCOUS_FLUID;
+  }
+};
+}  // namespace
+
 void register_builtin_plugins() {
   static bool done = false;
   if (done) return;
@@ -53,6 +154,10 @@ void register_builtin_plugins() {
   f.add("Default", [] { return new LawDefault(); });
   f.add("Avalanche", [] { return new LawAvalanche(); });
   f.add("StickedLinks", [] { return new LawStickedLinks(); });
+  auto& b = Factory<BodyForce>::instance();
+  b.add("AttractingPoint", [] { return new AttractingPoint(); });
+  b.add("PreferredDirection", [] { return new PreferredDirection(); });
+  b.add("ViscousFluid", [] { return new ViscousFluid(); });
 }
 
 // ------------------------------------------------------------- Rockable ----
@@ -293,7 +398,6 @@ bool Rockable::parse(std::istream& conf) {  // Rockable.cpp:643-1069
       bf->plug(this);
       bf->read(conf);
       bodyForce.reset(bf);
-      return fail("BodyForce plugins are evaluated on the host; the GPU step does not take them yet");
     } else if (tok == "DataExtractor") {  // Rockable.cpp:1003-1022 (kept for compatibility)
       std::string name; conf >> name;
       register_builtin_extractors();
@@ -608,6 +712,19 @@ bool Rockable::upload() {
   if (!ck(rk_upload_entries(ctx_, &en), "rk_upload_entries")) return false;
   if (!controls.empty() || servo.kind)
     if (!ck(rk_set_controls(ctx_, controls.data(), (int32_t)controls.size(), &servo), "rk_set_controls")) return false;
+  if (bodyForce) {
+    std::vector<double> bp;
+    const int kind = bodyForce->device_body_force(bp);
+    if (kind < 0) return fail("this BodyForce plugin has no GPU form");
+    const size_t n = P.size();
+    std::vector<double> vol(n);
+    for (size_t b = 0; b < n; b++) {
+      double h = P.homothety[b];
+      vol[b] = Shapes[P.shape[b]].volume * h * h * h;
+    }
+    if (!ck(rk_set_body_force(ctx_, kind, bp.data(), (int32_t)bp.size(), vol.data()), "rk_set_body_force"))
+      return false;
+  }
   uploaded_ = true;
   return true;
 }
@@ -651,6 +768,10 @@ bool Rockable::saveConf(const std::string& fname) {  // Rockable.cpp:440-610
   for (auto& kv : density)
     if (kv.second > 0.0) h << "density " << kv.first << " " << kv.second << '\n';
   h << "gravity " << gravity[0] << " " << gravity[1] << " " << gravity[2] << '\n';
+  if (bodyForce) {  // Rockable.cpp:470-473
+    h << "BodyForce ";
+    bodyForce->write(h);
+  }
   h << "ParamsInInterfaces " << paramsInInterfaces << "\ndynamicUpdateNL " << dynamicUpdateNL << '\n';
   if (dynamicUpdateNL) h << "dispUpdateNL " << dispUpdateNL << "\nangleUpdateNL " << angleUpdateNL * 180.0 / M_PI << '\n';
   h << "numericalDampingCoeff " << numericalDampingCoeff << "\nVelocityBarrier 0\nAngularVelocityBarrier 0\n"

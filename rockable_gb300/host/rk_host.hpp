@@ -47,6 +47,10 @@ class BodyForce {
   virtual void read(std::istream& is) = 0;
   virtual void write(std::ostream& os) = 0;
   virtual void getForceAndMoment(size_t ibody, double force[3], double moment[3]) = 0;
+  // the GPU step's form of the plugin: an RK_BF_* kind and the conf values
+  // read() took, in that order (rk_set_body_force); -1 for a plugin that has
+  // none (the step then refuses to run rather than evaluating it on the host)
+  virtual int device_body_force(std::vector<double>& params) const { (void)params; return -1; }
 };
 
 // DataExtractor (src/DataExtractors/DataExtractor.hpp:46-73).  exec() and

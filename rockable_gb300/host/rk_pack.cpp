@@ -286,6 +286,7 @@ struct Params {
   double tol;           // contact tolerance: a grain stops within this gap (m)
   uint64_t seed;
   int max_iters;        // largest number of moves of one grain
+  int tries;            // drop sites tried per grain (the lowest rest is kept)
 };
 
 // A contact of the grain being placed: the unit normal pushing it away from
@@ -323,14 +324,14 @@ struct Packer {
   // The grains at rest whose bounding spheres come within `reach` of grain
   // i's (a cell is one grain diameter, so one ring of cells is enough for a
   // reach below a grain radius).
-  void neighbours(int i, double reach, std::vector<int>& out) const {
+  void neighbours(int i, const V& p, double reach, std::vector<int>& out) const {
     out.clear();
-    int x0 = cx(pos[i].x), y0 = cy(pos[i].y), z0 = cz(pos[i].z);
+    int x0 = cx(p.x), y0 = cy(p.y), z0 = cz(p.z);
     for (int z = std::max(z0 - 1, 0); z <= std::min(z0 + 1, gz - 1); ++z)
       for (int y = std::max(y0 - 1, 0); y <= std::min(y0 + 1, gy - 1); ++y)
         for (int x = std::max(x0 - 1, 0); x <= std::min(x0 + 1, gx - 1); ++x)
           for (int j : cells[((size_t)z * gy + y) * gx + x]) {
-            V c = pos[i] - pos[j];
+            V c = p - pos[j];
             double rr = B[i].bound + B[j].bound + reach;
             if (dot(c, c) < rr * rr) out.push_back(j);
           }
@@ -338,8 +339,8 @@ struct Packer {
 
   // Gap between the rounded surfaces of grains i and j (negative when they
   // overlap) and the unit normal pushing i away from j.
-  double gap(int i, int j, V* n) const {
-    V c = pos[i] - pos[j];
+  double gap(int i, const V& p, int j, V* n) const {
+    V c = p - pos[j];
     double d = gjk(&rv[B[i].v0], B[i].nv, &rv[B[j].v0], B[j].nv, c, n);
     if (d < 0.0) {
       double l = std::sqrt(dot(c, c));
@@ -350,19 +351,19 @@ struct Packer {
   }
 
   // Contacts and near supports of grain i: grains, floor and side walls.
-  void supports(int i, const std::vector<int>& nb, std::vector<Contact>& out) const {
+  void supports(int i, const V& p, const std::vector<int>& nb, std::vector<Contact>& out) const {
     out.clear();
     for (int j : nb) {
       V n;
-      double g = gap(i, j, &n);
+      double g = gap(i, p, j, &n);
       out.push_back({n, g});
     }
     const Body& b = B[i];
-    out.push_back({{0, 0, 1}, pos[i].z + b.lo[2] - P.lo[2]});
-    out.push_back({{1, 0, 0}, pos[i].x + b.lo[0] - P.lo[0]});
-    out.push_back({{-1, 0, 0}, P.hi[0] - pos[i].x - b.hi[0]});
-    out.push_back({{0, 1, 0}, pos[i].y + b.lo[1] - P.lo[1]});
-    out.push_back({{0, -1, 0}, P.hi[1] - pos[i].y - b.hi[1]});
+    out.push_back({{0, 0, 1}, p.z + b.lo[2] - P.lo[2]});
+    out.push_back({{1, 0, 0}, p.x + b.lo[0] - P.lo[0]});
+    out.push_back({{-1, 0, 0}, P.hi[0] - p.x - b.hi[0]});
+    out.push_back({{0, 1, 0}, p.y + b.lo[1] - P.lo[1]});
+    out.push_back({{0, -1, 0}, P.hi[1] - p.y - b.hi[1]});
   }
 
   // The steepest descent direction of a grain that cannot move into its
@@ -404,15 +405,15 @@ struct Packer {
     return best;
   }
 
-  // Place grain i: fall and slide from its start until no descent is left.
-  bool settle(int i, long* moves) {
+  // Place grain i at p: fall and slide from there until no descent is left.
+  bool settle(int i, V& p, long* moves) const {
     std::vector<int> nb;
     std::vector<Contact> cs_;
     const double touch = 2.0 * P.tol;
     for (int it = 0; it < P.max_iters; ++it) {
       ++*moves;
-      neighbours(i, bmax, nb);
-      supports(i, nb, cs_);
+      neighbours(i, p, bmax, nb);
+      supports(i, p, nb, cs_);
       V u = descent(cs_, touch);
       if (dot(u, u) == 0.0) return true;
       // how far along u before any support can be touched: gap over the
@@ -425,7 +426,7 @@ struct Packer {
         else if (rate > 1e-12) step = 0.0;
       }
       if (step <= 0.25 * P.tol) return true;
-      pos[i] = pos[i] + step * u;
+      p = p + step * u;
     }
     return false;
   }
@@ -440,17 +441,34 @@ struct Packer {
     cells.assign((size_t)gx * gy * gz, {});
     std::vector<double> col_top((size_t)gx * gy, P.lo[2]);
     long moves = 0, at_rest = 0;
+    const int K = std::max(1, P.tries);
+    std::vector<V> cand(K);
+    std::vector<long> cmoves(K);
+    std::vector<char> crest(K);
     for (int i = 0; i < n; ++i) {
-      // a uniform random point of the footprint where the grain fits, just
-      // above the grains already under it
-      double x = P.lo[0] - B[i].lo[0] + rng.uniform() * ((P.hi[0] - B[i].hi[0]) - (P.lo[0] - B[i].lo[0]));
-      double y = P.lo[1] - B[i].lo[1] + rng.uniform() * ((P.hi[1] - B[i].hi[1]) - (P.lo[1] - B[i].lo[1]));
-      int x0 = cx(x), y0 = cy(y);
-      double top = P.lo[2];
-      for (int yy = std::max(y0 - 1, 0); yy <= std::min(y0 + 1, gy - 1); ++yy)
-        for (int xx = std::max(x0 - 1, 0); xx <= std::min(x0 + 1, gx - 1); ++xx) top = std::max(top, col_top[yy * gx + xx]);
-      pos[i] = {x, y, top - B[i].lo[2] + P.tol};
-      at_rest += settle(i, &moves);
+      // K uniform random points of the footprint where the grain fits, each
+      // just above the grains already under it; the grain is dropped from
+      // each and kept where it comes to rest lowest (the first such on ties)
+      for (int k = 0; k < K; ++k) {
+        double x = P.lo[0] - B[i].lo[0] + rng.uniform() * ((P.hi[0] - B[i].hi[0]) - (P.lo[0] - B[i].lo[0]));
+        double y = P.lo[1] - B[i].lo[1] + rng.uniform() * ((P.hi[1] - B[i].hi[1]) - (P.lo[1] - B[i].lo[1]));
+        int x0 = cx(x), y0 = cy(y);
+        double top = P.lo[2];
+        for (int yy = std::max(y0 - 1, 0); yy <= std::min(y0 + 1, gy - 1); ++yy)
+          for (int xx = std::max(x0 - 1, 0); xx <= std::min(x0 + 1, gx - 1); ++xx)
+            top = std::max(top, col_top[yy * gx + xx]);
+        cand[k] = {x, y, top - B[i].lo[2] + P.tol};
+        cmoves[k] = 0;
+      }
+#pragma omp parallel for schedule(dynamic, 1) if (K > 1)
+      for (int k = 0; k < K; ++k) crest[k] = settle(i, cand[k], &cmoves[k]);
+      int best = 0;
+      for (int k = 0; k < K; ++k) {
+        moves += cmoves[k];
+        if (k > 0 && cand[k].z < cand[best].z) best = k;
+      }
+      pos[i] = cand[best];
+      at_rest += crest[best];
       insert(i);
       int c = cy(pos[i].y) * gx + cx(pos[i].x);
       col_top[c] = std::max(col_top[c], pos[i].z + B[i].hi[2]);
@@ -468,11 +486,11 @@ struct Packer {
     for (int i = 0; i < n; ++i) {
       if (pos[i].z + B[i].lo[2] - P.lo[2] < 1e-6) floor_touch++;
       std::vector<int> nb;
-      neighbours(i, 1e-6, nb);
+      neighbours(i, pos[i], 1e-6, nb);
       for (int j : nb) {
         if (j <= i) continue;
         V nn;
-        double g = gap(i, j, &nn);
+        double g = gap(i, pos[i], j, &nn);
         if (g < 1e-6) touching++;
         worst = std::max(worst, -g);
       }
@@ -490,16 +508,16 @@ struct Packer {
 
 bool read_all(FILE* f, void* p, size_t bytes) { return fread(p, 1, bytes, f) == bytes; }
 
-// Input layout: int64 magic 0x524b5041434b3032 ("RKPACK02"), int64 nshapes,
+// Input layout: int64 magic 0x524b5041434b3033 ("RKPACK03"), int64 nshapes,
 // int32 nv[nshapes], double radius[nshapes], double vertices[3*sum(nv)],
 // int64 nbodies, int32 shape[n], double scale[n], double Q[4n] (w, x, y, z),
 // double volume[n], double params[8]: lo xyz, hi xyz, tol, seed;
-// int64 max_iters.
+// int64 max_iters, int64 tries.
 int read_input(const char* path, Packer& pk) {
   FILE* f = fopen(path, "rb");
   if (!f) return -1;
   int64_t magic = 0, ns = 0, n = 0;
-  bool ok = read_all(f, &magic, 8) && magic == 0x524b5041434b3032LL && read_all(f, &ns, 8) && ns > 0;
+  bool ok = read_all(f, &magic, 8) && magic == 0x524b5041434b3033LL && read_all(f, &ns, 8) && ns > 0;
   std::vector<int32_t> nv(ok ? ns : 0);
   std::vector<double> rad(ok ? ns : 0);
   ok = ok && read_all(f, nv.data(), 4 * ns) && read_all(f, rad.data(), 8 * ns);
@@ -510,9 +528,10 @@ int read_input(const char* path, Packer& pk) {
   std::vector<int32_t> shape(ok ? n : 0);
   std::vector<double> scale(ok ? n : 0), Q(ok ? 4 * n : 0), vol(ok ? n : 0);
   double prm[8];
-  int64_t iters = 0;
+  int64_t iters = 0, tries = 0;
   ok = ok && read_all(f, shape.data(), 4 * n) && read_all(f, scale.data(), 8 * n) && read_all(f, Q.data(), 32 * n) &&
-       read_all(f, vol.data(), 8 * n) && read_all(f, prm, sizeof prm) && read_all(f, &iters, 8);
+       read_all(f, vol.data(), 8 * n) && read_all(f, prm, sizeof prm) && read_all(f, &iters, 8) &&
+       read_all(f, &tries, 8);
   fclose(f);
   if (!ok) return -2;
   Params& P = pk.P;
@@ -523,6 +542,7 @@ int read_input(const char* path, Packer& pk) {
   P.tol = prm[6];
   P.seed = (uint64_t)prm[7];
   P.max_iters = (int)iters;
+  P.tries = (int)tries;
   pk.B.resize(n);
   pk.pos.assign(n, V{0, 0, 0});
   int64_t tot = 0;

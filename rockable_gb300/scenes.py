@@ -235,7 +235,7 @@ def deposit(rng, radii, half_x, half_y, z0, gap=1e-5):
     return pos
 
 
-PACK_MAGIC = 0x524b5041434b3032  # "RKPACK02"
+PACK_MAGIC = 0x524b5041434b3033  # "RKPACK03"
 
 
 def _cache_dir():
@@ -245,14 +245,16 @@ def _cache_dir():
     return d
 
 
-def pack(shapes, shape_of, Q, volume, lo, hi, scale=None, tol=1e-9, seed=SEED, max_iters=200, cache=True):
+def pack(shapes, shape_of, Q, volume, lo, hi, scale=None, tol=1e-9, seed=SEED, max_iters=200, tries=1, cache=True):
     """Loose random packing by sequential ballistic deposition with the exact
     grain geometry (the CPU packer host/rk_pack.cpp): the grains, with the
     given shapes (indices into `shapes`), uniform scale factors and
     orientations, one at a time from a seeded random point of the footprint
     [lo, hi] (x, y, side walls there), fall onto the floor lo z or the grains
     already there and slide without friction (translating only) until three
-    supports hold them, within `tol`; they never overlap.  Returns
+    supports hold them, within `tol`; they never overlap.  With tries > 1,
+    each grain is dropped from that many random points and kept where it
+    comes to rest lowest (denser packings).  Returns
     (positions (n, 3), stats).  The result is cached by the hash of its input
     (RK_SCENE_CACHE or the temp directory), so that the processes of one
     benchmark run pack once."""
@@ -268,7 +270,7 @@ def pack(shapes, shape_of, Q, volume, lo, hi, scale=None, tol=1e-9, seed=SEED, m
     parts = [np.array([PACK_MAGIC, len(shapes)], np.int64).tobytes(), nv.tobytes(), rad.tobytes(), verts.tobytes(),
              np.array([n], np.int64).tobytes(), np.asarray(shape_of, np.int32).tobytes(), scale.tobytes(),
              np.ascontiguousarray(Q, np.float64).tobytes(), np.asarray(volume, np.float64).tobytes(), prm.tobytes(),
-             np.array([max_iters], np.int64).tobytes()]
+             np.array([max_iters, tries], np.int64).tobytes()]
     blob = b"".join(parts)
     from . import build_ext
     exe = build_ext.build_packer()
@@ -294,16 +296,31 @@ def pack(shapes, shape_of, Q, volume, lo, hi, scale=None, tol=1e-9, seed=SEED, m
                                        "max_overlap": float(s[6])}
 
 
+def packing_stats(pos, vol, lo, hi, inset, st):
+    """Bulk solid fraction (grain volume with centres inside the packing's
+    box shrunk by `inset` on every side, over that box's volume: away from
+    the floor, the side walls and the rough top) and mean coordination
+    (2 x touching pairs / grains, the floor counted) of a packing."""
+    lo = np.asarray(lo, np.float64) + inset
+    hi = np.asarray(hi, np.float64) - inset
+    inside = np.all((pos >= lo) & (pos <= hi), axis=1)
+    st["solid_fraction_bulk"] = float(vol[inside].sum() / np.prod(hi - lo)) if np.all(hi > lo) else 0.0
+    st["coordination"] = 2.0 * st["touching_pairs"] / len(pos)
+    return st
+
+
 def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2700.0, kn=1e6, kt=1e6,
-                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), walls=False, semi=(0.005, 0.015)):
+                    en2=0.25, mu=0.4, dt=1e-6, column=(0.5, 0.5, 1.5), walls=False, semi=(0.005, 0.015), tries=16):
     """Granular column collapse: n hull grains (semi-axes U[0.5, 1.5] cm,
-    rounding 5 % of the smallest), each resting on a face, in a loose random
-    packing (sequential deposition with frictionless sliding, pack()) that
-    fills a 0.5 x 0.5 m column on a rigid floor plate (body 0) to about
-    1.2 m.  With walls, four vertical plates (bodies 1-4, listed in "walls")
-    confine the column as it was packed, to be removed (drop_bodies) when the
-    collapse starts; without, the walls are already released (t = 0 of the
-    collapse)."""
+    rounding 5 % of the smallest), each resting on a face, in a random
+    packing (sequential deposition with frictionless sliding, each grain
+    kept at the lowest of `tries` drop sites, pack()) that fills a
+    0.5 x 0.5 m column on a rigid floor plate (body 0) to about 1.1 m; the
+    grains touch (within 1e-9 m) but carry no load yet.  With walls, four
+    vertical plates (bodies 1-4, listed in
+    "walls") confine the column as it was packed, to be removed
+    (drop_bodies) when the collapse starts; without, the walls are already
+    released (t = 0 of the collapse)."""
     rng = np.random.default_rng(seed)
     shapes = [plate_shape("FLOOR", 1.5, 0.005)]
     shapes += [hull_shape(rng, "G%05d" % k, semi_lo=semi[0], semi_hi=semi[1]) for k in range(nshapes)]
@@ -311,8 +328,10 @@ def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2
     Q = stable_face_quaternions(rng, shapes, shape_of)
     vol = np.array([shapes[k]["volume"] for k in shape_of])
     hx, hy = 0.5 * column[0], 0.5 * column[1]
-    pos, st = pack(shapes, shape_of, Q, vol, (-hx, -hy, 0.005), (hx, hy, column[2]), seed=seed)
+    z0 = 0.005
+    pos, st = pack(shapes, shape_of, Q, vol, (-hx, -hy, z0), (hx, hy, column[2]), seed=seed, tries=tries)
     bmax = max(float(shapes[k]["bound"]) for k in np.unique(shape_of))
+    packing_stats(pos, vol, (-hx, -hy, z0), (hx, hy, st["top"]), 2.0 * bmax, st)
     wall_pos, wall_Q, wall_shape = [np.zeros(3)], [np.array([1.0, 0, 0, 0])], [0]
     if walls:
         rw = 0.005
@@ -337,14 +356,16 @@ def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2
 
 
 def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=2700.0, kn=1e6, kt=1e6, en2=0.25,
-                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=1e5, size=(0.005, 0.015)):
+                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=1e5, size=(0.005, 0.015), tries=16):
     """Dense isotropic compression: n hull grains (8-20 vertices, diameters
     uniform in `size`, ratio 1:3, by homothety of a library of shapes of
-    about 1 cm), packed loosely (pack()) in a cubic box, then enclosed by six
-    rigid walls (bodies 0-5: Xmin, Xmax, Ymin, Ymax, Zmin, Zmax) driven by
-    Rockable's tritriIsostaticCompression servo at `pressure` (DrivingSystem.
-    cpp:242-268: the min walls are held, the max walls pushed with pressure x
-    their face area); no gravity."""
+    about 1 cm), packed (pack(), the lowest of `tries` drop sites per grain)
+    in a box about as high as wide, then enclosed by six rigid walls (bodies
+    0-5: Xmin, Xmax, Ymin, Ymax, Zmin, Zmax) driven by Rockable's
+    tritriIsostaticCompression servo at `pressure` (DrivingSystem.cpp:
+    242-268: the min walls are held, the max walls pushed with pressure x
+    their face area); no gravity.  The grains touch but carry no load: the
+    servo loads them."""
     rng = np.random.default_rng(seed)
     lib = [hull_shape(rng, "G%05d" % k, semi_lo=0.004, semi_hi=0.006) for k in range(nshapes)]
     shape_of = rng.integers(0, nshapes, n)
@@ -352,20 +373,24 @@ def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=27
     h = rng.uniform(size[0], size[1], n) / lib_d[shape_of]
     Q = stable_face_quaternions(rng, lib, shape_of)
     vol = np.array([lib[k]["volume"] for k in shape_of]) * h ** 3
-    L = float((vol.sum() / 0.36) ** (1.0 / 3.0))  # a cube at a loose solid fraction
+    L = float((vol.sum() / 0.5) ** (1.0 / 3.0))  # about a cube at the packing's solid fraction
     pos, st = pack(lib, shape_of, Q, vol, (-0.5 * L, -0.5 * L, 0.0), (0.5 * L, 0.5 * L, 4.0 * L), scale=h,
-                   seed=seed)
+                   seed=seed, tries=tries)
     top = st["top"]
+    bmax = float(np.max(lib_d[shape_of] * h)) * 0.5
+    packing_stats(pos, vol, (-0.5 * L, -0.5 * L, 0.0), (0.5 * L, 0.5 * L, top), 2.0 * bmax, st)
+    # the box's faces (x, y, z): lo, hi
+    faces = np.array([[-0.5 * L, 0.5 * L], [-0.5 * L, 0.5 * L], [0.0, top]])
+    centre = faces.mean(axis=1)
     rw = 0.005
     half = 0.5 * max(L, top) + 0.02
     shapes = [plate_shape("WALL", half, rw)] + lib
     s2 = math.sqrt(0.5)
-    zc = 0.5 * top
-    wall_pos = [np.array([-0.5 * L - rw, 0, zc]), np.array([0.5 * L + rw, 0, zc]),
-                np.array([0, -0.5 * L - rw, zc]), np.array([0, 0.5 * L + rw, zc]),
-                np.array([0, 0, -rw]), np.array([0, 0, top + rw])]
+    zc = centre[2]
+    wall_pos = [np.array([faces[0, 0] - rw, 0, zc]), np.array([faces[0, 1] + rw, 0, zc]),
+                np.array([0, faces[1, 0] - rw, zc]), np.array([0, faces[1, 1] + rw, zc]),
+                np.array([0, 0, faces[2, 0] - rw]), np.array([0, 0, faces[2, 1] + rw])]
     wall_Q = [np.array([s2, 0, s2, 0])] * 2 + [np.array([s2, s2, 0, 0])] * 2 + [np.array([1.0, 0, 0, 0])] * 2
-    bmax = float(np.max(lib_d[shape_of] * h)) * 0.5
     out = _assemble(shapes, wall_pos, wall_Q, pos, Q, shape_of + 1, density, law, kn, kt, en2, mu, dt,
                     gravity=(0.0, 0.0, 0.0), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax, interVerlet=100 * dt,
                     name="iso_compression_%d" % n, wall_shape=0, homothety=h, wall_density=wall_density)
@@ -639,6 +664,47 @@ def set_scene_params(g, scene, t=0.0, numerical_damping=0.0):
     c = scene.get("controls")
     if c is not None:
         g.set_controls(c["type"], c["body"], c["value"], c["vec"], scene.get("servo"))
+
+
+def loaded(scene, steps, device=0, chunk=1000, report=None):
+    """The scene after `steps` DEM steps with its own parameters and laws in
+    the FP64 form (the reference arithmetic), walls and servo in place:
+    packed grains that touch but carry no load get loaded by gravity or by
+    the servo.  Then the walls listed in scene["walls"] are removed (the
+    start of a collapse).  Returns the new scene with the neighbour list and
+    its contact history ("entries") and a "load" record (steps, simulated
+    time, entries and active contacts per free body at the end)."""
+    from .abi import GpuScene
+    g = GpuScene(device=device)
+    g.upload_shapes(scene["shape_tables"])
+    g.upload_bodies(scene["bodies"], scene["n_driven"])
+    if scene.get("scene_of") is not None:
+        g.set_scenes(scene["scene_of"])
+    set_scene_params(g, scene)
+    if scene.get("entries") is not None:
+        g.upload_entries(scene["entries"])
+    else:
+        g.update_nl()
+    g.set_graphs(True)
+    done = 0
+    nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
+    while done < steps:
+        k = min(chunk, steps - done)
+        g.step(k)
+        done += k
+        if report is not None:
+            st = g.stats()
+            report.append((done, st["n_active"] / max(1, nfree), st["e_trans"]))
+    st = g.stats()
+    out = scene_from_gpu(scene, g)
+    g.close()
+    rec = {"steps": int(steps), "t": steps * scene["dt"], "active_per_free": st["n_active"] / max(1, nfree),
+           "entries": int(st["n_entries"])}
+    if scene.get("walls"):
+        out = drop_bodies(out, scene["walls"])
+        rec["released_walls"] = [int(w) for w in scene["walls"]]
+    out["load"] = rec
+    return out
 
 
 def scene_from_gpu(scene, g):

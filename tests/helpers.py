@@ -25,6 +25,9 @@ def gpu_from_oracle(o, device=0, form=RK_FORM_FP64):
         servo = {"kind": c["servo"][0], "icontr": c["servo"][1], "walls": c["servo"][2:8],
                  "pressure": c["pressure"]}
         g.set_controls(c["type"], c["body"], c["value"], c["vec"], servo)
+    kind, prm, vol = o.body_force()
+    if kind:
+        g.set_body_force(kind, prm, vol)
     return g
 
 

@@ -282,20 +282,21 @@ def test_mixed_per_result_relative_errors_settled_column(gpu_lib):
 
 def test_headline_contact_set_equals_fp64_rebuild_every_step(gpu_lib):
     """The headline form (mixed precision, learned skin with exact contact
-    detection) on a settled, contact-rich column for 1000 steps: at every
-    10th step its active sub-contact set equals the one the FP64 form finds
-    at the same positions from a neighbour list rebuilt from scratch (a
-    fresh context: rk_update_nl, then the load-time force evaluation)."""
+    detection) on a contact-rich column for 1000 steps: the dense pile,
+    loaded by gravity between walls for 6000 steps and released, collapses;
+    at every 10th step the headline form's active sub-contact set equals the
+    one the FP64 form finds at the same positions from a neighbour list
+    rebuilt from scratch (a fresh context: rk_update_nl, then the load-time
+    force evaluation)."""
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075), column=(0.15, 0.15, 1.5))
-    gs = scenes.settle(scene, steps=1500)
-    src = scenes.scene_from_gpu(scene, gs)
-    gs.close()
+    scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075), column=(0.15, 0.15, 1.5), walls=True)
+    src = scenes.loaded(scene, 6000)
     h = GpuScene(form=RK_FORM_MIXED)
     h.upload_shapes(src["shape_tables"])
     h.upload_bodies(src["bodies"], src["n_driven"])
     scenes.set_scene_params(h, src)
+    h.upload_entries(src["entries"])
     d = src["dVerlet"]
     h.set_skin(use_mlp=True, skin_min=0.1 * d, skin_max=4.0 * d, interval_min=2, interval_max=300, seed=7,
                exact_contacts=True)
@@ -327,7 +328,7 @@ def test_headline_contact_set_equals_fp64_rebuild_every_step(gpu_lib):
         active.append(len(fa))
         if ha != fa:
             mismatched.append((step, len(ha - fa), len(fa - ha)))
-    print("checked %d steps, active contacts %d..%d, mismatches %s, skin %s" % (
-        checked, min(active), max(active), mismatched[:10], h.skin_stats()))
-    assert checked == 100 and min(active) > 500
+    print("checked %d steps, load %s, active contacts %d..%d, mismatches %s, skin %s" % (
+        checked, src["load"], min(active), max(active), mismatched[:10], h.skin_stats()))
+    assert checked == 100 and np.mean(active) >= 2000  # at least one active sub-contact per grain
     assert not mismatched

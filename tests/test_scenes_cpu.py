@@ -45,8 +45,9 @@ def test_packing_is_dense_at_rest_without_overlap_and_seeded():
     sc = scenes.column_collapse(n=1500, nshapes=64, column=(0.2, 0.2, 1.5))
     st = sc["pack"]
     assert st["at_rest"] == 1500 and st["max_overlap"] <= 0.0
-    assert 2 * st["touching_pairs"] / 1500 >= 3.0  # coordination of the pile
-    assert st["solid_fraction"] > 0.2
+    # lowest of 16 drop sites per grain: a dense pile where grains touch
+    assert st["coordination"] >= 4.5 and st["coordination"] == 2 * st["touching_pairs"] / 1500
+    assert st["solid_fraction_bulk"] >= 0.48
     oracle.build()
     o = oracle.Oracle(scenes.write_conf(sc, tempfile.mkdtemp(prefix="rk_pack_")))
     o.update_nl()
@@ -55,7 +56,7 @@ def test_packing_is_dense_at_rest_without_overlap_and_seeded():
     assert len(e["dn"]) > 10 * 1500 and e["dn"].min() >= -2e-9
     b = sc["bodies"]
     pos, st2 = scenes.pack(sc["shapes"], b["shape"][1:], b["Q"][1:], b["mass"][1:] / 2700.0, (-0.1, -0.1, 0.005),
-                           (0.1, 0.1, 1.5), cache=False)
+                           (0.1, 0.1, 1.5), tries=16, cache=False)
     assert np.array_equal(pos, b["pos"][1:])
     assert all(st2[k] == st[k] for k in ["touching_pairs", "on_floor", "moves", "at_rest"])
 
