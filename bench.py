@@ -6,13 +6,14 @@ random packing (bulk solid fraction ~0.52, coordination ~5) that fills a
 0.5 x 0.5 m column about 1.1 m high on a rigid floor.  The packing is built
 on the CPU by the seeded packer (rockable_gb300/host/rk_pack.cpp, through
 scenes.column_collapse); its grains touch but carry no load.  Before any
-timing the pile is loaded by gravity between four walls with the scene's own
-parameters in the FP64 form (`--load-steps` DEM steps, scenes.loaded), then
-the walls are removed: every form starts from that loaded column at release,
-contact history included.  The reference arm (`--impl reference`), which
-must not load the GPU library, times the same packing at t = 0 before
-loading; the `cpu_baseline` leg times the same CPU path on the loaded state,
-so the two CPU rates can be compared.
+timing the pile settles by gravity between four walls with the scene's laws,
+stiffnesses and time step (`--load-steps` DEM steps with numerical damping,
+scenes.loaded), then the walls are removed: every form
+starts from that settled, contact-rich column at release, contact history
+included.  The reference arm (`--impl reference`), which
+must not load the GPU library, times the CPU path on the packing at t = 0;
+the `cpu_baseline` leg times it on the same state, and
+config.cpu_on_settled_state on the settled one the GPU forms run on.
 
 One bench step is one segment of `--segment` DEM steps (100: the fixed
 schedule's interVerlet), each DEM step one pass of the velocity-Verlet step
@@ -37,6 +38,9 @@ Legs of one run (rank 0 prints one JSON line):
   iso         : the 200k-grain isotropic compression (six servo walls at
                 100 kPa), plain FP64 and the headline form, with its own CPU
                 sample (the >= 50x target);
+  rockfall    : the breakable bonded rockfall (40 blocks x 500 grains,
+                Weibull vertex bonds made by the C++ host at load, 30 degree
+                slope, 10 m/s), plain FP64 and mixed, with their broken sets;
   batched     : many independent slope scenes in one context.
 `--impl reference` times the CPU path alone on the column workload and never
 loads the GPU library.
@@ -68,10 +72,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--segment", type=int, default=100, help="DEM steps per bench step")
     ap.add_argument("--n", type=int, default=50000, help="grains of the column")
-    ap.add_argument("--load-steps", type=int, default=20000,
-                    help="DEM steps that load the column by gravity between walls before the release")
-    ap.add_argument("--iso-load-steps", type=int, default=10000,
-                    help="DEM steps of servo compression before the compression box is timed")
+    ap.add_argument("--load-steps", type=int, default=40000,
+                    help="damped DEM steps that settle the column between walls before the release")
+    ap.add_argument("--iso-load-steps", type=int, default=25000,
+                    help="damped DEM steps of servo compression before the compression box is timed")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--iso-n", type=int, default=200000, help="grains of the compression box (0: skip)")
@@ -79,6 +83,8 @@ def parse():
     ap.add_argument("--ref-seconds", type=float, default=150.0, help="budget of the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--rock-clusters", type=int, default=40,
+                    help="500-grain bonded blocks of the rockfall workload (0: skip)")
     ap.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched slope workload (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-settle", type=int, default=3000)
@@ -460,6 +466,63 @@ def e2e_leg(g, scene, a, dist, ws, steps):
                     "pinned packed buffer, rk_step(%d), the same fields D2H back" % a.segment}
 
 
+def rockfall_workload(a, dev):
+    """The breakable bonded rockfall (scenes.rockfall_bonded: 40 blocks of
+    500 grains, vertex bonds with Weibull strengths, 30 degree slope,
+    10 m/s), loaded through the C++ host from its conf file: the host makes
+    the bonds at load (stickVerticesInClusters, setVariableStickParams) and
+    drives the engine context that is timed here.  Plain FP64 and mixed
+    forms from the same conf; after the timed steps, the broken interfaces
+    of the two forms are compared."""
+    from rockable_gb300 import scenes
+    from rockable_gb300.abi import HostScene, RK_FORM_MIXED
+    t0 = time.perf_counter()
+    sc = scenes.rockfall_bonded(nclusters=a.rock_clusters)
+    t_gen = time.perf_counter() - t0
+    conf = scenes.write_conf(sc, tempfile.mkdtemp(prefix="rk_rock_"))
+    nfree = len(sc["bodies"]["mass"]) - sc["n_driven"]
+    steps = max(2, a.steps // 4)
+    forms, broken, t_open = {}, {}, {}
+    for label in ["plain_fp64", "mixed"]:
+        t0 = time.perf_counter()
+        hs = HostScene(conf)
+        t_open[label] = time.perf_counter() - t0
+        g = hs.gpu
+        if label == "mixed":
+            g.set_form(RK_FORM_MIXED)
+        g.update_nl()
+        _, _, b0 = g.interfaces()
+        g.set_graphs(True)
+        g.autotune(2)
+        g.step(TUNE_STEPS)
+        g.synchronize()
+        clocks = Clocks()
+        clocks.start()
+        rep = g.step(steps * a.segment)
+        ms, launches = g.last_step_timing()
+        ck = clocks.stop()
+        st = g.stats()
+        _, _, bf = g.interfaces()
+        broken[label] = bf.copy()
+        e = g.entries()
+        forms[label] = {"value": nfree * steps * a.segment / (ms / 1e3), "ms": ms,
+                        "ms_per_dem_step": ms / (steps * a.segment), "gpu_launches": int(launches),
+                        "nl_rebuilds_in_timed": int(rep["nl_updates"]), "entries": int(st["n_entries"]),
+                        "active": int(st["n_active"]), "interfaces": int(len(bf)),
+                        "interfaces_broken_at_start": int(b0.sum()), "interfaces_broken": int(bf.sum()),
+                        "bonds_intact": int(np.sum(e["bond"] >= 0)), "clocks": ck}
+        hs.close()
+    same = bool(np.array_equal(broken["plain_fp64"], broken["mixed"]))
+    return {"workload": sc["name"], "bodies": len(sc["bodies"]["mass"]), "free_bodies": nfree, "law": sc["law"],
+            "clusters": sc["pack"]["clusters"], "per_cluster": sc["pack"]["per_cluster"],
+            "bond_eps": sc["bond_eps"], "slope_deg": 30.0, "v0": 10.0, "dem_steps_per_step": a.segment,
+            "steps": steps, "tune_steps": TUNE_STEPS, "forms": forms,
+            "mixed_vs_plain": forms["mixed"]["value"] / forms["plain_fp64"]["value"],
+            "broken_sets_equal_at_end": same,
+            "broken_set_difference": int(np.sum(broken["plain_fp64"] != broken["mixed"])),
+            "setup_s": {"generate": t_gen, "host_open": t_open}}
+
+
 def batched_workload(a, dev):
     """Many independent slope scenes (N ~ U{200..5000} grains each, slopes
     25-45 degrees, Default law) in ONE engine context: every launch covers all
@@ -556,7 +619,8 @@ def iso_workload(a, dev, dist, ws, order):
     out = {"workload": sc["name"], "bodies": len(sc["bodies"]["mass"]), "free_bodies": nfree,
            "law": sc["law"], "servo": "tritriIsostaticCompression at %g Pa, no gravity" % sc["servo"]["pressure"],
            "pack": sc["pack"], "load": sc["load"],
-           "state": "the packed box after %d DEM steps of servo compression (FP64 form)" % a.iso_load_steps,
+           "state": ("the packed box after %d DEM steps of servo compression with numerical damping 0.5 "
+                     "(scenes.loaded)" % a.iso_load_steps),
            "dem_steps_per_step": a.segment, "steps": steps, "warmup": 1,
            "forms": forms, "headline_form": order[-1],
            "headline_vs_plain": head["value"] / forms["plain_fp64"]["value"],
@@ -609,9 +673,16 @@ def main():
     e2e = None if a.no_e2e else e2e_leg(g, scene, a, dist, ws, a.steps)
     g.close()
     iso = iso_workload(a, dev, dist, ws, order) if (a.iso_n > 0 and rank == 0) else None
+    rockfall = rockfall_workload(a, dev) if (rank == 0 and a.rock_clusters > 0) else None
     batched = batched_workload(a, dev) if (rank == 0 and a.batch_scenes > 0) else None
-    cpu = cpu_baseline(scene, a.segment, a.cpu_seconds, "the loaded column at release") if (
-        rank == 0 and not a.no_cpu) else None
+    cpu = cpu_settled = None
+    if rank == 0 and not a.no_cpu:
+        # the reference arm's state (the packed column at t = 0, no walls),
+        # and the settled state the GPU forms are timed on
+        cpu = cpu_baseline(scenes.drop_bodies(packed, packed["walls"]), a.segment, a.cpu_seconds,
+                           "the packed column at t = 0 (the reference arm's state)")
+        cpu_settled = cpu_baseline(scene, a.segment, a.cpu_seconds, "the settled column at release (the GPU "
+                                   "forms' state)")
     if rank == 0:
         out = {"metric": METRIC, "value": head["value"], "unit": "particle-steps/s", "n_gpus": ws, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -626,16 +697,18 @@ def main():
                           "active_per_free": head["active_per_free"],
                           "nl_rebuilds_in_timed": head["nl_rebuilds_in_timed"], "dt": scene["dt"],
                           "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
-                          "pack": scene["pack"], "load": scene["load"],
-                          "state": ("the packed column loaded by gravity between four walls (%d DEM steps, FP64 "
-                                    "form), walls removed, then %d tuning and %d warm-up DEM steps of each form "
-                                    "before its timed ones" % (a.load_steps, TUNE_STEPS, a.warmup * a.segment)),
+                          "pack": scene["pack"], "load": scene["load"], "cpu_on_settled_state": cpu_settled,
+                          "state": ("the packed column settled by gravity between four walls (%d DEM steps with "
+                                    "numerical damping 0.5, scenes.loaded), walls removed, then %d tuning and %d "
+                                    "warm-up DEM steps of each form before its timed ones" % (
+                                        a.load_steps, TUNE_STEPS, a.warmup * a.segment)),
                           "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if head["entries"] * 240 + N * 600 >
                           129e6 else "working set below L2 size (no flush between steps: consecutive DEM steps reuse it)",
                           "parallelism": "replicas" if ws > 1 else "single GPU",
                           "setup_s": {"generate": t_gen, "load": t_load}},
                "gpu_launches": head["gpu_launches"], "wall_s": head["wall_s"], "clocks": head["clocks"],
-               "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "iso": iso, "batched": batched}
+               "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "iso": iso, "rockfall": rockfall,
+               "batched": batched}
         print(json.dumps(out), flush=True)
     if dist:
         dist.barrier()

@@ -175,15 +175,28 @@ class GpuScene:
     def __init__(self, device=0, form=RK_FORM_FP64, entry_capacity=0):
         self.L = load()
         self.h = P()
+        self._owned = True
         cfg = RkConfig(device, form, entry_capacity)
         rc = self.L.rk_create(C.byref(self.h), C.byref(cfg))
         if rc != RK_OK:
             raise RkError("rk_create failed: %s" % ERRORS.get(rc, rc))
         self._keep = []
 
+    @classmethod
+    def attach(cls, handle, owner):
+        """A view of a context created elsewhere (the C++ host's), kept alive
+        by `owner`; close() leaves the context to its owner."""
+        g = cls.__new__(cls)
+        g.L = load()
+        g.h = P(handle)
+        g._owned = False
+        g._keep = [owner]
+        return g
+
     def close(self):
         if self.h:
-            self.L.rk_destroy(self.h)
+            if self._owned:
+                self.L.rk_destroy(self.h)
             self.h = P()
 
     def __del__(self):
@@ -435,3 +448,59 @@ class GpuScene:
         s = RkStats()
         self._chk(self.L.rk_get_stats(self.h, C.byref(s)), "rk_get_stats")
         return {k: getattr(s, k) for k, _ in RkStats._fields_}
+
+
+# ------------------------------------------------------------ C++ host --
+HOSTPATH = os.path.join(os.path.dirname(LIBPATH), "librk_host.so")
+_host = None
+
+
+def load_host(path=HOSTPATH):
+    """Load librk_host.so, the C++ host (conf in, conf out) over librk_gpu."""
+    global _host
+    if _host is None:
+        if not os.path.exists(path):
+            raise RuntimeError("librk_host.so is not built (run __graft_entry__.build()): " + path)
+        load()
+        L = C.CDLL(path)
+        sig = {"rkh_open": (P, [C.c_char_p]), "rkh_error": (C.c_char_p, []), "rkh_close": (None, [P]),
+               "rkh_read_driving": (C.c_int, [P, C.c_char_p]), "rkh_run": (C.c_int, [P, C.c_long]),
+               "rkh_save_conf": (C.c_int, [P, C.c_char_p]), "rkh_context": (P, [P])}
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _host = L
+    return _host
+
+
+class HostScene:
+    """A conf file loaded by the C++ host (conf and shape parsing, the
+    preprocessing commands such as stickVerticesInClusters, the plugins),
+    which uploads it to an engine context; `gpu` is a GpuScene view of that
+    context for direct rk_* calls (rk_step, rk_set_form, downloads)."""
+
+    def __init__(self, conf, driving=None):
+        self.H = load_host()
+        self.h = self.H.rkh_open(conf.encode())
+        if not self.h:
+            raise RkError("rkh_open: " + self.H.rkh_error().decode())
+        if driving and self.H.rkh_read_driving(self.h, driving.encode()) != 0:
+            raise RkError("rkh_read_driving: " + self.H.rkh_error().decode())
+        self.gpu = GpuScene.attach(self.H.rkh_context(self.h), self)
+
+    def save_conf(self, path):
+        if self.H.rkh_save_conf(self.h, path.encode()) != 0:
+            raise RkError("rkh_save_conf: " + self.H.rkh_error().decode())
+
+    def close(self):
+        if self.h:
+            self.gpu.close()
+            self.H.rkh_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

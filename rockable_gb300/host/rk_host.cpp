@@ -853,7 +853,12 @@ bool Rockable::saveConf(const std::string& fname) {  // Rockable.cpp:440-610
 bool Rockable::run(long nsteps) {
   rk_step_report rep{};
   for (long s = 0; s < nsteps; s++) t += dt;
-  return ck(rk_step(ctx_, nsteps, &rep), "rk_step");
+  if (nsteps <= 0) return true;
+  // the last step records the contact geometry that a saveConf writes
+  if (nsteps > 1 && !ck(rk_step(ctx_, nsteps - 1, &rep), "rk_step")) return false;
+  if (!ck(rk_set_record_geometry(ctx_, 1), "rk_set_record_geometry")) return false;
+  const bool ok = ck(rk_step(ctx_, 1, &rep), "rk_step");
+  return ck(rk_set_record_geometry(ctx_, 0), "rk_set_record_geometry") && ok;
 }
 
 long Rockable::consoleRun(const std::string& outdir, long max_steps) {  // run.cpp + Rockable.cpp:2538-2746
@@ -978,8 +983,9 @@ int rkh_run(rkh_sim* s, long nsteps) {
   if (!s->R.run(nsteps)) { g_err = s->R.error(); return -1; }
   return 0;
 }
+rk_ctx* rkh_context(rkh_sim* s) { return s ? s->R.ctx() : nullptr; }
 int rkh_save_conf(rkh_sim* s, const char* path) {
-  if (!s->R.syncFromDevice(false) || !s->R.saveConf(path)) { g_err = s->R.error(); return -1; }
+  if (!s->R.syncFromDevice(true) || !s->R.saveConf(path)) { g_err = s->R.error(); return -1; }
   return 0;
 }
 }

@@ -219,4 +219,7 @@ int rkh_read_driving(rkh_sim* s, const char* path);
 long rkh_console_run(rkh_sim* s, const char* outdir, long max_steps);
 int rkh_run(rkh_sim* s, long nsteps);
 int rkh_save_conf(rkh_sim* s, const char* path);
+/* The engine context the host drives (owned by the host: valid until
+ * rkh_close), for direct rk_* calls on the loaded scene, e.g. rk_step. */
+rk_ctx* rkh_context(rkh_sim* s);
 }

@@ -296,6 +296,112 @@ def pack(shapes, shape_of, Q, volume, lo, hi, scale=None, tol=1e-9, seed=SEED, m
                                        "max_overlap": float(s[6])}
 
 
+def rockfall_bonded(nclusters=40, per=500, seed=SEED, nshapes=1024, semi=(0.005, 0.01), slope_deg=30.0,
+                    v0=10.0, density=2700.0, kn=1e7, kt=1e7, en2=0.25, mu=0.4, dt=1e-6, bond_kn=1e5,
+                    bond_kt=1e5, fn0_scale=1e3, fn0_m=5.0, ft0=1e3, eps=None, target_bonds=120000):
+    """Breakable bonded rockfall: `nclusters` blocks of `per` hull grains
+    (semi-axes U[0.5, 1.0] cm: 1-2 cm grains), each block packed on its own
+    (pack(), about a 10 cm cube) and given its own cluster id, in a grid
+    just above a rigid plate inclined at `slope_deg`, all moving at `v0`
+    straight down.  StickedLinks law: contacts at kn, and inner bonds made
+    at load by the conf's own preprocessing commands --
+    stickVerticesInClusters eps (PreproCommand_stickVerticesInClusters.cpp:
+    56-141: vertex-vertex bonds between grains of one cluster whose vertex
+    spheres come within eps) and setVariableStickParams fn0 inner
+    <fn0_scale> <fn0_m> 0 (PreproCommand_setVariableStickParams.cpp:57-94:
+    Weibull tensile strengths).  eps defaults to the distance that gives
+    about `target_bonds` vertex pairs.  The bonds' rest distance is zero
+    (the interface's dn0, never set by that command), so a bond made across
+    a gap starts in tension: at bond_kn = 1e5 N/m a gap of a few mm pulls
+    with a few hundred N, below the strengths, and the blocks hold together
+    until they hit the slope.  Returns a scene (for write_conf) with
+    "conf_extra" (bond parameters) and "conf_tail" (the two commands)."""
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(seed)
+    th = math.radians(slope_deg)
+    shapes = [plate_shape("SLOPE", 1.0, 0.01)]
+    shapes += [hull_shape(rng, "R%04d" % k, semi_lo=semi[0], semi_hi=semi[1]) for k in range(nshapes)]
+    bmax = max(float(sh["bound"]) for sh in shapes[1:])
+    side = 0.1
+    blocks = []
+    for c in range(nclusters):
+        so = rng.integers(1, nshapes + 1, per)
+        Qc = stable_face_quaternions(rng, shapes, so)
+        vol = np.array([shapes[k]["volume"] for k in so])
+        pos, st = pack(shapes, so, Qc, vol, (-0.5 * side, -0.5 * side, 0.0), (0.5 * side, 0.5 * side, 1.0),
+                       seed=seed + 1 + c, tries=16)
+        blocks.append((so, Qc, pos, st))
+    # the slope: plate through the origin, normal n, downhill direction u
+    n = np.array([math.sin(th), 0.0, math.cos(th)])
+    u = np.array([math.cos(th), 0.0, -math.sin(th)])
+    qs = np.array([math.cos(0.5 * th), 0.0, math.sin(0.5 * th), 0.0])
+    ncol = int(math.ceil(math.sqrt(nclusters * 1.6)))
+    nrow = int(math.ceil(nclusters / ncol))
+    pitch = 1.3 * side
+    P, Q, S, K = [], [], [], []
+    for c, (so, Qc, pos, st) in enumerate(blocks):
+        a, b = c % ncol, c // ncol
+        centre = (a - 0.5 * (ncol - 1)) * pitch * u + np.array([0.0, (b - 0.5 * (nrow - 1)) * pitch, 0.0])
+        p = pos + centre
+        # lift the block along the vertical until its lowest grain is 2 mm
+        # (plus the rounding) above the plate (grain extents from their
+        # bounding spheres)
+        r = np.array([shapes[k]["bound"] for k in so])
+        gap = (p @ n - r).min()
+        p = p + ((0.002 - gap) / n[2]) * np.array([0.0, 0.0, 1.0])
+        P.append(p)
+        Q.append(Qc)
+        S.append(so)
+        K.append(np.full(per, c + 1, np.int32))
+    pos = np.concatenate(P)
+    Qa = np.concatenate(Q)
+    so = np.concatenate(S)
+    cl = np.concatenate(K)
+    out = _assemble(shapes, [-0.01 * n], [qs], pos, Qa, so, density, "StickedLinks", kn, kt, en2, mu, dt,
+                    gravity=(0.0, 0.0, -9.81), DVerlet=0.2 * bmax, dVerlet=0.1 * bmax, interVerlet=100 * dt,
+                    name="rockfall_bonded_%dx%d" % (nclusters, per), wall_shape=0)
+    out["bodies"]["cluster"] = np.concatenate([[0], cl]).astype(np.int32)
+    out["bodies"]["vel"][1:] = [0.0, 0.0, -v0]
+    if eps is None:
+        # vertex spheres of grains of one cluster: pairs within eps + Ri + Rj
+        V, owner = [], []
+        for i in range(1, len(out["bodies"]["mass"])):
+            sh = shapes[out["bodies"]["shape"][i]]
+            q = out["bodies"]["Q"][i]
+            V.append(_qrot_np(q, np.asarray(sh["vertices"])) + out["bodies"]["pos"][i])
+            owner += [i] * len(sh["vertices"])
+        V = np.concatenate(V)
+        owner = np.asarray(owner)
+        rad = np.array([shapes[out["bodies"]["shape"][i]]["radius"] for i in owner])
+        tree = cKDTree(V)
+        pairs = tree.query_pairs(0.004, output_type="ndarray")
+        pairs = pairs[(owner[pairs[:, 0]] != owner[pairs[:, 1]]) &
+                      (out["bodies"]["cluster"][owner[pairs[:, 0]]] == out["bodies"]["cluster"][owner[pairs[:, 1]]])]
+        gaps = np.sort(np.linalg.norm(V[pairs[:, 0]] - V[pairs[:, 1]], axis=1) - rad[pairs[:, 0]] - rad[pairs[:, 1]])
+        eps = float(gaps[min(target_bonds, len(gaps)) - 1]) if len(gaps) else 0.001
+        eps = max(eps, 1e-6)
+    out["pack"] = {"clusters": nclusters, "per_cluster": per, "solid_fraction_bulk": float(np.mean(
+        [st["solid_fraction"] for *_, st in blocks])), "coordination": float(np.mean(
+        [2.0 * st["touching_pairs"] / per for *_, st in blocks]))}
+    out["bond_eps"] = eps
+    out["params"].update({"bond_kn": bond_kn, "bond_kt": bond_kt, "fn0_scale": fn0_scale, "fn0_m": fn0_m, "ft0": ft0})
+    out["conf_extra"] = ["%s 0 0 %r" % kv for kv in [
+        ("knInnerBond", bond_kn), ("ktInnerBond", bond_kt), ("krInnerBond", 0.0), ("en2InnerBond", en2),
+        ("fn0InnerBond", fn0_scale), ("ft0InnerBond", ft0), ("mom0InnerBond", 1e10), ("powInnerBond", 2.0)]]
+    out["conf_tail"] = ["stickVerticesInClusters %r" % eps,
+                        "setVariableStickParams fn0 inner %r %r 0" % (fn0_scale, fn0_m)]
+    return out
+
+
+def _qrot_np(q, v):
+    """Rotate the rows of v by the unit quaternion q = (w, x, y, z)."""
+    w, x, y, z = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                  [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                  [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+    return v @ R.T
+
+
 def packing_stats(pos, vol, lo, hi, inset, st):
     """Bulk solid fraction (grain volume with centres inside the packing's
     box shrunk by `inset` on every side, over that box's volume: away from
@@ -666,21 +772,34 @@ def set_scene_params(g, scene, t=0.0, numerical_damping=0.0):
         g.set_controls(c["type"], c["body"], c["value"], c["vec"], scene.get("servo"))
 
 
-def loaded(scene, steps, device=0, chunk=1000, report=None):
-    """The scene after `steps` DEM steps with its own parameters and laws in
-    the FP64 form (the reference arithmetic), walls and servo in place:
-    packed grains that touch but carry no load get loaded by gravity or by
-    the servo.  Then the walls listed in scene["walls"] are removed (the
-    start of a collapse).  Returns the new scene with the neighbour list and
-    its contact history ("entries") and a "load" record (steps, simulated
-    time, entries and active contacts per free body at the end)."""
-    from .abi import GpuScene
-    g = GpuScene(device=device)
+def loaded(scene, steps, device=0, damping=0.5, form=1, rebuild_steps=1000, chunk=2000, report=None):
+    """The scene settled by the DEM itself: `steps` DEM steps with the
+    scene's laws, stiffnesses, time step, gravity, walls and servo, plus
+    Rockable's numerical damping `damping` (Rockable.cpp:3814-3866), in the
+    given form (the mixed form by default: the result is only an initial
+    state) with a neighbour list rebuilt every `rebuild_steps` steps (the
+    damped grains move far less than dVerlet in that time).  The packer's
+    grains touch but carry no load and are not in rotational balance: here
+    they load their contacts, topple into place and come to rest.  Then the
+    walls listed in scene["walls"] are removed (the start of a collapse).
+    The stiffnesses never change, so the contact forces carried over (with
+    their history, "entries") hold the load without the damping.  Returns
+    the new scene and a "load" record (steps, damping, simulated time,
+    entries and active contacts per free body at the end, kinetic
+    energies)."""
+    from .abi import GpuScene, RK_LAW
+    g = GpuScene(device=device, form=form)
     g.upload_shapes(scene["shape_tables"])
     g.upload_bodies(scene["bodies"], scene["n_driven"])
     if scene.get("scene_of") is not None:
         g.set_scenes(scene["scene_of"])
-    set_scene_params(g, scene)
+    dt = scene["dt"]
+    g.set_params(t=0.0, dt=dt, gravity=scene["gravity"], DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
+                 interVerlet=rebuild_steps * dt, interVerletC=0.0, law=RK_LAW[scene["law"]],
+                 ngroup=scene["ngroup"], table=scene["table"], numerical_damping=damping)
+    c = scene.get("controls")
+    if c is not None:
+        g.set_controls(c["type"], c["body"], c["value"], c["vec"], scene.get("servo"))
     if scene.get("entries") is not None:
         g.upload_entries(scene["entries"])
     else:
@@ -688,18 +807,22 @@ def loaded(scene, steps, device=0, chunk=1000, report=None):
     g.set_graphs(True)
     done = 0
     nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
+    trace = []
     while done < steps:
         k = min(chunk, steps - done)
         g.step(k)
         done += k
-        if report is not None:
-            st = g.stats()
-            report.append((done, st["n_active"] / max(1, nfree), st["e_trans"]))
+        st = g.stats()
+        trace.append((done, round(st["n_active"] / max(1, nfree), 4), float("%.4g" % st["e_trans"])))
+    if report is not None:
+        report.extend(trace)
+    g.update_nl()  # the list for the scene's own schedule, from the final positions
     st = g.stats()
     out = scene_from_gpu(scene, g)
     g.close()
-    rec = {"steps": int(steps), "t": steps * scene["dt"], "active_per_free": st["n_active"] / max(1, nfree),
-           "entries": int(st["n_entries"])}
+    rec = {"steps": int(steps), "dt": dt, "numerical_damping": damping, "form": "mixed" if form == 1 else "fp64",
+           "t": steps * dt, "active_per_free": st["n_active"] / max(1, nfree), "entries": int(st["n_entries"]),
+           "e_trans": st["e_trans"], "e_rot": st["e_rot"], "trace": trace}
     if scene.get("walls"):
         out = drop_bodies(out, scene["walls"])
         rec["released_walls"] = [int(w) for w in scene["walls"]]
@@ -775,6 +898,7 @@ def write_conf(scene, directory, conf_name="input.conf", shape_name="shapes.shp"
     nd = scene["n_driven"]
     bound = float(np.max(np.array([scene["shapes"][k]["bound"] for k in b["shape"][nd:]]) * b["homothety"][nd:]))
     cs = 2.0 * bound + scene["DVerlet"]
+    lines += list(scene.get("conf_extra", []))
     lines += ["cellMinSizes %r %r %r" % (cs, cs, cs), "nDriven %d" % scene["n_driven"],
               "shapeFile %s" % shape_name, "precision 16", "Particles %d" % len(b["mass"])]
     for i in range(len(b["mass"])):
@@ -794,7 +918,7 @@ def write_conf(scene, directory, conf_name="input.conf", shape_name="shapes.shp"
                 list(e["ft"][k]) + list(e["mom"][k]) + [e["damp"][k]]
             lines.append("%d %d %d %d %d %s" % (e["i"][k], e["j"][k], e["type"][k], e["isub"][k], e["jsub"][k],
                                                 " ".join(_f(x) for x in vals)))
-    lines += ["Interfaces 0", ""]
+    lines += ["Interfaces 0"] + list(scene.get("conf_tail", [])) + [""]
     with open(os.path.join(directory, conf_name), "w") as f:
         f.write("\n".join(lines))
     sv = scene.get("servo")

@@ -67,4 +67,7 @@ def test_host_bond_setup_matches_oracle(golden_dir, oracle_lib, gpu_lib, tmp_pat
     ot, ht = open(tmp_path / "oracle.conf").read(), open(tmp_path / "host.conf").read()
     for name in ["Interfaces", "Interactions"]:
         a, b = _section(ot, name), _section(ht, name)
-        assert len(a) > 1 and a == b, (name, len(a), len(b), [x for x in zip(a, b) if x[0] != x[1]][:3])
+        diff = [(k, x, y) for k, (x, y) in enumerate(zip(a, b)) if x != y]
+        for k, x, y in diff[:3]:  # field by field
+            print(name, k, [(f, u, v) for f, (u, v) in enumerate(zip(x.split(), y.split())) if u != v])
+        assert len(a) > 1 and len(a) == len(b) and not diff, (name, len(a), len(b), len(diff))

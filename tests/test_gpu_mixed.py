@@ -283,7 +283,7 @@ def test_mixed_per_result_relative_errors_settled_column(gpu_lib):
 def test_headline_contact_set_equals_fp64_rebuild_every_step(gpu_lib):
     """The headline form (mixed precision, learned skin with exact contact
     detection) on a contact-rich column for 1000 steps: the dense pile,
-    loaded by gravity between walls for 6000 steps and released, collapses;
+    settled by gravity between walls for 20000 steps and released, collapses;
     at every 10th step the headline form's active sub-contact set equals the
     one the FP64 form finds at the same positions from a neighbour list
     rebuilt from scratch (a fresh context: rk_update_nl, then the load-time
@@ -291,7 +291,7 @@ def test_headline_contact_set_equals_fp64_rebuild_every_step(gpu_lib):
     from rockable_gb300 import scenes
     from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
     scene = scenes.column_collapse(n=2000, nshapes=64, semi=(0.0025, 0.0075), column=(0.15, 0.15, 1.5), walls=True)
-    src = scenes.loaded(scene, 6000)
+    src = scenes.loaded(scene, 20000)
     h = GpuScene(form=RK_FORM_MIXED)
     h.upload_shapes(src["shape_tables"])
     h.upload_bodies(src["bodies"], src["n_driven"])

@@ -11,7 +11,7 @@ from conftest import CONF
 CASE = "518_poly"
 LINES = {
     "AttractingPoint": "BodyForce AttractingPoint 0.01 -0.02 0.03 1000",
-    "ViscousFluid": "BodyForce ViscousFluid 1000",
+    "ViscousFluid": "BodyForce ViscousFluid 0.001",
     "PreferredDirection": "BodyForce PreferredDirection 0 0 2 1 1 0 0.001",
 }
 
