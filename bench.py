@@ -72,10 +72,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--segment", type=int, default=100, help="DEM steps per bench step")
     ap.add_argument("--n", type=int, default=50000, help="grains of the column")
-    ap.add_argument("--load-steps", type=int, default=40000,
-                    help="damped DEM steps that settle the column between walls before the release")
-    ap.add_argument("--iso-load-steps", type=int, default=25000,
-                    help="damped DEM steps of servo compression before the compression box is timed")
+    ap.add_argument("--load-steps", type=int, default=50000,
+                    help="damped DEM steps (2 x dt: 0.1 s) that settle the column between walls before the release")
+    ap.add_argument("--iso-load-steps", type=int, default=50000,
+                    help="damped DEM steps (2 x dt: 0.1 s) of servo compression before the box is timed")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--iso-n", type=int, default=200000, help="grains of the compression box (0: skip)")
@@ -83,6 +83,9 @@ def parse():
     ap.add_argument("--ref-seconds", type=float, default=150.0, help="budget of the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ncu-window", default="",
+                    help="form whose extra window (a rebuild and one segment, after its timed steps) is bracketed "
+                         "by cuProfilerStart/Stop, for ncu --profile-from-start off")
     ap.add_argument("--rock-clusters", type=int, default=40,
                     help="500-grain bonded blocks of the rockfall workload (0: skip)")
     ap.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched slope workload (0: skip)")
@@ -92,6 +95,17 @@ def parse():
 
 
 # ------------------------------------------------------------------ host --
+def cu_profiler(on):
+    """cuProfilerStart / cuProfilerStop (CUDA driver API) on the current
+    context: the window a profiler started with --profile-from-start off
+    records."""
+    import ctypes
+    lib = ctypes.CDLL("libcuda.so.1")
+    rc = (lib.cuProfilerStart if on else lib.cuProfilerStop)()
+    if rc != 0:
+        raise RuntimeError("cuProfiler%s failed: %d" % ("Start" if on else "Stop", rc))
+
+
 def cpu_info():
     """Model and logical cores of this host (lscpu when present)."""
     model = platform.processor() or platform.machine()
@@ -387,6 +401,13 @@ def time_form(scene, label, a, dev, dist, ws, steps, warmup):
     e.step(a.segment)
     prof = e.profile()
     e.set_profiling(False)
+    if a.ncu_window == label:  # the launch list of one rebuild and one segment, for ncu
+        e.synchronize()
+        cu_profiler(True)
+        e.update_nl()
+        e.step(a.segment)
+        e.synchronize()
+        cu_profiler(False)
     rec = {"value": job_rate(ws, nfree, steps * a.segment, ms), "ms": ms, "ms_per_step": ms / steps,
            "ms_per_dem_step": ms / (steps * a.segment), "wall_s": wall, "gpu_launches": int(launches),
            "nl_rebuilds_in_timed": int(rep["nl_updates"]), "entries": int(st["n_entries"]),
@@ -526,12 +547,14 @@ def rockfall_workload(a, dev):
 def batched_workload(a, dev):
     """Many independent slope scenes (N ~ U{200..5000} grains each, slopes
     25-45 degrees, Default law) in ONE engine context: every launch covers all
-    scenes, each step's launches replay as one CUDA graph.  Reports the
-    aggregate particle-steps/s, and each scene's own step time when it runs
-    alone in a context of its own (the spread, and the sum that batching
-    replaces)."""
+    scenes, each step's launches replay as one CUDA graph.  For the plain
+    FP64 form and the headline form (mixed + learned skin), the aggregate
+    particle-steps/s and each scene's own step time when it runs alone in a
+    context of its own (the spread, and the sum that batching replaces).
+    The replayed graph's step time against the sum of its kernels' event
+    times (launch by launch) measures what a persistent kernel could still
+    remove: the gaps between launches."""
     from rockable_gb300 import scenes
-    from rockable_gb300.abi import GpuScene
     t0 = time.perf_counter()
     bt = scenes.slope_batch(nscenes=a.batch_scenes)
     t_gen = time.perf_counter() - t0
@@ -541,61 +564,58 @@ def batched_workload(a, dev):
     g.close()
     t_settle = time.perf_counter() - t0
     nfree = int(sum(bt["free_per_scene"]))
-
-    def eng(sc, entries=None):
-        e = GpuScene(device=dev)
-        e.upload_shapes(sc["shape_tables"])
-        e.upload_bodies(sc["bodies"], sc["n_driven"])
-        if sc.get("scene_of") is not None:
-            e.set_scenes(sc["scene_of"])
-        scenes.set_scene_params(e, sc)
-        if entries is not None:
-            e.upload_entries(entries)
-        else:
-            e.update_nl()
-        e.set_graphs(True)
-        return e
-
-    e = eng(src, src["entries"])
-    e.autotune(2)
-    e.step(TUNE_STEPS)
-    e.step(max(3, a.warmup))
-    clocks = Clocks()
-    e.synchronize()
-    clocks.start()
-    rep = e.step(a.batch_steps)
-    ms, launches = e.last_step_timing()
-    ck = clocks.stop()
-    st = e.stats()
-    gst = e.graph_stats()
-    bsz = e.block_sizes()
-    e.set_profiling(True)
-    e.step(a.batch_steps)
-    prof = e.profile()
-    e.close()
-    solo = []
-    for k in range(len(bt["free_per_scene"])):
-        part = scenes.part_of(src, k)
-        p = eng(part)
-        p.step(3)
-        p.step(a.batch_steps)
-        pms, _ = p.last_step_timing()
-        solo.append(pms / a.batch_steps)
-        p.close()
-    solo = np.array(solo)
-    return {"workload": bt["name"], "scenes": len(solo), "free_bodies": nfree, "bodies": int(len(bt["scene_of"])),
-            "law": "Default", "form": "plain FP64, step graphs", "steps": a.batch_steps,
-            "value": nfree * a.batch_steps / (ms / 1000.0), "unit": "particle-steps/s",
-            "ms_per_step": ms / a.batch_steps, "gpu_launches": int(launches), "graph": gst,
-            "block_sizes": bsz,
-            "entries": int(st["n_entries"]), "active": int(st["n_active"]), "nl_rebuilds_in_timed": int(rep["nl_updates"]),
-            "clocks": ck,
+    out = {"workload": bt["name"], "scenes": int(a.batch_scenes), "free_bodies": nfree,
+           "bodies": int(len(bt["scene_of"])), "law": "Default", "steps": a.batch_steps, "unit": "particle-steps/s",
+           "forms": {}, "setup_s": {"generate": t_gen, "settle": t_settle}}
+    for label in ["plain_fp64", "mixed_learned_skin_exact"]:
+        e = engine(src, label, dev, SKIN[label])
+        e.autotune(2)
+        e.step(TUNE_STEPS)
+        e.step(max(3, a.warmup) * 10)
+        clocks = Clocks()
+        e.synchronize()
+        clocks.start()
+        rep = e.step(a.batch_steps)
+        ms, launches = e.last_step_timing()
+        ck = clocks.stop()
+        st = e.stats()
+        gst = e.graph_stats()
+        bsz = e.block_sizes()
+        e.set_profiling(True)
+        e.step(a.batch_steps)
+        prof = e.profile()
+        sk = e.skin_stats() if SKIN[label] else None
+        e.close()
+        kernels_ms = sum(w[0] for q, w in prof.items() if q != "nl_rebuild") / a.batch_steps
+        solo = []
+        for k in range(len(bt["free_per_scene"])):
+            p = engine(scenes.part_of(src, k), label, dev, SKIN[label])
+            p.step(3)
+            p.step(a.batch_steps)
+            pms, _ = p.last_step_timing()
+            solo.append(pms / a.batch_steps)
+            p.close()
+        solo = np.array(solo)
+        out["forms"][label] = {
+            "value": nfree * a.batch_steps / (ms / 1000.0), "ms_per_step": ms / a.batch_steps,
+            "gpu_launches": int(launches), "graph": gst, "block_sizes": bsz, "entries": int(st["n_entries"]),
+            "active": int(st["n_active"]), "nl_rebuilds_in_timed": int(rep["nl_updates"]), "clocks": ck,
+            "skin": sk,
             "solo_ms_per_step": {"min": float(solo.min()), "median": float(np.median(solo)),
                                  "p90": float(np.percentile(solo, 90)), "max": float(solo.max()),
                                  "sum": float(solo.sum())},
             "batched_vs_solo_sum": float(solo.sum() / (ms / a.batch_steps)),
             "phases_ms_per_step": {q: w[0] / a.batch_steps for q, w in prof.items()},
-            "setup_s": {"generate": t_gen, "settle": t_settle}}
+            "step_kernels_ms_per_step": kernels_ms}
+    head = out["forms"]["mixed_learned_skin_exact"]
+    out["value"] = head["value"]
+    out["headline_vs_plain"] = head["value"] / out["forms"]["plain_fp64"]["value"]
+    pl = out["forms"]["plain_fp64"]
+    out["persistent_kernel_bound"] = (
+        "graph replay: %.4f ms per step for step kernels timing %.4f ms launch by launch (plain FP64, rebuild "
+        "steps excluded from the latter): a persistent kernel could remove at most the difference" % (
+            pl["ms_per_step"], pl["step_kernels_ms_per_step"]))
+    return out
 
 
 def iso_workload(a, dev, dist, ws, order):
@@ -606,7 +626,7 @@ def iso_workload(a, dev, dist, ws, order):
     packed = scenes.iso_compression(n=a.iso_n)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
-    sc = scenes.loaded(packed, a.iso_load_steps, device=dev)
+    sc = scenes.loaded(packed, a.iso_load_steps, device=dev, dt_factor=2.0)
     t_load = time.perf_counter() - t0
     nfree = len(sc["bodies"]["mass"]) - sc["n_driven"]
     steps = max(2, a.steps // 4)
@@ -619,8 +639,8 @@ def iso_workload(a, dev, dist, ws, order):
     out = {"workload": sc["name"], "bodies": len(sc["bodies"]["mass"]), "free_bodies": nfree,
            "law": sc["law"], "servo": "tritriIsostaticCompression at %g Pa, no gravity" % sc["servo"]["pressure"],
            "pack": sc["pack"], "load": sc["load"],
-           "state": ("the packed box after %d DEM steps of servo compression with numerical damping 0.5 "
-                     "(scenes.loaded)" % a.iso_load_steps),
+           "state": ("the packed box after %d DEM steps (2 x dt) of servo compression with numerical damping "
+                     "0.5 (scenes.loaded)" % a.iso_load_steps),
            "dem_steps_per_step": a.segment, "steps": steps, "warmup": 1,
            "forms": forms, "headline_form": order[-1],
            "headline_vs_plain": head["value"] / forms["plain_fp64"]["value"],
@@ -652,7 +672,7 @@ def main():
     packed = scenes.column_collapse(n=a.n, walls=True)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
-    scene = scenes.loaded(packed, a.load_steps, device=dev)
+    scene = scenes.loaded(packed, a.load_steps, device=dev, dt_factor=2.0)
     t_load = time.perf_counter() - t0
     N = len(scene["bodies"]["mass"])
     nfree = N - scene["n_driven"]
@@ -698,8 +718,8 @@ def main():
                           "nl_rebuilds_in_timed": head["nl_rebuilds_in_timed"], "dt": scene["dt"],
                           "interVerlet_steps": int(round(scene["interVerlet"] / scene["dt"])),
                           "pack": scene["pack"], "load": scene["load"], "cpu_on_settled_state": cpu_settled,
-                          "state": ("the packed column settled by gravity between four walls (%d DEM steps with "
-                                    "numerical damping 0.5, scenes.loaded), walls removed, then %d tuning and %d "
+                          "state": ("the packed column settled by gravity between four walls (%d DEM steps of "
+                                    "2 x dt with numerical damping 0.5, scenes.loaded), walls removed, then %d tuning and %d "
                                     "warm-up DEM steps of each form before its timed ones" % (
                                         a.load_steps, TUNE_STEPS, a.warmup * a.segment)),
                           "l2": "inputs larger than L2 (entries + bodies > 129 MB)" if head["entries"] * 240 + N * 600 >

@@ -842,7 +842,7 @@ void rk_destroy(rk_ctx* x) {
     if (c.tev[k]) cudaEventDestroy(c.tev[k]);
   Scene& s = c.s;
   dfree(s.vert_ofs); dfree(s.edge_ofs); dfree(s.edges); dfree(s.face_ofs); dfree(s.face_vofs); dfree(s.face_verts);
-  dfree(s.svert); dfree(s.sradius); dfree(s.sobb);
+  dfree(s.svert); dfree(s.sradius); dfree(s.sobb); dfree(s.sbox); dfree(s.bbox);
   dfree(s.pos); dfree(s.vel); dfree(s.acc); dfree(s.Q); dfree(s.vrot); dfree(s.arot); dfree(s.force); dfree(s.moment);
   dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.inv_mi); dfree(s.shape); dfree(s.group); dfree(s.cluster);
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.gvr); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
@@ -915,13 +915,28 @@ int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
     }
   for (int f = 0; f < nf; f++)
     if (sh->face_vofs[f + 1] - sh->face_vofs[f] < 3) return fail(c, RK_ERR_ARG, "a face has fewer than 3 vertices");
+  // the box of each shape's vertices in its own frame (centre, half extents)
+  std::vector<double> sbox(6 * (size_t)ns);
+  for (int k = 0; k < ns; k++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int v = sh->vert_ofs[k]; v < sh->vert_ofs[k + 1]; v++)
+      for (int d = 0; d < 3; d++) {
+        lo[d] = std::min(lo[d], sh->vertices[3 * (int64_t)v + d]);
+        hi[d] = std::max(hi[d], sh->vertices[3 * (int64_t)v + d]);
+      }
+    for (int d = 0; d < 3; d++) {
+      sbox[6 * k + d] = 0.5 * (lo[d] + hi[d]);
+      sbox[6 * k + 3 + d] = 0.5 * (hi[d] - lo[d]);
+    }
+  }
   Scene& s = c.s;
   int rc;
   if ((rc = dupload(c, s.vert_ofs, sh->vert_ofs, ns + 1)) || (rc = dupload(c, s.edge_ofs, sh->edge_ofs, ns + 1)) ||
       (rc = dupload(c, s.edges, sh->edges, 2 * (int64_t)ne)) || (rc = dupload(c, s.face_ofs, sh->face_ofs, ns + 1)) ||
       (rc = dupload(c, s.face_vofs, sh->face_vofs, nf + 1)) ||
       (rc = dupload(c, s.face_verts, sh->face_verts, nfv)) || (rc = dupload(c, s.svert, sh->vertices, 3 * (int64_t)nv)) ||
-      (rc = dupload(c, s.sradius, sh->radius, ns)) || (rc = dupload(c, s.sobb, sh->obb, 15 * (int64_t)ns)))
+      (rc = dupload(c, s.sradius, sh->radius, ns)) || (rc = dupload(c, s.sobb, sh->obb, 15 * (int64_t)ns)) ||
+      (rc = dupload(c, s.sbox, sbox.data(), 6 * (int64_t)ns)))
     return rc;
   s.nshapes = ns;
   c.shape_radius.assign(sh->radius, sh->radius + ns);
@@ -979,6 +994,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.gv, (const double*)nullptr, 3 * nv)) || (rc = dupload(c, s.gvr, (const float*)nullptr, 3 * nv)) ||
       (rc = dupload(c, s.bobb, (const double*)nullptr, 15 * n)) ||
       (rc = dupload(c, s.bobbf, (const float*)nullptr, 15 * n)) ||
+      (rc = dupload(c, s.bbox, (const float*)nullptr, 15 * n)) ||
       (rc = dupload(c, s.baabb, (const float*)nullptr, 6 * n)) ||
       (rc = dupload(c, s.dpos, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.dq, (const double*)nullptr, 4 * n)) ||
       (rc = dupload(c, s.iofs, (const int64_t*)nullptr, n + 1)) ||

@@ -67,6 +67,7 @@ struct Scene {
   double* svert;   // 3 per shape vertex
   double* sradius;
   double* sobb;    // 15 per shape
+  double* sbox;    // 6 per shape: centre and half extents of the box of its vertices, in the shape frame
   // ---- bodies
   int64_t n;
   int64_t n_driven;
@@ -85,6 +86,8 @@ struct Scene {
   double* bobb;      // 15 per body (placed OBB, not enlarged)
   float* bobbf;      // float copy of bobb
   float* baabb;      // 6 per body: outward-rounded AABB of the OBB enlarged by DVerlet/2
+  float* bbox;       // 15 per body: the shape's vertex box placed (centre, 3 axes, half extents), float:
+                     // the root of the two-level pruning of the candidate sub-elements
   // dynamic guard
   double *dpos, *dq;  // 3n, 4n
   // ---- law

@@ -68,6 +68,19 @@ __global__ void k_body_obb(Scene s) {
   out[12] = o.ext.x; out[13] = o.ext.y; out[14] = o.ext.z;
   float* of = s.bobbf + 15 * b;  // float copy for the pair test's pre-classification
   for (int q = 0; q < 15; q++) of[q] = (float)out[q];
+  {  // the vertex box placed, in float (the pruning tests carry the rounding margin)
+    const double* sb = s.sbox + 6 * s.shape[b];
+    const V3 bc = v3(s.pos[3 * b], s.pos[3 * b + 1], s.pos[3 * b + 2]) + qrot(q, h * v3(sb[0], sb[1], sb[2]));
+    const V3 ax[3] = {qrot(q, v3(1, 0, 0)), qrot(q, v3(0, 1, 0)), qrot(q, v3(0, 0, 1))};
+    float* bx = s.bbox + 15 * b;
+    bx[0] = (float)bc.x; bx[1] = (float)bc.y; bx[2] = (float)bc.z;
+    for (int k = 0; k < 3; k++) {
+      bx[3 + 3 * k] = (float)ax[k].x;
+      bx[4 + 3 * k] = (float)ax[k].y;
+      bx[5 + 3 * k] = (float)ax[k].z;
+      bx[12 + k] = (float)(h * sb[3 + k]);
+    }
+  }
   const double d = 0.5 * s.DVerlet;
   const double ex = o.ext.x + d, ey = o.ext.y + d, ez = o.ext.z + d;
   const double hw[3] = {ex * fabs(o.e0.x) + ey * fabs(o.e1.x) + ez * fabs(o.e2.x),
@@ -632,6 +645,25 @@ __device__ __forceinline__ float pt_poly_d2(const Scene& s, const float4* sp, in
 // NEAR, so the NEAR set is exactly the one of testing every candidate.
 constexpr int kCandWarps = 4;  // warps per block
 
+// Root-versus-leaf test of the two-level pruning: true when a sub-element
+// sphere (centre, radius in .w) lies farther than `reach` from the other
+// body's vertex box bx (float: centre, 3 axes, half extents).  The box holds
+// that body's core, so such an element is farther than `reach` from every
+// sub-element of it; the margin covers the float rounding of the box, the
+// centre and the projections.
+__device__ __forceinline__ bool box_far(const float* bx, float4 c, float reach, float slack) {
+  const float dx = c.x - bx[0], dy = c.y - bx[1], dz = c.z - bx[2];
+  float d2 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float t = fabsf(dx * bx[3 + 3 * k] + dy * bx[4 + 3 * k] + dz * bx[5 + 3 * k]) - bx[12 + k];
+    if (t > 0.f) d2 += t * t;
+  }
+  float lim = c.w + reach;
+  lim = lim + 1e-4f * lim + slack + 1e-6f * (fabsf(dx) + fabsf(dy) + fabsf(dz) + bx[12] + bx[13] + bx[14]);
+  return d2 > lim * lim;
+}
+
 struct CandLists {
   uint16_t bv[64], pv[64];                   // owner / partner vertices
   uint16_t be[kMaxSub], pe[kMaxSub], pf[kMaxSub];  // owner edges, partner edges and faces
@@ -794,19 +826,36 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     const float glim = sum + 1e-4f * sum + slack;
     const float glim2 = glim * glim;
     const bool lower = b < p;  // vertex-vertex and edge-edge pairs are tested in the i < j direction only
-    const int nbv = warp_list(L.bv, nvb, lane, [&](int v) { return (((v < 32 ? m0 : m1) >> (v & 31)) & 1u) != 0u; });
-    const int npv = lower ? warp_list(L.pv, nvp, lane, [&](int w) { return !far(sp[w], cb, cb.w); }) : 0;
+    // Two-level pruning (the role of Rockable's per-shape OBB trees,
+    // Rockable.cpp:1440-1541, Shape.cpp:628-670): a sub-element stays in
+    // its list only when its sphere reaches the other body's bounding
+    // sphere and its vertex box (root against leaf); the products of the
+    // lists then test sphere against sphere (leaf against leaf) before the
+    // NEAR predicate.  Only elements that cannot be NEAR are dropped.
+    const float* bxb = s.bbox + 15 * b;
+    const float* bxp = s.bbox + 15 * p;
+    // an owner vertex meets the partner's edges up to dmax x their length
+    // beyond their ends (the vertex-edge projection test), so its reach
+    // grows by that much (an edge is at most the partner's diameter long)
+    const float vreach = sum + 2.f * (float)P.dmax * cp.w;
+    const int nbv = warp_list(L.bv, nvb, lane, [&](int v) {
+      return (((v < 32 ? m0 : m1) >> (v & 31)) & 1u) != 0u && !box_far(bxp, sb[v], vreach, slack);
+    });
+    const int npv = lower ? warp_list(L.pv, nvp, lane, [&](int w) {
+      return !far(sp[w], cb, cb.w) && !box_far(bxb, sp[w], sum, slack);
+    }) : 0;
     const int npe = warp_list(L.pe, nep, lane, [&](int e) {
       const float4 se = sp[nvp + e];
-      return !far(se, cb, cb.w + ve_ext * se.w);
+      const float4 sx = make_float4(se.x, se.y, se.z, ve_ext * se.w);  // the vertex-edge test's extended edge
+      return !far(se, cb, cb.w + sx.w) && !box_far(bxb, sx, sum, slack);
     });
     const int npf = warp_list(L.pf, nfp, lane, [&](int f) {
       const float4 sf = sp[nvp + nep + f];
-      return !far(sf, cb, cb.w + sf.w);
+      return !far(sf, cb, cb.w + sf.w) && !box_far(bxb, sf, sum, slack);
     });
     const int nbe = lower ? warp_list(L.be, neb, lane, [&](int e) {
       const float4 se = sb[nvb + e];
-      return !far(se, cp, cp.w + se.w);
+      return !far(se, cp, cp.w + se.w) && !box_far(bxp, se, sum, slack);
     }) : 0;
     // vertex-vertex
     for (int base = 0, tot = nbv * npv; base < tot; base += 32) {

@@ -462,10 +462,11 @@ def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2
 
 
 def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=2700.0, kn=1e6, kt=1e6, en2=0.25,
-                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=1e5, size=(0.005, 0.015), tries=16):
+                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=1e5, size=(0.01, 0.03), tries=16):
     """Dense isotropic compression: n hull grains (8-20 vertices, diameters
-    uniform in `size`, ratio 1:3, by homothety of a library of shapes of
-    about 1 cm), packed (pack(), the lowest of `tries` drop sites per grain)
+    uniform in `size`, 1-3 cm: ratio 1:3, by homothety of a library of
+    shapes of about 1 cm; at kn = 1e6 N/m and dt = 1e-6 s even the smallest
+    elongated grain rotates stably under several contacts), packed (pack(), the lowest of `tries` drop sites per grain)
     in a box about as high as wide, then enclosed by six rigid walls (bodies
     0-5: Xmin, Xmax, Ymin, Ymax, Zmin, Zmax) driven by Rockable's
     tritriIsostaticCompression servo at `pressure` (DrivingSystem.cpp:
@@ -772,10 +773,13 @@ def set_scene_params(g, scene, t=0.0, numerical_damping=0.0):
         g.set_controls(c["type"], c["body"], c["value"], c["vec"], scene.get("servo"))
 
 
-def loaded(scene, steps, device=0, damping=0.5, form=1, rebuild_steps=1000, chunk=2000, report=None):
+def loaded(scene, steps, device=0, damping=0.5, form=1, dt_factor=1.0, rebuild_steps=1000, chunk=2000,
+           report=None):
     """The scene settled by the DEM itself: `steps` DEM steps with the
-    scene's laws, stiffnesses, time step, gravity, walls and servo, plus
-    Rockable's numerical damping `damping` (Rockable.cpp:3814-3866), in the
+    scene's laws, stiffnesses, gravity, walls and servo, a time step
+    `dt_factor` times the scene's (kept well inside the contacts' and the
+    grains' rotational stability limits by the caller), plus Rockable's
+    numerical damping `damping` (Rockable.cpp:3814-3866), in the
     given form (the mixed form by default: the result is only an initial
     state) with a neighbour list rebuilt every `rebuild_steps` steps (the
     damped grains move far less than dVerlet in that time).  The packer's
@@ -793,7 +797,7 @@ def loaded(scene, steps, device=0, damping=0.5, form=1, rebuild_steps=1000, chun
     g.upload_bodies(scene["bodies"], scene["n_driven"])
     if scene.get("scene_of") is not None:
         g.set_scenes(scene["scene_of"])
-    dt = scene["dt"]
+    dt = scene["dt"] * dt_factor
     g.set_params(t=0.0, dt=dt, gravity=scene["gravity"], DVerlet=scene["DVerlet"], dVerlet=scene["dVerlet"],
                  interVerlet=rebuild_steps * dt, interVerletC=0.0, law=RK_LAW[scene["law"]],
                  ngroup=scene["ngroup"], table=scene["table"], numerical_damping=damping)

@@ -73,6 +73,43 @@ def test_batched_scenes_match_each_scene_alone(gpu_lib):
     assert total_entries == st["n_entries"]
 
 
+def test_batched_headline_form_matches_each_scene_alone(gpu_lib):
+    """The headline form (mixed precision, learned skin with exact contact
+    detection) over four batched slope scenes: every scene's bodies after
+    300 steps agree with the same scene run alone in that form within 1e-9
+    of each field's range (the skin of the batch decides its rebuilds for
+    all scenes at once, so the lists may be refreshed at other steps; the
+    contacts found are the same)."""
+    from rockable_gb300 import scenes
+    bt = scenes.slope_batch(nscenes=4, nmin=300, nmax=1500, nshapes=32)
+    gs = scenes.settle(bt, steps=2000, relax_steps=600)
+    bt = scenes.scene_from_gpu(bt, gs)
+    gs.close()
+
+    def headline(sc):
+        g = _engine(sc, 1, None, graphs=True)
+        d = sc["dVerlet"]
+        g.set_skin(use_mlp=True, skin_min=0.1 * d, skin_max=4.0 * d, interval_min=2, interval_max=300, seed=3,
+                   exact_contacts=True)
+        return g
+
+    whole = headline(bt)
+    whole.step(300)
+    wb = whole.bodies()
+    assert whole.stats()["n_active"] > 0
+    for k in range(4):
+        part = scenes.part_of(bt, k)
+        g = headline(part)
+        g.step(300)
+        pb = g.bodies()
+        idx = bt["index_of"][k]
+        for key in ["pos", "vel", "Q", "vrot"]:
+            rng = max(float(np.abs(pb[key]).max()), 1e-30)
+            assert float(np.abs(wb[key][idx] - pb[key]).max()) <= 1e-9 * rng, (k, key)
+        g.close()
+    whole.close()
+
+
 def test_autotuned_block_sizes_change_no_result(gpu_lib):
     from rockable_gb300 import scenes
     scene = scenes.column_collapse(n=3000, nshapes=64, semi=(0.0025, 0.0075))
