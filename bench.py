@@ -74,8 +74,8 @@ def parse():
     ap.add_argument("--n", type=int, default=50000, help="grains of the column")
     ap.add_argument("--load-steps", type=int, default=50000,
                     help="damped DEM steps (2 x dt: 0.1 s) that settle the column between walls before the release")
-    ap.add_argument("--iso-load-steps", type=int, default=50000,
-                    help="damped DEM steps (2 x dt: 0.1 s) of servo compression before the box is timed")
+    ap.add_argument("--iso-load-steps", type=int, default=30000,
+                    help="damped DEM steps (2 x dt: 0.06 s) of servo compression before the box is timed")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--iso-n", type=int, default=200000, help="grains of the compression box (0: skip)")

@@ -262,6 +262,11 @@ int64_t rk_num_interfaces(const rk_ctx* ctx);
 /* Any output pointer may be NULL. */
 int rk_download_bodies(rk_ctx* ctx, double* pos, double* vel, double* acc, double* Q, double* vrot, double* arot,
                        double* force, double* moment);
+/* Per-entry terms of the last force evaluation, 3 doubles each per entry in
+ * key order: the force on body i (body j receives its opposite) and the
+ * moments on i and on j -- the terms Rockable adds into the resultants
+ * (Rockable.cpp:2752-2789).  Meaningful for the active entries only. */
+int rk_download_contributions(rk_ctx* ctx, double* f, double* mi, double* mj);
 int rk_download_entries(rk_ctx* ctx, int32_t* i, int32_t* j, int32_t* type, int32_t* isub, int32_t* jsub, double* dn,
                         double* fn, double* ft, double* mom, double* damp, int32_t* bond, uint8_t* active, double* n,
                         double* pos, double* vel);

@@ -103,6 +103,7 @@ SIGNATURES = {
     "rk_upload_interfaces": (C.c_int, [P, C.POINTER(RkInterfaces)]),
     "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
     "rk_set_body_force": (C.c_int, [P, C.c_int, P, C.c_int32, P]),
+    "rk_download_contributions": (C.c_int, [P, P, P, P]),
     "rk_set_record_geometry": (C.c_int, [P, C.c_int]),
     "rk_set_form": (C.c_int, [P, C.c_int]),
     "rk_set_broadphase": (C.c_int, [P, C.c_int]),
@@ -434,6 +435,15 @@ class GpuScene:
             o.update(g)
         o["active"] = o["active"].astype(bool)
         return o
+
+    def contributions(self):
+        """Per-entry force on i and moments on i and j of the last force
+        evaluation (key order; meaningful for the active entries)."""
+        ne = self.n_entries
+        f, mi, mj = np.zeros((ne, 3)), np.zeros((ne, 3)), np.zeros((ne, 3))
+        if ne:
+            self._chk(self.L.rk_download_contributions(self.h, _p(f), _p(mi), _p(mj)), "rk_download_contributions")
+        return f, mi, mj
 
     def interfaces(self):
         n = self.L.rk_num_interfaces(self.h)

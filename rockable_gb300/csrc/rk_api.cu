@@ -1693,6 +1693,20 @@ __global__ void k_unpack_tsub(const uint32_t* ts, int64_t n, int* t, int* isub, 
   jsub[e] = tsub_jsub(ts[e]);
 }
 
+int rk_download_contributions(rk_ctx* x, double* f, double* mi, double* mj) {
+  if (!x) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  Scene& s = c.s;
+  if (s.ne == 0) return RK_OK;
+  const size_t d3 = 3 * (size_t)s.ne * sizeof(double);
+  if (f) CK(cudaMemcpyAsync(f, s.cf, d3, cudaMemcpyDeviceToHost, c.stream));
+  if (mi) CK(cudaMemcpyAsync(mi, s.cmi, d3, cudaMemcpyDeviceToHost, c.stream));
+  if (mj) CK(cudaMemcpyAsync(mj, s.cmj, d3, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return RK_OK;
+}
+
 int rk_download_entries(rk_ctx* x, int32_t* i, int32_t* j, int32_t* type, int32_t* isub, int32_t* jsub, double* dn,
                         double* fn, double* ft, double* mom, double* damp, int32_t* bond, uint8_t* active, double* n,
                         double* pos, double* vel) {

@@ -383,6 +383,7 @@ bool Rockable::parse(std::istream& conf) {  // Rockable.cpp:643-1069
         for (auto& b : bonds) conf >> b[0] >> b[1] >> b[2];
         F.i.push_back(bi); F.j.push_back(bj); F.nbonds.push_back((int)nbonds); F.dn0.push_back(dn0);
         F.params.insert(F.params.end(), par, par + 8); F.is_inner.push_back(1); F.bonds.push_back(bonds);
+        F.live.emplace_back(bonds.size(), 1);
       }
     } else if (tok == "stickVerticesInClusters") {
       double eps; conf >> eps;
@@ -485,11 +486,16 @@ void Rockable::stickVerticesInClusters(double eps) {
               F.params.insert(F.params.end(), par, par + 8);
               F.is_inner.push_back(1);
               F.bonds.emplace_back();
+              F.live.emplace_back();
             } else {
               fk = it->second;
             }
             int isub = (int)(iv - ofs[i]), jsub = (int)(jv - ofs[j]);
             F.bonds[fk].push_back({0, isub, jsub});
+            // PreproCommand_stickVerticesInClusters.cpp:127-133: the bonded
+            // interaction goes into a std::set, where an existing one with
+            // the same key stays as it was (without the bond)
+            F.live[fk].push_back(entry_of.count({(int64_t)i, (int64_t)j, 0, isub, jsub}) ? 0 : 1);
             F.nbonds[fk]++;
             newkeys.push_back({(int64_t)i, (int64_t)j, 0, isub, jsub});
           }
@@ -677,7 +683,7 @@ bool Rockable::upload() {
   for (size_t k : order) {
     Fs.i.push_back(F.i[k]); Fs.j.push_back(F.j[k]); Fs.nbonds.push_back(F.nbonds[k]); Fs.dn0.push_back(F.dn0[k]);
     Fs.params.insert(Fs.params.end(), F.params.begin() + 8 * k, F.params.begin() + 8 * k + 8);
-    Fs.is_inner.push_back(F.is_inner[k]); Fs.bonds.push_back(F.bonds[k]);
+    Fs.is_inner.push_back(F.is_inner[k]); Fs.bonds.push_back(F.bonds[k]); Fs.live.push_back(F.live[k]);
   }
   F = Fs;
   // entries sorted by key
@@ -699,7 +705,9 @@ bool Rockable::upload() {
   std::map<std::array<int64_t, 5>, size_t> pos_of;
   for (size_t k = 0; k < I.size(); k++) pos_of[key(k)] = k;
   for (size_t f = 0; f < F.i.size(); f++)
-    for (auto& b : F.bonds[f]) {
+    for (size_t q = 0; q < F.bonds[f].size(); q++) {
+      if (q < F.live[f].size() && !F.live[f][q]) continue;  // an interaction that kept no bond
+      const auto& b = F.bonds[f][q];
       auto it = pos_of.find({F.i[f], F.j[f], b[0], b[1], b[2]});
       if (it != pos_of.end()) I.bond[it->second] = (int32_t)f;
     }

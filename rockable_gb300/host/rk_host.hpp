@@ -125,6 +125,10 @@ struct Interfaces {  // BreakableInterface.hpp:48-77
   std::vector<int32_t> i, j, nbonds, is_inner;
   std::vector<double> dn0, params;  // params: 8 per interface
   std::vector<std::vector<std::array<int32_t, 3>>> bonds;  // (type, isub, jsub)
+  // per bond: 1 when it holds its interaction (stick set), 0 when the
+  // interaction existed before stickVerticesInClusters made the bond: the
+  // reference's set insert then keeps the old, unbonded interaction
+  std::vector<std::vector<uint8_t>> live;
   std::vector<uint8_t> broken;
 };
 

@@ -462,7 +462,7 @@ def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2
 
 
 def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=2700.0, kn=1e6, kt=1e6, en2=0.25,
-                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=1e5, size=(0.01, 0.03), tries=16):
+                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=None, size=(0.01, 0.03), tries=16):
     """Dense isotropic compression: n hull grains (8-20 vertices, diameters
     uniform in `size`, 1-3 cm: ratio 1:3, by homothety of a library of
     shapes of about 1 cm; at kn = 1e6 N/m and dt = 1e-6 s even the smallest
@@ -472,7 +472,9 @@ def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=27
     tritriIsostaticCompression servo at `pressure` (DrivingSystem.cpp:
     242-268: the min walls are held, the max walls pushed with pressure x
     their face area); no gravity.  The grains touch but carry no load: the
-    servo loads them."""
+    servo loads them.  The walls have the grains' density by default: heavy
+    walls, pushed at the servo's force across the loose top layer, gather a
+    momentum that crushes the first grains they meet."""
     rng = np.random.default_rng(seed)
     lib = [hull_shape(rng, "G%05d" % k, semi_lo=0.004, semi_hi=0.006) for k in range(nshapes)]
     shape_of = rng.integers(0, nshapes, n)

@@ -222,6 +222,8 @@ def per_result_errors(g0, g64, gm, n_driven):
       fn, ft   per active entry, |mixed - fp64| / max(|fp64|, 1e-6 x the
                step's median |fn|) (the floor keeps a contact that has just
                touched, with a force near zero, from dominating);
+      Mi, Mj   per active entry, the moment terms on i and on j, relative
+               in the same way (floor 1e-6 x the median |M|);
       force,   per free body, |mixed - fp64| / the sum of the magnitudes of
       moment   the body's active contact forces (its own force scale: a body
                near equilibrium has a small net force);
@@ -251,21 +253,33 @@ def per_result_errors(g0, g64, gm, n_driven):
         step = np.linalg.norm(b64[k][free] - g0[k][free], axis=1)
         out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1) / np.maximum(step, 1e-15)
     out["fn"], out["ft"] = fn_err, ft_err
+    (_, mi64, mj64), (_, mim, mjm) = g64.contributions(), gm.contributions()
+    for k, a64, am in [("Mi", mi64, mim), ("Mj", mj64, mjm)]:
+        m = np.linalg.norm(a64[both], axis=1)
+        fl = 1e-6 * float(np.median(m)) if len(m) else 1.0
+        out[k] = np.linalg.norm(am[both] - a64[both], axis=1) / np.maximum(m, max(fl, 1e-300))
     return {k: {"max": float(v.max()) if len(v) else 0.0, "p999": float(np.percentile(v, 99.9)) if len(v) else 0.0,
                 "within_1e-4": float(np.mean(v <= 1e-4)) if len(v) else 1.0, "n": int(len(v))}
             for k, v in out.items()}
 
 
 def test_mixed_per_result_relative_errors_settled_column(gpu_lib):
-    """One step from a settled, contact-rich column in both forms: per-result
-    relative errors (per_result_errors).  The normal and tangential forces of
-    99.9 % of the active contacts, the body resultants (relative to the body's
-    own contact forces) and the step's motion agree within 1e-4."""
+    """One step from a settled, contact-rich column in both forms (the dense
+    pile settled by gravity between walls for 20000 steps, scenes.loaded, and
+    released): per-result relative errors (per_result_errors).  The normal
+    and tangential forces and the moment terms of 99.9 % of the active
+    contacts, the body resultants (relative to the body's own contact
+    forces) and the step's motion agree within 1e-4."""
     from rockable_gb300 import scenes
-    from rockable_gb300.abi import RK_FORM_FP64, RK_FORM_MIXED
-    scene = scenes.column_collapse(n=3000, nshapes=128, semi=(0.0025, 0.0075))
-    gs = scenes.settle(scene, steps=2000)
-    gs.step(50)
+    from rockable_gb300.abi import GpuScene, RK_FORM_FP64, RK_FORM_MIXED
+    scene = scenes.column_collapse(n=3000, nshapes=128, semi=(0.0025, 0.0075), column=(0.2, 0.2, 1.5), walls=True)
+    src = scenes.loaded(scene, 20000)
+    gs = GpuScene(form=RK_FORM_FP64)
+    gs.upload_shapes(src["shape_tables"])
+    gs.upload_bodies(src["bodies"], src["n_driven"])
+    scenes.set_scene_params(gs, src)
+    gs.upload_entries(src["entries"])
+    scene = src
     g64 = clone(gs, scene, RK_FORM_FP64)
     gm = clone(gs, scene, RK_FORM_MIXED)
     g64.update_nl()
@@ -276,7 +290,7 @@ def test_mixed_per_result_relative_errors_settled_column(gpu_lib):
     r = per_result_errors(before, g64, gm, scene["n_driven"])
     print("per-result relative errors:", r)
     assert r["fn"]["n"] > 1000
-    for k in ["fn", "ft", "force", "moment", "pos", "Q"]:
+    for k in ["fn", "ft", "Mi", "Mj", "force", "moment", "pos", "Q"]:
         assert r[k]["p999"] <= 1e-4, (k, r[k])
 
 
