@@ -95,6 +95,17 @@ def parse():
 
 
 # ------------------------------------------------------------------ host --
+def guarded(fn, *args):
+    """A secondary workload of the bench line: its failure is reported in
+    its own object (with the error) instead of losing the headline line."""
+    try:
+        return fn(*args)
+    except Exception as ex:  # the engine's RkError, a memory limit, ...
+        import traceback
+        traceback.print_exc()
+        return {"error": "%s: %s" % (type(ex).__name__, ex)}
+
+
 def cu_profiler(on):
     """cuProfilerStart / cuProfilerStop (CUDA driver API) on the current
     context: the window a profiler started with --profile-from-start off
@@ -692,9 +703,9 @@ def main():
     roof = roofline(head, scene, consts, fp64)
     e2e = None if a.no_e2e else e2e_leg(g, scene, a, dist, ws, a.steps)
     g.close()
-    iso = iso_workload(a, dev, dist, ws, order) if (a.iso_n > 0 and rank == 0) else None
-    rockfall = rockfall_workload(a, dev) if (rank == 0 and a.rock_clusters > 0) else None
-    batched = batched_workload(a, dev) if (rank == 0 and a.batch_scenes > 0) else None
+    iso = guarded(iso_workload, a, dev, dist, ws, order) if (a.iso_n > 0 and rank == 0) else None
+    rockfall = guarded(rockfall_workload, a, dev) if (rank == 0 and a.rock_clusters > 0) else None
+    batched = guarded(batched_workload, a, dev) if (rank == 0 and a.batch_scenes > 0) else None
     cpu = cpu_settled = None
     if rank == 0 and not a.no_cpu:
         # the reference arm's state (the packed column at t = 0, no walls),

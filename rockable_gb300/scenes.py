@@ -788,6 +788,7 @@ def loaded(scene, steps, device=0, damping=0.5, form=1, dt_factor=1.0, rebuild_s
     grains touch but carry no load and are not in rotational balance: here
     they load their contacts, topple into place and come to rest.  Then the
     walls listed in scene["walls"] are removed (the start of a collapse).
+    A servo's pressure is ramped up over the first 60 % of the steps.
     The stiffnesses never change, so the contact forces carried over (with
     their history, "entries") hold the load without the damping.  Returns
     the new scene and a "load" record (steps, damping, simulated time,
@@ -814,8 +815,16 @@ def loaded(scene, steps, device=0, damping=0.5, form=1, dt_factor=1.0, rebuild_s
     done = 0
     nfree = len(scene["bodies"]["mass"]) - scene["n_driven"]
     trace = []
+    sv = scene.get("servo")
     while done < steps:
         k = min(chunk, steps - done)
+        if sv is not None and c is not None:
+            # the servo's pressure raised linearly over the first 60 % of the
+            # steps: the full pressure on a loose, rough top layer would push
+            # the walls deep into its few highest grains
+            ramp = dict(sv)
+            ramp["pressure"] = sv["pressure"] * min(1.0, (done + k) / (0.6 * steps))
+            g.set_controls(c["type"], c["body"], c["value"], c["vec"], ramp)
         g.step(k)
         done += k
         st = g.stats()

@@ -32,7 +32,11 @@ def clone(g_src, scene, form):
     return g
 
 
-def force_errors(g64, gm):
+def force_errors(g64, gm, n_driven=0):
+    """Largest errors of the step's contact forces and of the free bodies'
+    resultants, over the step's largest contact normal force (the driven
+    bodies' resultants, sums of thousands of FP32-rounded terms that feed no
+    state, are reported apart)."""
     e64, em = g64.entries(), gm.entries()
     assert len(e64["i"]) == len(em["i"])
     act = e64["active"]
@@ -42,8 +46,11 @@ def force_errors(g64, gm):
     err_fn = float(np.max(np.abs(e64["fn"][both] - em["fn"][both]))) / fmax if both.any() else 0.0
     err_ft = float(np.max(np.abs(e64["ft"][both] - em["ft"][both]))) / fmax if both.any() else 0.0
     b64, bm = g64.bodies(), gm.bodies()
-    err_F = float(np.max(np.abs(b64["force"] - bm["force"]))) / fmax
-    return {"flips": flips, "active": int(act.sum()), "fn": err_fn, "ft": err_ft, "F": err_F, "fmax": fmax}
+    dF = np.abs(b64["force"] - bm["force"]).max(axis=1)
+    err_F = float(dF[n_driven:].max()) / fmax
+    err_Fd = float(dF[:n_driven].max()) / fmax if n_driven else 0.0
+    return {"flips": flips, "active": int(act.sum()), "fn": err_fn, "ft": err_ft, "F": err_F, "F_driven": err_Fd,
+            "fmax": fmax}
 
 
 def test_mixed_one_step_518_friction(golden_dir, oracle_lib, gpu_lib):
@@ -78,7 +85,7 @@ def test_mixed_one_step_settled_column(gpu_lib):
     gm.update_nl()
     g64.step(1)
     gm.step(1)
-    r = force_errors(g64, gm)
+    r = force_errors(g64, gm, scene["n_driven"])
     print("column one step:", r)
     assert r["active"] > 1000
     assert r["flips"] <= max(1, r["active"] // 10000)
@@ -216,19 +223,22 @@ def test_mixed_free_flight_tracks_fp64():
     assert unit <= 1e-14
 
 
-def per_result_errors(g0, g64, gm, n_driven):
+def per_result_errors(g0, g64, gm, n_driven, bound):
     """Per-result relative errors of the mixed form against the FP64 form
     after one step from the same state (g0: the bodies before it):
       fn, ft   per active entry, |mixed - fp64| / max(|fp64|, 1e-6 x the
                step's median |fn|) (the floor keeps a contact that has just
                touched, with a force near zero, from dominating);
-      Mi, Mj   per active entry, the moment terms on i and on j, relative
-               in the same way (floor 1e-6 x the median |M|);
+      Mi, Mj   per active entry, the moment terms on i and on j over the
+               contact's largest possible moment |f| x (the body's bounding
+               radius) (a contact whose force passes near the centre has a
+               small moment that FP32 lever arms resolve only to that scale);
       force,   per free body, |mixed - fp64| / the sum of the magnitudes of
       moment   the body's active contact forces (its own force scale: a body
                near equilibrium has a small net force);
       pos, Q   per free body, |mixed - fp64| / the step's change |fp64 - before|
-               (with a floor of 1e-15).
+               (floors 1e-15 for pos, 1e-12 for Q: the unit quaternion is
+               renormalised every step, at FP64 rounding, 1e-16, of |Q| = 1).
     Returns, per quantity, the largest error, the 99.9th percentile and the
     fraction within 1e-4."""
     e64, em = g64.entries(), gm.entries()
@@ -249,15 +259,15 @@ def per_result_errors(g0, g64, gm, n_driven):
     have = scale[free] > 0
     for k in ["force", "moment"]:
         out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1)[have] / scale[free][have]
-    for k in ["pos", "Q"]:
+    for k, floor_k in [("pos", 1e-15), ("Q", 1e-12)]:
         step = np.linalg.norm(b64[k][free] - g0[k][free], axis=1)
-        out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1) / np.maximum(step, 1e-15)
+        out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1) / np.maximum(step, floor_k)
     out["fn"], out["ft"] = fn_err, ft_err
-    (_, mi64, mj64), (_, mim, mjm) = g64.contributions(), gm.contributions()
-    for k, a64, am in [("Mi", mi64, mim), ("Mj", mj64, mjm)]:
-        m = np.linalg.norm(a64[both], axis=1)
-        fl = 1e-6 * float(np.median(m)) if len(m) else 1.0
-        out[k] = np.linalg.norm(am[both] - a64[both], axis=1) / np.maximum(m, max(fl, 1e-300))
+    (f64, mi64, mj64), (_, mim, mjm) = g64.contributions(), gm.contributions()
+    fmag = np.linalg.norm(f64[both], axis=1)
+    for k, a64, am, owner in [("Mi", mi64, mim, e64["i"]), ("Mj", mj64, mjm, e64["j"])]:
+        scale = np.maximum(fmag * bound[owner[both]], 1e-300)
+        out[k] = np.linalg.norm(am[both] - a64[both], axis=1) / scale
     return {k: {"max": float(v.max()) if len(v) else 0.0, "p999": float(np.percentile(v, 99.9)) if len(v) else 0.0,
                 "within_1e-4": float(np.mean(v <= 1e-4)) if len(v) else 1.0, "n": int(len(v))}
             for k, v in out.items()}
@@ -287,7 +297,8 @@ def test_mixed_per_result_relative_errors_settled_column(gpu_lib):
     before = g64.bodies()
     g64.step(1)
     gm.step(1)
-    r = per_result_errors(before, g64, gm, scene["n_driven"])
+    bound = np.array([scene["shapes"][k]["bound"] for k in scene["bodies"]["shape"]]) * scene["bodies"]["homothety"]
+    r = per_result_errors(before, g64, gm, scene["n_driven"], bound)
     print("per-result relative errors:", r)
     assert r["fn"]["n"] > 1000
     for k in ["fn", "ft", "Mi", "Mj", "force", "moment", "pos", "Q"]:
