@@ -306,6 +306,10 @@ __global__ void k_glob_vertices(Scene s, int only_listed) {
     s.gvr[3 * k] = (float)r.x;
     s.gvr[3 * k + 1] = (float)r.y;
     s.gvr[3 * k + 2] = (float)r.z;
+    if (local == 0) {
+      const V3 p = ld3(s.pos, b);
+      s.posf[b] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)s.rad[b]);
+    }
   }
 }
 

@@ -83,6 +83,8 @@ struct Scene {
   double* gv;        // 3*nvert
   float* gvr;        // 3*nvert: the same vertices relative to their body's centre, in FP32 (the
                      // mixed form's test of clearly separated entries)
+  float4* posf;      // n: body centre rounded to FP32 and its Minkowski radius, written with the
+                     // world vertices (the same test)
   double* bobb;      // 15 per body (placed OBB, not enlarged)
   float* bobbf;      // float copy of bobb
   float* baabb;      // 6 per body: outward-rounded AABB of the OBB enlarged by DVerlet/2

@@ -109,8 +109,14 @@ __global__ void k_drift(Scene s) {
   e = fma(qd.v.y, qd.v.y, e);
   e = fma(qd.v.z, qd.v.z, e);
   const float ef = d2f(e);
-  const float cf = ef * (-0.5f + 0.375f * ef);
-  const double c = f2d(cf);
+  float cf = ef * (-0.5f + 0.375f * ef);
+  double c = f2d(cf);
+  if (!(fabsf(ef) < 1e-3f)) {
+    // a rotation too large for the two-term series (a violent kick): the
+    // exact normalisation, which keeps |Q| = 1 however fast the body spins
+    c = 1.0 / sqrt(1.0 + e) - 1.0;
+    cf = d2f(c);
+  }
   if (s.sk_path) {
     // learned-skin path bound (as in rk_body.cuh's k_drift): |dx| plus the
     // rotation bound 2ch(1 + ch) of the chord ch = |q_new - q| <= |dq| + |c| |qd|
@@ -145,21 +151,25 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
   const bool free_body = inb && b >= s.n_driven;
   const int hv = inb ? (int)s.is_heavy[b] : 1;
   const bool group_sum = free_body && (hv == 0 || hv == 3);
-  double a[6] = {0, 0, 0, 0, 0, 0};
+  // FP32 sums: the contributions were computed in FP32 (the narrow phase
+  // stores them widened, so the narrowing back is exact), and a sum of a
+  // body's few dozen terms in FP32 errs by less than their own rounding
+  // adds up to; the FP64 pipe, GB300's scarcest, stays free
+  float a[6] = {0, 0, 0, 0, 0, 0};
   if (group_sum) {
     const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1], j0 = s.jofs[b], j1 = s.jofs[b + 1];
     for (int64_t e = i0 + l; e < i1; e += kGatherLanes) {
       if (!s.act[e]) continue;
       const V3 f = ld3(s.cf, e), m = ld3(s.cmi, e);
-      a[0] += f.x; a[1] += f.y; a[2] += f.z;
-      a[3] += m.x; a[4] += m.y; a[5] += m.z;
+      a[0] += d2f(f.x); a[1] += d2f(f.y); a[2] += d2f(f.z);
+      a[3] += d2f(m.x); a[4] += d2f(m.y); a[5] += d2f(m.z);
     }
     for (int64_t p = j0 + l; p < j1; p += kGatherLanes) {
       const int64_t e = s.jlist[p];
       if (!s.act[e]) continue;
       const V3 f = ld3(s.cf, e), m = ld3(s.cmj, e);
-      a[0] -= f.x; a[1] -= f.y; a[2] -= f.z;
-      a[3] += m.x; a[4] += m.y; a[5] += m.z;
+      a[0] -= d2f(f.x); a[1] -= d2f(f.y); a[2] -= d2f(f.z);
+      a[3] += d2f(m.x); a[4] += d2f(m.y); a[5] += d2f(m.z);
     }
   }
 #pragma unroll
@@ -172,8 +182,8 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
       V3 F, M;
       if (group_sum) {
         init_resultant(s, b, F, M);
-        F = F + v3(a[0], a[1], a[2]);
-        M = M + v3(a[3], a[4], a[5]);
+        F = F + v3(f2d(a[0]), f2d(a[1]), f2d(a[2]));
+        M = M + v3(f2d(a[3]), f2d(a[4]), f2d(a[5]));
       } else {  // summed by k_gather_heavy
         F = ld3(s.force, b);
         M = ld3(s.moment, b);

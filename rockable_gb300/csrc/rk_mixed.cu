@@ -65,19 +65,27 @@ __device__ __forceinline__ double len64(V3 d, double& inv) {
 __device__ __forceinline__ F3 ldgvr(const float* g, int64_t k) { return f3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
 __device__ __forceinline__ float amax(F3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
 
-// Whether an entry is clearly apart, from FP32 geometry alone: its
-// sub-elements' vertices relative to body j's centre (the FP32 offsets gvr,
-// plus the FP64 difference of the two centres rounded once), the same
-// projection parameters as the FP64 path, and the separation's length.  The
-// overlap estimate dnf errs by a few ulps of the coordinates (below 1e-7 of
-// their magnitude), so an estimate above a margin of 2e-6 m plus 2e-6 of the
-// coordinates' magnitude proves dn > 0: the FP64 length, the contact point
-// and everything after are skipped, and dnf is kept as the entry's dn (a
-// separated entry's dn only matters through its sign).  When the projection
-// falls outside the edge or face, or a vertex-face contact's face is not a
-// triangle, the FP64 path decides.
-__device__ __forceinline__ bool apart_f32(const Scene& s, int type, int i, int j, int isub, int jsub, bool pre,
-                                          int4 G, F3 dxij, float rsum, float* dnf) {
+// What FP32 geometry alone proves about an entry: its sub-elements'
+// vertices relative to body j's centre (the FP32 offsets gvr, plus the
+// difference of the two centres rounded to FP32, posf), the same projection
+// parameters as the FP64 path, and the separation's length.
+//   kApart    the overlap estimate dnf errs by a few ulps of the coordinates
+//             (relative ones, and the centres' absolute ones: `cmag`), so an
+//             estimate above a margin of 2e-6 m plus 2e-6 of the relative
+//             coordinates' magnitude plus 4e-7 of the centres' proves dn > 0:
+//             the FP64 length, the contact point and everything after are
+//             skipped, and dnf is kept as the entry's dn (a separated entry's
+//             dn only matters through its sign);
+//   kOutside  the vertex-edge projection parameter or the edge-edge closest-
+//             point parameters lie outside their segment by more than their
+//             rounding error (bounded the same way, over the segments'
+//             lengths): the FP64 path would find the same (it takes these
+//             parameters in FP32 too) and drop the sub-contact;
+//   0         the FP64 path decides (near the thresholds, other polygons than
+//             triangles, nearly parallel edges).
+constexpr int kApart = 1, kOutside = 2;
+__device__ __forceinline__ int apart_f32(const Scene& s, int type, int i, int j, int isub, int jsub, bool pre,
+                                         int4 G, F3 dxij, float rsum, float cmag, float* dnf) {
   const float* g = s.gvr;
   auto gi = [&](int local) { return (int64_t)s.gv_ofs[i] + local; };
   auto gj = [&](int local) { return (int64_t)s.gv_ofs[j] + local; };
@@ -97,12 +105,17 @@ __device__ __forceinline__ bool apart_f32(const Scene& s, int type, int i, int j
     }
     const F3 a = ldgvr(g, pre ? G.x : gi(isub)) + dxij, p1 = ldgvr(g, k1), p2 = ldgvr(g, k2);
     const F3 E = p2 - p1, w = a - p1;
-    const float r = dotf(w, E) / dotf(E, E);
-    if (r <= 0.f || r >= 1.f) return false;
-    d = w - r * E;
+    const float E2 = dotf(E, E);
+    const float r = dotf(w, E) / E2;
     mag = fmaxf(amax(a), fmaxf(amax(p1), amax(p2)));
+    if (r <= 0.f || r >= 1.f) {
+      // r's error: that of w and E (a few ulps of the coordinates) over |E|
+      const float tol = 1e-5f + 4e-7f * (mag + cmag) * rsqrtf(E2) * (1.f + fabsf(r));
+      return (r < -tol || r > 1.f + tol) ? kOutside : 0;
+    }
+    d = w - r * E;
   } else if (type == 2) {
-    if (!(pre && G.w >= 0)) return false;  // polygons other than triangles: the FP64 path
+    if (!(pre && G.w >= 0)) return 0;  // polygons other than triangles: the FP64 path
     const F3 a = ldgvr(g, G.x) + dxij, A = ldgvr(g, G.y), B = ldgvr(g, G.z), C = ldgvr(g, G.w);
     const F3 bA = B - A, cA = C - A, w = a - A;
     F3 nn = crossf(bA, cA);
@@ -124,10 +137,10 @@ __device__ __forceinline__ bool apart_f32(const Scene& s, int type, int i, int j
     edge(z, bA);
     edge(bA, cA);
     edge(cA, z);
-    if (!odd) return false;
+    if (!odd) return 0;
     mag = fmaxf(amax(a), fmaxf(amax(A), fmaxf(amax(B), amax(C))));
     *dnf = dist - rsum;
-    return *dnf > 2e-6f + 2e-6f * mag;
+    return *dnf > 2e-6f + 2e-6f * mag + 4e-7f * cmag ? kApart : 0;
   } else {
     int64_t a1, a2, b1, b2;
     if (pre) { a1 = G.x; a2 = G.y; b1 = G.z; b2 = G.w; }
@@ -140,16 +153,23 @@ __device__ __forceinline__ bool apart_f32(const Scene& s, int type, int i, int j
     const F3 Ei = pi2 - pi1, Ej = pj2 - pj1, w = pi1 - pj1;
     const float c = dotf(Ei, Ei), dd = dotf(Ej, Ej), ee = dotf(Ei, Ej);
     float f = (c * dd) - (ee * ee);
-    if (fabsf(f) <= 1.0e-12f) return false;
+    if (fabsf(f) <= 1.0e-12f) return 0;
     f = 1.0f / f;
     const float a = dotf(Ei, w), b = dotf(Ej, w);
     const float ss = (ee * b - a * dd) * f, tt = (c * b - ee * a) * f;
-    if (ss <= 0.f || ss >= 1.f || tt <= 0.f || tt >= 1.f) return false;
-    d = (w + ss * Ei) - tt * Ej;
     mag = fmaxf(fmaxf(amax(pi1), amax(pi2)), fmaxf(amax(pj1), amax(pj2)));
+    if (ss <= 0.f || ss >= 1.f || tt <= 0.f || tt >= 1.f) {
+      // well-conditioned pairs only (the sine of the edges' angle above
+      // 0.1): the parameters' error is then a few ulps of the coordinates
+      // over the shorter edge, amplified by at most 100 by the solve
+      if (!(f * c * dd < 100.f)) return 0;
+      const float tol = 1e-5f + 4e-5f * (mag + cmag) * rsqrtf(fminf(c, dd)) * (1.f + fabsf(ss) + fabsf(tt));
+      return (ss < -tol || ss > 1.f + tol || tt < -tol || tt > 1.f + tol) ? kOutside : 0;
+    }
+    d = (w + ss * Ei) - tt * Ej;
   }
   *dnf = sqrtf(dotf(d, d)) - rsum;
-  return *dnf > 2e-6f + 2e-6f * mag;
+  return *dnf > 2e-6f + 2e-6f * mag + 4e-7f * cmag ? kApart : 0;
 }
 
 __global__ void k_narrow_force_mixed(Scene s) {
@@ -174,15 +194,21 @@ __global__ void k_narrow_force_mixed(Scene s) {
     double dn = 0.0;
     F3 n = f3(0, 0, 0), ci = f3(0, 0, 0);  // normal, contact point relative to x_i
     bool ok = true;
-    // clearly apart (and nothing else needed of it): FP32 alone decides
-    bool quick = false;
+    // clearly apart, or its projection clearly outside (and nothing else
+    // needed of it): FP32 alone decides
+    int quick = 0;
     if (bond < 0 && !s.record_geom && s.gvr) {
       float dnf = 0.f;
-      quick = apart_f32(s, type, i, j, isub, jsub, pre, G, tof(xi - xj), d2f(Ri + Rj), &dnf);
-      if (quick) dn = f2d(dnf);
+      const float4 pi = s.posf[i], pj = s.posf[j];
+      const F3 dxij = f3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+      const float cmag = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fmaxf(fabsf(pi.z), fmaxf(fabsf(pj.x),
+                         fmaxf(fabsf(pj.y), fabsf(pj.z)))));
+      quick = apart_f32(s, type, i, j, isub, jsub, pre, G, dxij, pi.w + pj.w, cmag, &dnf);
+      if (quick == kApart) dn = f2d(dnf);
+      else if (quick == kOutside) ok = false;
     }
     if (quick) {
-      // dn > 0 proven: separated, history untouched
+      // dn > 0 proven (separated, history untouched), or the sub-contact lost
     } else if (type == 0) {
       V3 a, b;
       if (pre) {
@@ -328,8 +354,9 @@ __global__ void k_narrow_force_mixed(Scene s) {
     }
     // a separated entry (no bond) keeps only its dn: the relative velocity,
     // the history and the law are skipped unless its geometry is recorded;
-    // a lost sub-contact restarts its history from zero
-    if (!ok) dn = 0.0;
+    // a lost sub-contact restarts its history from zero (its dn stored as
+    // -0.0: "lost, history zeroed", which the next step need not rewrite)
+    if (!ok) dn = -0.0;
     active = (dn < 0.0 || bond >= 0);
     double fn = 0.0;
     F3 ft = f3(0, 0, 0), mom = f3(0, 0, 0);
@@ -439,11 +466,18 @@ __global__ void k_narrow_force_mixed(Scene s) {
         st3m(s.cmj, e, crossf(cj, -f) - mom);
       }
     }
-    s.dn[e] = dn;
-    if (active || !ok) {
-      s.fn[e] = fn;
-      st3m(s.ft, e, ft);
-      st3m(s.mom, e, mom);
+    // stores that change nothing are skipped: a separated entry that was
+    // separated already (only dn's sign is used), a lost sub-contact that was
+    // lost already (dn -0.0, history zero); bonded entries always store
+    const bool lost_before = __double_as_longlong(dn_old) == (long long)0x8000000000000000ull;
+    const bool same = bond < 0 && ((quick == kApart && dn_old > 0.0) || (!ok && lost_before));
+    if (!same) {
+      s.dn[e] = dn;
+      if (active || !ok) {
+        s.fn[e] = fn;
+        st3m(s.ft, e, ft);
+        st3m(s.mom, e, mom);
+      }
     }
     s.act[e] = active ? 1 : 0;
   }

