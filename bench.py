@@ -472,13 +472,20 @@ def roofline(rec, scene, consts, fp64):
     return out
 
 
-def e2e_leg(g, scene, a, dist, ws, steps):
-    """The headline form through the C ABI with host-owned state: every bench
-    step uploads the kinematics (pos, vel, acc, Q, vrot, arot: 152 B per
-    body) from one pinned buffer, runs rk_step(segment) and downloads them
-    back (rk_upload/download_kinematics_packed)."""
+def e2e_leg(scene, label, a, dev, dist, ws, steps):
+    """The headline form through the C ABI with host-owned state, from the
+    same state and after the same tuning and warm-up steps as the timed leg
+    (a context of its own): every bench step uploads the kinematics (pos,
+    vel, acc, Q, vrot, arot: 152 B per body) from one pinned buffer, runs
+    rk_step(segment) and downloads them back (rk_upload/download_kinematics_
+    packed)."""
     N = len(scene["bodies"]["mass"])
     nfree = N - scene["n_driven"]
+    g = engine(scene, label, dev, SKIN[label])
+    g.autotune(2)
+    g.step(TUNE_STEPS)
+    if a.warmup:
+        g.step(a.warmup * a.segment)
     hb = pinned((19 * N,))
     g.download_kinematics_packed(hb)
     g.synchronize()
@@ -491,6 +498,7 @@ def e2e_leg(g, scene, a, dist, ws, steps):
         rebuilds += int(g.step(a.segment)["nl_updates"])
         g.download_kinematics_packed(hb)
     el = rank_max(time.perf_counter() - t0, dist)
+    g.close()
     return {"value": job_rate(ws, nfree, steps * a.segment, 1000.0 * el), "unit": "particle-steps/s",
             "h2d_bytes_per_step": int(N * 19 * 8), "d2h_bytes_per_step": int(N * 19 * 8), "steps": steps,
             "nl_rebuilds": rebuilds,
@@ -597,7 +605,7 @@ def batched_workload(a, dev):
         prof = e.profile()
         sk = e.skin_stats() if SKIN[label] else None
         e.close()
-        kernels_ms = sum(w[0] for q, w in prof.items() if q != "nl_rebuild") / a.batch_steps
+        kernels_ms = sum(w[0] for q, w in prof.items()) / a.batch_steps
         solo = []
         for k in range(len(bt["free_per_scene"])):
             p = engine(scenes.part_of(src, k), label, dev, SKIN[label])
@@ -623,9 +631,10 @@ def batched_workload(a, dev):
     out["headline_vs_plain"] = head["value"] / out["forms"]["plain_fp64"]["value"]
     pl = out["forms"]["plain_fp64"]
     out["persistent_kernel_bound"] = (
-        "graph replay: %.4f ms per step for step kernels timing %.4f ms launch by launch (plain FP64, rebuild "
-        "steps excluded from the latter): a persistent kernel could remove at most the difference" % (
-            pl["ms_per_step"], pl["step_kernels_ms_per_step"]))
+        "plain FP64: graph replay %.4f ms per step; the same kernels event-timed one phase at a time (launch by "
+        "launch, the same number of steps and rebuilds) %.4f ms per step: a persistent kernel could remove at "
+        "most the launch gaps left in the replay, max(0, %.4f) ms per step" % (
+            pl["ms_per_step"], pl["step_kernels_ms_per_step"], pl["ms_per_step"] - pl["step_kernels_ms_per_step"]))
     return out
 
 
@@ -689,20 +698,15 @@ def main():
     nfree = N - scene["n_driven"]
     order = [f.strip() for f in a.forms.split(",") if f.strip()]
     forms = {}
-    g = None
     for label in order:
         e, rec = time_form(scene, label, a, dev, dist, ws, a.steps, a.warmup)
         forms[label] = rec
-        if label == order[-1]:
-            g = e
-        else:
-            e.close()
+        e.close()
     head = forms[order[-1]]
     consts = profile_constants()
     fp64 = fp64_peak() if rank == 0 else None
     roof = roofline(head, scene, consts, fp64)
-    e2e = None if a.no_e2e else e2e_leg(g, scene, a, dist, ws, a.steps)
-    g.close()
+    e2e = None if a.no_e2e else e2e_leg(scene, order[-1], a, dev, dist, ws, a.steps)
     iso = guarded(iso_workload, a, dev, dist, ws, order) if (a.iso_n > 0 and rank == 0) else None
     rockfall = guarded(rockfall_workload, a, dev) if (rank == 0 and a.rock_clusters > 0) else None
     batched = guarded(batched_workload, a, dev) if (rank == 0 and a.batch_scenes > 0) else None
