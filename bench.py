@@ -74,8 +74,8 @@ def parse():
     ap.add_argument("--n", type=int, default=50000, help="grains of the column")
     ap.add_argument("--load-steps", type=int, default=50000,
                     help="damped DEM steps (2 x dt: 0.1 s) that settle the column between walls before the release")
-    ap.add_argument("--iso-load-steps", type=int, default=30000,
-                    help="damped DEM steps (2 x dt: 0.06 s) of servo compression before the box is timed")
+    ap.add_argument("--iso-load-steps", type=int, default=40000,
+                    help="damped DEM steps (0.02 s) of servo compression before the box is timed")
     ap.add_argument("--forms", default="plain_fp64,mixed,mixed_learned_skin_exact",
                     help="comma list of the forms to time (the last one is the headline)")
     ap.add_argument("--iso-n", type=int, default=200000, help="grains of the compression box (0: skip)")
@@ -646,7 +646,7 @@ def iso_workload(a, dev, dist, ws, order):
     packed = scenes.iso_compression(n=a.iso_n)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
-    sc = scenes.loaded(packed, a.iso_load_steps, device=dev, dt_factor=2.0)
+    sc = scenes.loaded(packed, a.iso_load_steps, device=dev)
     t_load = time.perf_counter() - t0
     nfree = len(sc["bodies"]["mass"]) - sc["n_driven"]
     steps = max(2, a.steps // 4)
@@ -659,8 +659,8 @@ def iso_workload(a, dev, dist, ws, order):
     out = {"workload": sc["name"], "bodies": len(sc["bodies"]["mass"]), "free_bodies": nfree,
            "law": sc["law"], "servo": "tritriIsostaticCompression at %g Pa, no gravity" % sc["servo"]["pressure"],
            "pack": sc["pack"], "load": sc["load"],
-           "state": ("the packed box after %d DEM steps (2 x dt) of servo compression with numerical damping "
-                     "0.5 (scenes.loaded)" % a.iso_load_steps),
+           "state": ("the packed box after %d DEM steps of servo compression with numerical damping 0.5 "
+                     "(scenes.loaded)" % a.iso_load_steps),
            "dem_steps_per_step": a.segment, "steps": steps, "warmup": 1,
            "forms": forms, "headline_form": order[-1],
            "headline_vs_plain": head["value"] / forms["plain_fp64"]["value"],

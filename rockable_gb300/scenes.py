@@ -462,11 +462,11 @@ def column_collapse(n=50000, seed=SEED, nshapes=4096, law="Avalanche", density=2
 
 
 def iso_compression(n=200000, seed=SEED, nshapes=4096, law="Default", density=2700.0, kn=1e6, kt=1e6, en2=0.25,
-                    mu=0.4, dt=1e-6, pressure=1e5, wall_density=None, size=(0.01, 0.03), tries=16):
+                    mu=0.4, dt=5e-7, pressure=1e5, wall_density=None, size=(0.01, 0.03), tries=16):
     """Dense isotropic compression: n hull grains (8-20 vertices, diameters
     uniform in `size`, 1-3 cm: ratio 1:3, by homothety of a library of
-    shapes of about 1 cm; at kn = 1e6 N/m and dt = 1e-6 s even the smallest
-    elongated grain rotates stably under several contacts), packed (pack(), the lowest of `tries` drop sites per grain)
+    shapes of about 1 cm; dt = 5e-7 s: at 1e-6 s the smallest grains of the
+    top layer, squeezed by the incoming walls, spin up without bound), packed (pack(), the lowest of `tries` drop sites per grain)
     in a box about as high as wide, then enclosed by six rigid walls (bodies
     0-5: Xmin, Xmax, Ymin, Ymax, Zmin, Zmax) driven by Rockable's
     tritriIsostaticCompression servo at `pressure` (DrivingSystem.cpp:
