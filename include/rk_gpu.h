@@ -262,6 +262,24 @@ int64_t rk_num_interfaces(const rk_ctx* ctx);
 /* Any output pointer may be NULL. */
 int rk_download_bodies(rk_ctx* ctx, double* pos, double* vel, double* acc, double* Q, double* vrot, double* arot,
                        double* force, double* moment);
+/* The Particles and Interactions sections of a conf file, formatted on the
+ * device as Rockable::saveConf writes them (Rockable.cpp:547-580): one line
+ * per body, "name group cluster homothety pos vel acc Q vrot arot", then one
+ * per entry with dn < 0 or a bond, in key order, "i j type isub jsub n dn pos
+ * vel fn ft mom damp"; every real number as printf("%.*e", precision), the
+ * contact normal rounded toward zero (Rockable.cpp:569-575), fields
+ * separated by one space, lines ended by '\n'.  The section headers
+ * ("Particles N", the "#name ..." comment line, "Interactions M") are the
+ * caller's, with M = *n_active.  The contact geometry (n, pos, vel) is the one
+ * recorded by the last step run with rk_set_record_geometry(1) (and by the
+ * load-time rk_accelerations).  precision in [0, 17].  Writes the bodies'
+ * text then the entries' into buf when cap is large enough (else returns
+ * RK_ERR_CAPACITY), and their lengths in bytes; with buf NULL, only the
+ * lengths.  rk_set_shape_names gives the shape names first (one per
+ * uploaded shape, no spaces). */
+int rk_set_shape_names(rk_ctx* ctx, const char* const* names, int32_t n);
+int rk_format_conf(rk_ctx* ctx, int32_t precision, char* buf, int64_t cap, int64_t* particles_len,
+                   int64_t* interactions_len, int64_t* n_active);
 /* Per-entry terms of the last force evaluation, 3 doubles each per entry in
  * key order: the force on body i (body j receives its opposite) and the
  * moments on i and on j -- the terms Rockable adds into the resultants

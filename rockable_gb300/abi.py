@@ -104,6 +104,9 @@ SIGNATURES = {
     "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
     "rk_set_body_force": (C.c_int, [P, C.c_int, P, C.c_int32, P]),
     "rk_download_contributions": (C.c_int, [P, P, P, P]),
+    "rk_set_shape_names": (C.c_int, [P, C.POINTER(C.c_char_p), C.c_int32]),
+    "rk_format_conf": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int64)]),
     "rk_set_record_geometry": (C.c_int, [P, C.c_int]),
     "rk_set_form": (C.c_int, [P, C.c_int]),
     "rk_set_broadphase": (C.c_int, [P, C.c_int]),
@@ -435,6 +438,22 @@ class GpuScene:
             o.update(g)
         o["active"] = o["active"].astype(bool)
         return o
+
+    def set_shape_names(self, names):
+        arr = (C.c_char_p * max(len(names), 1))(*[n.encode() for n in names])
+        self._chk(self.L.rk_set_shape_names(self.h, arr, len(names)), "rk_set_shape_names")
+
+    def format_conf(self, precision=16):
+        """(Particles lines, Interactions lines, number of the latter) of a
+        conf file, formatted on the device (rk_format_conf)."""
+        lp, li, na = C.c_int64(), C.c_int64(), C.c_int64()
+        self._chk(self.L.rk_format_conf(self.h, precision, None, 0, C.byref(lp), C.byref(li), C.byref(na)),
+                  "rk_format_conf")
+        buf = C.create_string_buffer(lp.value + li.value + 1)
+        self._chk(self.L.rk_format_conf(self.h, precision, buf, lp.value + li.value, C.byref(lp), C.byref(li),
+                                        C.byref(na)), "rk_format_conf")
+        raw = buf.raw[:lp.value + li.value].decode()
+        return raw[:lp.value], raw[lp.value:], na.value
 
     def contributions(self):
         """Per-entry force on i and moments on i and j of the last force

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "rk_conf.cuh"
 #include "rk_ctx.cuh"
 
 using namespace rk;
@@ -850,6 +851,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
   dfree(s.needres); dfree(s.scene_of); dfree(s.bf_surf);
+  dfree(c.name_chars); dfree(c.name_ofs);
   dfree(s.if_i); dfree(s.if_j); dfree(s.if_dn0); dfree(s.if_par); dfree(s.if_inner); dfree(s.if_broken);
   dfree(s.if_break); dfree(s.if_ofs); dfree(s.flags);
   free_entrybuf(c.eb[0]);
@@ -1692,6 +1694,101 @@ __global__ void k_unpack_tsub(const uint32_t* ts, int64_t n, int* t, int* isub, 
   t[e] = tsub_type(ts[e]);
   isub[e] = tsub_isub(ts[e]);
   jsub[e] = tsub_jsub(ts[e]);
+}
+
+int rk_set_shape_names(rk_ctx* x, const char* const* names, int32_t n) {
+  if (!x || n < 0 || (n > 0 && !names)) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_shapes || n != c.s.nshapes) return fail(c, RK_ERR_ARG, "one name per uploaded shape");
+  std::vector<int> ofs(n + 1, 0);
+  std::string all;
+  for (int k = 0; k < n; k++) {
+    if (!names[k]) return fail(c, RK_ERR_ARG, "a shape name is missing");
+    all += names[k];
+    ofs[k + 1] = (int)all.size();
+  }
+  int rc;
+  if ((rc = dupload(c, c.name_chars, all.data(), std::max<int64_t>((int64_t)all.size(), 1))) ||
+      (rc = dupload(c, c.name_ofs, ofs.data(), n + 1)))
+    return rc;
+  CK(cudaStreamSynchronize(c.stream));
+  c.have_names = true;
+  return RK_OK;
+}
+
+int rk_format_conf(rk_ctx* x, int32_t prec, char* buf, int64_t cap, int64_t* particles_len,
+                   int64_t* interactions_len, int64_t* n_active) {
+  if (!x || prec < 0 || prec > 17) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (!c.have_bodies || !c.have_names) return fail(c, RK_ERR_STATE, "upload the bodies and the shape names first");
+  Scene& s = c.s;
+  cudaStream_t st = c.stream;
+  const int64_t nb = s.n, ne = s.ne;
+  // bodies: one slot each, then the active entries: flags, their positions
+  char* slots = nullptr;
+  int64_t *lens = nullptr, *ofs = nullptr, *flag = nullptr;
+  void* tmp = nullptr;
+  char* out = nullptr;
+  int rc = RK_OK;
+  int64_t lp = 0, li = 0, na = 0;
+  auto cleanup = [&]() {
+    dfree(slots); dfree(lens); dfree(ofs); dfree(flag); dfree(out);
+    if (tmp) cudaFree(tmp);
+  };
+  const int64_t nmax = std::max<int64_t>(nb, ne) + 1;
+  if ((rc = dalloc(c, lens, nmax)) || (rc = dalloc(c, ofs, nmax)) || (rc = dalloc(c, flag, ne + 1))) {
+    cleanup();
+    return rc;
+  }
+  if (cudaMalloc(&tmp, scan_temp_bytes(nmax)) != cudaSuccess) {
+    cleanup();
+    return fail(c, RK_ERR_CUDA, "no device memory for the conf text");
+  }
+  if (ne > 0) {
+    k_conf_active<<<nblk(ne, 256), 256, 0, st>>>(s, flag);
+    cudaMemsetAsync(flag + ne, 0, sizeof(int64_t), st);
+    exclusive_scan_i64(flag, flag, ne + 1, tmp, st);
+    cudaMemcpyAsync(&na, flag + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+      cleanup();
+      return fail(c, RK_ERR_CUDA, "conf text: active entries");
+    }
+  }
+  // the two sections, one after the other
+  for (int part = 0; part < 2; part++) {
+    const int64_t nl = part == 0 ? nb : na;
+    const int slot = part == 0 ? kConfBodySlot : kConfEntrySlot;
+    int64_t& len = part == 0 ? lp : li;
+    if (nl == 0) continue;
+    dfree(slots);
+    if ((rc = dalloc(c, slots, nl * (int64_t)slot))) break;
+    if (part == 0) k_conf_bodies<<<nblk(nb, 128), 128, 0, st>>>(s, c.name_chars, c.name_ofs, prec, slots, lens);
+    else k_conf_entries<<<nblk(ne, 128), 128, 0, st>>>(s, flag, prec, slots, lens);
+    cudaMemsetAsync(lens + nl, 0, sizeof(int64_t), st);
+    exclusive_scan_i64(lens, ofs, nl + 1, tmp, st);
+    cudaMemcpyAsync(&len, ofs + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) { rc = fail(c, RK_ERR_CUDA, "conf text: formatting"); break; }
+    const int64_t at = part == 0 ? 0 : lp;
+    if (buf && at + len <= cap) {
+      dfree(out);
+      if ((rc = dalloc(c, out, std::max<int64_t>(len, 1)))) break;
+      k_conf_pack<<<nblk(nl * 32, 256), 256, 0, st>>>(slots, slot, ofs, lens, nl, out);
+      if (cudaMemcpyAsync(buf + at, out, (size_t)len, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess) {
+        rc = fail(c, RK_ERR_CUDA, "conf text: copy");
+        break;
+      }
+    }
+  }
+  cleanup();
+  if (rc) return rc;
+  if (particles_len) *particles_len = lp;
+  if (interactions_len) *interactions_len = li;
+  if (n_active) *n_active = na;
+  if (buf && lp + li > cap) return fail(c, RK_ERR_CAPACITY, "the conf text needs a larger buffer");
+  return RK_OK;
 }
 
 int rk_download_contributions(rk_ctx* x, double* f, double* mi, double* mj) {

@@ -151,6 +151,10 @@ struct Ctx {
   int64_t kin_stage_n = 0;
   std::vector<uint8_t> needres_host;
   int64_t bf_n = 0;  // body count the body force was set for
+  // shape names for the device-formatted conf text (rk_set_shape_names)
+  char* name_chars = nullptr;
+  int* name_ofs = nullptr;
+  bool have_names = false;
   // block-size autotuner of the step kernels (results do not depend on it)
   int64_t tune_left = 0, tune_total = 0;
   double tune_ms[4][5] = {};  // [kernel][candidate block size]

@@ -137,8 +137,24 @@ __device__ __forceinline__ int apart_f32(const Scene& s, int type, int i, int j,
     edge(z, bA);
     edge(bA, cA);
     edge(cA, z);
-    if (!odd) return 0;
     mag = fmaxf(amax(a), fmaxf(amax(A), fmaxf(amax(B), amax(C))));
+    if (!odd) {
+      // the projection clearly outside the triangle: farther than the
+      // rounding of the coordinates beyond one of its edges (in the plane,
+      // on the side away from the third vertex)
+      const float tol = 1e-9f + 1e-6f * (mag + cmag);
+      const F3 Pv = P, cA2 = cA;
+      const float o = dotf(crossf(bA, cA2), nn);  // the triangle's winding about nn
+      if (!(fabsf(o) > 0.f)) return 0;
+      const F3 ed[3] = {bA, cA2 - bA, -cA2};
+      const F3 st[3] = {f3(0, 0, 0), bA, cA2};
+      for (int q = 0; q < 3; q++) {
+        const F3 e = ed[q];
+        const float side = dotf(crossf(e, Pv - st[q]), nn) * rsqrtf(dotf(e, e));
+        if ((o > 0.f ? -side : side) > tol) return kOutside;
+      }
+      return 0;
+    }
     *dnf = dist - rsum;
     return *dnf > 2e-6f + 2e-6f * mag + 4e-7f * cmag ? kApart : 0;
   } else {

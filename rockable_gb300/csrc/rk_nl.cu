@@ -568,6 +568,65 @@ __device__ __forceinline__ bool lines_far(G3 p1, G3 q1, G3 p2, G3 q2, float lim2
   return rn * rn > lim2 * nn;
 }
 
+// Float acceptance in front of the FP64 NEAR predicates (Rockable's, above):
+// from the float world coordinates of the sub-elements (the vertex spheres'
+// centres, rounded to nearest from the FP64 world vertices: errors of a few
+// 1e-8 of the coordinates' magnitude `mag`), each returns true only when the
+// FP64 predicate is true for sure -- its distance within `alim` (the NEAR
+// distance shrunk by the rejection's rounding margin) and its projection
+// parameters or point inside their ranges by more than their rounding error.
+// Otherwise the FP64 predicate decides.
+__device__ __forceinline__ bool accept_vv(G3 a, G3 b, float alim) {
+  const G3 d = gsub(a, b);
+  return alim > 0.f && gdot(d, d) <= alim * alim;
+}
+__device__ __forceinline__ bool accept_ve(G3 p, G3 a, G3 b, float alim, float dmax, float mag) {
+  const G3 E = gsub(b, a), w = gsub(p, a);
+  const float E2 = gdot(E, E);
+  if (!(alim > 0.f) || !(E2 > 0.f)) return false;
+  const float r = gdot(w, E) / E2;
+  const float tol = 1e-5f + 4e-6f * mag * rsqrtf(E2) * (1.f + fabsf(r));
+  if (!(r >= -dmax + tol && r <= 1.f + dmax - tol)) return false;
+  const G3 d = gmad(w, -r, E);
+  return gdot(d, d) <= alim * alim;
+}
+__device__ __forceinline__ bool accept_vf_tri(G3 p, G3 A, G3 B, G3 C, float alim, float mag) {
+  if (!(alim > 0.f)) return false;
+  const G3 bA = gsub(B, A), cA = gsub(C, A), w = gsub(p, A);
+  G3 n = gcross(bA, cA);
+  const float nn = gdot(n, n);
+  if (!(nn > 0.f)) return false;
+  const float inv = rsqrtf(nn);
+  n = {n.x * inv, n.y * inv, n.z * inv};
+  const float dist = gdot(w, n);
+  if (!(fabsf(dist) <= alim)) return false;
+  const G3 P = gmad(w, -dist, n);
+  const float tol = 1e-9f + 1e-6f * mag;
+  const G3 ed[3] = {bA, gsub(cA, bA), {-cA.x, -cA.y, -cA.z}};
+  const G3 st[3] = {{0.f, 0.f, 0.f}, bA, cA};
+  for (int q = 0; q < 3; q++) {  // counter-clockwise about n: inside is to the left of every edge
+    const float side = gdot(gcross(ed[q], gsub(P, st[q])), n) * rsqrtf(gdot(ed[q], ed[q]));
+    if (!(side > tol)) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ bool accept_ee(G3 pi0, G3 pi1, G3 pj0, G3 pj1, float alim, float mag) {
+  if (!(alim > 0.f)) return false;
+  const G3 Ei = gsub(pi1, pi0), Ej = gsub(pj1, pj0), w = gsub(pi0, pj0);
+  const float c = gdot(Ei, Ei), d = gdot(Ej, Ej), e = gdot(Ei, Ej);
+  const float f = c * d - e * e;
+  // well away from the FP64 test's parallel threshold (1e-12) and from
+  // parallel edges (the sine of their angle above 0.1)
+  if (!(f > 2e-12f + 0.01f * c * d)) return false;
+  const float a = gdot(Ei, w), b = gdot(Ej, w);
+  const float fi = 1.f / f;
+  const float ss = (e * b - a * d) * fi, tt = (c * b - e * a) * fi;
+  const float tol = 1e-5f + 4e-5f * mag * rsqrtf(fminf(c, d)) * (1.f + fabsf(ss) + fabsf(tt));
+  if (!(ss >= tol && ss <= 1.f - tol && tt >= tol && tt <= 1.f - tol)) return false;
+  const G3 n = gsub(gmad(pi0, ss, Ei), gmad(pj0, tt, Ej));
+  return gdot(n, n) <= alim * alim;
+}
+
 // squared distance of two segments: the closest-point parameters minimise
 // |p1 + s d1 - p2 - t d2| over [0,1]^2 (interior stationary point, else the
 // best clamped edge of the square)
@@ -629,6 +688,17 @@ __device__ __forceinline__ float pt_poly_d2(const Scene& s, const float4* sp, in
   for (int k = 0; k < nbv; k++)
     best = fminf(best, pt_seg_d2(p, gpt(sp[fv[k]]), gpt(sp[fv[k + 1 == nbv ? 0 : k + 1]])));
   return best;
+}
+
+// accept_vf_tri on a face of the partner's shape (triangles only: other
+// polygons go to the FP64 predicate)
+__device__ __forceinline__ bool accept_vf(const Scene& s, const float4* sp, int sh, int f, G3 p, float alim,
+                                          float mag) {
+  const int fo = s.face_ofs[sh] + f;
+  const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
+  if (nbv != 3) return false;
+  const int* fv = s.face_verts + v0;
+  return accept_vf_tri(p, gpt(sp[fv[0]]), gpt(sp[fv[1]]), gpt(sp[fv[2]]), alim, mag);
 }
 
 // Candidate sub-contacts of the half-pairs: one warp per half-pair (owner b
@@ -825,6 +895,8 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
     const float glim = sum + 1e-4f * sum + slack;
     const float glim2 = glim * glim;
+    const float alim = sum - (1e-4f * sum + slack);  // float acceptance: the NEAR distance shrunk by the margin
+    const float dmaxf = (float)P.dmax;
     const bool lower = b < p;  // vertex-vertex and edge-edge pairs are tested in the i < j direction only
     // Two-level pruning (the role of Rockable's per-shape OBB trees,
     // Rockable.cpp:1440-1541, Shape.cpp:628-670): a sub-element stays in
@@ -869,7 +941,7 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
           const G3 d = gsub(gpt(sb[v]), gpt(sp[w]));
           ok = gdot(d, d) <= glim2;
         } else {
-          ok = !far(sb[v], sp[w], 0.f) && near_vv(P, v, w);
+          ok = !far(sb[v], sp[w], 0.f) && (accept_vv(gpt(sb[v]), gpt(sp[w]), alim) || near_vv(P, v, w));
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 0u, (uint32_t)v, (uint32_t)w), lane, out, cap, counter);
@@ -891,9 +963,9 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
           // exact rejection first: Rockable's vertex-edge test accepts a
           // projection slightly off the edge, never a line distance above it
           const int eo = s.edge_ofs[P.sp] + e;
-          ok = !far(sb[v], se, ve_ext * se.w) &&
-               pt_line_d2(gpt(sb[v]), gpt(sp[s.edges[2 * eo]]), gpt(sp[s.edges[2 * eo + 1]])) <= glim2 &&
-               near_ve(s, P, v, e);
+          const G3 pv = gpt(sb[v]), e0 = gpt(sp[s.edges[2 * eo]]), e1 = gpt(sp[s.edges[2 * eo + 1]]);
+          ok = !far(sb[v], se, ve_ext * se.w) && pt_line_d2(pv, e0, e1) <= glim2 &&
+               (accept_ve(pv, e0, e1, alim, dmaxf, mag) || near_ve(s, P, v, e));
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 1u, (uint32_t)v, (uint32_t)e), lane, out, cap, counter);
@@ -909,7 +981,8 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         const float4 sf = sp[nvp + nep + f];
         if (GEOM) ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2;
         else  // exact rejection first: NEAR needs the polygon within reach
-          ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2 && near_vf(s, P, v, f);
+          ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2 &&
+               (accept_vf(s, sp, P.sp, f, gpt(sb[v]), alim, mag) || near_vf(s, P, v, f));
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 2u, (uint32_t)v, (uint32_t)f), lane, out, cap, counter);
     }
@@ -934,10 +1007,10 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         } else {
           // exact rejection first: NEAR needs the edges' lines within reach
           const int ob = s.edge_ofs[P.sb] + e1, op = s.edge_ofs[P.sp] + e2;
-          ok = !far(s1, s2, s1.w + s2.w) &&
-               !lines_far(gpt(sb[s.edges[2 * ob]]), gpt(sb[s.edges[2 * ob + 1]]), gpt(sp[s.edges[2 * op]]),
-                          gpt(sp[s.edges[2 * op + 1]]), glim2) &&
-               near_ee(s, P, e1, e2);
+          const G3 a0 = gpt(sb[s.edges[2 * ob]]), a1 = gpt(sb[s.edges[2 * ob + 1]]);
+          const G3 b0 = gpt(sp[s.edges[2 * op]]), b1 = gpt(sp[s.edges[2 * op + 1]]);
+          ok = !far(s1, s2, s1.w + s2.w) && !lines_far(a0, a1, b0, b1, glim2) &&
+               (accept_ee(a0, a1, b0, b1, alim, mag) || near_ee(s, P, e1, e2));
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 3u, (uint32_t)e1, (uint32_t)e2), lane, out, cap, counter);

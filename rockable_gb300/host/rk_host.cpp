@@ -3,7 +3,6 @@
 
 #include <algorithm>
 #include <array>
-#include <cfenv>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -643,6 +642,11 @@ bool Rockable::upload() {
   rk_shapes sh{(int32_t)Shapes.size(), vo.data(), vx.data(), eo.data(), ed.data(), fo.data(), fvo.data(), fv.data(),
                rad.data(), obb.data()};
   if (!ck(rk_upload_shapes(ctx_, &sh), "rk_upload_shapes")) return false;
+  {  // for the device-formatted conf text
+    std::vector<const char*> names;
+    for (auto& sp : Shapes) names.push_back(sp.name.c_str());
+    if (!ck(rk_set_shape_names(ctx_, names.data(), (int32_t)names.size()), "rk_set_shape_names")) return false;
+  }
   rk_bodies b{(int64_t)P.size(), (int64_t)nDriven, P.pos.data(), P.vel.data(), P.acc.data(), P.Q.data(),
               P.vrot.data(), P.arot.data(), P.homothety.data(), P.mass.data(), P.inertia.data(), P.shape.data(),
               P.group.data(), P.cluster.data()};
@@ -761,12 +765,6 @@ bool Rockable::syncFromDevice(bool geometry) {
   return true;
 }
 
-static void put(std::string& o, int prec, double v) {
-  char b[64];
-  snprintf(b, sizeof b, "%.*e", prec, v);
-  o += b;
-}
-
 bool Rockable::saveConf(const std::string& fname) {  // Rockable.cpp:440-610
   std::ostringstream h;
   h << "Rockable 21-08-2022\n";
@@ -800,41 +798,18 @@ bool Rockable::saveConf(const std::string& fname) {  // Rockable.cpp:440-610
   if (sl != std::string::npos) shp = shp.substr(sl + 1);
   h << "shapeFile " << shp << "\nprecision " << precision << '\n';
   std::string o = h.str();
-  const int pr = precision;
+  // the Particles and Interactions sections are formatted on the device from
+  // its own state (rk_format_conf: the same printf rounding, the contact
+  // normal toward zero), one copy of text instead of the state
+  int64_t lp = 0, li = 0, na = 0;
+  if (!ck(rk_format_conf(ctx_, precision, nullptr, 0, &lp, &li, &na), "rk_format_conf")) return false;
+  std::string txt((size_t)(lp + li), '\0');
+  if (!ck(rk_format_conf(ctx_, precision, &txt[0], lp + li, &lp, &li, &na), "rk_format_conf")) return false;
   o += "Particles " + std::to_string(P.size()) + "\n";
   o += "#name group cluster homothety pos.x pos.y pos.z vel.x vel.y vel.z acc.x acc.y acc.z Q.w Q.x Q.y Q.z vrot.x vrot.y vrot.z arot.x arot.y arot.z\n";
-  for (size_t i = 0; i < P.size(); i++) {
-    o += Shapes[P.shape[i]].name + ' ' + std::to_string(P.group[i]) + ' ' + std::to_string(P.cluster[i]) + ' ';
-    put(o, pr, P.homothety[i]);
-    const double* fields[6] = {&P.pos[3 * i], &P.vel[3 * i], &P.acc[3 * i], &P.Q[4 * i], &P.vrot[3 * i], &P.arot[3 * i]};
-    const int len[6] = {3, 3, 3, 4, 3, 3};
-    for (int f = 0; f < 6; f++)
-      for (int d = 0; d < len[f]; d++) { o += ' '; put(o, pr, fields[f][d]); }
-    o += '\n';
-  }
-  // active = dn < 0 or bonded (Rockable.cpp:3005-3029), from the stored history
-  I.active.resize(I.size());
-  for (size_t k = 0; k < I.size(); k++) I.active[k] = (I.dn[k] < 0.0 || I.bond[k] >= 0) ? 1 : 0;
-  size_t na = 0;
-  for (size_t k = 0; k < I.size(); k++) na += I.active[k];
+  o.append(txt, 0, (size_t)lp);
   o += "Interactions " + std::to_string(na) + "\n";
-  const int prev = fegetround();
-  for (size_t k = 0; k < I.size(); k++) {
-    if (!(I.active.size() > k && I.active[k])) continue;
-    o += std::to_string(I.i[k]) + ' ' + std::to_string(I.j[k]) + ' ' + std::to_string(I.type[k]) + ' ' +
-         std::to_string(I.isub[k]) + ' ' + std::to_string(I.jsub[k]);
-    fesetround(FE_TOWARDZERO);  // the normal is written truncated (Rockable.cpp:569-575)
-    for (int d = 0; d < 3; d++) { o += ' '; put(o, pr, I.n[3 * k + d]); }
-    fesetround(prev);
-    o += ' '; put(o, pr, I.dn[k]);
-    for (int d = 0; d < 3; d++) { o += ' '; put(o, pr, I.pos[3 * k + d]); }
-    for (int d = 0; d < 3; d++) { o += ' '; put(o, pr, I.vel[3 * k + d]); }
-    o += ' '; put(o, pr, I.fn[k]);
-    for (int d = 0; d < 3; d++) { o += ' '; put(o, pr, I.ft[3 * k + d]); }
-    for (int d = 0; d < 3; d++) { o += ' '; put(o, pr, I.mom[3 * k + d]); }
-    o += ' '; put(o, pr, I.damp[k]);
-    o += '\n';
-  }
+  o.append(txt, (size_t)lp, (size_t)li);
   size_t nf = 0;
   for (size_t f = 0; f < F.i.size(); f++) nf += !(F.broken.size() > f && F.broken[f]);
   o += "Interfaces " + std::to_string(nf) + "\n";
