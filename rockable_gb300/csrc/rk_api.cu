@@ -96,7 +96,7 @@ int ensure_entry_capacity(Ctx& c, int which, int64_t n) {
     Scene& s = c.s;
     if ((rc = dalloc(c, s.act, cap)) || (rc = dalloc(c, s.cf, 3 * cap)) || (rc = dalloc(c, s.cmi, 3 * cap)) ||
         (rc = dalloc(c, s.cmj, 3 * cap)) || (rc = dalloc(c, s.jlist, cap)) || (rc = dalloc(c, s.nperm, cap)) ||
-        (rc = dalloc(c, s.egv, cap)))
+        (rc = dalloc(c, s.egv, cap)) || (rc = dalloc(c, s.slow, cap)))
       return rc;
     c.contrib_cap = cap;
   }
@@ -200,6 +200,10 @@ int read_flags(Ctx& c) {
   CK(cudaMemcpyAsync(c.h_flags, c.s.flags, FLAG_COUNT * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                      c.stream));
   CK(cudaStreamSynchronize(c.stream));
+  if (c.h_flags[FLAG_ERROR]) {
+    c.err = "mixed narrow phase: an entry's type run disagrees with the entry order (entries skipped)";
+    return RK_ERR_STATE;
+  }
   return 0;
 }
 
@@ -848,7 +852,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.inv_mi); dfree(s.shape); dfree(s.group); dfree(s.cluster);
   dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.gvr); dfree(s.posf); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
-  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv);
+  dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv); dfree(s.slow);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
   dfree(s.needres); dfree(s.scene_of); dfree(s.bf_surf);
   dfree(c.name_chars); dfree(c.name_ofs);

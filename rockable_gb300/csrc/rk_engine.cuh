@@ -129,6 +129,8 @@ struct Scene {
   int64_t* jsplit;  // n: first j-side slot of body b whose entry follows b's own block
   int* jlist;     // ne
   int* nperm;     // ne: entries grouped by sub-contact type (the narrow phase's thread order)
+  int* slow;      // ne: the mixed narrow phase's entries for the full path, in the regions of
+                  // nperm's type runs (type t from flags[FLAG_TOFS + t])
   // ne: global vertex indices of each entry's sub-elements (k_entry_gv, after every list change):
   // vertex-vertex (a, b), vertex-edge (a, p1, p2), vertex-triangle (a, A, B, C; w = -1 for
   // faces of more than 3 vertices), edge-edge (pi1, pi2, pj1, pj2)
@@ -171,11 +173,15 @@ struct Scene {
   int64_t* if_ofs;    // n+1 (interfaces sorted by i)
   // ---- device flags and counters (pinned-readable block)
   unsigned long long* flags;  // [0] need_update, [1] n_active, [2] n_broken_step, [3] guard max pos2 bits,
-                              // [4] guard max rot bits, [5] guard reset pending, [6] error code
+                              // [4] guard max rot bits, [5] guard reset pending, [6] error code,
+                              // [7] 1 + index of a body with non-finite state, [8..11] entries of
+                              // each type in `slow` (zero between steps), [12] arrival ticket of
+                              // the full-path kernel's blocks, [13..17] first nperm position of
+                              // each type (and ne)
 };
 
 enum { FLAG_NEED_UPDATE = 0, FLAG_NACTIVE = 1, FLAG_NBROKEN = 2, FLAG_GPOS = 3, FLAG_GROT = 4, FLAG_GRESET = 5,
-       FLAG_ERROR = 6, FLAG_NONFINITE = 7, FLAG_COUNT = 8 };  // [7]: 1 + index of a body with non-finite state
+       FLAG_ERROR = 6, FLAG_NONFINITE = 7, FLAG_NSLOW = 8, FLAG_SLOW_TICKET = 12, FLAG_TOFS = 13, FLAG_COUNT = 18 };
 
 // step kernels (rk_step.cu)
 int launch_controls_pre(const Scene& s, cudaStream_t st);

@@ -12,7 +12,9 @@
 //         point, the relative velocity, the tangential force and rolling
 //         moment, and the force / moment contributions; and a first test
 //         that proves most entries of a dense list apart (apart_f32), which
-//         then skip the FP64 path altogether.
+//         then skip the FP64 path altogether: pass 1 (k_narrow_mixed_quick)
+//         settles those and lists the others by type, pass 2
+//         (k_narrow_mixed_full) runs the FP64 path on the lists.
 // An overlap dn is a small difference of lengths of the order of the
 // particle size, which FP32 cannot resolve; all the other quantities are well
 // conditioned.  Compiled with fused multiply-adds allowed.
@@ -84,6 +86,11 @@ __device__ __forceinline__ float amax(F3 a) { return fmaxf(fabsf(a.x), fmaxf(fab
 //   0         the FP64 path decides (near the thresholds, other polygons than
 //             triangles, nearly parallel edges).
 constexpr int kApart = 1, kOutside = 2;
+
+// dn stored as -0.0: a lost sub-contact whose history is zero already
+__device__ __forceinline__ bool lost_before(double dn) {
+  return __double_as_longlong(dn) == (long long)0x8000000000000000ull;
+}
 __device__ __forceinline__ int apart_f32(const Scene& s, int type, int i, int j, int isub, int jsub, bool pre,
                                          int4 G, F3 dxij, float rsum, float cmag, float* dnf) {
   const float* g = s.gvr;
@@ -188,14 +195,11 @@ __device__ __forceinline__ int apart_f32(const Scene& s, int type, int i, int j,
   return *dnf > 2e-6f + 2e-6f * mag + 4e-7f * cmag ? kApart : 0;
 }
 
-__global__ void k_narrow_force_mixed(Scene s) {
-  if (step_halted(s)) return;
-  // threads follow the entries grouped by sub-contact type (fewer divergent
-  // branches per warp); every entry is computed on its own
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// The full path of entry e (everything the FP32 proof did not settle);
+// returns whether the entry is active.
+__device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
   bool active = false;
-  if (k < s.ne) {
-    const int64_t e = s.nperm[k];
+  {
     const int i = s.ei[e], j = s.ej[e];
     const uint32_t ts = s.etsub[e];
     const int type = tsub_type(ts), isub = tsub_isub(ts), jsub = tsub_jsub(ts);
@@ -210,22 +214,7 @@ __global__ void k_narrow_force_mixed(Scene s) {
     double dn = 0.0;
     F3 n = f3(0, 0, 0), ci = f3(0, 0, 0);  // normal, contact point relative to x_i
     bool ok = true;
-    // clearly apart, or its projection clearly outside (and nothing else
-    // needed of it): FP32 alone decides
-    int quick = 0;
-    if (bond < 0 && !s.record_geom && s.gvr) {
-      float dnf = 0.f;
-      const float4 pi = s.posf[i], pj = s.posf[j];
-      const F3 dxij = f3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
-      const float cmag = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fmaxf(fabsf(pi.z), fmaxf(fabsf(pj.x),
-                         fmaxf(fabsf(pj.y), fabsf(pj.z)))));
-      quick = apart_f32(s, type, i, j, isub, jsub, pre, G, dxij, pi.w + pj.w, cmag, &dnf);
-      if (quick == kApart) dn = f2d(dnf);
-      else if (quick == kOutside) ok = false;
-    }
-    if (quick) {
-      // dn > 0 proven (separated, history untouched), or the sub-contact lost
-    } else if (type == 0) {
+    if (type == 0) {
       V3 a, b;
       if (pre) {
         a = gvg(s.gv, G.x);
@@ -482,11 +471,9 @@ __global__ void k_narrow_force_mixed(Scene s) {
         st3m(s.cmj, e, crossf(cj, -f) - mom);
       }
     }
-    // stores that change nothing are skipped: a separated entry that was
-    // separated already (only dn's sign is used), a lost sub-contact that was
+    // stores that change nothing are skipped: a lost sub-contact that was
     // lost already (dn -0.0, history zero); bonded entries always store
-    const bool lost_before = __double_as_longlong(dn_old) == (long long)0x8000000000000000ull;
-    const bool same = bond < 0 && ((quick == kApart && dn_old > 0.0) || (!ok && lost_before));
+    const bool same = bond < 0 && !ok && lost_before(dn_old);
     if (!same) {
       s.dn[e] = dn;
       if (active || !ok) {
@@ -497,16 +484,126 @@ __global__ void k_narrow_force_mixed(Scene s) {
     }
     s.act[e] = active ? 1 : 0;
   }
-  unsigned m = __ballot_sync(0xffffffffu, active);
-  if ((threadIdx.x & 31) == 0 && m) atomicAdd(&s.flags[FLAG_NACTIVE], (unsigned long long)__popc(m));
+  return active;
+}
+
+// Pass 1, every entry (threads follow the entries grouped by sub-contact
+// type: fewer divergent branches per warp): an entry of no bond that FP32
+// proves clearly apart or with its projection clearly outside (apart_f32)
+// is finished here with FP32 alone -- a separated entry keeps its history
+// and takes the FP32 estimate as its dn (only its sign is used), a lost
+// sub-contact restarts its history from zero (dn -0.0) -- and stores only
+// what changes.  The others go to the list of their type (one atomic per
+// warp and type) for pass 2.  Warps of pass 1 thus issue almost no FP64
+// instruction, and the FP64 path runs on dense warps of the entries that
+// need it (on GB300, where each warp-wide FP64 instruction is expensive,
+// a warp whose lanes mostly skip the FP64 path still pays for all of it).
+__global__ void k_narrow_mixed_quick(Scene s) {
+  if (step_halted(s)) return;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool slow = false;
+  int type = 0, e = 0;
+  if (k < s.ne) {
+    e = s.nperm[k];
+    const int bond = s.bond[e];
+    const uint32_t ts = s.etsub[e];
+    type = tsub_type(ts);
+    int quick = 0;
+    float dnf = 0.f;
+    if (bond < 0 && !s.record_geom && s.gvr) {
+      const int i = s.ei[e], j = s.ej[e];
+      const int4 G = s.egv_ok ? s.egv[e] : make_int4(-1, -1, -1, -1);
+      const float4 pi = s.posf[i], pj = s.posf[j];
+      const F3 dxij = f3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+      const float cmag = fmaxf(fmaxf(fabsf(pi.x), fabsf(pi.y)), fmaxf(fabsf(pi.z), fmaxf(fabsf(pj.x),
+                         fmaxf(fabsf(pj.y), fabsf(pj.z)))));
+      quick = apart_f32(s, type, i, j, tsub_isub(ts), tsub_jsub(ts), s.egv_ok != 0, G, dxij, pi.w + pj.w, cmag,
+                        &dnf);
+    }
+    if (quick == kApart) {  // dn > 0 proven: separated, history untouched
+      const double dn_old = s.dn[e];
+      if (!(dn_old > 0.0)) s.dn[e] = f2d(dnf);
+      s.act[e] = 0;
+    } else if (quick == kOutside) {  // the sub-contact lost
+      if (!lost_before(s.dn[e])) {
+        s.dn[e] = -0.0;
+        s.fn[e] = 0.0;
+        const F3 z = f3(0, 0, 0);
+        st3m(s.ft, e, z);
+        st3m(s.mom, e, z);
+      }
+      s.act[e] = 0;
+    } else {
+      slow = true;
+    }
+  }
+  const int lane = threadIdx.x & 31;
+  for (int t = 0; t < 4; t++) {
+    const unsigned bal = __ballot_sync(0xffffffffu, slow && type == t);
+    if (!bal) continue;
+    unsigned long long base = 0;
+    if (lane == __ffs(bal) - 1) base = atomicAdd(&s.flags[FLAG_NSLOW + t], (unsigned long long)__popc(bal));
+    base = __shfl_sync(0xffffffffu, base, __ffs(bal) - 1);
+    if (slow && type == t) {
+      const unsigned long long at = s.flags[FLAG_TOFS + t] + base + __popc(bal & ((1u << lane) - 1u));
+      if (at < s.flags[FLAG_TOFS + t + 1]) s.slow[at] = e;
+      else atomicOr(&s.flags[FLAG_ERROR], 1ull);  // cannot happen while nperm and its type runs agree
+    }
+  }
+}
+
+// Pass 2: the full path over the four lists, one after the other, by whole
+// warps (grid-stride); the last block to finish empties the lists for the
+// next step.
+constexpr int kSlowThreads = 128;
+__global__ void __launch_bounds__(kSlowThreads) k_narrow_mixed_full(Scene s) {
+  if (step_halted(s)) return;
+  int64_t cnt[4], total = 0;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {  // (a list never exceeds its type run)
+    cnt[t] = min((int64_t)s.flags[FLAG_NSLOW + t], (int64_t)(s.flags[FLAG_TOFS + t + 1] - s.flags[FLAG_TOFS + t]));
+    total += cnt[t];
+  }
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * kSlowThreads) >> 5;
+  for (int64_t base = ((blockIdx.x * (int64_t)kSlowThreads + threadIdx.x) >> 5) * 32; base < total;
+       base += nwarps * 32) {
+    const int64_t q = base + lane;
+    bool active = false;
+    if (q < total) {
+      int t = 0;
+      int64_t r = q;
+#pragma unroll
+      for (int u = 0; u < 3; u++)  // the list of q (constant indices: cnt stays in registers)
+        if (t == u && r >= cnt[u]) {
+          r -= cnt[u];
+          t = u + 1;
+        }
+      active = narrow_mixed_full(s, s.slow[(int64_t)s.flags[FLAG_TOFS + t] + r]);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, active);
+    if (lane == 0 && m) atomicAdd(&s.flags[FLAG_NACTIVE], (unsigned long long)__popc(m));
+  }
+  __syncthreads();  // every thread of the block has read the counts
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long arrived = atomicAdd(&s.flags[FLAG_SLOW_TICKET], 1ull);
+    if (arrived == gridDim.x - 1ull) {
+      for (int t = 0; t < 4; t++) s.flags[FLAG_NSLOW + t] = 0ull;
+      s.flags[FLAG_SLOW_TICKET] = 0ull;
+    }
+  }
 }
 
 int launch_narrow_force_mixed(const Scene& s, cudaStream_t st) {
   if (s.ne <= 0) return 0;
   const int t = s.tpb[0] > 0 ? s.tpb[0] : 128;
-  k_narrow_force_mixed<<<(unsigned)((s.ne + t - 1) / t), t, 0, st>>>(s);
-  return 1;
+  k_narrow_mixed_quick<<<(unsigned)((s.ne + t - 1) / t), t, 0, st>>>(s);
+  // enough warps for every entry to have a lane, up to 16 blocks per SM
+  const int64_t blocks = std::min<int64_t>((s.ne + kSlowThreads - 1) / kSlowThreads, 152 * 16);
+  k_narrow_mixed_full<<<(unsigned)blocks, kSlowThreads, 0, st>>>(s);
+  return 2;
 }
-cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a) { return cudaFuncGetAttributes(a, k_narrow_force_mixed); }
+cudaError_t narrow_mixed_attributes(cudaFuncAttributes* a) { return cudaFuncGetAttributes(a, k_narrow_mixed_quick); }
 
 }  // namespace rk

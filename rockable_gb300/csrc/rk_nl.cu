@@ -158,7 +158,7 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
   }
 }
 
-// bodies whose resultant is summed by a block (see k_gather_heavy): in the
+// bodies whose resultant is summed by a warp (see k_gather_heavy): in the
 // step when the resultant is used, on demand otherwise; and the vertices of
 // the bodies with entries (the only ones the step's narrow phase reads), in
 // per-body runs whose order between bodies does not matter
@@ -220,8 +220,9 @@ __device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
 // (Rockable.cpp:1627-1654), decided in float where the answer is clear: a
 // separation along one of the six face axes by more than the rounding
 // margin makes the FP64 test false as well, and one box's centre inside the
-// other (shrunk by the margin) makes it true as well; only the cases in
-// between run the FP64 test, so the result is the FP64 test's.
+// other (shrunk by the margin) makes it true as well; then the nine edge-edge
+// axes the same way (false only); only the cases in between run the FP64
+// test, so the result is the FP64 test's.
 __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, int64_t j) {
   const float* A = s.bobbf + 15 * i;
   const float* B = s.bobbf + 15 * j;
@@ -236,8 +237,10 @@ __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, in
                     ea[0] + ea[1] + ea[2] + eb[0] + eb[1] + eb[2];
   const float m = 1e-6f * mag + 1e-9f;
   bool in_a = true, in_b = true;
+  float ta[3];
   for (int a = 0; a < 3; a++) {  // face axes of A
-    const float t = fabsf(tx * A[3 + 3 * a] + ty * A[4 + 3 * a] + tz * A[5 + 3 * a]);
+    ta[a] = tx * A[3 + 3 * a] + ty * A[4 + 3 * a] + tz * A[5 + 3 * a];
+    const float t = fabsf(ta[a]);
     const float r = ea[a] + eb[0] * fabsf(R[a][0]) + eb[1] * fabsf(R[a][1]) + eb[2] * fabsf(R[a][2]);
     if (t > r + m) return false;
     in_a = in_a && t < ea[a] - m;
@@ -249,6 +252,18 @@ __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, in
     in_b = in_b && t < eb[b] - m;
   }
   if (in_a || in_b) return true;
+  // the nine edge-edge axes A_a x B_b, in A's frame; one more product level
+  // than the face axes, hence the wider margin
+  const float mc = 4e-6f * mag + 1e-9f;
+  for (int a = 0; a < 3; a++) {
+    const int a1 = a == 2 ? 0 : a + 1, a2 = a == 0 ? 2 : a - 1;
+    for (int b = 0; b < 3; b++) {
+      const int b1 = b == 2 ? 0 : b + 1, b2 = b == 0 ? 2 : b - 1;
+      const float r = ea[a1] * fabsf(R[a2][b]) + ea[a2] * fabsf(R[a1][b]) + eb[b1] * fabsf(R[a][b2]) +
+                      eb[b2] * fabsf(R[a][b1]);
+      if (fabsf(ta[a2] * R[a1][b] - ta[a1] * R[a2][b]) > r + mc) return false;
+    }
+  }
   Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
   enlarge(oi, 0.5 * s.DVerlet);
   enlarge(oj, 0.5 * s.DVerlet);
@@ -377,9 +392,14 @@ __global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys,
 
 // With `only` (a partial refresh), body i enumerates its pairs when it is
 // flagged, with every neighbour that is not flagged or has a larger index.
+// One thread per body and neighbour column (the nine (x, y) columns around
+// its cell): nine times the threads of a body loop, for the latency of the
+// key searches and of the pair tests.
 __global__ void k_grid_pairs(Scene s, const uint8_t* only, const uint64_t* keys, int64_t nnorm, float inv_cell,
                              uint64_t* pairs, int64_t cap, unsigned long long* counter) {
-  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t k = t / 9;
+  const int col = (int)(t - 9 * k);
   if (k >= nnorm) return;
   const CellFormat f = cell_format(s);
   const uint64_t key = keys[k];
@@ -392,21 +412,18 @@ __global__ void k_grid_pairs(Scene s, const uint8_t* only, const uint64_t* keys,
   // z is the lowest field of the cell code: the three cells (x, y, z-1..z+1)
   // of a neighbour column are one contiguous key range
   const int z0 = max(cz - 1, 0), z1 = min(cz + 1, f.max);
-  for (int dx = -1; dx <= 1; dx++)
-    for (int dy = -1; dy <= 1; dy++) {
-      const int x = cx + dx, y = cy + dy;
-      if (x < 0 || y < 0 || x > f.max || y > f.max) continue;
-      const uint64_t first = cell_code(scene, x, y, z0, f) << 21;
-      const uint64_t last = cell_code(scene, x, y, z1, f);
-      for (int64_t q = lower_bound_u64(keys, nnorm, first); q < nnorm && (keys[q] >> 21) <= last; q++) {
-        const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
-        if (only ? (j == i || (only[j] && j < i)) : (j <= i)) continue;
-        const int64_t lo = min(i, j), hi = max(i, j);
-        if (!pair_predicate(s, lo, hi)) continue;
-        unsigned long long at = atomicAdd(counter, 1ull);
-        if ((int64_t)at < cap) pairs[at] = ((uint64_t)lo << 21) | (uint64_t)hi;
-      }
-    }
+  const int x = cx + col / 3 - 1, y = cy + col % 3 - 1;
+  if (x < 0 || y < 0 || x > f.max || y > f.max) return;
+  const uint64_t first = cell_code(scene, x, y, z0, f) << 21;
+  const uint64_t last = cell_code(scene, x, y, z1, f);
+  for (int64_t q = lower_bound_u64(keys, nnorm, first); q < nnorm && (keys[q] >> 21) <= last; q++) {
+    const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
+    if (only ? (j == i || (only[j] && j < i)) : (j <= i)) continue;
+    const int64_t lo = min(i, j), hi = max(i, j);
+    if (!pair_predicate(s, lo, hi)) continue;
+    unsigned long long at = atomicAdd(counter, 1ull);
+    if ((int64_t)at < cap) pairs[at] = ((uint64_t)lo << 21) | (uint64_t)hi;
+  }
 }
 
 // oversized body o against every body j of its scene (each pair once)
@@ -568,63 +585,68 @@ __device__ __forceinline__ bool lines_far(G3 p1, G3 q1, G3 p2, G3 q2, float lim2
   return rn * rn > lim2 * nn;
 }
 
-// Float acceptance in front of the FP64 NEAR predicates (Rockable's, above):
-// from the float world coordinates of the sub-elements (the vertex spheres'
-// centres, rounded to nearest from the FP64 world vertices: errors of a few
-// 1e-8 of the coordinates' magnitude `mag`), each returns true only when the
-// FP64 predicate is true for sure -- its distance within `alim` (the NEAR
-// distance shrunk by the rejection's rounding margin) and its projection
-// parameters or point inside their ranges by more than their rounding error.
-// Otherwise the FP64 predicate decides.
+// Float classification in front of the FP64 NEAR predicates (Rockable's,
+// above): from the float world coordinates of the sub-elements (the vertex
+// spheres' centres, rounded to nearest from the FP64 world vertices: errors
+// of a few 1e-8 of the coordinates' magnitude `mag`), each returns 1 only
+// when the FP64 predicate is true for sure -- its distance within `alim` (the
+// NEAR distance shrunk by the rejection's rounding margin) and its projection
+// parameters or point inside their ranges by more than their rounding error
+// -- and -1 only when it is false for sure: a projection parameter or point
+// outside its range by more than that error.  On 0 the FP64 predicate
+// decides.  (The distance rejections sit at the call sites.)
 __device__ __forceinline__ bool accept_vv(G3 a, G3 b, float alim) {
   const G3 d = gsub(a, b);
   return alim > 0.f && gdot(d, d) <= alim * alim;
 }
-__device__ __forceinline__ bool accept_ve(G3 p, G3 a, G3 b, float alim, float dmax, float mag) {
+__device__ __forceinline__ int classify_ve(G3 p, G3 a, G3 b, float alim, float dmax, float mag) {
   const G3 E = gsub(b, a), w = gsub(p, a);
   const float E2 = gdot(E, E);
-  if (!(alim > 0.f) || !(E2 > 0.f)) return false;
+  if (!(E2 > 0.f)) return 0;
   const float r = gdot(w, E) / E2;
   const float tol = 1e-5f + 4e-6f * mag * rsqrtf(E2) * (1.f + fabsf(r));
-  if (!(r >= -dmax + tol && r <= 1.f + dmax - tol)) return false;
+  if (r < -dmax - tol || r > 1.f + dmax + tol) return -1;  // the FP64 projection test fails too
+  if (!(alim > 0.f) || !(r >= -dmax + tol && r <= 1.f + dmax - tol)) return 0;
   const G3 d = gmad(w, -r, E);
-  return gdot(d, d) <= alim * alim;
+  return gdot(d, d) <= alim * alim ? 1 : 0;
 }
-__device__ __forceinline__ bool accept_vf_tri(G3 p, G3 A, G3 B, G3 C, float alim, float mag) {
-  if (!(alim > 0.f)) return false;
+__device__ __forceinline__ int classify_vf_tri(G3 p, G3 A, G3 B, G3 C, float alim, float mag) {
   const G3 bA = gsub(B, A), cA = gsub(C, A), w = gsub(p, A);
   G3 n = gcross(bA, cA);
   const float nn = gdot(n, n);
-  if (!(nn > 0.f)) return false;
+  // a well-shaped triangle (the sine of its angle at A above 1e-3), so that
+  // the float normal and in-plane distances carry only rounding errors
+  if (!(nn > 1e-6f * gdot(bA, bA) * gdot(cA, cA))) return 0;
   const float inv = rsqrtf(nn);
   n = {n.x * inv, n.y * inv, n.z * inv};
   const float dist = gdot(w, n);
-  if (!(fabsf(dist) <= alim)) return false;
   const G3 P = gmad(w, -dist, n);
-  const float tol = 1e-9f + 1e-6f * mag;
+  const float tol = 1e-9f + 2e-6f * mag;
   const G3 ed[3] = {bA, gsub(cA, bA), {-cA.x, -cA.y, -cA.z}};
   const G3 st[3] = {{0.f, 0.f, 0.f}, bA, cA};
+  bool inside = true;
   for (int q = 0; q < 3; q++) {  // counter-clockwise about n: inside is to the left of every edge
     const float side = gdot(gcross(ed[q], gsub(P, st[q])), n) * rsqrtf(gdot(ed[q], ed[q]));
-    if (!(side > tol)) return false;
+    if (side < -tol) return -1;  // projection outside the triangle: even crossing number in FP64 too
+    inside = inside && side > tol;
   }
-  return true;
+  return inside && alim > 0.f && fabsf(dist) <= alim ? 1 : 0;
 }
-__device__ __forceinline__ bool accept_ee(G3 pi0, G3 pi1, G3 pj0, G3 pj1, float alim, float mag) {
-  if (!(alim > 0.f)) return false;
+__device__ __forceinline__ int classify_ee(G3 pi0, G3 pi1, G3 pj0, G3 pj1, float alim, float mag) {
   const G3 Ei = gsub(pi1, pi0), Ej = gsub(pj1, pj0), w = gsub(pi0, pj0);
   const float c = gdot(Ei, Ei), d = gdot(Ej, Ej), e = gdot(Ei, Ej);
   const float f = c * d - e * e;
   // well away from the FP64 test's parallel threshold (1e-12) and from
   // parallel edges (the sine of their angle above 0.1)
-  if (!(f > 2e-12f + 0.01f * c * d)) return false;
+  if (!(f > 2e-12f + 0.01f * c * d)) return 0;
   const float a = gdot(Ei, w), b = gdot(Ej, w);
   const float fi = 1.f / f;
   const float ss = (e * b - a * d) * fi, tt = (c * b - e * a) * fi;
   const float tol = 1e-5f + 4e-5f * mag * rsqrtf(fminf(c, d)) * (1.f + fabsf(ss) + fabsf(tt));
-  if (!(ss >= tol && ss <= 1.f - tol && tt >= tol && tt <= 1.f - tol)) return false;
+  if (ss < -tol || ss > 1.f + tol || tt < -tol || tt > 1.f + tol) return -1;  // closest points off an edge
+  if (!(alim > 0.f) || !(ss >= tol && ss <= 1.f - tol && tt >= tol && tt <= 1.f - tol)) return 0;
   const G3 n = gsub(gmad(pi0, ss, Ei), gmad(pj0, tt, Ej));
-  return gdot(n, n) <= alim * alim;
+  return gdot(n, n) <= alim * alim ? 1 : 0;
 }
 
 // squared distance of two segments: the closest-point parameters minimise
@@ -690,16 +712,19 @@ __device__ __forceinline__ float pt_poly_d2(const Scene& s, const float4* sp, in
   return best;
 }
 
-// accept_vf_tri on a face of the partner's shape (triangles only: other
+// classify_vf_tri on a face of the partner's shape (triangles only: other
 // polygons go to the FP64 predicate)
-__device__ __forceinline__ bool accept_vf(const Scene& s, const float4* sp, int sh, int f, G3 p, float alim,
-                                          float mag) {
+__device__ __forceinline__ int classify_vf(const Scene& s, const float4* sp, int sh, int f, G3 p, float alim,
+                                           float mag) {
   const int fo = s.face_ofs[sh] + f;
   const int v0 = s.face_vofs[fo], nbv = s.face_vofs[fo + 1] - v0;
-  if (nbv != 3) return false;
+  if (nbv != 3) return 0;
   const int* fv = s.face_verts + v0;
-  return accept_vf_tri(p, gpt(sp[fv[0]]), gpt(sp[fv[1]]), gpt(sp[fv[2]]), alim, mag);
+  return classify_vf_tri(p, gpt(sp[fv[0]]), gpt(sp[fv[1]]), gpt(sp[fv[2]]), alim, mag);
 }
+
+// the float class decides unless it is 0
+#define RK_DECIDE(cls, exact) ([&] { const int c_ = (cls); return c_ > 0 || (c_ == 0 && (exact)); }())
 
 // Candidate sub-contacts of the half-pairs: one warp per half-pair (owner b
 // -> partner p).  The lanes first compute, in parallel, the owner vertices
@@ -965,7 +990,7 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
           const int eo = s.edge_ofs[P.sp] + e;
           const G3 pv = gpt(sb[v]), e0 = gpt(sp[s.edges[2 * eo]]), e1 = gpt(sp[s.edges[2 * eo + 1]]);
           ok = !far(sb[v], se, ve_ext * se.w) && pt_line_d2(pv, e0, e1) <= glim2 &&
-               (accept_ve(pv, e0, e1, alim, dmaxf, mag) || near_ve(s, P, v, e));
+               RK_DECIDE(classify_ve(pv, e0, e1, alim, dmaxf, mag), near_ve(s, P, v, e));
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 1u, (uint32_t)v, (uint32_t)e), lane, out, cap, counter);
@@ -982,7 +1007,7 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         if (GEOM) ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2;
         else  // exact rejection first: NEAR needs the polygon within reach
           ok = !far(sb[v], sf, sf.w) && pt_poly_d2(s, sp, P.sp, f, gpt(sb[v])) <= glim2 &&
-               (accept_vf(s, sp, P.sp, f, gpt(sb[v]), alim, mag) || near_vf(s, P, v, f));
+               RK_DECIDE(classify_vf(s, sp, P.sp, f, gpt(sb[v]), alim, mag), near_vf(s, P, v, f));
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 2u, (uint32_t)v, (uint32_t)f), lane, out, cap, counter);
     }
@@ -1010,7 +1035,7 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
           const G3 a0 = gpt(sb[s.edges[2 * ob]]), a1 = gpt(sb[s.edges[2 * ob + 1]]);
           const G3 b0 = gpt(sp[s.edges[2 * op]]), b1 = gpt(sp[s.edges[2 * op + 1]]);
           ok = !far(s1, s2, s1.w + s2.w) && !lines_far(a0, a1, b0, b1, glim2) &&
-               (accept_ee(a0, a1, b0, b1, alim, mag) || near_ee(s, P, e1, e2));
+               RK_DECIDE(classify_ee(a0, a1, b0, b1, alim, mag), near_ee(s, P, e1, e2));
         }
       }
       warp_emit(ok, entry_key((uint32_t)b, (uint32_t)p, 3u, (uint32_t)e1, (uint32_t)e2), lane, out, cap, counter);
@@ -1252,8 +1277,8 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
     c.kernels += 16;
     for (int attempt = 0; attempt < 4; attempt++) {
       RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
-      k_grid_pairs<<<nblk(N - nover, 128), 128, 0, st>>>(s, only, w.gkeys, N - nover, inv, w.pairs, w.pair_cap,
-                                                          w.counter);
+      k_grid_pairs<<<nblk(9 * (N - nover), 128), 128, 0, st>>>(s, only, w.gkeys, N - nover, inv, w.pairs,
+                                                                w.pair_cap, w.counter);
       if (nover > 0) {
         dim3 g2(nblk(N, 128), (unsigned)nover);
         k_over_pairs<<<g2, 128, 0, st>>>(s, only, w.gover, w.gis_over, w.pairs, w.pair_cap, w.counter);
@@ -1409,10 +1434,15 @@ __global__ void k_type_keys(const uint32_t* etsub, int64_t ne, uint64_t* keys) {
   if (e >= ne) return;
   keys[e] = ((uint64_t)tsub_type(etsub[e]) << 40) | (uint64_t)e;
 }
-__global__ void k_type_perm(const uint64_t* keys, int64_t ne, int* perm) {
+// perm, and the first position of each type in it (tofs[4] = ne)
+__global__ void k_type_perm(const uint64_t* keys, int64_t ne, int* perm, unsigned long long* tofs) {
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= ne) return;
   perm[k] = (int)(keys[k] & ((1ull << 40) - 1));
+  const int t = (int)(keys[k] >> 40), tp = k > 0 ? (int)(keys[k - 1] >> 40) : -1;
+  for (int u = tp + 1; u <= t; u++) tofs[u] = (unsigned long long)k;
+  if (k == ne - 1)
+    for (int u = t + 1; u <= 4; u++) tofs[u] = (unsigned long long)ne;
 }
 
 // Order in which the narrow phase visits the entries: by sub-contact type,
@@ -1428,7 +1458,7 @@ static int entry_order(Ctx& c) {
   }
   k_type_keys<<<nblk(ne, 256), 256, 0, c.stream>>>(s.etsub, ne, w.jkeys);
   radix_sort_u64(w.jkeys, w.jtmp, ne, 40, 42, w.tmp, c.stream);
-  k_type_perm<<<nblk(ne, 256), 256, 0, c.stream>>>(w.jkeys, ne, s.nperm);
+  k_type_perm<<<nblk(ne, 256), 256, 0, c.stream>>>(w.jkeys, ne, s.nperm, s.flags + FLAG_TOFS);
   c.kernels += 5;
   return 0;
 }

@@ -372,67 +372,59 @@ __global__ void k_narrow_force(Scene s) {
 }
 
 // ----------------------------------------------------------------- K3 ----
-// Bodies with many entries (walls, floors): a block loads a chunk of the
-// body's entries in the serial order in parallel, then one thread adds the
-// chunk in that order -- the same sums as the one-thread loop, without its
-// memory latency.
-constexpr int kHeavyChunk = 256;
-__global__ void __launch_bounds__(kHeavyChunk) k_gather_heavy(Scene s, const int* list) {
+// Bodies with many entries: one warp per body.  The lanes load 32 positions
+// of the serial order at a time (the j-side entries before the body's own
+// block, its block, the rest of the j-side: jsplit), and lanes 0-5 each add
+// one of the six components (F.x, F.y, F.z, M.x, M.y, M.z) of those 32
+// contributions, broadcast by shuffles, in that order: the same sums as the
+// one-thread loop (F - f added as F + (-f), which IEEE arithmetic makes the
+// same number), six short chains instead of one long one.
+constexpr int kHeavyWarps = 4;  // warps per block
+__global__ void __launch_bounds__(32 * kHeavyWarps) k_gather_heavy(Scene s, const int* list, int count) {
   if (step_halted(s)) return;
-  __shared__ double sf[kHeavyChunk][3], sm[kHeavyChunk][3];
-  __shared__ int sgn[kHeavyChunk];
-  __shared__ int64_t split;
-  const int b = list[blockIdx.x];
-  const int t = threadIdx.x;
+  const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= count) return;
+  const int b = list[w];
   const int64_t i0 = s.iofs[b], i1 = s.iofs[b + 1];
-  const int64_t j0 = s.jofs[b], j1 = s.jofs[b + 1];
-  if (t == 0) {  // first j-side slot whose entry follows b's own block
-    int64_t lo = j0, hi = j1;
-    while (lo < hi) {
-      int64_t m = (lo + hi) >> 1;
-      if (s.jlist[m] < i0) lo = m + 1;
-      else hi = m;
-    }
-    split = lo;
-  }
-  __syncthreads();
-  const int64_t nA = split - j0, nB = i1 - i0, nC = j1 - split;
-  const int64_t L = nA + nB + nC;
+  const int64_t j0 = s.jofs[b], j1 = s.jofs[b + 1], js = s.jsplit[b];
+  const int64_t nA = js - j0, nB = i1 - i0, L = nA + nB + (j1 - js);
   V3 F, M;
-  if (t == 0) init_resultant(s, b, F, M);
-  for (int64_t c0 = 0; c0 < L; c0 += kHeavyChunk) {
-    const int64_t p = c0 + t;
-    int sign = 0;
+  init_resultant(s, b, F, M);
+  const double start[6] = {F.x, F.y, F.z, M.x, M.y, M.z};
+  double acc = lane < 6 ? start[lane] : 0.0;
+  for (int64_t c0 = 0; c0 < L; c0 += 32) {
+    const int64_t p = c0 + lane;
+    int valid = 0;
+    double c[6] = {0, 0, 0, 0, 0, 0};
     if (p < L) {
       int64_t e;
       bool jside;
       if (p < nA) { e = s.jlist[j0 + p]; jside = true; }
       else if (p < nA + nB) { e = i0 + (p - nA); jside = false; }
-      else { e = s.jlist[split + (p - nA - nB)]; jside = true; }
+      else { e = s.jlist[js + (p - nA - nB)]; jside = true; }
       if (s.act[e]) {
-        sign = jside ? -1 : 1;
-        V3 f = ld3(s.cf, e), m = jside ? ld3(s.cmj, e) : ld3(s.cmi, e);
-        sf[t][0] = f.x; sf[t][1] = f.y; sf[t][2] = f.z;
-        sm[t][0] = m.x; sm[t][1] = m.y; sm[t][2] = m.z;
+        valid = 1;
+        const V3 f = ld3(s.cf, e), m = jside ? ld3(s.cmj, e) : ld3(s.cmi, e);
+        c[0] = jside ? -f.x : f.x;
+        c[1] = jside ? -f.y : f.y;
+        c[2] = jside ? -f.z : f.z;
+        c[3] = m.x; c[4] = m.y; c[5] = m.z;
       }
     }
-    sgn[t] = sign;
-    __syncthreads();
-    if (t == 0) {
-      const int nk = (int)min((int64_t)kHeavyChunk, L - c0);
-      for (int k = 0; k < nk; k++) {
-        if (sgn[k] == 0) continue;
-        V3 f = v3(sf[k][0], sf[k][1], sf[k][2]);
-        F = sgn[k] > 0 ? F + f : F - f;
-        M = M + v3(sm[k][0], sm[k][1], sm[k][2]);
-      }
+    const unsigned any = __ballot_sync(0xffffffffu, valid);
+    const int nk = (int)min((int64_t)32, L - c0);
+    for (int k = 0; k < nk; k++) {
+      if (!((any >> k) & 1u)) continue;
+      const double v0 = __shfl_sync(0xffffffffu, c[0], k), v1 = __shfl_sync(0xffffffffu, c[1], k);
+      const double v2 = __shfl_sync(0xffffffffu, c[2], k), v3_ = __shfl_sync(0xffffffffu, c[3], k);
+      const double v4 = __shfl_sync(0xffffffffu, c[4], k), v5 = __shfl_sync(0xffffffffu, c[5], k);
+      const double v = lane == 0 ? v0 : lane == 1 ? v1 : lane == 2 ? v2 : lane == 3 ? v3_ : lane == 4 ? v4 : v5;
+      if (lane < 6) acc = acc + v;
     }
-    __syncthreads();
   }
-  if (t == 0) {
-    st3(s.force, b, F);
-    st3(s.moment, b, M);
-  }
+  if (lane < 3) s.force[3 * (int64_t)b + lane] = acc;
+  else if (lane < 6) s.moment[3 * (int64_t)b + lane - 3] = acc;
 }
 
 // ----------------------------------------------------------------- K4 ----
@@ -599,13 +591,15 @@ int max_tpb(int which, int form_mixed) {
 int launch_gather_heavy(const Scene& s, cudaStream_t st) {
   if (s.nheavy <= 0) return 0;
   if (s.fast_body) return launch_fused_heavy(s, s.heavy, (int)s.nheavy, st);
-  k_gather_heavy<<<s.nheavy, kHeavyChunk, 0, st>>>(s, s.heavy);
+  k_gather_heavy<<<(unsigned)((s.nheavy + kHeavyWarps - 1) / kHeavyWarps), 32 * kHeavyWarps, 0, st>>>(
+      s, s.heavy, (int)s.nheavy);
   return 1;
 }
 int launch_gather_heavy_lazy(const Scene& s, cudaStream_t st) {
   if (s.nheavy_lazy <= 0) return 0;
   if (s.fast_body) return launch_fused_heavy(s, s.heavy_lazy, (int)s.nheavy_lazy, st);
-  k_gather_heavy<<<s.nheavy_lazy, kHeavyChunk, 0, st>>>(s, s.heavy_lazy);
+  k_gather_heavy<<<(unsigned)((s.nheavy_lazy + kHeavyWarps - 1) / kHeavyWarps), 32 * kHeavyWarps, 0, st>>>(
+      s, s.heavy_lazy, (int)s.nheavy_lazy);
   return 1;
 }
 int launch_breakage(const Scene& s, cudaStream_t st) {
