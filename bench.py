@@ -61,7 +61,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s @1 GB300: plain FP64 vs mixed+learned-skin, <=1e-4 rel force err"
 TUNE_STEPS = 10  # untimed block-size tuning steps (rk_set_autotune, 2 rounds of 5 sizes)
-PROFILE = os.path.join(ROOT, "profiles", "step_kernels_column_50k.md")
+PROFILE = os.path.join(ROOT, "profiles", "step_kernels_column_30k_headline.md")
 
 
 def parse():

@@ -850,7 +850,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.svert); dfree(s.sradius); dfree(s.sobb); dfree(s.sbox); dfree(s.bbox);
   dfree(s.pos); dfree(s.vel); dfree(s.acc); dfree(s.Q); dfree(s.vrot); dfree(s.arot); dfree(s.force); dfree(s.moment);
   dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.inv_mi); dfree(s.shape); dfree(s.group); dfree(s.cluster);
-  dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.gvr); dfree(s.posf); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
+  dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.gvr); dfree(s.posf); dfree(s.rotm); dfree(s.gsum); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv); dfree(s.slow);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
@@ -1001,7 +1001,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.bobb, (const double*)nullptr, 15 * n)) ||
       (rc = dupload(c, s.bobbf, (const float*)nullptr, 15 * n)) ||
       (rc = dupload(c, s.bbox, (const float*)nullptr, 15 * n)) ||
-      (rc = dalloc(c, s.posf, n)) ||
+      (rc = dalloc(c, s.posf, n)) || (rc = dalloc(c, s.rotm, 9 * n)) || (rc = dalloc(c, s.gsum, 6 * n)) ||
       (rc = dupload(c, s.baabb, (const float*)nullptr, 6 * n)) ||
       (rc = dupload(c, s.dpos, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.dq, (const double*)nullptr, 4 * n)) ||
       (rc = dupload(c, s.iofs, (const int64_t*)nullptr, n + 1)) ||

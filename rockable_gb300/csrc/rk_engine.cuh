@@ -85,6 +85,9 @@ struct Scene {
                      // mixed form's test of clearly separated entries)
   float4* posf;      // n: body centre rounded to FP32 and its Minkowski radius, written with the
                      // world vertices (the same test)
+  float* gsum;       // 6 per body: the mixed form's FP32 contact sums (force, moment) of the step
+  double* rotm;      // 9 per body: the mixed form's FP64 rotation matrix of Q (row-major), written
+                     // each step with gvr; its FP64 path places the few vertices it needs from it
   double* bobb;      // 15 per body (placed OBB, not enlarged)
   float* bobbf;      // float copy of bobb
   float* baabb;      // 6 per body: outward-rounded AABB of the OBB enlarged by DVerlet/2
@@ -204,6 +207,7 @@ __device__ __forceinline__ bool step_halted(const Scene& s) { return s.sk_ctl !=
 
 int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st);
+int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);
 int launch_skin_begin(const Scene& s, cudaStream_t st);

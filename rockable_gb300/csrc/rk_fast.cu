@@ -133,24 +133,28 @@ __global__ void k_drift(Scene s) {
 
 // Resultants, Newton-Euler and the second half-kick (Rockable.cpp:3837-3866,
 // 2084-2117 in the FP64 form); driven bodies take the generic FP64 path.
-// kGatherLanes lanes per body: each sums every kGatherLanes-th of the body's
-// active entries (its own block, then its j-side list), the lanes' sums are
-// reduced by shuffles in a fixed order, and the first lane does the
-// Newton-Euler update.  A body's serial sum would be a chain of ~50 dependent
-// loads on a dense list; the mixed form promises no serial order, and this
-// order is the same on every run.  Bodies summed by k_gather_heavy (one
-// block each) read that kernel's resultant.
-__global__ void k_gather_accel(Scene s, int apply_kick) {
+// Two kernels:
+//   k_gather_sums    kGatherLanes lanes per body: each lane sums every
+//                    kGatherLanes-th of the body's active entries (its own
+//                    block, then its j-side list), the lanes' sums are
+//                    reduced by shuffles in a fixed order, and the first lane
+//                    stores them (6 floats per body).  A body's serial sum
+//                    would be a chain of ~50 dependent loads on a dense list;
+//                    the mixed form promises no serial order, and this order
+//                    is the same on every run.
+//   k_gather_accel   one thread per body: the resultant, Newton-Euler and
+//                    the kick, whose FP64 instructions (the state is FP64)
+//                    then run on full warps instead of on one lane in
+//                    kGatherLanes (a warp issues an instruction once for all
+//                    its lanes); every thread of both kernels has work.
+// Bodies summed by k_gather_heavy (one block each) read that kernel's
+// resultant.
+__global__ void k_gather_sums(Scene s) {
   if (step_halted(s)) return;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t b = t / kGatherLanes;
   const int l = (int)(t % kGatherLanes);
-  float kin[12] = {};
-  bool have = false;
-  const bool inb = b < s.n;
-  const bool free_body = inb && b >= s.n_driven;
-  const int hv = inb ? (int)s.is_heavy[b] : 1;
-  const bool group_sum = free_body && (hv == 0 || hv == 3);
+  const bool group_sum = b < s.n && b >= s.n_driven && (s.is_heavy[b] == 0 || s.is_heavy[b] == 3);
   // FP32 sums: the contributions were computed in FP32 (the narrow phase
   // stores them widened, so the narrowing back is exact), and a sum of a
   // body's few dozen terms in FP32 errs by less than their own rounding
@@ -175,12 +179,24 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
 #pragma unroll
   for (int d = 0; d < 6; d++)
     for (int o = kGatherLanes / 2; o > 0; o >>= 1) a[d] += __shfl_xor_sync(0xffffffffu, a[d], o);
-  if (inb && l == 0) {
+  if (group_sum && l == 0)
+#pragma unroll
+    for (int d = 0; d < 6; d++) s.gsum[6 * b + d] = a[d];
+}
+
+__global__ void k_gather_accel(Scene s, int apply_kick) {
+  if (step_halted(s)) return;
+  float kin[12] = {};
+  bool have = false;
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b < s.n) {
     if (b < s.n_driven) {
       gather_body(s, b, apply_kick);
     } else {
+      const int hv = (int)s.is_heavy[b];
       V3 F, M;
-      if (group_sum) {
+      if (hv == 0 || hv == 3) {
+        const float* a = s.gsum + 6 * b;
         init_resultant(s, b, F, M);
         F = F + v3(f2d(a[0]), f2d(a[1]), f2d(a[2]));
         M = M + v3(f2d(a[3]), f2d(a[4]), f2d(a[5]));
@@ -221,10 +237,55 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
       have = true;
     }
   }
-  // the learned skin's guard on the state this step leaves (all lanes; one
-  // body per group)
-  if (s.sk_out && apply_kick) skin_guard_body_t<CvtBits>(s, (inb && l == 0) ? b : s.n, have, kin);
+  // the learned skin's guard on the state this step leaves (every thread)
+  if (s.sk_out && apply_kick) skin_guard_body_t<CvtBits>(s, b < s.n ? b : s.n, have, kin);
   if (s.sk_ctl) skin_batch_step_end(s);
+}
+
+// The mixed form's per-step body frames, in place of the FP64 world vertices:
+// one thread per body computes the FP64 rotation matrix of its quaternion
+// (the matrix of qrot, Particle.cpp:55-65 places the vertices with it) for
+// the narrow phase's FP64 path, which places only the vertices of the
+// entries it computes, and its FP32 copy; then the block's threads write the
+// FP32 offsets (world vertex - centre, the FP32 test's coordinates) of all
+// the block's bodies' vertices, coalesced, from the FP32 matrix.  The FP64
+// work per body is one matrix instead of one rotation per vertex.
+__global__ void k_body_frames(Scene s) {
+  if (step_halted(s)) return;
+  extern __shared__ float fr[];  // [blockDim.x][10]: the FP32 matrix and homothety
+  const int64_t b0 = blockIdx.x * (int64_t)blockDim.x;
+  const int64_t b = b0 + threadIdx.x;
+  if (b < s.n) {
+    const Q4 q = ldq(s.Q, b);
+    const double xx = q.v.x * q.v.x, yy = q.v.y * q.v.y, zz = q.v.z * q.v.z;
+    const double xy = q.v.x * q.v.y, xz = q.v.x * q.v.z, yz = q.v.y * q.v.z;
+    const double sx = q.s * q.v.x, sy = q.s * q.v.y, sz = q.s * q.v.z;
+    const double R[9] = {1.0 - 2.0 * (yy + zz), 2.0 * (xy - sz),       2.0 * (xz + sy),
+                         2.0 * (xy + sz),       1.0 - 2.0 * (xx + zz), 2.0 * (yz - sx),
+                         2.0 * (xz - sy),       2.0 * (yz + sx),       1.0 - 2.0 * (xx + yy)};
+    double* out = s.rotm + 9 * b;
+#pragma unroll
+    for (int d = 0; d < 9; d++) {
+      out[d] = R[d];
+      fr[10 * threadIdx.x + d] = d2f(R[d]);
+    }
+    fr[10 * threadIdx.x + 9] = d2f(s.hom[b]);
+    const V3 p = ld3(s.pos, b);
+    s.posf[b] = make_float4(d2f(p.x), d2f(p.y), d2f(p.z), d2f(s.rad[b]));
+  }
+  __syncthreads();
+  const int64_t bend = min(b0 + (int64_t)blockDim.x, s.n);
+  if (b0 >= bend) return;
+  const int64_t k1 = s.gv_ofs[bend];
+  for (int64_t k = s.gv_ofs[b0] + threadIdx.x; k < k1; k += blockDim.x) {
+    const int bb = s.gv_body[k];
+    const float* f = fr + 10 * (bb - b0);
+    const double* sv = s.svert + 3 * ((int64_t)s.vert_ofs[s.shape[bb]] + (k - s.gv_ofs[bb]));
+    const float ux = f[9] * d2f(sv[0]), uy = f[9] * d2f(sv[1]), uz = f[9] * d2f(sv[2]);
+    s.gvr[3 * k] = f[0] * ux + f[1] * uy + f[2] * uz;
+    s.gvr[3 * k + 1] = f[3] * ux + f[4] * uy + f[5] * uz;
+    s.gvr[3 * k + 2] = f[6] * ux + f[7] * uy + f[8] * uz;
+  }
 }
 
 // Resultant of a body with many entries (one block per body): threads sum
@@ -276,13 +337,18 @@ int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_
   mx::k_drift<<<blocks, threads, 0, st>>>(s);
   return 1;
 }
+int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_t st) {
+  mx::k_body_frames<<<blocks, threads, 10 * sizeof(float) * threads, st>>>(s);
+  return 1;
+}
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st) {
   fused::k_glob_vertices<<<blocks, threads, 0, st>>>(s, only_listed);
   return 1;
 }
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st) {
+  mx::k_gather_sums<<<(unsigned)((s.n * kGatherLanes + 255) / 256), 256, 0, st>>>(s);
   mx::k_gather_accel<<<blocks, threads, 0, st>>>(s, apply_kick);
-  return 1;
+  return 2;
 }
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st) {
   mx::k_gather_heavy<<<count, mx::kHeavyThreads, 0, st>>>(s, list);
@@ -290,7 +356,7 @@ int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t 
 }
 cudaError_t fused_attributes(int which, cudaFuncAttributes* a) {
   if (which == 1) return cudaFuncGetAttributes(a, mx::k_gather_accel);
-  if (which == 2) return cudaFuncGetAttributes(a, fused::k_glob_vertices);
+  if (which == 2) return cudaFuncGetAttributes(a, mx::k_body_frames);
   return cudaFuncGetAttributes(a, mx::k_drift);
 }
 

@@ -3,7 +3,9 @@
 // Same inputs, outputs and semantics as k_narrow_force (rk_step.cu: update of
 // Interaction.cpp:143-326, ForceLaw_*.cpp laws, contributions of
 // Rockable.cpp:2752-2789), with the arithmetic split by what it needs:
-//   FP64  vertex positions, the separation vector of the two sub-elements and
+//   FP64  vertex positions (placed with the step's FP64 rotation matrix of each
+//         body, rotm: only the vertices of the entries on the FP64 path), the
+//         separation vector of the two sub-elements and
 //         its length (hence dn), the face normal of a vertex-face contact
 //         (FP32 reciprocal-sqrt seed refined by two FP64 Newton steps), the
 //         history dn and the Avalanche normal-force increment;
@@ -48,11 +50,19 @@ __device__ __forceinline__ void st3m(double* a, int64_t k, F3 v) {
   a[3 * k + 1] = f2d(v.y);
   a[3 * k + 2] = f2d(v.z);
 }
-__device__ __forceinline__ V3 gvm(const double* g, int k) { return v3(g[3 * k], g[3 * k + 1], g[3 * k + 2]); }
-__device__ __forceinline__ V3 gvg(const double* g, int k) {
-  const int64_t q = 3 * (int64_t)k;
-  return v3(g[q], g[q + 1], g[q + 2]);
+// FP64 world position of vertex `local` of body b: pos + R (h v), R the
+// step's rotation matrix of the body (rotm, written by the body-frame kernel)
+__device__ __forceinline__ V3 vtx64(const Scene& s, int b, int local) {
+  const double* sv = s.svert + 3 * ((int64_t)s.vert_ofs[s.shape[b]] + local);
+  const double h = s.hom[b];
+  const double ux = h * sv[0], uy = h * sv[1], uz = h * sv[2];
+  const double* R = s.rotm + 9 * (int64_t)b;
+  return v3(s.pos[3 * (int64_t)b] + (R[0] * ux + R[1] * uy + R[2] * uz),
+            s.pos[3 * (int64_t)b + 1] + (R[3] * ux + R[4] * uy + R[5] * uz),
+            s.pos[3 * (int64_t)b + 2] + (R[6] * ux + R[7] * uy + R[8] * uz));
 }
+// the same for global vertex index k of body b
+__device__ __forceinline__ V3 vtx64g(const Scene& s, int b, int64_t k) { return vtx64(s, b, (int)(k - s.gv_ofs[b])); }
 
 // |d| in FP64 from an FP32 reciprocal-sqrt seed and two Newton steps
 __device__ __forceinline__ double len64(V3 d, double& inv) {
@@ -217,11 +227,11 @@ __device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
     if (type == 0) {
       V3 a, b;
       if (pre) {
-        a = gvg(s.gv, G.x);
-        b = gvg(s.gv, G.y);
+        a = vtx64g(s, i, G.x);
+        b = vtx64g(s, j, G.y);
       } else {
-        a = gvm(s.gv + 3 * s.gv_ofs[i], isub);
-        b = gvm(s.gv + 3 * s.gv_ofs[j], jsub);
+        a = vtx64(s, i, isub);
+        b = vtx64(s, j, jsub);
       }
       V3 d = a - b;
       double inv;
@@ -232,15 +242,14 @@ __device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
     } else if (type == 1) {
       V3 a, p1, p2;
       if (pre) {
-        a = gvg(s.gv, G.x);
-        p1 = gvg(s.gv, G.y);
-        p2 = gvg(s.gv, G.z);
+        a = vtx64g(s, i, G.x);
+        p1 = vtx64g(s, j, G.y);
+        p2 = vtx64g(s, j, G.z);
       } else {
-        const double* gj = s.gv + 3 * s.gv_ofs[j];
         const int eo = s.edge_ofs[s.shape[j]] + jsub;
-        p1 = gvm(gj, s.edges[2 * eo]);
-        p2 = gvm(gj, s.edges[2 * eo + 1]);
-        a = gvm(s.gv + 3 * s.gv_ofs[i], isub);
+        p1 = vtx64(s, j, s.edges[2 * eo]);
+        p2 = vtx64(s, j, s.edges[2 * eo + 1]);
+        a = vtx64(s, i, isub);
       }
       V3 E = p2 - p1, w = a - p1;
       F3 Ef = tof(E), wf = tof(w);
@@ -259,24 +268,23 @@ __device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
       // a triangle's three vertices come from the table; other polygons
       // walk the shape's face list
       const bool tri = pre && G.w >= 0;
-      const double* gj = s.gv + 3 * (tri ? (int64_t)0 : s.gv_ofs[j]);
       const int* fv = nullptr;
       int nbv = 3;
       V3 A, B, C, a;
       if (tri) {
-        A = gvg(s.gv, G.y);
-        B = gvg(s.gv, G.z);
-        C = gvg(s.gv, G.w);
-        a = gvg(s.gv, G.x);
+        A = vtx64g(s, j, G.y);
+        B = vtx64g(s, j, G.z);
+        C = vtx64g(s, j, G.w);
+        a = vtx64g(s, i, G.x);
       } else {
         const int fo = s.face_ofs[s.shape[j]] + jsub;
         const int v0 = s.face_vofs[fo];
         nbv = s.face_vofs[fo + 1] - v0;
         fv = s.face_verts + v0;
-        A = gvm(gj, fv[0]);
-        B = gvm(gj, fv[1]);
-        C = gvm(gj, fv[nbv - 1]);
-        a = pre ? gvg(s.gv, G.x) : gvm(s.gv + 3 * s.gv_ofs[i], isub);
+        A = vtx64(s, j, fv[0]);
+        B = vtx64(s, j, fv[1]);
+        C = vtx64(s, j, fv[nbv - 1]);
+        a = pre ? vtx64g(s, i, G.x) : vtx64(s, i, isub);
       }
       V3 w = a - A;
       V3 nn = cross(B - A, C - A);
@@ -308,7 +316,7 @@ __device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
         for (int iva = 0; iva < nbv; ++iva) {
           int ivb = iva + 1;
           if (ivb == nbv) ivb = 0;
-          edge(tof(gvm(gj, fv[iva]) - A), tof(gvm(gj, fv[ivb]) - A));
+          edge(tof(vtx64(s, j, fv[iva]) - A), tof(vtx64(s, j, fv[ivb]) - A));
         }
       }
       if (odd) {
@@ -321,18 +329,16 @@ __device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
     } else {
       V3 pi1, pi2, pj1, pj2;
       if (pre) {
-        pi1 = gvg(s.gv, G.x);
-        pi2 = gvg(s.gv, G.y);
-        pj1 = gvg(s.gv, G.z);
-        pj2 = gvg(s.gv, G.w);
+        pi1 = vtx64g(s, i, G.x);
+        pi2 = vtx64g(s, i, G.y);
+        pj1 = vtx64g(s, j, G.z);
+        pj2 = vtx64g(s, j, G.w);
       } else {
-        const double* gi = s.gv + 3 * s.gv_ofs[i];
-        const double* gj = s.gv + 3 * s.gv_ofs[j];
         const int eoi = s.edge_ofs[s.shape[i]] + isub, eoj = s.edge_ofs[s.shape[j]] + jsub;
-        pi1 = gvm(gi, s.edges[2 * eoi]);
-        pi2 = gvm(gi, s.edges[2 * eoi + 1]);
-        pj1 = gvm(gj, s.edges[2 * eoj]);
-        pj2 = gvm(gj, s.edges[2 * eoj + 1]);
+        pi1 = vtx64(s, i, s.edges[2 * eoi]);
+        pi2 = vtx64(s, i, s.edges[2 * eoi + 1]);
+        pj1 = vtx64(s, j, s.edges[2 * eoj]);
+        pj2 = vtx64(s, j, s.edges[2 * eoj + 1]);
       }
       V3 Ei = pi2 - pi1, Ej = pj2 - pj1, w = pi1 - pj1;
       F3 Eif = tof(Ei), Ejf = tof(Ej), wf = tof(w);

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "rk_bits.cuh"
 #include "rk_ctx.cuh"
 
 namespace rk {
@@ -67,18 +68,18 @@ __global__ void k_body_obb(Scene s) {
   out[9] = o.e2.x; out[10] = o.e2.y; out[11] = o.e2.z;
   out[12] = o.ext.x; out[13] = o.ext.y; out[14] = o.ext.z;
   float* of = s.bobbf + 15 * b;  // float copy for the pair test's pre-classification
-  for (int q = 0; q < 15; q++) of[q] = (float)out[q];
+  for (int q = 0; q < 15; q++) of[q] = d2f(out[q]);
   {  // the vertex box placed, in float (the pruning tests carry the rounding margin)
     const double* sb = s.sbox + 6 * s.shape[b];
     const V3 bc = v3(s.pos[3 * b], s.pos[3 * b + 1], s.pos[3 * b + 2]) + qrot(q, h * v3(sb[0], sb[1], sb[2]));
     const V3 ax[3] = {qrot(q, v3(1, 0, 0)), qrot(q, v3(0, 1, 0)), qrot(q, v3(0, 0, 1))};
     float* bx = s.bbox + 15 * b;
-    bx[0] = (float)bc.x; bx[1] = (float)bc.y; bx[2] = (float)bc.z;
+    bx[0] = d2f(bc.x); bx[1] = d2f(bc.y); bx[2] = d2f(bc.z);
     for (int k = 0; k < 3; k++) {
-      bx[3 + 3 * k] = (float)ax[k].x;
-      bx[4 + 3 * k] = (float)ax[k].y;
-      bx[5 + 3 * k] = (float)ax[k].z;
-      bx[12 + k] = (float)(h * sb[3 + k]);
+      bx[3 + 3 * k] = d2f(ax[k].x);
+      bx[4 + 3 * k] = d2f(ax[k].y);
+      bx[5 + 3 * k] = d2f(ax[k].z);
+      bx[12 + k] = d2f(h * sb[3 + k]);
     }
   }
   const double d = 0.5 * s.DVerlet;
@@ -99,7 +100,9 @@ __global__ void k_body_obb(Scene s) {
 
 // Bounding spheres of every sub-element (vertices, edges, faces) in world
 // coordinates, as floats with the radius rounded up: the conservative filter
-// in front of the FP64 NEAR predicates.
+// in front of the FP64 NEAR predicates.  Conversions between FP64 and FP32
+// use the integer-pipe routines of rk_bits.cuh (round to nearest), which
+// keep the scarce FP64 pipe for the differences.
 __global__ void k_spheres(Scene s, int64_t nsph) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= nsph) return;
@@ -112,9 +115,11 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
   const int f0 = s.face_ofs[sh];
   if (local < nv) {  // vertex: its position; the body bound is the largest vertex distance
     const int v = local;
-    s.sph[k] = make_float4((float)g[3 * v], (float)g[3 * v + 1], (float)g[3 * v + 2], 0.f);
-    const double dx = g[3 * v] - s.pos[3 * b], dy = g[3 * v + 1] - s.pos[3 * b + 1], dz = g[3 * v + 2] - s.pos[3 * b + 2];
-    const float d = __double2float_ru(sqrt(dx * dx + dy * dy + dz * dz));
+    s.sph[k] = make_float4(d2f(g[3 * v]), d2f(g[3 * v + 1]), d2f(g[3 * v + 2]), 0.f);
+    const float dx = d2f(g[3 * v] - s.pos[3 * b]), dy = d2f(g[3 * v + 1] - s.pos[3 * b + 1]),
+                dz = d2f(g[3 * v + 2] - s.pos[3 * b + 2]);
+    // rounded up: a few float roundings of relative 6e-8 each, covered by 1e-6
+    const float d = sqrtf(dx * dx + dy * dy + dz * dz) * (1.f + 1e-6f) + 1e-30f;
     atomicMax(reinterpret_cast<unsigned int*>(s.bnd) + b, __float_as_uint(d));  // non-negative floats order as their bits
   } else {
     // Edge (midpoint, half length) or face (centroid, largest vertex
@@ -138,9 +143,9 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
     float cx = 0.f, cy = 0.f, cz = 0.f;
     for (int q = 1; q < cnt; q++) {
       const V3 d = g3(g, vl[q]) - o;
-      cx += (float)d.x;
-      cy += (float)d.y;
-      cz += (float)d.z;
+      cx += d2f(d.x);
+      cy += d2f(d.y);
+      cz += d2f(d.z);
     }
     const float inv = 1.f / (float)cnt;
     cx *= inv;
@@ -149,10 +154,10 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
     float r2 = cx * cx + cy * cy + cz * cz;  // vertex 0
     for (int q = 1; q < cnt; q++) {
       const V3 d = g3(g, vl[q]) - o;
-      const float ex = (float)d.x - cx, ey = (float)d.y - cy, ez = (float)d.z - cz;
+      const float ex = d2f(d.x) - cx, ey = d2f(d.y) - cy, ez = d2f(d.z) - cz;
       r2 = fmaxf(r2, ex * ex + ey * ey + ez * ez);
     }
-    const float px = (float)(o.x + (double)cx), py = (float)(o.y + (double)cy), pz = (float)(o.z + (double)cz);
+    const float px = d2f(o.x + f2d(cx)), py = d2f(o.y + f2d(cy)), pz = d2f(o.z + f2d(cz));
     const float mag = fmaxf(fmaxf(fabsf(px), fabsf(py)), fabsf(pz));
     s.sph[k] = make_float4(px, py, pz, sqrtf(r2) * (1.f + 1e-5f) + 1e-6f * mag + 1e-9f);
   }
@@ -221,8 +226,9 @@ __device__ __forceinline__ bool has_iface(const Scene& s, int i, int j) {
 // separation along one of the six face axes by more than the rounding
 // margin makes the FP64 test false as well, and one box's centre inside the
 // other (shrunk by the margin) makes it true as well; then the nine edge-edge
-// axes the same way (false only); only the cases in between run the FP64
-// test, so the result is the FP64 test's.
+// axes the same way, and an overlap by more than the margin along all
+// fifteen axes makes it true; only the cases in between run the FP64 test,
+// so the result is the FP64 test's.
 __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, int64_t j) {
   const float* A = s.bobbf + 15 * i;
   const float* B = s.bobbf + 15 * j;
@@ -237,6 +243,7 @@ __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, in
                     ea[0] + ea[1] + ea[2] + eb[0] + eb[1] + eb[2];
   const float m = 1e-6f * mag + 1e-9f;
   bool in_a = true, in_b = true;
+  bool clear = true;  // every axis so far overlaps by more than its margin
   float ta[3];
   for (int a = 0; a < 3; a++) {  // face axes of A
     ta[a] = tx * A[3 + 3 * a] + ty * A[4 + 3 * a] + tz * A[5 + 3 * a];
@@ -244,12 +251,14 @@ __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, in
     const float r = ea[a] + eb[0] * fabsf(R[a][0]) + eb[1] * fabsf(R[a][1]) + eb[2] * fabsf(R[a][2]);
     if (t > r + m) return false;
     in_a = in_a && t < ea[a] - m;
+    clear = clear && t < r - m;
   }
   for (int b = 0; b < 3; b++) {  // face axes of B
     const float t = fabsf(tx * B[3 + 3 * b] + ty * B[4 + 3 * b] + tz * B[5 + 3 * b]);
     const float r = eb[b] + ea[0] * fabsf(R[0][b]) + ea[1] * fabsf(R[1][b]) + ea[2] * fabsf(R[2][b]);
     if (t > r + m) return false;
     in_b = in_b && t < eb[b] - m;
+    clear = clear && t < r - m;
   }
   if (in_a || in_b) return true;
   // the nine edge-edge axes A_a x B_b, in A's frame; one more product level
@@ -261,9 +270,14 @@ __device__ __forceinline__ bool obb_pair_intersect(const Scene& s, int64_t i, in
       const int b1 = b == 2 ? 0 : b + 1, b2 = b == 0 ? 2 : b - 1;
       const float r = ea[a1] * fabsf(R[a2][b]) + ea[a2] * fabsf(R[a1][b]) + eb[b1] * fabsf(R[a][b2]) +
                       eb[b2] * fabsf(R[a][b1]);
-      if (fabsf(ta[a2] * R[a1][b] - ta[a1] * R[a2][b]) > r + mc) return false;
+      const float t = fabsf(ta[a2] * R[a1][b] - ta[a1] * R[a2][b]);
+      if (t > r + mc) return false;
+      clear = clear && t < r - mc;
     }
   }
+  // no axis separates in FP64 either when all fifteen overlap by more than
+  // their margins: the FP64 test is true
+  if (clear) return true;
   Obb oi = load_obb(s.bobb + 15 * i), oj = load_obb(s.bobb + 15 * j);
   enlarge(oi, 0.5 * s.DVerlet);
   enlarge(oj, 0.5 * s.DVerlet);
@@ -824,8 +838,8 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     uint32_t m0, m1;
     if (GEOM) {
       const float4* sbv = s.sph + s.sph_ofs[b];
-      const float4 cpp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
-      const float reach = (float)(P.Rb + P.Rp + P.dmax);
+      const float4 cpp = make_float4(d2f(s.pos[3 * p]), d2f(s.pos[3 * p + 1]), d2f(s.pos[3 * p + 2]), s.bnd[p]);
+      const float reach = d2f(P.Rb + P.Rp + P.dmax);
       bool hit0 = false, hit1 = false;
       for (int half = 0; half < 2; half++) {
         const int v = lane + 32 * half;
@@ -847,17 +861,19 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
       Obb op = load_obb(s.bobb + 15 * p);
       enlarge(op, P.dmax);
       const double r = P.Rb + P.dmax;
-      // Float pre-test along the partner box's own axes (the first three
-      // axes of the separating-axis test): separated there by more than the
-      // rounding margin -> the FP64 test is false as well; the vertex inside
-      // the box shrunk by the margin -> the FP64 test is true as well; only
-      // the cases in between run the FP64 test, so the mask is unchanged.
-      const float fcx = (float)op.c.x, fcy = (float)op.c.y, fcz = (float)op.c.z;
-      const float fe[3][3] = {{(float)op.e0.x, (float)op.e0.y, (float)op.e0.z},
-                              {(float)op.e1.x, (float)op.e1.y, (float)op.e1.z},
-                              {(float)op.e2.x, (float)op.e2.y, (float)op.e2.z}};
-      const float fext[3] = {(float)op.ext.x, (float)op.ext.y, (float)op.ext.z};
-      const float fr = (float)r;
+      // Float pre-test of the fifteen axes of the separating-axis test (the
+      // partner box's axes, the cube's -- the world axes -- and their
+      // cross products): separated along one by more than the rounding
+      // margin -> the FP64 test is false as well; the vertex inside the box
+      // shrunk by the margin, or an overlap by more than the margin along
+      // all fifteen -> the FP64 test is true as well; only the cases in
+      // between run the FP64 test, so the mask is unchanged.
+      const float fcx = d2f(op.c.x), fcy = d2f(op.c.y), fcz = d2f(op.c.z);
+      const float fe[3][3] = {{d2f(op.e0.x), d2f(op.e0.y), d2f(op.e0.z)},
+                              {d2f(op.e1.x), d2f(op.e1.y), d2f(op.e1.z)},
+                              {d2f(op.e2.x), d2f(op.e2.y), d2f(op.e2.z)}};
+      const float fext[3] = {d2f(op.ext.x), d2f(op.ext.y), d2f(op.ext.z)};
+      const float fr = d2f(r);
       const float4* sbv = s.sph + s.sph_ofs[b];
       const float mag = fmaxf(fmaxf(fabsf(fcx), fabsf(fcy)), fabsf(fcz)) + fext[0] + fext[1] + fext[2] + fr;
       bool hit0 = false, hit1 = false;
@@ -865,19 +881,42 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
         const int v = lane + 32 * half;
         if (v < nvb) {
           const float4 pv = sbv[v];
-          const float dx = pv.x - fcx, dy = pv.y - fcy, dz = pv.z - fcz;
-          bool out = false, in = true;
-          for (int i = 0; i < 3; i++) {
-            const float t = fabsf(dx * fe[i][0] + dy * fe[i][1] + dz * fe[i][2]);
+          const float dw[3] = {pv.x - fcx, pv.y - fcy, pv.z - fcz};
+          bool out = false, in = true, clear = true;
+          float tb[3];
+          for (int i = 0; i < 3; i++) {  // the box's axes
+            tb[i] = dw[0] * fe[i][0] + dw[1] * fe[i][1] + dw[2] * fe[i][2];
+            const float t = fabsf(tb[i]);
             const float lim = fext[i] + fr * (fabsf(fe[i][0]) + fabsf(fe[i][1]) + fabsf(fe[i][2]));
             const float m = 1e-6f * (mag + t) + 1e-9f;
             out = out || t > lim + m;
             in = in && t < fext[i] - m;
+            clear = clear && t < lim - m;
+          }
+          if (!out && !in) {
+            const float m = 1e-6f * mag + 1e-9f, mc = 4e-6f * mag + 1e-9f;
+            for (int j = 0; j < 3; j++) {  // the world axes
+              const float t = fabsf(dw[j]);
+              const float lim = fext[0] * fabsf(fe[0][j]) + fext[1] * fabsf(fe[1][j]) + fext[2] * fabsf(fe[2][j]) + fr;
+              out = out || t > lim + m;
+              clear = clear && t < lim - m;
+            }
+            for (int i = 0; i < 3; i++) {  // box axis i x world axis j
+              const int i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;
+              for (int j = 0; j < 3; j++) {
+                const int j1 = j == 2 ? 0 : j + 1, j2 = j == 0 ? 2 : j - 1;
+                const float t = fabsf(tb[i2] * fe[i1][j] - tb[i1] * fe[i2][j]);
+                const float lim = fext[i1] * fabsf(fe[i2][j]) + fext[i2] * fabsf(fe[i1][j]) +
+                                  fr * (fabsf(fe[i][j2]) + fabsf(fe[i][j1]));
+                out = out || t > lim + mc;
+                clear = clear && t < lim - mc;
+              }
+            }
           }
           bool hit;
           if (out) {
             hit = false;
-          } else if (in) {
+          } else if (in || clear) {
             hit = true;
           } else {
             Obb sub;
@@ -903,9 +942,9 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     // farther apart than the NEAR distance allows cannot be NEAR
     const float4* sb = s.sph + s.sph_ofs[b];
     const float4* sp = s.sph + s.sph_ofs[p];
-    const float sum = (float)(P.Rb + P.Rp + P.dmax);
-    const float4 cb = make_float4((float)s.pos[3 * b], (float)s.pos[3 * b + 1], (float)s.pos[3 * b + 2], s.bnd[b]);
-    const float4 cp = make_float4((float)s.pos[3 * p], (float)s.pos[3 * p + 1], (float)s.pos[3 * p + 2], s.bnd[p]);
+    const float sum = d2f(P.Rb + P.Rp + P.dmax);
+    const float4 cb = make_float4(d2f(s.pos[3 * b]), d2f(s.pos[3 * b + 1]), d2f(s.pos[3 * b + 2]), s.bnd[b]);
+    const float4 cp = make_float4(d2f(s.pos[3 * p]), d2f(s.pos[3 * p + 1]), d2f(s.pos[3 * p + 2]), s.bnd[p]);
     // margin for the float rounding of coordinates of magnitude up to `mag`
     // (about 16 ulps of it) on top of a relative 1e-4
     const float mag = fmaxf(fmaxf(fmaxf(fabsf(cb.x), fabsf(cb.y)), fabsf(cb.z)) + cb.w,
@@ -917,11 +956,11 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
       lim = lim + 1e-4f * lim + slack;
       return dx * dx + dy * dy + dz * dz > lim * lim;
     };
-    const float ve_ext = (float)(1.0 + 2.0 * P.dmax);
+    const float ve_ext = d2f(1.0 + 2.0 * P.dmax);
     const float glim = sum + 1e-4f * sum + slack;
     const float glim2 = glim * glim;
     const float alim = sum - (1e-4f * sum + slack);  // float acceptance: the NEAR distance shrunk by the margin
-    const float dmaxf = (float)P.dmax;
+    const float dmaxf = d2f(P.dmax);
     const bool lower = b < p;  // vertex-vertex and edge-edge pairs are tested in the i < j direction only
     // Two-level pruning (the role of Rockable's per-shape OBB trees,
     // Rockable.cpp:1440-1541, Shape.cpp:628-670): a sub-element stays in
@@ -934,7 +973,7 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
     // an owner vertex meets the partner's edges up to dmax x their length
     // beyond their ends (the vertex-edge projection test), so its reach
     // grows by that much (an edge is at most the partner's diameter long)
-    const float vreach = sum + 2.f * (float)P.dmax * cp.w;
+    const float vreach = sum + 2.f * dmaxf * cp.w;
     const int nbv = warp_list(L.bv, nvb, lane, [&](int v) {
       return (((v < 32 ? m0 : m1) >> (v & 31)) & 1u) != 0u && !box_far(bxp, sb[v], vreach, slack);
     });

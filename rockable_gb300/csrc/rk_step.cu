@@ -557,7 +557,13 @@ int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all) {
   const int64_t nv = all ? s.nvert : s.nlv;
   if (nv <= 0) return 0;
   const int t = tpb_or(s, 2, 256);
-  if (s.fast_body) return launch_fused_glob(s, nblk(nv, t), t, all ? 0 : 1, st);
+  if (s.fast_body) {
+    // the mixed form's step needs only the FP32 offsets and the FP64 frames;
+    // a list update needs the FP64 world vertices as well
+    int k = launch_body_frames(s, nblk(s.n, t), t, st);
+    if (all) k += launch_fused_glob(s, nblk(nv, t), t, 0, st);
+    return k;
+  }
   exact::k_glob_vertices<<<nblk(nv, t), t, 0, st>>>(s, all ? 0 : 1);
   return 1;
 }
@@ -572,7 +578,7 @@ int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st) {
   // (a batched skin step zeroes it in k_skin_begin)
   if (s.sk_out && apply_kick && !s.sk_ctl) cudaMemsetAsync(s.sk_out, 0, 8 * sizeof(unsigned int), st);
   const int t = tpb_or(s, 1, 128);
-  if (s.fast_body) return launch_fused_gather(s, nblk(s.n * kGatherLanes, t), t, apply_kick, st);
+  if (s.fast_body) return launch_fused_gather(s, nblk(s.n, t), t, apply_kick, st);  // one body per thread
   exact::k_gather_accel<<<nblk(s.n, t), t, 0, st>>>(s, apply_kick);
   return 1;
 }
