@@ -366,6 +366,8 @@ typedef struct rk_skin_stats {
   int64_t partial_bodies; /* bodies refreshed by them, summed */
   int64_t train_steps;    /* optimiser steps of the network so far */
   int64_t windows;        /* training windows in its replay buffer */
+  double rebuild_ms;      /* device time of a full rebuild (exponential average of the measured ones) */
+  double partial_ms;      /* device time of a partial refresh (the same) */
 } rk_skin_stats;
 int rk_set_skin(rk_ctx* ctx, const rk_skin_config* cfg);
 int rk_get_skin_stats(rk_ctx* ctx, rk_skin_stats* out);

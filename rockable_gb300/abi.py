@@ -77,7 +77,8 @@ class RkSkinConfig(C.Structure):
 class RkSkinStats(C.Structure):
     _fields_ = [("rebuilds", I64), ("forced", I64), ("scheduled", I64), ("skin", C.c_double), ("interval", I64),
                 ("last_rate", C.c_double), ("predicted_rate", C.c_double), ("loss", C.c_double),
-                ("partial", I64), ("partial_bodies", I64), ("train_steps", I64), ("windows", I64)]
+                ("partial", I64), ("partial_bodies", I64), ("train_steps", I64), ("windows", I64),
+                ("rebuild_ms", C.c_double), ("partial_ms", C.c_double)]
 
 
 class RkStepReport(C.Structure):

@@ -863,7 +863,7 @@ void rk_destroy(rk_ctx* x) {
   NLWork& w = c.w;
   dfree(w.pairs); dfree(w.hp); dfree(w.hp_tmp); dfree(w.hp_mask); dfree(w.cand); dfree(w.cand_tmp);
   dfree(w.flag); dfree(w.stale); dfree(w.stale_src); dfree(w.fkey); dfree(w.fsrc); dfree(w.jkeys); dfree(w.jtmp);
-  dfree(w.tmp); dfree(w.counter); dfree(w.gkeys); dfree(w.gtmp); dfree(w.gover); dfree(w.gis_over);
+  dfree(w.tmp); dfree(w.counter); dfree(w.gkeys); dfree(w.gtmp); dfree(w.gover); dfree(w.gis_over); dfree(w.gmark);
   if (w.gstat) cudaFree(w.gstat);
   if (w.split) cudaEventDestroy(w.split);
   dfree(c.kin_stage);
@@ -1426,6 +1426,8 @@ int rk_get_skin_stats(rk_ctx* x, rk_skin_stats* o) {
   o->partial_bodies = k.partial_bodies;
   o->train_steps = (int64_t)k.adam_step;
   o->windows = (int64_t)k.rx.size();
+  o->rebuild_ms = k.rebuild_ms;
+  o->partial_ms = k.partial_ms;
   return RK_OK;
 }
 

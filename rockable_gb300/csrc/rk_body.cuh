@@ -287,13 +287,15 @@ __global__ void k_drift(Scene s) {
 // global vertex k of body b: pos + Q (h v)
 // With only_listed, the vertices of s.lv (the bodies with neighbour-list
 // entries): within a step only the narrow phase reads these positions, and
-// only for bodies in the list; a list update recomputes every body first.
-__global__ void k_glob_vertices(Scene s, int only_listed) {
+// only for bodies in the list; a list update recomputes every body first
+// (a partial refresh, the bodies of its pairs: `mark`).
+__global__ void k_glob_vertices(Scene s, int only_listed, const uint8_t* mark) {
   if (step_halted(s)) return;
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= (only_listed ? s.nlv : s.nvert)) return;
   if (only_listed) k = s.lv[k];
   int b = s.gv_body[k];
+  if (mark && !mark[b]) return;
   int local = (int)(k - s.gv_ofs[b]);
   int sh = s.shape[b];
   double h = s.hom[b];

@@ -48,6 +48,8 @@ struct NLWork {
   uint64_t* gtmp = nullptr;
   int* gover = nullptr;
   uint8_t* gis_over = nullptr;
+  uint8_t* gmark = nullptr;  // bodies of the pairs of a partial refresh
+  int64_t mark_cap = 0;
   void* gstat = nullptr;
 };
 

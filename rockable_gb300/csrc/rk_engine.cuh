@@ -190,7 +190,8 @@ enum { FLAG_NEED_UPDATE = 0, FLAG_NACTIVE = 1, FLAG_NBROKEN = 2, FLAG_GPOS = 3, 
 int launch_controls_pre(const Scene& s, cudaStream_t st);
 int launch_drift(const Scene& s, cudaStream_t st);
 // all = false: only bodies with neighbour-list entries (the step's use)
-int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all = false);
+// all: every body's vertices (a list update), or with `mark` those of the marked bodies
+int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all = false, const uint8_t* mark = nullptr);
 int launch_narrow_force(const Scene& s, cudaStream_t st);
 int launch_narrow_force_mixed(const Scene& s, cudaStream_t st);
 int launch_gather_accel(const Scene& s, int apply_kick, cudaStream_t st);
@@ -206,7 +207,8 @@ int max_tpb(int which, int form_mixed);
 __device__ __forceinline__ bool step_halted(const Scene& s) { return s.sk_ctl != nullptr && s.sk_ctl[0] != 0u; }
 
 int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
-int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st);
+int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, const uint8_t* mark,
+                      cudaStream_t st);
 int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);

@@ -341,8 +341,9 @@ int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_
   mx::k_body_frames<<<blocks, threads, 10 * sizeof(float) * threads, st>>>(s);
   return 1;
 }
-int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, cudaStream_t st) {
-  fused::k_glob_vertices<<<blocks, threads, 0, st>>>(s, only_listed);
+int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, const uint8_t* mark,
+                      cudaStream_t st) {
+  fused::k_glob_vertices<<<blocks, threads, 0, st>>>(s, only_listed, mark);
   return 1;
 }
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st) {

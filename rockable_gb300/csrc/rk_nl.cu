@@ -100,33 +100,39 @@ __global__ void k_body_obb(Scene s) {
 
 // Bounding spheres of every sub-element (vertices, edges, faces) in world
 // coordinates, as floats with the radius rounded up: the conservative filter
-// in front of the FP64 NEAR predicates.  Conversions between FP64 and FP32
-// use the integer-pipe routines of rk_bits.cuh (round to nearest), which
-// keep the scarce FP64 pipe for the differences.
-__global__ void k_spheres(Scene s, int64_t nsph) {
+// in front of the FP64 NEAR predicates.  A vertex sphere's centre is its FP64
+// world vertex rounded to nearest (the float NEAR classification relies on
+// that); everything else comes from the FP32 vertex offsets gvr (world vertex
+// - body centre, written with the world vertices; relative error below 4e-7),
+// so that the kernel issues no FP64 arithmetic: GB300's FP64 pipe made it
+// FP64-bound.  Conversions use the integer-pipe routines of rk_bits.cuh.
+__global__ void k_spheres(Scene s, int64_t nsph, const uint8_t* mark) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= nsph) return;
   const int b = s.sph_body[k];
+  if (mark && !mark[b]) return;
   const int local = (int)(k - s.sph_ofs[b]);
   const int sh = s.shape[b];
-  const double* g = s.gv + 3 * s.gv_ofs[b];
+  const int64_t g0 = s.gv_ofs[b];
+  const double* g = s.gv + 3 * g0;
+  const float* gr = s.gvr + 3 * g0;
   const int nv = s.vert_ofs[sh + 1] - s.vert_ofs[sh];
   const int e0 = s.edge_ofs[sh], ne = s.edge_ofs[sh + 1] - e0;
   const int f0 = s.face_ofs[sh];
   if (local < nv) {  // vertex: its position; the body bound is the largest vertex distance
     const int v = local;
     s.sph[k] = make_float4(d2f(g[3 * v]), d2f(g[3 * v + 1]), d2f(g[3 * v + 2]), 0.f);
-    const float dx = d2f(g[3 * v] - s.pos[3 * b]), dy = d2f(g[3 * v + 1] - s.pos[3 * b + 1]),
-                dz = d2f(g[3 * v + 2] - s.pos[3 * b + 2]);
-    // rounded up: a few float roundings of relative 6e-8 each, covered by 1e-6
-    const float d = sqrtf(dx * dx + dy * dy + dz * dz) * (1.f + 1e-6f) + 1e-30f;
+    const float dx = gr[3 * v], dy = gr[3 * v + 1], dz = gr[3 * v + 2];
+    // rounded up: the offsets' error and a few float roundings, covered by 2e-6
+    const float d = sqrtf(dx * dx + dy * dy + dz * dz) * (1.f + 2e-6f) + 1e-30f;
     atomicMax(reinterpret_cast<unsigned int*>(s.bnd) + b, __float_as_uint(d));  // non-negative floats order as their bits
   } else {
     // Edge (midpoint, half length) or face (centroid, largest vertex
-    // distance), in float on FP64 offsets from the element's first vertex;
-    // the float centre is off the exact one by rounding, so the radius is the
-    // largest distance from that float centre, scaled up by 1e-5 and padded
-    // by 1e-6 of the coordinate magnitude: the sphere still holds the element.
+    // distance), from the FP32 offsets relative to the element's first
+    // vertex; the float centre is off the exact one by rounding, so the
+    // radius is the largest distance from that float centre, scaled up by
+    // 1e-5 and padded by 1e-6 of the coordinate magnitude: the sphere still
+    // holds the element.
     const bool edge = local < nv + ne;
     const int* vl;
     int cnt;
@@ -139,13 +145,12 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
       vl = s.face_verts + v0;
       cnt = s.face_vofs[f0 + f + 1] - v0;
     }
-    const V3 o = g3(g, vl[0]);
+    const float ox = gr[3 * vl[0]], oy = gr[3 * vl[0] + 1], oz = gr[3 * vl[0] + 2];
     float cx = 0.f, cy = 0.f, cz = 0.f;
     for (int q = 1; q < cnt; q++) {
-      const V3 d = g3(g, vl[q]) - o;
-      cx += d2f(d.x);
-      cy += d2f(d.y);
-      cz += d2f(d.z);
+      cx += gr[3 * vl[q]] - ox;
+      cy += gr[3 * vl[q] + 1] - oy;
+      cz += gr[3 * vl[q] + 2] - oz;
     }
     const float inv = 1.f / (float)cnt;
     cx *= inv;
@@ -153,11 +158,10 @@ __global__ void k_spheres(Scene s, int64_t nsph) {
     cz *= inv;
     float r2 = cx * cx + cy * cy + cz * cz;  // vertex 0
     for (int q = 1; q < cnt; q++) {
-      const V3 d = g3(g, vl[q]) - o;
-      const float ex = d2f(d.x) - cx, ey = d2f(d.y) - cy, ez = d2f(d.z) - cz;
+      const float ex = (gr[3 * vl[q]] - ox) - cx, ey = (gr[3 * vl[q] + 1] - oy) - cy, ez = (gr[3 * vl[q] + 2] - oz) - cz;
       r2 = fmaxf(r2, ex * ex + ey * ey + ez * ez);
     }
-    const float px = d2f(o.x + f2d(cx)), py = d2f(o.y + f2d(cy)), pz = d2f(o.z + f2d(cz));
+    const float px = d2f(g[3 * vl[0]]) + cx, py = d2f(g[3 * vl[0] + 1]) + cy, pz = d2f(g[3 * vl[0] + 2]) + cz;
     const float mag = fmaxf(fmaxf(fabsf(px), fabsf(py)), fabsf(pz));
     s.sph[k] = make_float4(px, py, pz, sqrtf(r2) * (1.f + 1e-5f) + 1e-6f * mag + 1e-9f);
   }
@@ -457,6 +461,16 @@ __global__ void k_over_pairs(Scene s, const uint8_t* only, const int* over, cons
 __global__ void k_mark_over(const int* over, int nover, uint8_t* is_over) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < nover) is_over[over[k]] = 1;
+}
+
+// the two bodies of every pair of a partial refresh (their world vertices
+// and spheres are the only ones its candidate tests read)
+__global__ void k_mark_pair_bodies(const uint64_t* pairs, int64_t np, uint8_t* mark) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  const uint64_t p = pairs[k];
+  mark[p >> 21] = 1;
+  mark[p & ((1u << 21) - 1)] = 1;
 }
 
 __global__ void k_half_pairs(const uint64_t* pairs, int64_t np, uint64_t* hp) {
@@ -773,6 +787,23 @@ __device__ __forceinline__ bool box_far(const float* bx, float4 c, float reach, 
   return d2 > lim * lim;
 }
 
+// The owner-vertex cull's FP64 test (Rockable.cpp:1385-1391): the cube of
+// half-size r around vertex v against the partner's OBB enlarged by dmax.
+// Not inlined: inlined, the compiler evaluated it for every vertex and
+// selected the result (about 300 FP64 operations per vertex), although the
+// float pre-test leaves it to fewer than one vertex in 4000.
+__device__ __noinline__ bool cull_fp64(const double* obb, double dmax, const double* gb, int v, double r) {
+  Obb op = load_obb(obb);
+  enlarge(op, dmax);
+  Obb sub;
+  sub.c = g3(gb, v);
+  sub.e0 = v3(1, 0, 0);
+  sub.e1 = v3(0, 1, 0);
+  sub.e2 = v3(0, 0, 1);
+  sub.ext = v3(r, r, r);
+  return obb_intersect(op, sub);
+}
+
 struct CandLists {
   uint16_t bv[64], pv[64];                   // owner / partner vertices
   uint16_t be[kMaxSub], pe[kMaxSub], pf[kMaxSub];  // owner edges, partner edges and faces
@@ -919,13 +950,7 @@ k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t*
           } else if (in || clear) {
             hit = true;
           } else {
-            Obb sub;
-            sub.c = g3(P.gb, v);
-            sub.e0 = v3(1, 0, 0);
-            sub.e1 = v3(0, 1, 0);
-            sub.e2 = v3(0, 0, 1);
-            sub.ext = v3(r, r, r);
-            hit = obb_intersect(op, sub);
+            hit = cull_fp64(s.bobb + 15 * p, P.dmax, P.gb, v, r);
           }
           if (half == 0) hit0 = hit;
           else hit1 = hit;
@@ -1250,12 +1275,20 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   const int64_t N = s.n;
   if (N <= 0) return 0;
   RKCHK(cudaMemsetAsync(s.flags + FLAG_NONFINITE, 0, sizeof(unsigned long long), st));
-  c.kernels += launch_glob_vertices(s, st, true);  // the step computed only the listed bodies' vertices
-  k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
+  // The boxes of every body; the world vertices and the sub-element spheres
+  // (the step computed only the listed bodies' vertices) of every body for a
+  // full build, of the bodies of the visited pairs for a partial refresh
+  // (after the pairs are known).
+  const bool defer = only != nullptr;
   const int64_t nsph = c.nsph;
   RKCHK(cudaMemsetAsync(s.bnd, 0, (size_t)N * sizeof(float), st));
-  if (nsph > 0) k_spheres<<<nblk(nsph, 256), 256, 0, st>>>(s, nsph);
-  c.kernels += 2;
+  if (!defer) {
+    c.kernels += launch_glob_vertices(s, st, true);
+    if (nsph > 0) k_spheres<<<nblk(nsph, 256), 256, 0, st>>>(s, nsph, nullptr);
+    c.kernels++;
+  }
+  k_body_obb<<<nblk(N, 128), 128, 0, st>>>(s);
+  c.kernels++;
   {  // a body whose state is no longer finite: stop here, loudly
     unsigned long long bad = 0;
     RKCHK(cudaMemcpyAsync(&bad, s.flags + FLAG_NONFINITE, sizeof bad, cudaMemcpyDeviceToHost, st));
@@ -1350,6 +1383,17 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
     }
   }
   if (np < 0) { c.err = "pair buffer kept overflowing"; return RK_ERR_CAPACITY; }
+  if (defer) {  // the bodies of the visited pairs: world vertices and spheres
+    if (w.mark_cap < N) {
+      if ((rc = grow(c, w.gmark, w.mark_cap, N))) return rc;
+      w.mark_cap = N;
+    }
+    RKCHK(cudaMemsetAsync(w.gmark, 0, (size_t)N, st));
+    if (np > 0) k_mark_pair_bodies<<<nblk(np, 256), 256, 0, st>>>(w.pairs, np, w.gmark);
+    c.kernels += 1 + launch_glob_vertices(s, st, true, w.gmark);
+    if (nsph > 0) k_spheres<<<nblk(nsph, 256), 256, 0, st>>>(s, nsph, w.gmark);
+    c.kernels++;
+  }
   c.last_cell = cell;
   c.last_nover = nover;
   if (w.timing_split && w.split) RKCHK(cudaEventRecord(w.split, st));

@@ -553,7 +553,7 @@ int launch_drift(const Scene& s, cudaStream_t st) {
   exact::k_drift<<<nblk(nf, t), t, 0, st>>>(s);
   return 1;
 }
-int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all) {
+int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all, const uint8_t* mark) {
   const int64_t nv = all ? s.nvert : s.nlv;
   if (nv <= 0) return 0;
   const int t = tpb_or(s, 2, 256);
@@ -561,10 +561,10 @@ int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all) {
     // the mixed form's step needs only the FP32 offsets and the FP64 frames;
     // a list update needs the FP64 world vertices as well
     int k = launch_body_frames(s, nblk(s.n, t), t, st);
-    if (all) k += launch_fused_glob(s, nblk(nv, t), t, 0, st);
+    if (all) k += launch_fused_glob(s, nblk(nv, t), t, 0, mark, st);
     return k;
   }
-  exact::k_glob_vertices<<<nblk(nv, t), t, 0, st>>>(s, all ? 0 : 1);
+  exact::k_glob_vertices<<<nblk(nv, t), t, 0, st>>>(s, all ? 0 : 1, all ? mark : nullptr);
   return 1;
 }
 int launch_narrow_force(const Scene& s, cudaStream_t st) {
