@@ -850,7 +850,7 @@ void rk_destroy(rk_ctx* x) {
   dfree(s.svert); dfree(s.sradius); dfree(s.sobb); dfree(s.sbox); dfree(s.bbox);
   dfree(s.pos); dfree(s.vel); dfree(s.acc); dfree(s.Q); dfree(s.vrot); dfree(s.arot); dfree(s.force); dfree(s.moment);
   dfree(s.hom); dfree(s.mass); dfree(s.inertia); dfree(s.rad); dfree(s.inv_mi); dfree(s.shape); dfree(s.group); dfree(s.cluster);
-  dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.gvr); dfree(s.posf); dfree(s.rotm); dfree(s.gsum); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
+  dfree(s.gv_ofs); dfree(s.gv_body); dfree(s.lv); dfree(s.gv); dfree(s.gvr); dfree(s.posf); dfree(s.rotm); dfree(s.gsum); dfree(s.uv64); dfree(s.uvf); dfree(s.bobb); dfree(s.bobbf); dfree(s.baabb); dfree(s.dpos); dfree(s.dq);
   dfree(s.table); dfree(s.controls);
   dfree(s.act); dfree(s.cf); dfree(s.cmi); dfree(s.cmj); dfree(s.iofs); dfree(s.jofs); dfree(s.jsplit); dfree(s.jlist); dfree(s.nperm); dfree(s.egv); dfree(s.slow);
   dfree(s.heavy); dfree(s.is_heavy); dfree(s.sph); dfree(s.sph_ofs); dfree(s.sph_body); dfree(s.heavy_lazy); dfree(s.bnd);
@@ -900,6 +900,7 @@ int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
   cudaSetDevice(c.device);
   const int ns = sh->nshapes;
   const int nv = sh->vert_ofs[ns], ne = sh->edge_ofs[ns], nf = sh->face_ofs[ns], nfv = sh->face_vofs[nf];
+  const std::vector<int> nv_before = c.shape_nv, ne_before = c.shape_ne, nf_before = c.shape_nf;
   c.shape_nv.assign(ns, 0);
   c.shape_ne.assign(ns, 0);
   c.shape_nf.assign(ns, 0);
@@ -947,6 +948,22 @@ int rk_upload_shapes(rk_ctx* x, const rk_shapes* sh) {
   s.nshapes = ns;
   c.shape_radius.assign(sh->radius, sh->radius + ns);
   c.have_shapes = true;
+  if (c.have_bodies && c.s.n > 0) {  // bodies placed on the new shape tables: same element counts only
+    bool same = true;
+    for (int64_t b = 0; b < c.s.n && b < (int64_t)c.body_shape.size() && same; b++) {
+      const int q = c.body_shape[b];
+      same = q < ns && q < (int)nv_before.size() && c.shape_nv[q] == nv_before[q] && c.shape_ne[q] == ne_before[q] &&
+             c.shape_nf[q] == nf_before[q];
+    }
+    if (!same) {
+      c.have_bodies = false;
+      c.s.n = 0;
+      c.s.ne = 0;
+      return fail(c, RK_ERR_STATE, "new shape tables change the bodies' vertex, edge or face counts: upload the bodies again");
+    }
+    c.kernels += launch_body_verts(c.s, c.stream);
+    CK(cudaGetLastError());
+  }
   return RK_OK;
 }
 
@@ -1002,6 +1019,7 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
       (rc = dupload(c, s.bobbf, (const float*)nullptr, 15 * n)) ||
       (rc = dupload(c, s.bbox, (const float*)nullptr, 15 * n)) ||
       (rc = dalloc(c, s.posf, n)) || (rc = dalloc(c, s.rotm, 9 * n)) || (rc = dalloc(c, s.gsum, 6 * n)) ||
+      (rc = dalloc(c, s.uv64, 3 * std::max<int64_t>(nv, 1))) || (rc = dalloc(c, s.uvf, std::max<int64_t>(nv, 1))) ||
       (rc = dupload(c, s.baabb, (const float*)nullptr, 6 * n)) ||
       (rc = dupload(c, s.dpos, (const double*)nullptr, 3 * n)) || (rc = dupload(c, s.dq, (const double*)nullptr, 4 * n)) ||
       (rc = dupload(c, s.iofs, (const int64_t*)nullptr, n + 1)) ||
@@ -1033,6 +1051,9 @@ int rk_upload_bodies(rk_ctx* x, const rk_bodies* b) {
   s.n = n;
   s.n_driven = b->n_driven;
   s.nvert = nv;
+  launch_body_verts(s, c.stream);
+  c.kernels++;
+  CK(cudaGetLastError());
   c.body_shape.assign(b->shape, b->shape + n);
   c.body_hom.assign(b->homothety, b->homothety + n);
   s.ne = 0;

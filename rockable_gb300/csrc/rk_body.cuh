@@ -296,11 +296,8 @@ __global__ void k_glob_vertices(Scene s, int only_listed, const uint8_t* mark) {
   if (only_listed) k = s.lv[k];
   int b = s.gv_body[k];
   if (mark && !mark[b]) return;
-  int local = (int)(k - s.gv_ofs[b]);
-  int sh = s.shape[b];
-  double h = s.hom[b];
-  const double* sv = s.svert + 3 * (int64_t)(s.vert_ofs[sh] + local);
-  V3 u = h * v3(sv[0], sv[1], sv[2]);
+  const int local = (int)(k - s.gv_ofs[b]);
+  const V3 u = v3(s.uv64[3 * k], s.uv64[3 * k + 1], s.uv64[3 * k + 2]);  // h v, computed at upload
   V3 r = qrot(ldq(s.Q, b), u);
   V3 g = ld3(s.pos, b) + r;
   st3(s.gv, k, g);

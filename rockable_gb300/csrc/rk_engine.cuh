@@ -85,6 +85,9 @@ struct Scene {
                      // mixed form's test of clearly separated entries)
   float4* posf;      // n: body centre rounded to FP32 and its Minkowski radius, written with the
                      // world vertices (the same test)
+  double* uv64;      // 3*nvert: each body vertex scaled by the body's homothety, h v, in the shape
+                     // frame (written at upload: what every placement of a vertex starts from)
+  float4* uvf;       // nvert: the same rounded to FP32
   float* gsum;       // 6 per body: the mixed form's FP32 contact sums (force, moment) of the step
   double* rotm;      // 9 per body: the mixed form's FP64 rotation matrix of Q (row-major), written
                      // each step with gvr; its FP64 path places the few vertices it needs from it
@@ -210,6 +213,7 @@ int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, const uint8_t* mark,
                       cudaStream_t st);
 int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
+int launch_body_verts(const Scene& s, cudaStream_t st);
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);
 int launch_skin_begin(const Scene& s, cudaStream_t st);

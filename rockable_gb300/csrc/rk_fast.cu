@@ -252,7 +252,7 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
 // work per body is one matrix instead of one rotation per vertex.
 __global__ void k_body_frames(Scene s) {
   if (step_halted(s)) return;
-  extern __shared__ float fr[];  // [blockDim.x][10]: the FP32 matrix and homothety
+  extern __shared__ float fr[];  // [blockDim.x][10]: the FP32 matrix (and a pad)
   const int64_t b0 = blockIdx.x * (int64_t)blockDim.x;
   const int64_t b = b0 + threadIdx.x;
   if (b < s.n) {
@@ -269,7 +269,7 @@ __global__ void k_body_frames(Scene s) {
       out[d] = R[d];
       fr[10 * threadIdx.x + d] = d2f(R[d]);
     }
-    fr[10 * threadIdx.x + 9] = d2f(s.hom[b]);
+    fr[10 * threadIdx.x + 9] = 0.f;
     const V3 p = ld3(s.pos, b);
     s.posf[b] = make_float4(d2f(p.x), d2f(p.y), d2f(p.z), d2f(s.rad[b]));
   }
@@ -278,10 +278,9 @@ __global__ void k_body_frames(Scene s) {
   if (b0 >= bend) return;
   const int64_t k1 = s.gv_ofs[bend];
   for (int64_t k = s.gv_ofs[b0] + threadIdx.x; k < k1; k += blockDim.x) {
-    const int bb = s.gv_body[k];
-    const float* f = fr + 10 * (bb - b0);
-    const double* sv = s.svert + 3 * ((int64_t)s.vert_ofs[s.shape[bb]] + (k - s.gv_ofs[bb]));
-    const float ux = f[9] * d2f(sv[0]), uy = f[9] * d2f(sv[1]), uz = f[9] * d2f(sv[2]);
+    const float* f = fr + 10 * (s.gv_body[k] - b0);
+    const float4 u = s.uvf[k];  // h v, FP32
+    const float ux = u.x, uy = u.y, uz = u.z;
     s.gvr[3 * k] = f[0] * ux + f[1] * uy + f[2] * uz;
     s.gvr[3 * k + 1] = f[3] * ux + f[4] * uy + f[5] * uz;
     s.gvr[3 * k + 2] = f[6] * ux + f[7] * uy + f[8] * uz;

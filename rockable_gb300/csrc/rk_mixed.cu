@@ -50,19 +50,18 @@ __device__ __forceinline__ void st3m(double* a, int64_t k, F3 v) {
   a[3 * k + 1] = f2d(v.y);
   a[3 * k + 2] = f2d(v.z);
 }
-// FP64 world position of vertex `local` of body b: pos + R (h v), R the
-// step's rotation matrix of the body (rotm, written by the body-frame kernel)
-__device__ __forceinline__ V3 vtx64(const Scene& s, int b, int local) {
-  const double* sv = s.svert + 3 * ((int64_t)s.vert_ofs[s.shape[b]] + local);
-  const double h = s.hom[b];
-  const double ux = h * sv[0], uy = h * sv[1], uz = h * sv[2];
+// FP64 world position of global vertex k of body b: pos + R (h v), R the
+// step's rotation matrix of the body (rotm, written by the body-frame
+// kernel), h v from the per-vertex table uv64
+__device__ __forceinline__ V3 vtx64g(const Scene& s, int b, int64_t k) {
+  const double ux = s.uv64[3 * k], uy = s.uv64[3 * k + 1], uz = s.uv64[3 * k + 2];
   const double* R = s.rotm + 9 * (int64_t)b;
   return v3(s.pos[3 * (int64_t)b] + (R[0] * ux + R[1] * uy + R[2] * uz),
             s.pos[3 * (int64_t)b + 1] + (R[3] * ux + R[4] * uy + R[5] * uz),
             s.pos[3 * (int64_t)b + 2] + (R[6] * ux + R[7] * uy + R[8] * uz));
 }
-// the same for global vertex index k of body b
-__device__ __forceinline__ V3 vtx64g(const Scene& s, int b, int64_t k) { return vtx64(s, b, (int)(k - s.gv_ofs[b])); }
+// the same for vertex `local` of body b
+__device__ __forceinline__ V3 vtx64(const Scene& s, int b, int local) { return vtx64g(s, b, s.gv_ofs[b] + local); }
 
 // |d| in FP64 from an FP32 reciprocal-sqrt seed and two Newton steps
 __device__ __forceinline__ double len64(V3 d, double& inv) {

@@ -545,6 +545,25 @@ static inline int tpb_or(const Scene& s, int k, int d) { return s.tpb[k] > 0 ? s
 
 // The per-body kernels come in two builds (rk_body.cuh): exact (this file,
 // no contraction) and fused (rk_fast.cu), the latter for the mixed form.
+// h v of every body vertex (shape frame), FP64 and FP32: a vertex's
+// placement then reads one record instead of the chain body -> shape ->
+// shape vertex offset -> shape vertex.
+__global__ void k_body_verts(Scene s) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= s.nvert) return;
+  const int b = s.gv_body[k];
+  const double* sv = s.svert + 3 * ((int64_t)s.vert_ofs[s.shape[b]] + (k - s.gv_ofs[b]));
+  const double h = s.hom[b];
+  const double u[3] = {h * sv[0], h * sv[1], h * sv[2]};
+  for (int d = 0; d < 3; d++) s.uv64[3 * k + d] = u[d];
+  s.uvf[k] = make_float4((float)u[0], (float)u[1], (float)u[2], 0.f);
+}
+int launch_body_verts(const Scene& s, cudaStream_t st) {
+  if (s.nvert <= 0) return 0;
+  k_body_verts<<<nblk(s.nvert, 256), 256, 0, st>>>(s);
+  return 1;
+}
+
 int launch_drift(const Scene& s, cudaStream_t st) {
   int64_t nf = s.n - s.n_driven;
   if (nf <= 0) return 0;
