@@ -353,45 +353,92 @@ __global__ void k_grid_sum(Scene s, double* sum) {
   if ((threadIdx.x & 31) == 0) atomicAdd(sum, e);
 }
 
-__global__ void k_grid_max(Scene s, float lim, unsigned int* maxbits) {
+// float <-> unsigned with the same order (for atomic min / max)
+__device__ __forceinline__ unsigned int ord_of(float f) {
+  const unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+static inline float float_of_ord(unsigned int o) {
+  const unsigned int u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+// the largest extent among bodies not larger than lim, and the range of all
+// bodies' box centres (ordered bits: lo[3] from all-ones, hi[3] from zero)
+__global__ void k_grid_max(Scene s, float lim, unsigned int* maxbits, unsigned int* lo, unsigned int* hi) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   float e = 0.f;
+  unsigned int cl[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, ch[3] = {0u, 0u, 0u};
   if (b < s.n) {
-    e = extent_of(s.baabb + 6 * b);
+    const float* bb = s.baabb + 6 * b;
+    e = extent_of(bb);
     if (!(e <= lim)) e = 0.f;
+    for (int a = 0; a < 3; a++) cl[a] = ch[a] = ord_of(0.5f * (bb[a] + bb[3 + a]));
   }
-  for (int o = 16; o > 0; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(e));
+  for (int o = 16; o > 0; o >>= 1) {
+    e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    for (int a = 0; a < 3; a++) {
+      cl[a] = min(cl[a], __shfl_xor_sync(0xffffffffu, cl[a], o));
+      ch[a] = max(ch[a], __shfl_xor_sync(0xffffffffu, ch[a], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(maxbits, __float_as_uint(e));
+    for (int a = 0; a < 3; a++) {
+      atomicMin(lo + a, cl[a]);
+      atomicMax(hi + a, ch[a]);
+    }
+  }
 }
 
-// Cell code of the sort key (42 bits above the 21 body bits).  One scene:
-// 14 bits per axis.  Several scenes: the scene index (mod 512) in the top 9
-// bits and 11 bits per axis, so bodies of different scenes that share a
-// region of space fall in different cells.  Coordinates are clamped at the
-// edges of the range; clamping keeps neighbouring cells neighbours, so the
-// search stays conservative (far bodies only share a cell, filtered later).
-// The largest coordinate stays one below all-ones so that no cell code equals
-// the all-ones key that sorts the oversized bodies last.
+// Cell code of the sort key (above the 21 body bits): per axis as many bits
+// as the cells the bodies' box centres span (plus one spare cell on each
+// side), at most 14 (11 with several scenes); several scenes: the scene
+// index (mod 512) above them, so bodies of different scenes that share a
+// region of space fall in different cells.  The fewer bits, the fewer
+// passes of the key sort.  Coordinates are clamped at the edges of the
+// range; clamping keeps neighbouring cells neighbours, so the search stays
+// conservative (far bodies only share a cell, filtered later).  The largest
+// coordinate stays one below all-ones so that no cell code equals the
+// all-ones key that sorts the oversized bodies last.
 struct CellFormat {
-  int bits, off, max;  // per-axis bits, offset of cell 0, largest coordinate
+  int bits[3], off[3], max[3];  // per-axis bits, offset of cell 0, largest coordinate
+  int total;                    // bits of the code (with the scene's)
   bool batched;
 };
-__device__ __forceinline__ CellFormat cell_format(const Scene& s) {
-  return s.scene_of ? CellFormat{11, 1024, 2046, true} : CellFormat{14, 8192, 16382, false};
+static CellFormat make_cell_format(bool batched, float inv_cell, const float lo[3], const float hi[3]) {
+  CellFormat f;
+  f.batched = batched;
+  f.total = batched ? 9 : 0;
+  const int cap = batched ? 11 : 14;
+  for (int a = 0; a < 3; a++) {
+    double c0 = std::floor((double)lo[a] * inv_cell), c1 = std::floor((double)hi[a] * inv_cell);
+    if (!(c0 <= c1) || !std::isfinite(c0) || !std::isfinite(c1)) c0 = c1 = 0.0;
+    const double range = c1 - c0 + 1.0;  // cells spanned; coordinates 1..range, spare 0 and range + 1
+    int b = 1;
+    while (b < cap && (double)((1 << b) - 2) < range + 1.0) b++;
+    f.bits[a] = b;
+    f.max[a] = (1 << b) - 2;
+    f.off[a] = (int)std::max(-1e9, std::min(1e9, 1.0 - c0));
+    f.total += b;
+  }
+  return f;
 }
 
-__device__ __forceinline__ int cell_coord(float x, float inv_cell, const CellFormat& f) {
-  float v = floorf(x * inv_cell) + (float)f.off;
-  v = fminf(fmaxf(v, 0.f), (float)f.max);
+__device__ __forceinline__ int cell_coord(float x, float inv_cell, const CellFormat& f, int a) {
+  float v = floorf(x * inv_cell) + (float)f.off[a];
+  v = fminf(fmaxf(v, 0.f), (float)f.max[a]);
   return (int)v;
 }
 
 __device__ __forceinline__ uint64_t cell_code(uint64_t scene, int x, int y, int z, const CellFormat& f) {
-  const uint64_t c = ((uint64_t)x << (2 * f.bits)) | ((uint64_t)y << f.bits) | (uint64_t)z;
-  return f.batched ? ((scene & 511u) << 33) | c : c;
+  const uint64_t c = ((uint64_t)x << (f.bits[1] + f.bits[2])) | ((uint64_t)y << f.bits[2]) | (uint64_t)z;
+  return f.batched ? ((scene & 511u) << (f.bits[0] + f.bits[1] + f.bits[2])) | c : c;
 }
 
-__global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys, int* over,
+__global__ void k_grid_keys(Scene s, CellFormat f, float cell, float inv_cell, uint64_t* keys, int* over,
                             unsigned long long* nover) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
@@ -401,40 +448,42 @@ __global__ void k_grid_keys(Scene s, float cell, float inv_cell, uint64_t* keys,
     over[atomicAdd(nover, 1ull)] = (int)b;
     return;
   }
-  const CellFormat f = cell_format(s);
-  const int cx = cell_coord(0.5f * (bb[0] + bb[3]), inv_cell, f), cy = cell_coord(0.5f * (bb[1] + bb[4]), inv_cell, f),
-            cz = cell_coord(0.5f * (bb[2] + bb[5]), inv_cell, f);
+  const int cx = cell_coord(0.5f * (bb[0] + bb[3]), inv_cell, f, 0), cy = cell_coord(0.5f * (bb[1] + bb[4]), inv_cell, f, 1),
+            cz = cell_coord(0.5f * (bb[2] + bb[5]), inv_cell, f, 2);
   const uint64_t scene = f.batched ? (uint64_t)(uint32_t)s.scene_of[b] : 0u;
   keys[b] = (cell_code(scene, cx, cy, cz, f) << 21) | (uint64_t)b;
 }
 
 // With `only` (a partial refresh), body i enumerates its pairs when it is
 // flagged, with every neighbour that is not flagged or has a larger index.
-// One thread per body and neighbour column (the nine (x, y) columns around
-// its cell): nine times the threads of a body loop, for the latency of the
-// key searches and of the pair tests.
-__global__ void k_grid_pairs(Scene s, const uint8_t* only, const uint64_t* keys, int64_t nnorm, float inv_cell,
+// kGridLanes threads per body and neighbour column (the nine (x, y) columns
+// around its cell), each testing every kGridLanes-th body of the column:
+// short chains of dependent loads (key, boxes, interfaces) per thread.
+constexpr int kGridLanes = 4;
+__global__ void k_grid_pairs(Scene s, CellFormat f, const uint8_t* only, const uint64_t* keys, int64_t nnorm,
                              uint64_t* pairs, int64_t cap, unsigned long long* counter) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t k = t / 9;
-  const int col = (int)(t - 9 * k);
+  const int lane = (int)(t % kGridLanes);
+  const int64_t g = t / kGridLanes;
+  const int64_t k = g / 9;
+  const int col = (int)(g - 9 * k);
   if (k >= nnorm) return;
-  const CellFormat f = cell_format(s);
   const uint64_t key = keys[k];
   const int64_t i = (int64_t)(key & ((1u << 21) - 1));
   if (only && !only[i]) return;
   const uint64_t code = key >> 21;
-  const uint64_t amask = (1u << f.bits) - 1u;
-  const uint64_t scene = f.batched ? (code >> 33) : 0u;
-  const int cx = (int)((code >> (2 * f.bits)) & amask), cy = (int)((code >> f.bits) & amask), cz = (int)(code & amask);
+  const int bxyz = f.bits[0] + f.bits[1] + f.bits[2];
+  const uint64_t scene = f.batched ? (code >> bxyz) : 0u;
+  const int cx = (int)((code >> (f.bits[1] + f.bits[2])) & ((1u << f.bits[0]) - 1u));
+  const int cy = (int)((code >> f.bits[2]) & ((1u << f.bits[1]) - 1u)), cz = (int)(code & ((1u << f.bits[2]) - 1u));
   // z is the lowest field of the cell code: the three cells (x, y, z-1..z+1)
   // of a neighbour column are one contiguous key range
-  const int z0 = max(cz - 1, 0), z1 = min(cz + 1, f.max);
+  const int z0 = max(cz - 1, 0), z1 = min(cz + 1, f.max[2]);
   const int x = cx + col / 3 - 1, y = cy + col % 3 - 1;
-  if (x < 0 || y < 0 || x > f.max || y > f.max) return;
+  if (x < 0 || y < 0 || x > f.max[0] || y > f.max[1]) return;
   const uint64_t first = cell_code(scene, x, y, z0, f) << 21;
   const uint64_t last = cell_code(scene, x, y, z1, f);
-  for (int64_t q = lower_bound_u64(keys, nnorm, first); q < nnorm && (keys[q] >> 21) <= last; q++) {
+  for (int64_t q = lower_bound_u64(keys, nnorm, first) + lane; q < nnorm && (keys[q] >> 21) <= last; q += kGridLanes) {
     const int64_t j = (int64_t)(keys[q] & ((1u << 21) - 1));
     if (only ? (j == i || (only[j] && j < i)) : (j <= i)) continue;
     const int64_t lo = min(i, j), hi = max(i, j);
@@ -1260,6 +1309,13 @@ static int ensure_tmp(Ctx& c, int64_t bytes) {
   return 0;
 }
 
+// bits of the largest body index: the sorts skip the key bits no body uses
+static int body_bits(int64_t n) {
+  int b = 1;
+  while (b < 21 && ((int64_t)1 << b) < n) b++;
+  return b;
+}
+
 static int64_t read_i64(Ctx& c, const int64_t* d) {
   int64_t v = 0;
   cudaMemcpyAsync(&v, d, sizeof v, cudaMemcpyDeviceToHost, c.stream);
@@ -1308,7 +1364,7 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   if (!w.counter) RKCHK(cudaMalloc(&w.counter, 64));
   int64_t np = -1;
   bool use_grid = (c.broadphase == 2) || (c.broadphase == 0 && N > 4096);
-  float cell = 0.f;
+  float cell = 0.f, clo[3] = {0.f, 0.f, 0.f}, chi[3] = {0.f, 0.f, 0.f};
   int64_t nover = 0;
   if (use_grid) {
     // cell size: the largest extent among bodies not larger than 4x the mean
@@ -1325,32 +1381,41 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
     RKCHK(cudaMemcpyAsync(&mean_sum, w.gstat, 8, cudaMemcpyDeviceToHost, st));
     RKCHK(cudaStreamSynchronize(st));
     const float lim = (float)(4.0 * mean_sum / (double)N);
-    k_grid_max<<<nblk(N, 256), 256, 0, st>>>(s, lim, (unsigned int*)((char*)w.gstat + 8));
-    unsigned int mb = 0;
-    RKCHK(cudaMemcpyAsync(&mb, (char*)w.gstat + 8, 4, cudaMemcpyDeviceToHost, st));
+    // gstat: [8] largest extent bits, [24] centre range (3 ordered minima, 3 maxima)
+    RKCHK(cudaMemsetAsync((char*)w.gstat + 24, 0xff, 12, st));
+    k_grid_max<<<nblk(N, 256), 256, 0, st>>>(s, lim, (unsigned int*)((char*)w.gstat + 8),
+                                             (unsigned int*)((char*)w.gstat + 24), (unsigned int*)((char*)w.gstat + 36));
+    unsigned int mb[10] = {};
+    RKCHK(cudaMemcpyAsync(mb, (char*)w.gstat + 8, 40, cudaMemcpyDeviceToHost, st));
     RKCHK(cudaStreamSynchronize(st));
-    std::memcpy(&cell, &mb, 4);
+    std::memcpy(&cell, &mb[0], 4);
+    for (int a = 0; a < 3; a++) {
+      clo[a] = float_of_ord(mb[4 + a]);
+      chi[a] = float_of_ord(mb[7 + a]);
+    }
     cell *= 1.01f;
     c.kernels += 2;
     if (!(cell > 0.f)) use_grid = false;
   }
   if (use_grid) {
     const float inv = 1.0f / cell;
+    const CellFormat fmt = make_cell_format(s.scene_of != nullptr, inv, clo, chi);
     RKCHK(cudaMemsetAsync((char*)w.gstat + 16, 0, 8, st));
     RKCHK(cudaMemsetAsync(w.gis_over, 0, N, st));
-    k_grid_keys<<<nblk(N, 256), 256, 0, st>>>(s, cell, inv, w.gkeys, w.gover, (unsigned long long*)((char*)w.gstat + 16));
+    k_grid_keys<<<nblk(N, 256), 256, 0, st>>>(s, fmt, cell, inv, w.gkeys, w.gover,
+                                              (unsigned long long*)((char*)w.gstat + 16));
     unsigned long long no_ = 0;
     RKCHK(cudaMemcpyAsync(&no_, (char*)w.gstat + 16, 8, cudaMemcpyDeviceToHost, st));
     RKCHK(cudaStreamSynchronize(st));
     nover = (int64_t)no_;
     if ((rc = ensure_tmp(c, (int64_t)sort_temp_bytes(N)))) return rc;
-    radix_sort_u64(w.gkeys, w.gtmp, N, 21, 63, w.tmp, st);
+    radix_sort_u64(w.gkeys, w.gtmp, N, 21, 21 + fmt.total, w.tmp, st);
     if (nover > 0) k_mark_over<<<nblk(nover, 256), 256, 0, st>>>(w.gover, (int)nover, w.gis_over);
     c.kernels += 16;
     for (int attempt = 0; attempt < 4; attempt++) {
       RKCHK(cudaMemsetAsync(w.counter, 0, 8, st));
-      k_grid_pairs<<<nblk(9 * (N - nover), 128), 128, 0, st>>>(s, only, w.gkeys, N - nover, inv, w.pairs,
-                                                                w.pair_cap, w.counter);
+      k_grid_pairs<<<nblk(9 * kGridLanes * (N - nover), 128), 128, 0, st>>>(s, fmt, only, w.gkeys, N - nover,
+                                                                             w.pairs, w.pair_cap, w.counter);
       if (nover > 0) {
         dim3 g2(nblk(N, 128), (unsigned)nover);
         k_over_pairs<<<g2, 128, 0, st>>>(s, only, w.gover, w.gis_over, w.pairs, w.pair_cap, w.counter);
@@ -1412,7 +1477,7 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   if (np > 0) {
     k_half_pairs<<<nblk(np, 256), 256, 0, st>>>(w.pairs, np, w.hp);
     c.kernels++;
-    radix_sort_u64(w.hp, w.hp_tmp, nhp, 0, 48, w.tmp, st);
+    radix_sort_u64(w.hp, w.hp_tmp, nhp, 0, 21 + body_bits(N), w.tmp, st);  // (owner << 21) | partner
     c.kernels += 13;
   }
   // ---- candidates: appended by one warp per half-pair, then sorted by key
@@ -1447,7 +1512,12 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
     w.cand_hint = ncand + ncand / 8;
     if (ncand > 1) {
       if ((rc = ensure_tmp(c, (int64_t)sort_temp_bytes(ncand)))) return rc;
-      radix_sort_u64(w.cand, w.cand_tmp, ncand, 0, 64, w.tmp, st);
+      // A stable sort by (owner, partner) alone orders the keys completely:
+      // one warp appends a half-pair's candidates, in its sweeps' order
+      // (vertex-vertex, vertex-edge, vertex-face, edge-edge, each by
+      // ascending sub-element indices, i.e. by ascending key), chunk after
+      // chunk with increasing atomically reserved offsets.
+      radix_sort_u64(w.cand, w.cand_tmp, ncand, 22, 43 + body_bits(N), w.tmp, st);
       c.kernels += 25;
     }
   }
