@@ -146,6 +146,13 @@ struct Ctx {
   int broadphase = 0;  // 0 automatic, 1 all pairs, 2 grid
   float last_cell = 0.f;
   int64_t last_nover = 0;
+  // grid of the last full build (cell size, range of the box centres): a
+  // partial refresh reuses it -- any cell size finds every pair (bodies
+  // larger than a cell are tested against all), and coordinates outside the
+  // range are clamped, which only adds candidates -- and saves two reductions
+  // and their host round trips
+  float grid_lo[3] = {0.f, 0.f, 0.f}, grid_hi[3] = {0.f, 0.f, 0.f};
+  int64_t grid_n = -1;  // bodies of that build (-1: none yet)
   bool forces_stale = false;
   bool more_steps_follow = false;  // inside rk_step, before its last step
   int64_t nsph = 0;                // sub-element spheres of all bodies

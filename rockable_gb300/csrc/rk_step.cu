@@ -573,7 +573,7 @@ int launch_drift(const Scene& s, cudaStream_t st) {
   return 1;
 }
 int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all, const uint8_t* mark) {
-  const int64_t nv = all ? s.nvert : s.nlv;
+  const int64_t nv = all || s.fast_body ? s.nvert : s.nlv;
   if (nv <= 0) return 0;
   const int t = tpb_or(s, 2, 256);
   if (s.fast_body) {
