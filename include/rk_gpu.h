@@ -285,6 +285,28 @@ int rk_format_conf(rk_ctx* ctx, int32_t precision, char* buf, int64_t cap, int64
  * moments on i and on j -- the terms Rockable adds into the resultants
  * (Rockable.cpp:2752-2789).  Meaningful for the active entries only. */
 int rk_download_contributions(rk_ctx* ctx, double* f, double* mi, double* mj);
+
+/* ---- data extractors on the device (src/DataExtractors/*.cpp; the host keeps
+ * the DataExtractor classes, file formats and cadence, and calls these
+ * instead of downloading the state).  Extremes, counts and the picked entry
+ * are exact; means are tree sums in a fixed order (same value on every run;
+ * they may differ from the reference's serial sum in the last bits).
+ * MeanVelocity::record (DataExtractor_MeanVelocity.cpp:24-32): mean |v| over all bodies. */
+int rk_extract_mean_velocity(rk_ctx* ctx, double* mean);
+/* dnStat::record (DataExtractor_dnStat.cpp:35-68) over the active entries (dn < 0 or bonded):
+ * out[10] = dnMin, dnMax, dnMean, dnMeanNeg, dnMeanPos, nbNeg, nbPos, contact point of the first
+ * entry with dnMin (the stored geometry: record it on the last step, rk_set_record_geometry). */
+int rk_extract_dn_stat(rk_ctx* ctx, double* out);
+/* ClusterAABB::record (DataExtractor_ClusterAABB.cpp:31-65): out[7] = 1 when the cluster has a body
+ * (else all zero, the reference's default box), then min[3], max[3] of its bodies' vertices
+ * enlarged by their Minkowski radii. */
+int rk_extract_cluster_aabb(rk_ctx* ctx, int32_t cluster, double* out);
+/* DuoBalance::record (DataExtractor_DuoBalance.cpp:31-85): out[4] = sub-contacts of the pair
+ * (i, j), either way round, with dn < 0, by type (VV, VE, VF, EE). */
+int rk_extract_duo_balance(rk_ctx* ctx, int32_t i, int32_t j, int64_t* out);
+/* TrackBody::record (DataExtractor_TrackBody.cpp:67-80): out[25] = pos[3], vel[3], acc[3], Q[4],
+ * vrot[3], arot[3], force[3], moment[3] of body b. */
+int rk_download_body(rk_ctx* ctx, int64_t b, double* out);
 int rk_download_entries(rk_ctx* ctx, int32_t* i, int32_t* j, int32_t* type, int32_t* isub, int32_t* jsub, double* dn,
                         double* fn, double* ft, double* mom, double* damp, int32_t* bond, uint8_t* active, double* n,
                         double* pos, double* vel);

@@ -105,6 +105,11 @@ SIGNATURES = {
     "rk_set_controls": (C.c_int, [P, C.POINTER(RkControl), C.c_int32, C.POINTER(RkServo)]),
     "rk_set_body_force": (C.c_int, [P, C.c_int, P, C.c_int32, P]),
     "rk_download_contributions": (C.c_int, [P, P, P, P]),
+    "rk_extract_mean_velocity": (C.c_int, [P, P]),
+    "rk_extract_dn_stat": (C.c_int, [P, P]),
+    "rk_extract_cluster_aabb": (C.c_int, [P, C.c_int32, P]),
+    "rk_extract_duo_balance": (C.c_int, [P, C.c_int32, C.c_int32, P]),
+    "rk_download_body": (C.c_int, [P, I64, P]),
     "rk_set_shape_names": (C.c_int, [P, C.POINTER(C.c_char_p), C.c_int32]),
     "rk_format_conf": (C.c_int, [P, C.c_int32, C.c_char_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int64)]),
@@ -464,6 +469,42 @@ class GpuScene:
         if ne:
             self._chk(self.L.rk_download_contributions(self.h, _p(f), _p(mi), _p(mj)), "rk_download_contributions")
         return f, mi, mj
+
+    # ---- data extractors on the device (src/DataExtractors/*.cpp)
+    def mean_velocity(self):
+        """MeanVelocity: mean |v| over all bodies."""
+        m = np.zeros(1)
+        self._chk(self.L.rk_extract_mean_velocity(self.h, _p(m)), "rk_extract_mean_velocity")
+        return float(m[0])
+
+    def dn_stat(self):
+        """dnStat over the active entries: dict of dnMin, dnMax, dnMean,
+        dnMeanNeg, dnMeanPos, nbNeg, nbPos and pos (contact point of dnMin)."""
+        o = np.zeros(10)
+        self._chk(self.L.rk_extract_dn_stat(self.h, _p(o)), "rk_extract_dn_stat")
+        return {"dnMin": o[0], "dnMax": o[1], "dnMean": o[2], "dnMeanNeg": o[3], "dnMeanPos": o[4],
+                "nbNeg": int(o[5]), "nbPos": int(o[6]), "pos": o[7:10].copy()}
+
+    def cluster_aabb(self, cluster):
+        """ClusterAABB: (min[3], max[3]) of the cluster's bodies' vertices
+        enlarged by their radii (zeros for an empty cluster)."""
+        o = np.zeros(7)
+        self._chk(self.L.rk_extract_cluster_aabb(self.h, int(cluster), _p(o)), "rk_extract_cluster_aabb")
+        return o[1:4].copy(), o[4:7].copy()
+
+    def duo_balance(self, i, j):
+        """DuoBalance: sub-contacts of the pair (i, j) with dn < 0, by type."""
+        o = np.zeros(4, dtype=np.int64)
+        self._chk(self.L.rk_extract_duo_balance(self.h, int(i), int(j), _p(o)), "rk_extract_duo_balance")
+        return o
+
+    def body(self, b):
+        """TrackBody's fields of body b: dict of pos, vel, acc, Q, vrot, arot,
+        force, moment."""
+        o = np.zeros(25)
+        self._chk(self.L.rk_download_body(self.h, int(b), _p(o)), "rk_download_body")
+        return {"pos": o[0:3], "vel": o[3:6], "acc": o[6:9], "Q": o[9:13], "vrot": o[13:16], "arot": o[16:19],
+                "force": o[19:22], "moment": o[22:25]}
 
     def interfaces(self):
         n = self.L.rk_num_interfaces(self.h)

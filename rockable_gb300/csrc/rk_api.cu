@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "rk_conf.cuh"
+#include "rk_extract.cuh"
 #include "rk_ctx.cuh"
 
 using namespace rk;
@@ -867,6 +868,8 @@ void rk_destroy(rk_ctx* x) {
   if (w.gstat) cudaFree(w.gstat);
   if (w.split) cudaEventDestroy(w.split);
   dfree(c.kin_stage);
+  dfree(c.ext_part);
+  dfree(c.ext_u);
   dfree(c.d_ke);
   {
     Skin& k = c.skin;
@@ -1815,6 +1818,133 @@ int rk_format_conf(rk_ctx* x, int32_t prec, char* buf, int64_t cap, int64_t* par
   if (interactions_len) *interactions_len = li;
   if (n_active) *n_active = na;
   if (buf && lp + li > cap) return fail(c, RK_ERR_CAPACITY, "the conf text needs a larger buffer");
+  return RK_OK;
+}
+
+// ------------------------------------------------------- data extractors ----
+static int ext_scratch(Ctx& c) {
+  int rc;
+  if (!c.ext_part && (rc = dalloc(c, c.ext_part, 8 * kExtBlocks))) return rc;
+  if (!c.ext_u && (rc = dalloc(c, c.ext_u, 8))) return rc;
+  return 0;
+}
+
+int rk_extract_mean_velocity(rk_ctx* x, double* mean) {
+  if (!x || !mean) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  const Scene& s = c.s;
+  if (s.n <= 0) return fail(c, RK_ERR_STATE, "no bodies");
+  int rc;
+  if ((rc = ext_scratch(c))) return rc;
+  k_ext_speed<<<kExtBlocks, kExtThreads, 0, c.stream>>>(s, c.ext_part);
+  c.kernels++;
+  double part[kExtBlocks];
+  CK(cudaMemcpyAsync(part, c.ext_part, sizeof part, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  double m = 0.0;
+  for (int k = 0; k < kExtBlocks; k++) m += part[k];
+  *mean = m / (double)s.n;
+  return RK_OK;
+}
+
+int rk_extract_dn_stat(rk_ctx* x, double* out) {
+  if (!x || !out) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  const Scene& s = c.s;
+  double mn = 1e20, mx = -1e20, sum = 0.0, sneg = 0.0, nneg = 0.0, spos = 0.0, npos = 0.0;
+  double pmin[3] = {0.0, 0.0, 0.0};
+  if (s.ne > 0) {
+    int rc;
+    if ((rc = ext_scratch(c))) return rc;
+    k_ext_dn<<<kExtBlocks, kExtThreads, 0, c.stream>>>(s, c.ext_part);
+    c.kernels++;
+    double part[8 * kExtBlocks];
+    CK(cudaMemcpyAsync(part, c.ext_part, sizeof part, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    int64_t imn = INT64_MAX;
+    for (int k = 0; k < kExtBlocks; k++) {
+      const double* p = part + 8 * k;
+      sum += p[0];
+      sneg += p[1];
+      nneg += p[2];
+      spos += p[3];
+      npos += p[4];
+      const int64_t ik = p[6] >= 9.2e18 ? INT64_MAX : (int64_t)p[6];
+      if (ik != INT64_MAX && (p[5] < mn || (!(mn < p[5]) && ik < imn))) {
+        mn = p[5];
+        imn = ik;
+      }
+      if (p[7] > mx) mx = p[7];
+    }
+    if (imn != INT64_MAX) {
+      CK(cudaMemcpyAsync(pmin, s.gpos + 3 * imn, sizeof pmin, cudaMemcpyDeviceToHost, c.stream));
+      CK(cudaStreamSynchronize(c.stream));
+    }
+  }
+  if (nneg > 0.0) sneg /= nneg;
+  if (npos > 0.0) spos /= npos;
+  if (nneg > 0.0 || npos > 0.0) sum /= (nneg + npos);
+  const double o[10] = {mn, mx, sum, sneg, spos, nneg, npos, pmin[0], pmin[1], pmin[2]};
+  for (int k = 0; k < 10; k++) out[k] = o[k];
+  return RK_OK;
+}
+
+int rk_extract_cluster_aabb(rk_ctx* x, int32_t cluster, double* out) {
+  if (!x || !out) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  const Scene& s = c.s;
+  for (int k = 0; k < 7; k++) out[k] = 0.0;
+  if (s.nvert <= 0) return RK_OK;
+  int rc;
+  if ((rc = ext_scratch(c))) return rc;
+  const unsigned long long init[7] = {~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
+  CK(cudaMemcpyAsync(c.ext_u, init, sizeof init, cudaMemcpyHostToDevice, c.stream));
+  k_ext_cluster_box<<<nblk(s.nvert, 256), 256, 0, c.stream>>>(s, cluster, c.ext_u);
+  c.kernels++;
+  unsigned long long r[7];
+  CK(cudaMemcpyAsync(r, c.ext_u, sizeof r, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (r[6]) {  // else the zero box of an empty cluster, as the reference prints it
+    out[0] = 1.0;
+    for (int k = 0; k < 6; k++) out[1 + k] = ext_unord(r[k]);
+  }
+  return RK_OK;
+}
+
+int rk_extract_duo_balance(rk_ctx* x, int32_t i, int32_t j, int64_t* out) {
+  if (!x || !out) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  const Scene& s = c.s;
+  for (int k = 0; k < 4; k++) out[k] = 0;
+  if (s.ne <= 0) return RK_OK;
+  int rc;
+  if ((rc = ext_scratch(c))) return rc;
+  CK(cudaMemsetAsync(c.ext_u, 0, 4 * sizeof(unsigned long long), c.stream));
+  k_ext_duo<<<nblk(s.ne, 256), 256, 0, c.stream>>>(s, i, j, c.ext_u);
+  c.kernels++;
+  unsigned long long r[4];
+  CK(cudaMemcpyAsync(r, c.ext_u, sizeof r, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  for (int k = 0; k < 4; k++) out[k] = (int64_t)r[k];
+  return RK_OK;
+}
+
+int rk_download_body(rk_ctx* x, int64_t b, double* out) {
+  if (!x || !out) return RK_ERR_ARG;
+  Ctx& c = x->c;
+  cudaSetDevice(c.device);
+  if (b < 0 || b >= c.s.n) return fail(c, RK_ERR_ARG, "body index out of range");
+  settle_lazy_forces(c);  // a driven body's resultant summed on demand
+  int rc;
+  if ((rc = ext_scratch(c))) return rc;
+  k_ext_body<<<1, 32, 0, c.stream>>>(c.s, b, c.ext_part);
+  c.kernels++;
+  CK(cudaMemcpyAsync(out, c.ext_part, 25 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
   return RK_OK;
 }
 

@@ -134,6 +134,8 @@ struct Ctx {
   int64_t kernels = 0;
   unsigned long long* h_flags = nullptr;  // pinned mirror of the device flag block
   double* d_ke = nullptr;
+  double* ext_part = nullptr;             // the extractors' per-block partial results
+  unsigned long long* ext_u = nullptr;    // their atomic extremes and counts
   int64_t ke_blocks = 0;
   // contributions and per-step arrays (single-buffered)
   int64_t contrib_cap = 0;

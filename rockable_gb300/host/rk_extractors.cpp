@@ -107,6 +107,7 @@ void record_body(const Rockable& box, std::ofstream& f, int ib, const Imposed& i
 }
 
 // TrackBody: ibody filename nrec -- one body's kinematics and resultant
+// (with a GPU context: that body's fields only, rk_download_body)
 class TrackBody : public DataExtractor {
   int ibody{0};
   Imposed imp;
@@ -120,7 +121,28 @@ class TrackBody : public DataExtractor {
     columnDoc.assign(std::begin(kBodyColumns), std::end(kBodyColumns));
   }
   void init() override { imp.find(*box, ibody); }
-  void record() override { record_body(*box, recordFile, ibody, imp); }
+  bool onDevice() const override { return box && box->ctx(); }
+  void record() override {
+    if (!onDevice()) {
+      record_body(*box, recordFile, ibody, imp);
+      return;
+    }
+    double o[25];
+    if (rk_download_body(box->ctx(), ibody, o) != RK_OK) return;
+    double force[3] = {o[19], o[20], o[21]};
+    imp.subtract(*box, force);
+    recordFile << box->t << ' ';
+    put3(recordFile, o);
+    recordFile << ' ';
+    put3(recordFile, o + 3);
+    recordFile << ' ' << o[9] << ' ' << o[10] << ' ' << o[11] << ' ' << o[12] << ' ';
+    put3(recordFile, o + 13);
+    recordFile << ' ';
+    put3(recordFile, force);
+    recordFile << ' ';
+    put3(recordFile, o + 22);
+    recordFile << std::endl << std::flush;
+  }
 };
 
 // MeanVelocity: filename nrec -- mean speed over all bodies
@@ -132,14 +154,19 @@ class MeanVelocity : public DataExtractor {
     nstep = std::numeric_limits<int>::max();
     docString << " nrec = " << nrec;
   }
+  bool onDevice() const override { return box && box->ctx(); }
   void record() override {
-    const Particles& P = box->P;
     double m = 0.0;
-    for (size_t b = 0; b < P.size(); b++) {
-      const double* v = &P.vel[3 * b];
-      m += std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (onDevice()) {
+      if (rk_extract_mean_velocity(box->ctx(), &m) != RK_OK) return;
+    } else {
+      const Particles& P = box->P;
+      for (size_t b = 0; b < P.size(); b++) {
+        const double* v = &P.vel[3 * b];
+        m += std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      }
+      m /= (double)P.size();
     }
-    m /= (double)P.size();
     recordFile << box->t << ' ' << m << std::endl << std::flush;
   }
 };
@@ -157,10 +184,20 @@ class DnStat : public DataExtractor {
                  "nbNeg",   "nbPos", "pos.x of dnMin", "pos.y of dnMin", "pos.z of dnMin"};
   }
   bool needsGeometry() const override { return true; }
+  bool onDevice() const override { return box && box->ctx(); }
   void record() override {
     const Interactions& I = box->I;
     double mn = 1e20, mx = -1e20, meanNeg = 0.0, meanPos = 0.0, nNeg = 0.0, nPos = 0.0, mean = 0.0;
     double pmin[3] = {0.0, 0.0, 0.0};
+    if (onDevice()) {
+      double o[10];
+      if (rk_extract_dn_stat(box->ctx(), o) != RK_OK) return;
+      recordFile << box->t << ' ' << o[0] << ' ' << o[1] << ' ' << o[2] << ' ' << o[3] << ' ' << o[4] << ' '
+                 << (int)o[5] << ' ' << (int)o[6] << ' ';
+      put3(recordFile, o + 7);
+      recordFile << std::endl << std::flush;
+      return;
+    }
     for (size_t e = 0; e < I.size(); e++) {
       if (!I.active[e]) continue;
       const double dn = I.dn[e];
@@ -220,7 +257,18 @@ class ClusterAABB : public DataExtractor {
     docString << "icluster = " << icluster << ", nrec = " << nrec;
     columnDoc = {"Time", "aabb.min.x", "aabb.min.y", "aabb.min.z", "aabb.max.x", "aabb.max.y", "aabb.max.z"};
   }
+  bool onDevice() const override { return box && box->ctx(); }
   void record() override {
+    if (onDevice()) {
+      double o[7];
+      if (rk_extract_cluster_aabb(box->ctx(), icluster, o) != RK_OK) return;
+      recordFile << box->t << ' ';
+      put3(recordFile, o + 1);
+      recordFile << ' ';
+      put3(recordFile, o + 4);
+      recordFile << std::endl << std::flush;
+      return;
+    }
     const Particles& P = box->P;
     Box3 bx;
     for (size_t b = 0; b < P.size(); b++) {
@@ -256,12 +304,19 @@ class DuoBalance : public DataExtractor {
     docString << "first particle = " << bi << ", second particle = " << bj << ", nrec = " << nrec;
     columnDoc = {"Time", "nvv", "nve", "nvf", "nee", "(nvv + nve + nvf + nee) x weight"};
   }
+  bool onDevice() const override { return box && box->ctx(); }
   void record() override {
     const Interactions& I = box->I;
     size_t n[4] = {0, 0, 0, 0};
-    for (size_t e = 0; e < I.size(); e++) {
-      const bool pair = (I.i[e] == bi && I.j[e] == bj) || (I.i[e] == bj && I.j[e] == bi);
-      if (pair && I.dn[e] < 0.0 && I.type[e] >= 0 && I.type[e] < 4) n[I.type[e]]++;
+    if (onDevice()) {
+      int64_t d[4];
+      if (rk_extract_duo_balance(box->ctx(), bi, bj, d) != RK_OK) return;
+      for (int k = 0; k < 4; k++) n[k] = (size_t)d[k];
+    } else {
+      for (size_t e = 0; e < I.size(); e++) {
+        const bool pair = (I.i[e] == bi && I.j[e] == bj) || (I.i[e] == bj && I.j[e] == bi);
+        if (pair && I.dn[e] < 0.0 && I.type[e] >= 0 && I.type[e] < 4) n[I.type[e]]++;
+      }
     }
     // no contact-partnership weights on this engine (ContactPartnership None)
     recordFile << box->t << "   " << n[0] << ' ' << n[1] << ' ' << n[2] << ' ' << n[3] << "\n" << '\n' << std::flush;

@@ -911,7 +911,9 @@ long Rockable::consoleRun(const std::string& outdir, long max_steps) {  // run.c
       interConfC_ = 0.0;
     }
     if (!dataExtractors.empty() && due(s_last, false)) {
-      if (!save && !syncFromDevice(geo)) return -1;
+      bool mirror = false;  // the extractors that read the host mirror need it downloaded
+      for (auto& de : dataExtractors) mirror = mirror || !de->onDevice();
+      if (!save && mirror && !syncFromDevice(geo)) return -1;
       for (auto& de : dataExtractors) {
         if (de->nstep > 0 && s_last % de->nstep == 0) de->exec();
         if (de->nrec > 0 && s_last % de->nrec == 0) de->record();

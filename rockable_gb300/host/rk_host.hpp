@@ -56,7 +56,10 @@ class BodyForce {
 // DataExtractor (src/DataExtractors/DataExtractor.hpp:46-73).  exec() and
 // record() see the host mirror of the state, downloaded at their cadence
 // (consoleRun: exec when step % nstep == 0, record when step % nrec == 0, with
-// the reference's step counter, Rockable.cpp:2580, 2717-2738).
+// the reference's step counter, Rockable.cpp:2580, 2717-2738) -- except the
+// extractors that reduce on the device (onDevice()): with a GPU context they
+// read their few numbers through the rk_extract_* calls, and the mirror is
+// not downloaded for them.
 class DataExtractor {
  public:
   Rockable* box{nullptr};
@@ -74,6 +77,8 @@ class DataExtractor {
   virtual void end() {}
   // record() reads the contact points of the entries (downloaded only on demand)
   virtual bool needsGeometry() const { return false; }
+  // record() and exec() read the device, not the host mirror
+  virtual bool onDevice() const { return false; }
   // the entry of extractedDataDoc.txt (DataExtractor.cpp: generateHelp)
   virtual void generateHelp(std::ostream& os);
 };
