@@ -91,3 +91,59 @@ def test_device_extractors_match_a_serial_restatement(gpu_lib, tmp_path, form):
         for k in ["pos", "vel", "acc", "Q", "vrot", "arot", "force", "moment"]:
             assert np.array_equal(r[k], B[k][b]), (b, k)
     h.close()
+
+
+def test_host_runner_records_the_device_extractors_like_its_conf(golden_dir, gpu_lib, tmp_path):
+    """The C++ runner with a dataExtractors.txt: MeanVelocity, dnStat,
+    DuoBalance and TrackBody now reduce on the device; their lines at the
+    time of the last conf file agree with that conf's Particles and
+    Interactions sections (the data files print 6 significant digits)."""
+    import os
+    import subprocess
+    from conftest import CONF, ROOT
+    d = golden_dir / "512_particles"
+    conf_in = (d / CONF["512_particles"]).read_text()
+    inter = conf_in.split("\nInteractions ")[1].splitlines()[1:]
+    rows = [l.split() for l in inter if l.strip() and not l.startswith("#")]
+    touching = [(int(r[0]), int(r[1])) for r in rows if len(r) > 8 and float(r[8]) < 0.0]
+    pi, pj = max(set(touching), key=touching.count)
+    (tmp_path / "dataExtractors.txt").write_text(
+        "MeanVelocity mv.txt 1\ndnStat dn.txt 1\nDuoBalance %d %d duo.txt 1\nTrackBody 10 tb.txt 1\n" % (pi, pj))
+    for f in os.listdir(d):
+        if not f.endswith(".conf"):
+            (tmp_path / f).write_bytes((d / f).read_bytes())
+    cli = os.path.join(ROOT, "rockable_gb300", "_lib", "rockable-gb300")
+    r = subprocess.run([cli, str(d / CONF["512_particles"]), "-o", str(tmp_path / "out")], cwd=str(tmp_path),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    outs = sorted((p for p in (tmp_path / "out").iterdir() if p.name.startswith("conf")),
+                  key=lambda p: int(p.name[4:]))
+    last = outs[-1].read_text()
+    t = [l.split()[1] for l in last.splitlines() if l.startswith("t ")][0]
+    key = "%g" % float(t)
+
+    def line(name):
+        ls = [l.split() for l in (tmp_path / name).read_text().splitlines() if l.strip()]
+        hit = [l for l in ls if l[0] == key]
+        assert hit, (name, key, ls[-3:])
+        return [float(x) for x in hit[-1][1:]]
+
+    P = [l.split() for l in last.split("\nParticles ")[1].splitlines()[2:]]
+    P = [p for p in P if len(p) >= 23]
+    vel = np.array([[float(x) for x in p[7:10]] for p in P])
+    mv = line("mv.txt")[0]
+    ref = np.mean(np.sqrt(np.sum(vel ** 2, axis=1)))
+    assert abs(mv - ref) <= 1e-5 * abs(ref), (mv, ref)
+    I = [l.split() for l in last.split("\nInteractions ")[1].splitlines()[1:]]
+    I = [x for x in I if len(x) > 8 and not x[0].startswith("#")]
+    dn = np.array([float(x[8]) for x in I])
+    ds = line("dn.txt")
+    assert abs(ds[0] - dn.min()) <= 1e-5 * abs(dn.min()) and int(ds[5]) == int(np.sum(dn < 0.0))
+    duo = [0, 0, 0, 0]
+    for x in I:
+        if float(x[8]) < 0.0 and {int(x[0]), int(x[1])} == {pi, pj}:
+            duo[int(x[2])] += 1
+    assert [int(v) for v in line("duo.txt")[:4]] == duo
+    tb = line("tb.txt")
+    p10 = np.array([float(x) for x in P[10][4:7]])
+    assert np.allclose(tb[0:3], p10, rtol=1e-5, atol=1e-12)
