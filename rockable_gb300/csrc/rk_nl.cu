@@ -886,8 +886,10 @@ __device__ __forceinline__ void warp_emit(bool ok, uint64_t key, int lane, uint6
   }
 }
 
+// The FP64 variant asks for 4 blocks per SM (128 registers, a few spills to
+// L1) instead of 3 at 166 registers: it is latency-bound.
 template <bool GEOM>
-__global__ void __launch_bounds__(32 * kCandWarps)
+__global__ void __launch_bounds__(32 * kCandWarps, GEOM ? 1 : 4)
 k_candidates(Scene s, const uint64_t* hp, int64_t nhp, uint32_t* mask, uint64_t* out, int64_t cap,
              unsigned long long* counter) {
   __shared__ CandLists lists[kCandWarps];
