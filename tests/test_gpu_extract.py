@@ -103,8 +103,8 @@ def test_host_runner_records_the_device_extractors_like_its_conf(golden_dir, gpu
     from conftest import CONF, ROOT
     d = golden_dir / "512_particles"
     conf_in = (d / CONF["512_particles"]).read_text()
-    inter = conf_in.split("\nInteractions ")[1].splitlines()[1:]
-    rows = [l.split() for l in inter if l.strip() and not l.startswith("#")]
+    ls = conf_in.split("\nInteractions ")[1].splitlines()
+    rows = [l.split() for l in ls[1:] if not l.startswith("#")][:int(ls[0].split()[0])]
     touching = [(int(r[0]), int(r[1])) for r in rows if len(r) > 8 and float(r[8]) < 0.0]
     pi, pj = max(set(touching), key=touching.count)
     (tmp_path / "dataExtractors.txt").write_text(
@@ -113,6 +113,7 @@ def test_host_runner_records_the_device_extractors_like_its_conf(golden_dir, gpu
         if not f.endswith(".conf"):
             (tmp_path / f).write_bytes((d / f).read_bytes())
     cli = os.path.join(ROOT, "rockable_gb300", "_lib", "rockable-gb300")
+    (tmp_path / "out").mkdir()
     r = subprocess.run([cli, str(d / CONF["512_particles"]), "-o", str(tmp_path / "out")], cwd=str(tmp_path),
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -128,14 +129,18 @@ def test_host_runner_records_the_device_extractors_like_its_conf(golden_dir, gpu
         assert hit, (name, key, ls[-3:])
         return [float(x) for x in hit[-1][1:]]
 
-    P = [l.split() for l in last.split("\nParticles ")[1].splitlines()[2:]]
-    P = [p for p in P if len(p) >= 23]
+    def section(text, name):  # the N lines of a conf section "name N" (after its column header, if any)
+        ls = text.split("\n" + name + " ")[1].splitlines()
+        n = int(ls[0].split()[0])
+        body = [l for l in ls[1:] if not l.startswith("#")]
+        return [l.split() for l in body[:n]]
+
+    P = section(last, "Particles")
     vel = np.array([[float(x) for x in p[7:10]] for p in P])
     mv = line("mv.txt")[0]
     ref = np.mean(np.sqrt(np.sum(vel ** 2, axis=1)))
     assert abs(mv - ref) <= 1e-5 * abs(ref), (mv, ref)
-    I = [l.split() for l in last.split("\nInteractions ")[1].splitlines()[1:]]
-    I = [x for x in I if len(x) > 8 and not x[0].startswith("#")]
+    I = section(last, "Interactions")
     dn = np.array([float(x[8]) for x in I])
     ds = line("dn.txt")
     assert abs(ds[0] - dn.min()) <= 1e-5 * abs(dn.min()) and int(ds[5]) == int(np.sum(dn < 0.0))
