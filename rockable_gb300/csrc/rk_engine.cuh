@@ -209,10 +209,11 @@ int max_tpb(int which, int form_mixed);
 // a batched skin step after the guard asked for a refresh: the kernel does nothing
 __device__ __forceinline__ bool step_halted(const Scene& s) { return s.sk_ctl != nullptr && s.sk_ctl[0] != 0u; }
 
-int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, const uint8_t* mark,
                       cudaStream_t st);
-int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_t st);
+// with_drift: the step's launch, which makes the free bodies' drift first (the mixed form
+// has no separate drift launch: launch_drift returns 0 for it)
+int launch_body_frames(const Scene& s, unsigned blocks, int threads, int with_drift, cudaStream_t st);
 int launch_body_verts(const Scene& s, cudaStream_t st);
 int launch_fused_gather(const Scene& s, unsigned blocks, int threads, int apply_kick, cudaStream_t st);
 int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t st);

@@ -84,10 +84,7 @@ __device__ __forceinline__ f3v euler_f(f3v I, f3v iI, f3v w, f3v M) {
 
 // First half of the velocity-Verlet step for the free bodies (the FP64 form:
 // Rockable.cpp:2056-2083 through rk_body.cuh's k_drift).
-__global__ void k_drift(Scene s) {
-  if (step_halted(s)) return;
-  const int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= s.n) return;
+__device__ __forceinline__ void drift_body(const Scene& s, int64_t i) {
   const float dt = d2f(s.dt), dt_2 = d2f(s.dt_2), dt2_2 = d2f(s.dt2_2);
   const V3 p = ld3(s.pos, i), v = ld3(s.vel, i), w = ld3(s.vrot, i);
   const Q4 q = ldq(s.Q, i);
@@ -129,6 +126,11 @@ __global__ void k_drift(Scene s) {
   st3(s.vel, i, addinc(v, dt_2 * af));
   st3(s.vrot, i, addinc(w, dt_2 * lf));
   stq(s.Q, i, q4(fma(c, qd.s, qd.s), fma(c, qd.v.x, qd.v.x), fma(c, qd.v.y, qd.v.y), fma(c, qd.v.z, qd.v.z)));
+}
+__global__ void k_drift(Scene s) {
+  if (step_halted(s)) return;
+  const int64_t i = s.n_driven + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < s.n) drift_body(s, i);
 }
 
 // Resultants, Newton-Euler and the second half-kick (Rockable.cpp:3837-3866,
@@ -250,12 +252,18 @@ __global__ void k_gather_accel(Scene s, int apply_kick) {
 // FP32 offsets (world vertex - centre, the FP32 test's coordinates) of all
 // the block's bodies' vertices, coalesced, from the FP32 matrix.  The FP64
 // work per body is one matrix instead of one rotation per vertex.
+// With DRIFT (the step's launch), each free body's thread first makes its
+// drift (the first half of the velocity-Verlet step, above), so that the
+// frames read the state the drift just wrote: one launch and one pass over
+// the bodies instead of two.
+template <bool DRIFT>
 __global__ void k_body_frames(Scene s) {
   if (step_halted(s)) return;
   extern __shared__ float fr[];  // [blockDim.x][10]: the FP32 matrix (and a pad)
   const int64_t b0 = blockIdx.x * (int64_t)blockDim.x;
   const int64_t b = b0 + threadIdx.x;
   if (b < s.n) {
+    if (DRIFT && b >= s.n_driven) drift_body(s, b);
     const Q4 q = ldq(s.Q, b);
     const double xx = q.v.x * q.v.x, yy = q.v.y * q.v.y, zz = q.v.z * q.v.z;
     const double xy = q.v.x * q.v.y, xz = q.v.x * q.v.z, yz = q.v.y * q.v.z;
@@ -332,12 +340,9 @@ __global__ void __launch_bounds__(kHeavyThreads) k_gather_heavy(Scene s, const i
 
 }  // namespace mx
 
-int launch_fused_drift(const Scene& s, unsigned blocks, int threads, cudaStream_t st) {
-  mx::k_drift<<<blocks, threads, 0, st>>>(s);
-  return 1;
-}
-int launch_body_frames(const Scene& s, unsigned blocks, int threads, cudaStream_t st) {
-  mx::k_body_frames<<<blocks, threads, 10 * sizeof(float) * threads, st>>>(s);
+int launch_body_frames(const Scene& s, unsigned blocks, int threads, int with_drift, cudaStream_t st) {
+  if (with_drift) mx::k_body_frames<true><<<blocks, threads, 10 * sizeof(float) * threads, st>>>(s);
+  else mx::k_body_frames<false><<<blocks, threads, 10 * sizeof(float) * threads, st>>>(s);
   return 1;
 }
 int launch_fused_glob(const Scene& s, unsigned blocks, int threads, int only_listed, const uint8_t* mark,
@@ -356,7 +361,7 @@ int launch_fused_heavy(const Scene& s, const int* list, int count, cudaStream_t 
 }
 cudaError_t fused_attributes(int which, cudaFuncAttributes* a) {
   if (which == 1) return cudaFuncGetAttributes(a, mx::k_gather_accel);
-  if (which == 2) return cudaFuncGetAttributes(a, mx::k_body_frames);
+  if (which == 2) return cudaFuncGetAttributes(a, mx::k_body_frames<true>);
   return cudaFuncGetAttributes(a, mx::k_drift);
 }
 

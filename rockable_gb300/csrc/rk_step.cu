@@ -568,7 +568,7 @@ int launch_drift(const Scene& s, cudaStream_t st) {
   int64_t nf = s.n - s.n_driven;
   if (nf <= 0) return 0;
   const int t = tpb_or(s, 3, 128);
-  if (s.fast_body) return launch_fused_drift(s, nblk(nf, t), t, st);
+  if (s.fast_body) return 0;  // made by the step's body-frame launch (launch_glob_vertices)
   exact::k_drift<<<nblk(nf, t), t, 0, st>>>(s);
   return 1;
 }
@@ -579,7 +579,7 @@ int launch_glob_vertices(const Scene& s, cudaStream_t st, bool all, const uint8_
   if (s.fast_body) {
     // the mixed form's step needs only the FP32 offsets and the FP64 frames;
     // a list update needs the FP64 world vertices as well
-    int k = launch_body_frames(s, nblk(s.n, t), t, st);
+    int k = launch_body_frames(s, nblk(s.n, t), t, all ? 0 : 1, st);
     if (all) k += launch_fused_glob(s, nblk(nv, t), t, 0, mark, st);
     return k;
   }
